@@ -1,0 +1,338 @@
+"""Benchmark of the SICC GB300 receive path (one JSON line on stdout).
+
+Workload (default, ``bp_osd_128_64``): the QC (128,64) code, BPSK over AWGN,
+65,536 frames per batch at Eb/N0 = 2 dB and 3 dB, layered normalized min-sum
+(alpha 0.75, at most 20 iterations, early stop) with order-2 OSD (1 + 64 +
+2016 tests) on every frame whose syndrome fails.  One step decodes one batch
+at each Eb/N0 (131,072 codewords, 8.39 Mbit of information).  Inputs are
+seeded synthetic LLRs; several distinct batches are kept resident on the GPU
+(larger than L2 together) and cycled between steps.
+
+Metric: information-bit throughput in Mbit/s (sum of k over decoded codewords
+divided by the timed wall time), with the frame error rate of each Eb/N0
+point reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the reference's CPU decoder for the same workload
+on the host cores: its flooding normalized min-sum (restated bit-exactly in
+the oracle) plus the oracle's OSD restatement, on a bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "sicc-baseband-proto_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+EBN0 = (2.0, 3.0)
+BATCH = 65536
+RESIDENT_BATCHES = 4  # per Eb/N0: 8 x 33.5 MB of LLRs resident, > 129 MB of L2
+ITERS, ALPHA = 20, 0.75
+OSD_ORDER, OSD_FLIP, OSD_TESTS = 2, 64, 4096
+WORKLOAD = "bp_osd_128_64"
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC = os.path.join(ROOT, "profiles", "bp_layered_128_64_traffic.json")
+
+
+def peaks():
+    try:
+        with open(PEAKS) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- CPU baseline
+def _cpu_worker(args):
+    llr, iters, alpha = args
+    from oracle import Oracle
+    from sicc_gb300 import codes
+    o = Oracle()
+    c = codes.short_code()
+    oc = o.code(c.n, c.m, c.row_ptr, c.col_ind)
+    t0 = time.perf_counter()
+    info, used = oc.bp_osd_batch(llr, schedule=0, max_iter=iters, alpha=alpha, osd_order=OSD_ORDER,
+                                 osd_max_flip=OSD_FLIP, osd_max_tests=OSD_TESTS)
+    return time.perf_counter() - t0, info, used
+
+
+def cpu_decode(pool, workers, llr):
+    chunks = np.array_split(llr, workers)
+    t0 = time.perf_counter()
+    res = pool.map(_cpu_worker, [(c, ITERS, ALPHA) for c in chunks])
+    wall = time.perf_counter() - t0
+    info = np.concatenate([r[1] for r in res])
+    used = np.concatenate([r[2] for r in res])
+    return wall, info, used
+
+
+def make_inputs(batch, n_batches, seed0):
+    from sicc_gb300 import channel, codes
+    code = codes.short_code()
+    out = {}
+    for e in EBN0:
+        out[e] = [channel.awgn_llrs(code, batch, e, seed=seed0 + int(e * 100) + 7 * b) for b in range(n_batches)]
+    return code, out
+
+
+# -------------------------------------------------------------- clock sampler
+class ClockSampler:
+    def __init__(self, index=0):
+        self.index, self.rows, self.proc = index, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[0]) for r in self.rows if len(r) >= 7 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 7 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 7 for i in range(4) if r[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+# ------------------------------------------------------------------- our arm
+def run_ours(args, rank, world):
+    import torch
+    from sicc_gb300 import fec
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+
+    code, inputs = make_inputs(BATCH, RESIDENT_BATCHES, seed0=1000 * (rank + 1))
+    # CPU baseline pool: spawned before the first GPU call of this process
+    pool = workers = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        workers = os.cpu_count() or 1
+        pool = mp.get_context("spawn").Pool(workers)
+
+    stream = torch.cuda.current_stream()
+    d_llr = {e: [torch.from_numpy(x[2]).cuda() for x in inputs[e]] for e in EBN0}
+    d_info = torch.zeros((BATCH, code.k), dtype=torch.uint8, device="cuda")
+    d_used = torch.zeros(BATCH, dtype=torch.uint8, device="cuda")
+    d_ok = torch.zeros(BATCH, dtype=torch.uint8, device="cuda")
+    d_it = torch.zeros(BATCH, dtype=torch.uint8, device="cuda")
+    dec = fec.StreamBpOsdDecoder(code, max_batch=BATCH, max_iter=ITERS, normalization=ALPHA, offset=0.0,
+                                 damping=0.0, min_abs_llr_accept=0.0, osd_order=OSD_ORDER, osd_max_flip=OSD_FLIP,
+                                 osd_max_tests=OSD_TESTS)
+
+    def step(s):
+        for e in EBN0:
+            dec.decode_device_batch(d_llr[e][s % RESIDENT_BATCHES], d_info, d_ok, d_used, d_it, stream=stream)
+
+    for s in range(args.warmup):
+        step(s)
+    torch.cuda.synchronize()
+    dec.set_timing(True)
+    clocks = ClockSampler(dev)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for s in range(args.steps):
+        step(s)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    calls, bp_ms, osd_ms, osd_cw = dec.kernel_ms()
+    dec.set_timing(False)
+    if world > 1:
+        dist.barrier()
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+
+    # frame error rate and iterations on one resident batch per Eb/N0
+    fer, mean_iter, osd_frac = {}, {}, {}
+    edge_updates = 0
+    for e in EBN0:
+        info_true = inputs[e][0][0]
+        dec.decode_device_batch(d_llr[e][0], d_info, d_ok, d_used, d_it, stream=stream)
+        torch.cuda.synchronize()
+        got = d_info.cpu().numpy()
+        fer[f"{e:g}dB"] = float(np.mean(np.any(got != info_true, axis=1)))
+        it = d_it.cpu().numpy().astype(np.int64)
+        mean_iter[f"{e:g}dB"] = float(it.mean())
+        osd_frac[f"{e:g}dB"] = float(d_used.cpu().numpy().mean())
+        edge_updates += int(it.sum()) * code.edges
+
+    bits_per_step = len(EBN0) * BATCH * code.k
+    value = world * bits_per_step * args.steps / (elapsed_ms * 1e-3) / 1e6
+
+    # ---- end to end through the reference-facing C ABI with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        dec_api = fec.StreamBpOsdDecoder(code, max_batch=BATCH, min_batch=BATCH, max_iter=ITERS, normalization=ALPHA,
+                                         offset=0.0, damping=0.0, min_abs_llr_accept=0.0, osd_order=OSD_ORDER,
+                                         osd_max_flip=OSD_FLIP, osd_max_tests=OSD_TESTS)
+        pinned = {}
+        for e in EBN0:
+            pinned[e] = []
+            for b in range(2):
+                h = torch.empty((BATCH, code.n), dtype=torch.float32, pin_memory=True)
+                h.numpy()[:] = inputs[e][b][2]
+                pinned[e].append(h.numpy())
+        for s in range(min(args.warmup, 2)):
+            for e in EBN0:
+                dec_api.decode(pinned[e][s % 2])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s in range(args.steps):
+            for e in EBN0:
+                dec_api.decode(pinned[e][s % 2])
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": round(world * bits_per_step * args.steps / e2e_s / 1e6, 3), "unit": "Mbit/s",
+               "h2d_bytes_per_step": len(EBN0) * BATCH * code.n * 4,
+               "d2h_bytes_per_step": len(EBN0) * BATCH * (code.k + 1),
+               "api": "cuda_osd_submit_codewords + cuda_osd_flush + cuda_osd_poll_ready (pinned host LLRs)"}
+
+    # ---- roofline of the dominant kernel (layered BP) ----
+    peak, peak_kind = peaks()
+    bytes_per_cw = 4 * code.n + code.k + 3  # LLR in; info bits, success, OSD flag, iterations out
+    avg_bp_ms = bp_ms / max(calls, 1)
+    alg_bytes = BATCH * bytes_per_cw
+    achieved = alg_bytes / (avg_bp_ms * 1e-3) / 1e9
+    traffic = None
+    try:
+        with open(TRAFFIC) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    except Exception:
+        pass
+    roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 5), "traffic": traffic, "peak_source": peak_kind,
+                "kernel": "bp_layered_kernel<8>", "algorithmic_bytes_per_launch": alg_bytes,
+                "avg_launch_ms": round(avg_bp_ms, 4), "osd_avg_launch_ms": round(osd_ms / max(calls, 1), 4),
+                "edge_updates_per_s": round(edge_updates / len(EBN0) / (avg_bp_ms * 1e-3), 1),
+                "note": "BP is issue-bound (shared-memory resident messages); HBM fraction shown per contract"}
+
+    cpu = None
+    if pool is not None:
+        sample = {e: inputs[e][1][2][: args.cpu_sample] for e in EBN0}
+        wall = 0.0
+        for e in EBN0:
+            w, _, _ = cpu_decode(pool, workers, sample[e])
+            wall += w
+        pool.close()
+        cpu = {"value": round(len(EBN0) * args.cpu_sample * code.k / wall / 1e6, 4), "unit": "Mbit/s",
+               "cores": workers, "kind": "port",
+               "sample": f"{args.cpu_sample} frames at each of 2 and 3 dB (flooding min-sum alpha 0.75, 20 "
+                         f"iterations, order-2 OSD on failures), {workers} worker processes"}
+
+    if rank == 0:
+        line = {"metric": "info-bit Mbps BP+OSD (128,64), Eb/N0 2 and 3 dB", "value": round(value, 3),
+                "unit": "Mbit/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": round(elapsed_ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded BPSK/AWGN LLRs)",
+                "config": {"workload": WORKLOAD, "code": "QC (128,64) 4x8 base Z=16", "frames_per_batch": BATCH,
+                           "ebn0_db": list(EBN0), "bp": f"layered NMS alpha {ALPHA}, <= {ITERS} iterations",
+                           "osd": f"order {OSD_ORDER}, {1 + OSD_FLIP + OSD_FLIP * (OSD_FLIP - 1) // 2} tests",
+                           "l2": f"{2 * RESIDENT_BATCHES} resident batches of 33.5 MB cycled (> L2)",
+                           "parallelism": f"replicas x{world}"},
+                "fer": fer, "mean_iterations": mean_iter, "osd_fraction": osd_frac,
+                "gpu_launches": args.steps * len(EBN0) * 2, "clocks": clk, "roofline": roofline,
+                "e2e": e2e, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------- reference arm
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    workers = os.cpu_count() or 1
+    pool = mp.get_context("spawn").Pool(workers)
+    code, inputs = make_inputs(args.cpu_sample, 1, seed0=1000)
+    for _ in range(min(args.warmup, 1)):
+        cpu_decode(pool, workers, inputs[EBN0[0]][0][2][: workers * 8])
+    wall = 0.0
+    fer = {}
+    for s in range(args.steps):
+        for e in EBN0:
+            w, info, _ = cpu_decode(pool, workers, inputs[e][0][2])
+            wall += w
+            if s == 0:
+                fer[f"{e:g}dB"] = float(np.mean(np.any(info != inputs[e][0][0], axis=1)))
+    pool.close()
+    bits = args.steps * len(EBN0) * args.cpu_sample * code.k
+    value = bits / wall / 1e6
+    sample = (f"{args.cpu_sample} frames at each of 2 and 3 dB per step: the reference's flooding min-sum "
+              f"(alpha 0.75, 20 iterations) + order-2 OSD on failures, {workers} worker processes")
+    line = {"impl": "reference", "metric": "info-bit Mbps BP+OSD (128,64), Eb/N0 2 and 3 dB",
+            "value": round(value, 4), "unit": "Mbit/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(wall * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded BPSK/AWGN LLRs)",
+            "config": {"workload": WORKLOAD, "code": "QC (128,64) 4x8 base Z=16", "ebn0_db": list(EBN0),
+                       "frames_per_step": len(EBN0) * args.cpu_sample, "parallelism": "host cores"},
+            "fer": fer, "gpu_launches": 0,
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mbit/s", "cores": workers, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "Mbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=4096)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", args.gpus if "RANK" in os.environ else 1))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,531 @@
+// OFDM receive kernels for sm_103a.
+//
+// sync_kernel (one CTA per frame) restates the CPU receiver's frame search
+// (uhd_ldpc_ofdm_link.cpp:5123-5329): Schmidl-Cox metric
+//   P(d) = sum_{i<L} conj(x[d+i]) x[d+i+L],  E1 = sum |x[d+i]|^2,  E2 = sum |x[d+i+L]|^2,
+//   metric(d) = |P|^2 / max(E1*E2, 1e-18);
+// the earliest candidate over the threshold (or the global maximum), then a
+// full-preamble cross-correlation refinement within +-radius, then the CFO
+// arg(sum conj(x[s+i]) x[s+i+L]) * fs / (2 pi L).  Candidates are scanned in
+// passes of 256 x 17 from a shared-memory copy of the samples: each pass
+// computes the window sums at 256 chunk starts warp-cooperatively and slides
+// them 17 candidates per thread (the odd chunk keeps shared-memory reads on
+// distinct banks).
+//
+// demod_kernel (grid = frames x data-symbol groups) fuses the demodulator of
+// gpu_ofdm_pipeline.cu:566-672 / uhd_ldpc_ofdm_link.cpp:5350-5521: CFO
+// derotation and CP strip while loading, a shared-memory Stockham FFT
+// (radix 4, plus one radix-2 stage for odd log2 N), LS pilot estimates with
+// linear interpolation, MMSE equalisation and max-log LLRs.  The max-log
+// search runs per constellation axis: for Gray square QAM the minimum of
+// fl(dI^2) + fl(dQ^2) over a bit-constrained set splits into the two axis
+// minima (single-precision addition is monotone in each argument), so the
+// result equals the exhaustive 2^bps search of the reference bit for bit
+// given the same equalised symbol.
+#include "ofdm_kernels.h"
+
+#include <algorithm>
+#include <cfloat>
+
+namespace sicc {
+
+namespace {
+
+constexpr int kSyncThreads = 256;
+constexpr int kSyncChunk = 17;
+constexpr int kSyncPass = kSyncThreads * kSyncChunk;
+constexpr int kMaxRefine = 1024;  // 2 * radius + 1
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(__fsub_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)),
+                       __fadd_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+
+__device__ __forceinline__ float2 cmulconj(float2 a, float2 b)  // a * conj(b)
+{
+    return make_float2(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)),
+                       __fsub_rn(__fmul_rn(a.y, b.x), __fmul_rn(a.x, b.y)));
+}
+
+__device__ __forceinline__ float cnorm(float2 a) { return __fadd_rn(__fmul_rn(a.x, a.x), __fmul_rn(a.y, a.y)); }
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kSyncThreads)
+sync_kernel(const float2* __restrict__ samples, long long stride, const int* __restrict__ counts, int count,
+            const float2* __restrict__ preamble, SyncParams p, SyncOut* __restrict__ out)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* win = reinterpret_cast<float2*>(smem_raw);                 // [kSyncPass + pre_len]
+    float* metric = reinterpret_cast<float*>(win + kSyncPass + p.pre_len);  // [kSyncPass]
+    float4* chunk = reinterpret_cast<float4*>(metric + kSyncPass);     // [kSyncThreads] P.re, P.im, E1, E2
+    __shared__ float red[4][kSyncThreads / 32];
+    __shared__ float rmetric[kMaxRefine];
+    __shared__ int s_best;
+    __shared__ float s_bestm;
+
+    const int f = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float2* x = samples + static_cast<long long>(f) * stride;
+    const int avail = counts ? counts[f] : count;
+    const int L = p.half_len, pre = p.pre_len;
+    SyncOut res{0, -1, 0.0f, 0.0f, 0.0f, -1};
+    int limit = avail - pre + 1;
+    if (p.max_search > 0) limit = min(limit, p.max_search + 1);
+
+    float gbest_m = -1.0f;  // global-maximum mode
+    int gbest_d = -1;
+    int coarse = -1;
+    float coarse_m = 0.0f;
+    bool done = (limit <= 0);
+
+    for (int base = 0; !done && base < limit; base += kSyncPass) {
+        const int span = min(kSyncPass + pre, avail - base);
+        for (int i = tid; i < kSyncPass + pre; i += kSyncThreads) win[i] = (i < span) ? x[base + i] : make_float2(0.f, 0.f);
+        __syncthreads();
+        // window sums at chunk starts, one warp per chunk
+        for (int t = warp; t < kSyncThreads; t += kSyncThreads / 32) {
+            const int d0 = t * kSyncChunk;
+            float pr = 0.f, pi = 0.f, e1 = 0.f, e2 = 0.f;
+            for (int i = lane; i < L; i += 32) {
+                const float2 a = win[d0 + i], b = win[d0 + i + L];
+                const float2 c = cmulconj(b, a);  // conj(a) * b
+                pr += c.x;
+                pi += c.y;
+                e1 += cnorm(a);
+                e2 += cnorm(b);
+            }
+            pr = warp_sum(pr);
+            pi = warp_sum(pi);
+            e1 = warp_sum(e1);
+            e2 = warp_sum(e2);
+            if (lane == 0) chunk[t] = make_float4(pr, pi, e1, e2);
+        }
+        __syncthreads();
+        {
+            float4 w = chunk[tid];
+            const int d0 = tid * kSyncChunk;
+            for (int c = 0; c < kSyncChunk; ++c) {
+                const int d = d0 + c;
+                const float den = fmaxf(w.z * w.w, 1e-18f);
+                metric[d] = (base + d < limit) ? (w.x * w.x + w.y * w.y) / den : -1.0f;
+                const float2 x0 = win[d], x1 = win[d + L], x2 = win[d + pre];
+                const float2 add = cmulconj(x2, x1), sub = cmulconj(x1, x0);
+                w.x += add.x - sub.x;
+                w.y += add.y - sub.y;
+                w.z += cnorm(x1) - cnorm(x0);
+                w.w += cnorm(x2) - cnorm(x1);
+            }
+        }
+        __syncthreads();
+        if (p.mode == 1) {
+            // global maximum, first occurrence (strict >)
+            float bm = -1.0f;
+            int bd = 0x7fffffff;
+            for (int c = 0; c < kSyncChunk; ++c) {
+                const int d = tid * kSyncChunk + c;
+                const float m = metric[d];
+                if (m > bm) { bm = m; bd = d; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const float om = __shfl_xor_sync(0xffffffffu, bm, o);
+                const int od = __shfl_xor_sync(0xffffffffu, bd, o);
+                if (om > bm || (om == bm && od < bd)) { bm = om; bd = od; }
+            }
+            if (lane == 0) { red[0][warp] = bm; red[1][warp] = __int_as_float(bd); }
+            __syncthreads();
+            if (tid == 0) {
+                for (int w = 0; w < kSyncThreads / 32; ++w) {
+                    const float m = red[0][w];
+                    const int d = __float_as_int(red[1][w]);
+                    if (m > gbest_m || (m == gbest_m && base + d < gbest_d)) { gbest_m = m; gbest_d = base + d; }
+                }
+            }
+            __syncthreads();
+            continue;
+        }
+        // earliest crossing in this pass; refine each crossing in order until one succeeds
+        int from = 0;
+        while (true) {
+            int first = 0x7fffffff;
+            for (int c = 0; c < kSyncChunk; ++c) {
+                const int d = tid * kSyncChunk + c;
+                if (d >= from && metric[d] >= p.threshold) { first = min(first, d); break; }
+            }
+            first = __reduce_min_sync(0xffffffffu, static_cast<unsigned>(first));
+            if (lane == 0) red[0][warp] = __int_as_float(first);
+            __syncthreads();
+            if (tid == 0) {
+                int m = 0x7fffffff;
+                for (int w = 0; w < kSyncThreads / 32; ++w) m = min(m, __float_as_int(red[0][w]));
+                s_best = m;
+            }
+            __syncthreads();
+            const int d = s_best;
+            __syncthreads();
+            if (d == 0x7fffffff) break;  // next pass
+            // refine around base + d over [lo, hi]
+            const int cand = base + d;
+            const int lo = max(0, cand - p.radius);
+            const int hi = min(avail - pre, cand + p.radius);
+            if (tid == 0) { s_best = cand; s_bestm = 0.0f; }
+            __syncthreads();
+            for (int dd = lo + warp; dd <= hi; dd += kSyncThreads / 32) {
+                float cr = 0.f, ci = 0.f, eng = 0.f;
+                for (int i = lane; i < pre; i += 32) {
+                    const float2 y = x[dd + i], q = preamble[i];
+                    const float2 c = cmulconj(y, q);
+                    cr += c.x;
+                    ci += c.y;
+                    eng += cnorm(y);
+                }
+                cr = warp_sum(cr);
+                ci = warp_sum(ci);
+                eng = warp_sum(eng);
+                if (lane == 0) rmetric[dd - lo] = (cr * cr + ci * ci) / fmaxf(eng * p.pre_energy, 1e-18f);
+            }
+            __syncthreads();
+            if (tid == 0) {
+                float bm = 0.0f;
+                int bd = cand;
+                for (int dd = lo; dd <= hi; ++dd) {
+                    const float m = rmetric[dd - lo];
+                    if (m > bm) { bm = m; bd = dd; }
+                }
+                s_best = bd;
+                s_bestm = bm;
+            }
+            __syncthreads();
+            if (s_bestm >= p.threshold) {
+                coarse = cand;
+                coarse_m = metric[d] >= 0.0f ? metric[d] : 0.0f;
+                res.start = s_best;
+                res.fine = s_bestm;
+                res.found = (p.frame_len > 0 && s_best + p.frame_len > avail) ? 2 : 1;
+                done = true;
+                break;
+            }
+            from = d + 1;
+        }
+        __syncthreads();
+    }
+
+    if (p.mode == 1) {  // broadcast the global maximum found by thread 0
+        __syncthreads();
+        if (tid == 0) { s_best = gbest_d; s_bestm = gbest_m; }
+        __syncthreads();
+        gbest_d = s_best;
+        gbest_m = s_bestm;
+        __syncthreads();
+    }
+    if (p.mode == 1 && gbest_d >= 0 && gbest_m >= p.threshold) {
+        const int cand = gbest_d;
+        const int lo = max(0, cand - p.radius);
+        const int hi = min(limit - 1, cand + p.radius);
+        for (int dd = lo + warp; dd <= hi; dd += kSyncThreads / 32) {
+            float cr = 0.f, ci = 0.f, eng = 0.f;
+            for (int i = lane; i < pre; i += 32) {
+                const float2 y = x[dd + i], q = preamble[i];
+                const float2 c = cmulconj(y, q);
+                cr += c.x;
+                ci += c.y;
+                eng += cnorm(y);
+            }
+            cr = warp_sum(cr);
+            ci = warp_sum(ci);
+            eng = warp_sum(eng);
+            if (lane == 0) rmetric[dd - lo] = (cr * cr + ci * ci) / fmaxf(eng * p.pre_energy, 1e-18f);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            float bm = 0.0f;
+            int bd = cand;
+            for (int dd = lo; dd <= hi; ++dd)
+                if (rmetric[dd - lo] > bm) { bm = rmetric[dd - lo]; bd = dd; }
+            s_best = bd;
+            s_bestm = bm;
+        }
+        __syncthreads();
+        coarse = cand;
+        coarse_m = gbest_m;
+        if (s_bestm >= p.threshold) {
+            res.start = s_best;
+            res.fine = s_bestm;
+            res.found = 1;
+        } else {
+            res.fine = s_bestm;
+        }
+    }
+
+    if (res.found == 1) {
+        const int s0 = res.start;
+        float ar = 0.f, ai = 0.f;
+        for (int i = tid; i < L; i += kSyncThreads) {
+            const float2 c = cmulconj(x[s0 + i + L], x[s0 + i]);  // conj(x[s0+i]) * x[s0+i+L]
+            ar += c.x;
+            ai += c.y;
+        }
+        ar = warp_sum(ar);
+        ai = warp_sum(ai);
+        if (lane == 0) { red[2][warp] = ar; red[3][warp] = ai; }
+        __syncthreads();
+        if (tid == 0) {
+            float sr = 0.f, si = 0.f;
+            for (int w = 0; w < kSyncThreads / 32; ++w) { sr += red[2][w]; si += red[3][w]; }
+            res.cfo_hz = atan2f(si, sr) * p.sample_rate / (2.0f * 3.14159265358979323846f * static_cast<float>(L));
+        }
+    }
+    if (tid == 0) {
+        res.coarse = coarse_m;
+        res.coarse_start = coarse;
+        out[f] = res;
+    }
+}
+
+void launch_sync(const float2* samples, long long stride, const int* counts, int count, int frames,
+                 const float2* preamble, const SyncParams& p, SyncOut* out, cudaStream_t st)
+{
+    if (frames <= 0) return;
+    const size_t smem = static_cast<size_t>(kSyncPass + p.pre_len) * sizeof(float2) +
+                        static_cast<size_t>(kSyncPass) * sizeof(float) + kSyncThreads * sizeof(float4);
+    if (smem > 200 * 1024) throw InvalidArgument("preamble too long for the sync kernel");
+    if (2 * p.radius + 1 > kMaxRefine || p.radius < 0) throw InvalidArgument("refinement radius must be 0..511");
+    check_cuda(cudaFuncSetAttribute(sync_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+               "cudaFuncSetAttribute(sync)");
+    sync_kernel<<<frames, kSyncThreads, smem, st>>>(samples, stride, counts, count, preamble, p, out);
+    check_cuda(cudaGetLastError(), "sync_kernel launch");
+}
+
+// ---------------------------------------------------------------------------
+// demodulator
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr int kDemodThreads = 256;
+constexpr int kMaxPilotsPerCta = 4;
+
+// Stockham autosort FFT of `nfft` points held in buf[0] (natural order in and
+// out); returns the buffer that holds the result.
+__device__ float2* fft_stockham(float2* a, float2* b, int nfft, const float2* __restrict__ tw)
+{
+    int ns = 1;
+    const int q = nfft >> 2;
+    while (ns * 4 <= nfft) {
+        for (int j = threadIdx.x; j < q; j += blockDim.x) {
+            const int k = j & (ns - 1);
+            const int step = nfft / (4 * ns);
+            float2 a0 = a[j], a1 = a[j + q], a2 = a[j + 2 * q], a3 = a[j + 3 * q];
+            if (ns > 1) {
+                a1 = cmul(a1, __ldg(tw + k * step));
+                a2 = cmul(a2, __ldg(tw + 2 * k * step));
+                a3 = cmul(a3, __ldg(tw + 3 * k * step));
+            }
+            const float2 b0 = make_float2(a0.x + a2.x, a0.y + a2.y);
+            const float2 b1 = make_float2(a0.x - a2.x, a0.y - a2.y);
+            const float2 b2 = make_float2(a1.x + a3.x, a1.y + a3.y);
+            const float2 b3 = make_float2(a1.y - a3.y, a3.x - a1.x);  // -i (a1 - a3)
+            const int o = (j / ns) * ns * 4 + k;
+            b[o] = make_float2(b0.x + b2.x, b0.y + b2.y);
+            b[o + ns] = make_float2(b1.x + b3.x, b1.y + b3.y);
+            b[o + 2 * ns] = make_float2(b0.x - b2.x, b0.y - b2.y);
+            b[o + 3 * ns] = make_float2(b1.x - b3.x, b1.y - b3.y);
+        }
+        __syncthreads();
+        float2* t = a;
+        a = b;
+        b = t;
+        ns *= 4;
+    }
+    if (ns < nfft) {  // one radix-2 stage
+        const int h = nfft >> 1;
+        for (int j = threadIdx.x; j < h; j += blockDim.x) {
+            const int k = j & (ns - 1);
+            const float2 a0 = a[j];
+            const float2 a1 = cmul(a[j + h], __ldg(tw + k * (nfft / (2 * ns))));
+            const int o = (j / ns) * ns * 2 + k;
+            b[o] = make_float2(a0.x + a1.x, a0.y + a1.y);
+            b[o + ns] = make_float2(a0.x - a1.x, a0.y - a1.y);
+        }
+        __syncthreads();
+        a = b;
+    }
+    return a;
+}
+
+// Loads symbol `sym` of a frame (CP stripped, CFO derotated) into buf.
+__device__ void load_symbol(const DemodView& v, const float2* __restrict__ x, float cfo_norm, int sym, float2* buf)
+{
+    const int off = v.pre_len + sym * (v.nfft + v.cp) + v.cp;
+    for (int i = threadIdx.x; i < v.nfft; i += blockDim.x) {
+        const int n = off + i;  // sample index from the frame start
+        const float2 s = x[n];
+        float sn, cs;
+        // exp(-j 2 pi cfo n / fs) with cfo_norm = cfo / fs
+        sincospif(-2.0f * cfo_norm * static_cast<float>(n), &sn, &cs);
+        buf[i] = cmul(s, make_float2(cs, sn));
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ float sq_dist(float x, float c)
+{
+    const float d = __fsub_rn(x, c);
+    return __fmul_rn(d, d);
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kDemodThreads)
+demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, const SyncOut* __restrict__ sync,
+             float* __restrict__ llr, long long llr_stride, int symbols_per_cta)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* buf0 = reinterpret_cast<float2*>(smem_raw);
+    float2* buf1 = buf0 + v.nfft;
+    float2* hp = buf1 + v.nfft;  // [kMaxPilotsPerCta][active_sc]
+    __shared__ int s_pilot_of[kMaxPilotsPerCta];
+
+    const int f = blockIdx.x;
+    const int ds0 = blockIdx.y * symbols_per_cta;
+    const int ds1 = min(v.num_data, ds0 + symbols_per_cta);
+    if (ds0 >= ds1) return;
+    int start = 0;
+    float cfo = 0.0f;
+    if (sync) {
+        const SyncOut so = sync[f];
+        if (so.found != 1) {
+            // no frame: zero LLRs (the caller sees found != 1 in the sync result)
+            float* dst = llr + static_cast<long long>(f) * llr_stride;
+            for (int i = ds0 * v.active_sc * v.bits_per_symbol + threadIdx.x; i < ds1 * v.active_sc * v.bits_per_symbol;
+                 i += blockDim.x)
+                dst[i] = 0.0f;
+            return;
+        }
+        start = so.start;
+        cfo = so.cfo_hz;
+    }
+    const float2* x = samples + static_cast<long long>(f) * stride + start;
+    const float cfo_norm = cfo / v.sample_rate;
+
+    // pilots referenced by this CTA's data symbols
+    int pmin = 0x7fffffff, pmax = -1;
+    for (int d = ds0; d < ds1; ++d) {
+        pmin = min(pmin, min(v.interp_p0[d], v.interp_p1[d]));
+        pmax = max(pmax, max(v.interp_p0[d], v.interp_p1[d]));
+    }
+    const int npil = v.use_pilot_est ? (pmax - pmin + 1) : 0;
+    for (int q = 0; q < npil && q < kMaxPilotsPerCta; ++q) {
+        const int p = pmin + q;
+        load_symbol(v, x, cfo_norm, v.pilot_symbols[p], buf0);
+        const float2* Y = fft_stockham(buf0, buf1, v.nfft, v.twiddle);
+        for (int sc = threadIdx.x; sc < v.active_sc; sc += blockDim.x) {
+            const float2 y = Y[v.used_bins[sc]];
+            const float2 pil = v.pilot_grid[static_cast<size_t>(p) * v.active_sc + sc];
+            const float den = fmaxf(cnorm(pil), 1e-9f);
+            const float2 t = cmulconj(y, pil);
+            hp[q * v.active_sc + sc] = make_float2(__fdiv_rn(t.x, den), __fdiv_rn(t.y, den));
+        }
+        if (threadIdx.x == 0) s_pilot_of[q] = p;
+        __syncthreads();
+    }
+
+    const int bps = v.bits_per_symbol;
+    const int abits = bps >> 1;
+    const int levels = 1 << abits;
+    float* out = llr + static_cast<long long>(f) * llr_stride;
+    for (int d = ds0; d < ds1; ++d) {
+        load_symbol(v, x, cfo_norm, v.data_symbols[d], buf0);
+        const float2* Y = fft_stockham(buf0, buf1, v.nfft, v.twiddle);
+        const int q0 = v.interp_p0[d] - pmin, q1 = v.interp_p1[d] - pmin;
+        const float al = v.interp_alpha[d];
+        const float w0 = __fsub_rn(1.0f, al);
+        for (int sc = threadIdx.x; sc < v.active_sc; sc += blockDim.x) {
+            const float2 y = Y[v.used_bins[sc]];
+            float2 h = make_float2(1.0f, 0.0f);
+            if (v.use_pilot_est) {
+                const float2 h0 = hp[q0 * v.active_sc + sc], h1 = hp[q1 * v.active_sc + sc];
+                h = make_float2(__fadd_rn(__fmul_rn(h0.x, w0), __fmul_rn(h1.x, al)),
+                                __fadd_rn(__fmul_rn(h0.y, w0), __fmul_rn(h1.y, al)));
+            }
+            const float h2 = fmaxf(cnorm(h), 1e-9f);
+            const float2 t = cmulconj(y, h);
+            const float den = __fadd_rn(h2, v.noise_var);
+            const float ex = __fdiv_rn(t.x, den), ey = __fdiv_rn(t.y, den);
+            const float sig = fmaxf(__fdiv_rn(v.noise_var, h2), 1e-8f);
+            float* o = out + (static_cast<long long>(d) * v.active_sc + sc) * bps;
+            if (bps == 1) {
+                const float dy = __fmul_rn(ey, ey);
+                const float d0 = __fadd_rn(sq_dist(ex, 1.0f), dy), d1 = __fadd_rn(sq_dist(ex, -1.0f), dy);
+                o[0] = __fdiv_rn(__fsub_rn(d1, d0), sig);
+                continue;
+            }
+            // per-axis squared distances and minima
+            float mi_all = FLT_MAX, mq_all = FLT_MAX;
+            float mi0[3], mi1[3], mq0[3], mq1[3];
+#pragma unroll
+            for (int b = 0; b < 3; ++b) { mi0[b] = mi1[b] = mq0[b] = mq1[b] = INFINITY; }
+            for (int g = 0; g < levels; ++g) {
+                const float lv = v.axis_levels[g];
+                const float di = sq_dist(ex, lv), dq = sq_dist(ey, lv);
+                mi_all = fminf(mi_all, di);
+                mq_all = fminf(mq_all, dq);
+#pragma unroll
+                for (int b = 0; b < 3; ++b) {
+                    if (b < abits) {
+                        const int bit = (g >> (abits - 1 - b)) & 1;
+                        if (bit) { mi1[b] = fminf(mi1[b], di); mq1[b] = fminf(mq1[b], dq); }
+                        else { mi0[b] = fminf(mi0[b], di); mq0[b] = fminf(mq0[b], dq); }
+                    }
+                }
+            }
+            float vals[6];
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                if (b < abits) {
+                    vals[b] = __fdiv_rn(__fsub_rn(__fadd_rn(mi1[b], mq_all), __fadd_rn(mi0[b], mq_all)), sig);
+                    vals[abits + b] = __fdiv_rn(__fsub_rn(__fadd_rn(mi_all, mq1[b]), __fadd_rn(mi_all, mq0[b])), sig);
+                }
+            }
+            if (bps == 4) {
+                *reinterpret_cast<float4*>(o) = make_float4(vals[0], vals[1], vals[2], vals[3]);
+            } else if (bps == 2) {
+                *reinterpret_cast<float2*>(o) = make_float2(vals[0], vals[1]);
+            } else {
+                for (int b = 0; b < bps; ++b) o[b] = vals[b];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+void launch_demod(const DemodView& v, const float2* samples, long long stride, const SyncOut* sync, int frames,
+                  float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta)
+{
+    if (frames <= 0 || v.num_data <= 0) return;
+    if (v.nfft < 4 || (v.nfft & (v.nfft - 1))) throw InvalidArgument("nfft must be a power of two >= 4");
+    if (v.bits_per_symbol != 1 && v.bits_per_symbol != 2 && v.bits_per_symbol != 4 && v.bits_per_symbol != 6)
+        throw InvalidArgument("bits_per_symbol must be 1, 2, 4 or 6");
+    int spc = symbols_per_cta;
+    if (spc <= 0) {
+        const int groups = (v.num_data + 3) / 4;
+        spc = (v.num_data + groups - 1) / groups;
+    }
+    const size_t smem = (2 * static_cast<size_t>(v.nfft) + kMaxPilotsPerCta * static_cast<size_t>(v.active_sc)) *
+                        sizeof(float2);
+    check_cuda(cudaFuncSetAttribute(demod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+               "cudaFuncSetAttribute(demod)");
+    const dim3 grid(frames, (v.num_data + spc - 1) / spc);
+    demod_kernel<<<grid, kDemodThreads, smem, st>>>(v, samples, stride, sync, llr, llr_stride, spc);
+    check_cuda(cudaGetLastError(), "demod_kernel launch");
+}
+
+}  // namespace sicc

@@ -1,0 +1,62 @@
+// OFDM receive kernels: Schmidl-Cox timing/CFO sync and the fused demodulator.
+#pragma once
+
+#include "sicc_common.h"
+
+namespace sicc {
+
+// Result of one frame search; mirrors the reference's DeviceSyncResult
+// (gpu_ofdm_pipeline.cu:398-404) plus the fields of the CPU SyncResult
+// (uhd_ldpc_ofdm_link.cpp:350-357).
+struct SyncOut {
+    int found;       // 1 found, 2 incomplete frame, 0 not found
+    int start;       // refined start sample (0-based)
+    float coarse;    // Schmidl-Cox metric at the coarse candidate
+    float fine;      // full-preamble correlation metric at the refined start
+    float cfo_hz;
+    int coarse_start;
+};
+
+struct SyncParams {
+    int half_len;         // L
+    int pre_len;          // 2L
+    int radius;           // refinement radius (samples)
+    float threshold;
+    float sample_rate;
+    int mode;             // 0: earliest crossing (find_frame_vector_earliest), 1: global maximum (find_frame)
+    int max_search;       // > 0 limits the candidates to [0, max_search]
+    int frame_len;        // > 0: report "incomplete" when the refined frame runs past the buffer
+    float pre_energy;     // sum |preamble|^2
+};
+
+// One CTA per frame.  samples: frame f starts at samples + f*stride and holds
+// counts[f] (or `count` when counts is null) samples.
+void launch_sync(const float2* samples, long long stride, const int* counts, int count, int frames,
+                 const float2* preamble, const SyncParams& p, SyncOut* out, cudaStream_t st);
+
+// Static demodulation tables resident on the device.
+struct DemodView {
+    int nfft, cp, num_symbols, active_sc, bits_per_symbol, pre_len;
+    int num_pilots, num_data;
+    float sample_rate;
+    float noise_var;
+    int use_pilot_est;
+    const int* used_bins;      // [active_sc] natural FFT bin of each active subcarrier
+    const int* pilot_symbols;  // [num_pilots]
+    const int* data_symbols;   // [num_data]
+    const int* interp_p0;      // [num_data]
+    const int* interp_p1;      // [num_data]
+    const float* interp_alpha; // [num_data]
+    const float2* pilot_grid;  // [num_pilots][active_sc]
+    const float2* twiddle;     // [nfft]: exp(-2 pi i j / nfft)
+    const float* axis_levels;  // [2^(bps/2)] constellation amplitude by Gray axis index (bps >= 2)
+};
+
+// Fused demodulator: CFO derotation + CP strip + FFT + LS pilot estimate +
+// interpolation + MMSE equalisation + max-log LLR.  Frame f's samples start at
+// samples + f*stride + sync[f].start (sync may be null: start 0, cfo 0 unless
+// `cfo_override` is used); LLRs go to llr + f*llr_stride.
+void launch_demod(const DemodView& v, const float2* samples, long long stride, const SyncOut* sync, int frames,
+                  float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta = 0);
+
+}  // namespace sicc

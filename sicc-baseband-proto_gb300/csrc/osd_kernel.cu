@@ -1,0 +1,324 @@
+// Ordered-statistics decoding (OSD) for sm_103a: one warp per codeword.
+//
+// Restates cpu_bp_osd_decode.m:187-305 (the reference's MATLAB BP-OSD):
+//   1. stable descending sort of |llr| (ties: lower index first);
+//   2. systematic form of the column-permuted generator G = [I_k | P]: the
+//      pivots are the first k linearly independent positions in reliability
+//      order (the most reliable basis), found by a column scan over a
+//      bit-packed row-reduced copy of G held in registers (64-bit XOR rows);
+//   3. base candidate = hard decisions on the basis; flip candidates over the
+//      weakest basis positions in the enumeration order of MATLAB nchoosek;
+//   4. metric = sum of |llr| over positions where the candidate differs from
+//      the hard decision, accumulated in decreasing-reliability order in
+//      single precision; the first candidate with the smallest metric wins
+//      (strict <, cpu_bp_osd_decode.m:222), realised as a minimum over
+//      (metric bits, test index) keys.
+// Candidates are evaluated by all 32 lanes in parallel; each candidate's
+// difference vector is the base difference XOR at most three reduced rows.
+#include "bp_kernels.h"
+
+#include <algorithm>
+
+namespace sicc {
+
+namespace {
+
+constexpr int kOsdWarps = 8;
+
+template <int NW, int KR>
+struct OsdSmem {
+    uint32_t relbits[NW * 64];
+    float rel_sorted[NW * 64];
+    int16_t perm[NW * 64];
+    int16_t rowpiv[KR * 32];  // row id -> pivot index
+    int16_t flip[KR * 32];    // weakness rank -> pivot index
+    uint32_t hard_orig[NW * 2];
+    unsigned long long rows[KR * 32][NW];  // reduced rows by pivot index
+    int16_t mrb_pos[KR * 32];
+};
+
+__device__ __forceinline__ unsigned long long shfl_u64(unsigned long long v, int src)
+{
+    const unsigned lo = __shfl_sync(0xffffffffu, static_cast<unsigned>(v), src);
+    const unsigned hi = __shfl_sync(0xffffffffu, static_cast<unsigned>(v >> 32), src);
+    return (static_cast<unsigned long long>(hi) << 32) | lo;
+}
+
+__device__ __forceinline__ unsigned long long shfl_xor_u64(unsigned long long v, int m)
+{
+    const unsigned lo = __shfl_xor_sync(0xffffffffu, static_cast<unsigned>(v), m);
+    const unsigned hi = __shfl_xor_sync(0xffffffffu, static_cast<unsigned>(v >> 32), m);
+    return (static_cast<unsigned long long>(hi) << 32) | lo;
+}
+
+}  // namespace
+
+template <int NW, int KR>
+__global__ void __launch_bounds__(kOsdWarps * 32)
+osd_kernel(OsdView ov, OsdIO io)
+{
+    constexpr int KW = (KR + 1) / 2;
+    __shared__ OsdSmem<NW, KR> sm_all[kOsdWarps];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    OsdSmem<NW, KR>& s = sm_all[warp];
+    const int n = ov.n, k = ov.k;
+    const int count = io.count_ptr ? *io.count_ptr : io.count;
+    const int total_warps = gridDim.x * kOsdWarps;
+
+    for (int item = blockIdx.x * kOsdWarps + warp; item < count; item += total_warps) {
+        const int cw = io.index ? io.index[item] : item;
+        const float* src = io.llr + static_cast<size_t>(item) * n;
+        // ---- 1. reliabilities, hard decisions, stable descending rank ----
+        for (int i = lane; i < NW * 64; i += 32) {
+            const float x = (i < n) ? src[i] : 0.0f;
+            s.relbits[i] = (i < n) ? __float_as_uint(fabsf(x)) : 0u;
+            const unsigned hb = __ballot_sync(0xffffffffu, (i < n) && (x < 0.0f));
+            if (lane == 0) s.hard_orig[i >> 5] = hb;
+        }
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) {
+            const uint32_t bi = s.relbits[i];
+            int r = 0;
+            for (int j = 0; j < n; ++j) {
+                const uint32_t bj = s.relbits[j];
+                r += (bj > bi) || (bj == bi && j < i);
+            }
+            s.perm[r] = static_cast<int16_t>(i);
+            s.rel_sorted[r] = __uint_as_float(bi);
+        }
+        __syncwarp();
+        // hard decisions in sorted order
+        unsigned long long hard_sorted[NW];
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            unsigned lo, hi;
+            {
+                const int j = w * 64 + lane;
+                const int o = (j < n) ? s.perm[j] : 0;
+                lo = __ballot_sync(0xffffffffu, (j < n) && ((s.hard_orig[o >> 5] >> (o & 31)) & 1u));
+            }
+            {
+                const int j = w * 64 + 32 + lane;
+                const int o = (j < n) ? s.perm[j] : 0;
+                hi = __ballot_sync(0xffffffffu, (j < n) && ((s.hard_orig[o >> 5] >> (o & 31)) & 1u));
+            }
+            hard_sorted[w] = (static_cast<unsigned long long>(hi) << 32) | lo;
+        }
+        // ---- 2. permuted generator rows via ballots over column vectors ----
+        unsigned long long rows[KR][NW];
+#pragma unroll
+        for (int a = 0; a < KR; ++a)
+#pragma unroll
+            for (int w = 0; w < NW; ++w) rows[a][w] = 0ull;
+#pragma unroll
+        for (int q = 0; q < NW * 2; ++q) {
+            const int j = q * 32 + lane;
+            unsigned long long col[KW];
+#pragma unroll
+            for (int x = 0; x < KW; ++x) col[x] = 0ull;
+            if (j < n) {
+                const int o = s.perm[j];
+                if (o < k) {
+                    col[o >> 6] = 1ull << (o & 63);
+                } else {
+#pragma unroll
+                    for (int x = 0; x < KW; ++x) col[x] = ov.pcols[static_cast<size_t>(o - k) * ov.kw + x];
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < KR; ++a) {
+                for (int rl = 0; rl < 32; ++rl) {
+                    const int r = a * 32 + rl;
+                    const unsigned b = __ballot_sync(0xffffffffu, (r < k) && ((col[r >> 6] >> (r & 63)) & 1ull));
+                    if (lane == rl)
+                        rows[a][q >> 1] |= static_cast<unsigned long long>(b) << ((q & 1) * 32);
+                }
+            }
+        }
+        // ---- 3. column-scan elimination: pivots = most reliable basis ----
+        unsigned pivoted = 0;  // bit a: my row in slot a is a pivot row
+        int rank = 0;
+        for (int j = 0; j < n && rank < k; ++j) {
+            const int wj = j >> 6;
+            const unsigned long long bj = 1ull << (j & 63);
+            int ps = -1, pl = 0;
+#pragma unroll
+            for (int a = 0; a < KR; ++a) {
+                const int r = a * 32 + lane;
+                const bool cand = (r < k) && !((pivoted >> a) & 1u) && (rows[a][wj] & bj);
+                const unsigned bal = __ballot_sync(0xffffffffu, cand);
+                if (ps < 0 && bal) {
+                    ps = a;
+                    pl = __ffs(bal) - 1;
+                }
+            }
+            if (ps < 0) continue;  // dependent position
+            unsigned long long pw[NW];
+#pragma unroll
+            for (int w = 0; w < NW; ++w) {
+                unsigned long long mine = 0ull;
+#pragma unroll
+                for (int a = 0; a < KR; ++a)
+                    if (a == ps) mine = rows[a][w];
+                pw[w] = shfl_u64(mine, pl);
+            }
+#pragma unroll
+            for (int a = 0; a < KR; ++a) {
+                const bool is_p = (a == ps) && (lane == pl);
+                if (!is_p && (rows[a][wj] & bj)) {
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) rows[a][w] ^= pw[w];
+                }
+                if (is_p) pivoted |= 1u << a;
+            }
+            if (lane == 0) {
+                s.rowpiv[ps * 32 + pl] = static_cast<int16_t>(rank);
+                s.mrb_pos[rank] = static_cast<int16_t>(j);
+            }
+            ++rank;
+        }
+        __syncwarp();
+        if (rank < k) {  // generator not full rank: cannot happen for a valid code table
+            if (lane == 0 && io.out_metric) io.out_metric[cw] = -1.0f;
+            continue;
+        }
+        // ---- 4. reduced rows by pivot index; base difference vector ----
+        unsigned long long acc[NW];
+#pragma unroll
+        for (int w = 0; w < NW; ++w) acc[w] = 0ull;
+#pragma unroll
+        for (int a = 0; a < KR; ++a) {
+            const int r = a * 32 + lane;
+            if (r < k) {
+                const int t = s.rowpiv[r];
+#pragma unroll
+                for (int w = 0; w < NW; ++w) s.rows[t][w] = rows[a][w];
+                const int pj = s.mrb_pos[t];
+                if ((hard_sorted[pj >> 6] >> (pj & 63)) & 1ull) {
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) acc[w] ^= rows[a][w];
+                }
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc[w] ^= shfl_xor_u64(acc[w], o);
+            acc[w] ^= hard_sorted[w];  // base difference from the hard decision
+        }
+        // ---- 5. flip pool: basis positions, weakest first (stable) ----
+        for (int t = lane; t < k; t += 32) {
+            const uint32_t bt = __float_as_uint(s.rel_sorted[s.mrb_pos[t]]);
+            int r = 0;
+            for (int u = 0; u < k; ++u) {
+                const uint32_t bu = __float_as_uint(s.rel_sorted[s.mrb_pos[u]]);
+                r += (bu < bt) || (bu == bt && u < t);
+            }
+            if (r < ov.pool) s.flip[r] = static_cast<int16_t>(t);
+        }
+        __syncwarp();
+        // ---- 6. all candidates in parallel ----
+        unsigned long long best_key = ~0ull;
+        for (int q = lane; q < ov.num_tests; q += 32) {
+            unsigned long long d[NW];
+#pragma unroll
+            for (int w = 0; w < NW; ++w) d[w] = acc[w];
+            if (q > 0) {
+                const uint32_t cmb = ov.combos[q - 1];
+#pragma unroll
+                for (int f = 0; f < 3; ++f) {
+                    const uint32_t fi = (cmb >> (10 * f)) & 0x3FFu;
+                    if (fi != 0x3FFu) {
+                        const int t = s.flip[fi];
+#pragma unroll
+                        for (int w = 0; w < NW; ++w) d[w] ^= s.rows[t][w];
+                    }
+                }
+            }
+            float metric = 0.0f;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) {
+                unsigned long long bits = d[w];
+                while (bits) {
+                    const int b = __ffsll(static_cast<long long>(bits)) - 1;
+                    metric = __fadd_rn(metric, s.rel_sorted[w * 64 + b]);
+                    bits &= bits - 1;
+                }
+            }
+            const unsigned long long key = (static_cast<unsigned long long>(__float_as_uint(metric)) << 32) |
+                                           static_cast<unsigned>(q);
+            best_key = key < best_key ? key : best_key;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long other = shfl_xor_u64(best_key, o);
+            best_key = other < best_key ? other : best_key;
+        }
+        // ---- 7. winner -> original positions ----
+        const int qbest = static_cast<int>(best_key & 0xffffffffull);
+        unsigned long long d[NW];
+#pragma unroll
+        for (int w = 0; w < NW; ++w) d[w] = acc[w];
+        if (qbest > 0) {
+            const uint32_t cmb = ov.combos[qbest - 1];
+#pragma unroll
+            for (int f = 0; f < 3; ++f) {
+                const uint32_t fi = (cmb >> (10 * f)) & 0x3FFu;
+                if (fi != 0x3FFu) {
+                    const int t = s.flip[fi];
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) d[w] ^= s.rows[t][w];
+                }
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < NW; ++w) d[w] ^= hard_sorted[w];  // decoded codeword in sorted order
+        for (int j = lane; j < n; j += 32) {
+            const int o = s.perm[j];
+            const uint8_t bit = static_cast<uint8_t>((d[j >> 6] >> (j & 63)) & 1ull);
+            if (io.out_info && o < k) io.out_info[static_cast<size_t>(cw) * io.info_stride + o] = bit;
+            if (io.out_code) io.out_code[static_cast<size_t>(cw) * n + o] = bit;
+        }
+        if (lane == 0) {
+            if (io.out_metric) io.out_metric[cw] = __uint_as_float(static_cast<unsigned>(best_key >> 32));
+            if (io.used_osd) io.used_osd[cw] = 1;
+        }
+        __syncwarp();
+    }
+}
+
+template <int NW, int KR>
+static void launch_osd_t(const OsdView& ov, const OsdIO& io, int max_items, cudaStream_t st, int ctas)
+{
+    if (ctas <= 0) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, osd_kernel<NW, KR>, kOsdWarps * 32, 0) !=
+                cudaSuccess ||
+            per_sm <= 0)
+            per_sm = 1;
+        ctas = per_sm * device_sm_count();
+        ctas = std::max(1, std::min(ctas, (max_items + kOsdWarps - 1) / kOsdWarps));
+    }
+    osd_kernel<NW, KR><<<ctas, kOsdWarps * 32, 0, st>>>(ov, io);
+    check_cuda(cudaGetLastError(), "osd_kernel launch");
+}
+
+void launch_osd(const OsdView& ov, const OsdIO& io, int max_items, cudaStream_t st, int warps_per_cta, int ctas)
+{
+    (void)warps_per_cta;
+    if (max_items <= 0) return;
+    const int nw = (ov.n + 63) / 64;
+    const int kr = (ov.k + 31) / 32;
+    const int NW = nw <= 1 ? 1 : (nw <= 2 ? 2 : 4);
+    const int KR = kr <= 1 ? 1 : (kr <= 2 ? 2 : 4);
+    if (nw > 4 || kr > 4) throw InvalidArgument("OSD kernel supports n <= 256 and k <= 128");
+#define SICC_OSD_CASE(A, B) \
+    if (NW == A && KR == B) { launch_osd_t<A, B>(ov, io, max_items, st, ctas); return; }
+    SICC_OSD_CASE(1, 1) SICC_OSD_CASE(1, 2) SICC_OSD_CASE(2, 1) SICC_OSD_CASE(2, 2)
+    SICC_OSD_CASE(2, 4) SICC_OSD_CASE(4, 2) SICC_OSD_CASE(4, 4) SICC_OSD_CASE(4, 1) SICC_OSD_CASE(1, 4)
+#undef SICC_OSD_CASE
+    throw InvalidArgument("unsupported OSD shape");
+}
+
+}  // namespace sicc

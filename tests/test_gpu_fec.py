@@ -1,0 +1,276 @@
+"""GPU parity of the LDPC decoders against the oracle and the reference fixtures.
+
+Bar: bit-exact for hard decisions, iteration counts, success flags, OSD
+codewords and metrics; posterior LLRs bit-exact against the single-precision
+oracle of the same schedule and within 1e-4 (relative to the largest
+posterior magnitude of the codeword) of the double-precision oracle.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from sicc_gb300 import channel, codes
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+pytestmark = pytest.mark.gpu
+
+
+def _dev(torch, a, dtype=None):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _run_csr(torch, dec, llr, n):
+    B = llr.shape[0]
+    d_llr = _dev(torch, llr)
+    d_bits = torch.zeros((B, n), dtype=torch.uint8, device="cuda")
+    d_ok = torch.zeros(B, dtype=torch.uint8, device="cuda")
+    d_app = torch.zeros((B, n), dtype=torch.float32, device="cuda")
+    d_it = torch.zeros(B, dtype=torch.uint8, device="cuda")
+    dec.decode_device_batch(d_llr, d_bits, d_ok, d_app, d_it, stream=torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    return d_bits.cpu().numpy(), d_ok.cpu().numpy(), d_app.cpu().numpy(), d_it.cpu().numpy()
+
+
+def _llr_sweep(code, per_point=256, points=(1.0, 2.0, 3.0, 4.0), seed=100):
+    out = [channel.awgn_llrs(code, per_point, e, seed + i)[2] for i, e in enumerate(points)]
+    return np.concatenate(out)
+
+
+@pytest.mark.parametrize("alpha,beta,iters", [(0.75, 0.0, 20), (0.8, 0.15, 8)])
+def test_layered_bp_matches_oracle_bit_exact(cuda, oracle, alpha, beta, iters):
+    from sicc_gb300 import fec
+    torch = cuda
+    code = codes.short_code()
+    oc = oracle.code(code.n, code.m, code.row_ptr, code.col_ind)
+    llr = _llr_sweep(code)
+    dec = fec.CsrBpDecoder.for_code(code, max_batch=llr.shape[0], max_iter=iters, normalization=alpha,
+                                    offset=beta, schedule=fec.FLAT_LAYERED)
+    bits, ok, app, it = _run_csr(torch, dec, llr, code.n)
+    for i, x in enumerate(llr):
+        o_ok, o_bits, o_app, _, o_it, _ = oc.layered(x, iters, alpha, beta)
+        assert ok[i] == o_ok and it[i] == o_it, i
+        assert np.array_equal(bits[i], o_bits), i
+        assert np.array_equal(app[i].view(np.uint32), o_app.view(np.uint32)), i
+
+
+def test_layered_posteriors_within_1e4_of_fp64(cuda, oracle):
+    from sicc_gb300 import fec
+    torch = cuda
+    code = codes.short_code()
+    oc = oracle.code(code.n, code.m, code.row_ptr, code.col_ind)
+    llr = _llr_sweep(code, per_point=128, seed=300)
+    dec = fec.CsrBpDecoder.for_code(code, max_batch=llr.shape[0], max_iter=20, normalization=0.75)
+    bits, ok, app, it = _run_csr(torch, dec, llr, code.n)
+    same_hard = 0
+    for i, x in enumerate(llr):
+        ok64, bits64, app64, it64 = oc.layered_f64(x, 20, 0.75)
+        if np.array_equal(bits[i], bits64):
+            same_hard += 1
+        if it[i] == it64 and np.array_equal(bits[i], bits64):
+            err = np.max(np.abs(app[i] - app64)) / max(np.max(np.abs(app64)), 1.0)
+            assert err <= 1e-4, (i, err)
+    assert same_hard / len(llr) >= 0.9999 or len(llr) - same_hard <= 0
+
+
+@pytest.mark.parametrize("iters,norm,key", [(20, 0.75, "flood"), (8, 0.80, "flood8")])
+def test_flooding_bp_matches_reference_fixture(cuda, oracle, iters, norm, key):
+    from sicc_gb300 import fec
+    torch = cuda
+    g = dict(np.load(os.path.join(GOLDEN, "fec_short_code.npz")))
+    code = codes.short_code()
+    dec = fec.CsrBpDecoder.for_code(code, max_batch=512, max_iter=iters, normalization=norm, schedule=fec.FLOODING)
+    bits, ok, app, it = _run_csr(torch, dec, g["llr"], code.n)
+    assert np.array_equal(bits, g[key + "_bits"])
+    assert np.array_equal(ok, g[key + "_ok"])
+    assert np.array_equal(it.astype(np.int32), g[key + "_iter"])
+    oc = oracle.code(code.n, code.m, code.row_ptr, code.col_ind)
+    for i in range(0, len(g["llr"]), 7):
+        o = oc.flooding_ref(g["llr"][i], iters, norm)
+        assert np.array_equal(app[i].view(np.uint32), o[2].view(np.uint32))
+
+
+def test_flooding_damping_matches_oracle(cuda, oracle):
+    from sicc_gb300 import fec
+    torch = cuda
+    code = codes.short_code()
+    oc = oracle.code(code.n, code.m, code.row_ptr, code.col_ind)
+    llr = _llr_sweep(code, per_point=64, seed=500)
+    dec = fec.CsrBpDecoder.for_code(code, max_batch=llr.shape[0], max_iter=20, normalization=0.8, offset=0.15,
+                                    damping=0.15, schedule=fec.FLOODING)
+    bits, ok, app, it = _run_csr(torch, dec, llr, code.n)
+    for i, x in enumerate(llr):
+        o = oc.flooding(x, 20, 0.8, 0.15, 0.15)
+        assert ok[i] == o[0] and it[i] == o[4] and np.array_equal(bits[i], o[1])
+        assert np.array_equal(app[i].view(np.uint32), o[2].view(np.uint32))
+
+
+def test_colored_layered_schedule_matches_oracle(cuda, oracle):
+    from sicc_gb300 import fec
+    torch = cuda
+    code = codes.qc_code(4, 8, 16, 7)
+    oc = oracle.code(code.n, code.m, code.row_ptr, code.col_ind)
+    order, _, _ = oc.color_order()
+    llr = _llr_sweep(code, per_point=32, seed=700)
+    dec = fec.CsrBpDecoder.for_code(code, max_batch=llr.shape[0], max_iter=20, normalization=0.75,
+                                    schedule=fec.COLORED_LAYERED)
+    bits, ok, app, it = _run_csr(torch, dec, llr, code.n)
+    for i, x in enumerate(llr):
+        o = oc.layered(x, 20, 0.75, row_order=order)
+        assert ok[i] == o[0] and it[i] == o[4] and np.array_equal(app[i].view(np.uint32), o[2].view(np.uint32))
+
+
+def _osd_expect(oracle, table, code, llr, order=2, max_flip=64, max_tests=4096):
+    return oracle.osd(table, code.n, code.k, llr, order, max_flip, max_tests)
+
+
+def test_osd_kernel_bit_exact(cuda, oracle):
+    from sicc_gb300 import fec
+    torch = cuda
+    code = codes.short_code()
+    oc = oracle.code(code.n, code.m, code.row_ptr, code.col_ind)
+    table = oc.systematic_parity()
+    dec = fec.StreamBpOsdDecoder(code, max_batch=512, max_iter=20, normalization=0.75, offset=0.0, damping=0.0,
+                                 min_abs_llr_accept=0.0, osd_order=2, osd_max_flip=64, osd_max_tests=4096)
+    rows = [_llr_sweep(code, per_point=48, seed=900)]
+    # BP posteriors of failing frames, the OSD input of the stream decoder
+    post = []
+    for x in _llr_sweep(code, per_point=64, points=(1.5, 2.0), seed=950):
+        r = oc.layered(x, 20, 0.75)
+        if not r[0]:
+            post.append(r[3])
+    rows.append(np.array(post, np.float32))
+    llr = np.concatenate(rows).astype(np.float32)
+    d_llr = _dev(torch, llr)
+    d_info = torch.zeros((len(llr), code.k), dtype=torch.uint8, device="cuda")
+    d_code = torch.zeros((len(llr), code.n), dtype=torch.uint8, device="cuda")
+    d_dist = torch.zeros(len(llr), dtype=torch.float32, device="cuda")
+    from sicc_gb300 import _lib
+    _lib.check(_lib.load().sicc_osd_decode_device(dec.handle, d_llr.data_ptr(), len(llr), d_info.data_ptr(),
+                                                  d_code.data_ptr(), d_dist.data_ptr(), None), "osd")
+    torch.cuda.synchronize()
+    cw, dist = d_code.cpu().numpy(), d_dist.cpu().numpy()
+    for i, x in enumerate(llr):
+        out, metric, _, _ = _osd_expect(oracle, table, code, x)
+        assert np.array_equal(cw[i], out), i
+        assert np.float32(metric).view(np.uint32) == dist[i].view(np.uint32), i
+        assert oc.syndrome_weight(cw[i]) == 0
+
+
+def _oracle_bp_osd(oracle, oc, table, code, x, alpha=0.75, iters=20):
+    ok, bits, app, best, it, bw = oc.layered(x, iters, alpha)
+    if ok:
+        return bits[: code.k], False
+    out, _, _, _ = oracle.osd(table, code.n, code.k, best)
+    return out[: code.k], True
+
+
+@pytest.mark.parametrize("count", [1, 37, 600])
+def test_stream_decoder_api_matches_oracle(cuda, oracle, count):
+    from sicc_gb300 import fec
+    code = codes.short_code()
+    oc = oracle.code(code.n, code.m, code.row_ptr, code.col_ind)
+    table = oc.systematic_parity()
+    info_true, _, llr = channel.awgn_llrs(code, count, 2.0, seed=count)
+    dec = fec.StreamBpOsdDecoder(code, max_batch=256, min_batch=64, max_iter=20, normalization=0.75, offset=0.0,
+                                 damping=0.0, min_abs_llr_accept=0.0)
+    info, used = dec.decode(llr)
+    n_osd = 0
+    for i, x in enumerate(llr):
+        exp, osd = _oracle_bp_osd(oracle, oc, table, code, x)
+        n_osd += osd
+        assert np.array_equal(info[i], exp), i
+    assert used == n_osd
+    st = dec.stats()
+    assert st["decoded_codewords"] == count and st["submitted_codewords"] == count
+
+
+def test_stream_decoder_device_submit_and_async_window(cuda, oracle):
+    from sicc_gb300 import fec
+    torch = cuda
+    code = codes.short_code()
+    oc = oracle.code(code.n, code.m, code.row_ptr, code.col_ind)
+    table = oc.systematic_parity()
+    dec = fec.StreamBpOsdDecoder(code, max_batch=64, min_batch=48, max_iter=20, normalization=0.75, offset=0.0,
+                                 damping=0.0, min_abs_llr_accept=0.0)
+    frames = [channel.awgn_llrs(code, 20, 2.5, seed=40 + f)[2] for f in range(5)]
+    for f, x in enumerate(frames):
+        dec.submit(_dev(torch, x), np.full(20, f), np.arange(20), device=True)
+    dec.flush()
+    got = {}
+    while len(got) < 100:
+        info, ts, ids, blk, used = dec.poll(100)
+        assert len(info) > 0
+        for r in range(len(info)):
+            got[(int(ids[r]), int(blk[r]))] = info[r]
+    for f, x in enumerate(frames):
+        for b in range(20):
+            exp, _ = _oracle_bp_osd(oracle, oc, table, code, x[b])
+            assert np.array_equal(got[(f, b)], exp)
+
+
+def test_device_batch_entry_matches_stream_api(cuda, oracle):
+    from sicc_gb300 import fec
+    torch = cuda
+    code = codes.short_code()
+    oc = oracle.code(code.n, code.m, code.row_ptr, code.col_ind)
+    table = oc.systematic_parity()
+    _, _, llr = channel.awgn_llrs(code, 3000, 2.0, seed=77)
+    dec = fec.StreamBpOsdDecoder(code, max_batch=4096, max_iter=20, normalization=0.75, offset=0.0, damping=0.0,
+                                 min_abs_llr_accept=0.0)
+    d_info = torch.zeros((3000, code.k), dtype=torch.uint8, device="cuda")
+    d_used = torch.zeros(3000, dtype=torch.uint8, device="cuda")
+    d_ok = torch.zeros(3000, dtype=torch.uint8, device="cuda")
+    dec.decode_device_batch(_dev(torch, llr), d_info, d_ok, d_used, stream=torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    info = d_info.cpu().numpy()
+    used = d_used.cpu().numpy()
+    for i in range(0, 3000, 3):
+        exp, osd = _oracle_bp_osd(oracle, oc, table, code, llr[i])
+        assert np.array_equal(info[i], exp) and bool(used[i]) == osd, i
+
+
+def test_default_ccsds_code_and_osd_only_decoder(cuda, oracle):
+    from sicc_gb300 import fec
+    g = dict(np.load(os.path.join(GOLDEN, "fec_short_code.npz")))
+    oc = oracle.code(128, 64, g["ccsds_row_ptr"], g["ccsds_col_ind"])
+    table = oc.systematic_parity()
+    rng = np.random.default_rng(3)
+    sigma2 = channel.sigma2_for(0.5, 3.0)
+    llr = ((2 / sigma2) * (1 + np.sqrt(sigma2) * rng.standard_normal((300, 128)))).astype(np.float32)  # all-zero cw
+    dec = fec.StreamBpOsdDecoder(None, max_batch=512)
+    info, used = dec.decode(llr)
+    assert info.shape == (300, 64)
+    assert (info.sum(axis=1) != 0).mean() < 0.2  # all-zero codeword known answer (BO:467-476)
+    osd = fec.OsdOnlyDecoder(max_batch=128)
+    oinfo, dist, ms, mbps = osd.decode(llr)
+    for i in range(300):
+        out, metric, _, _ = oracle.osd(table, 128, 64, llr[i], 2, 64, 4096)
+        assert np.array_equal(oinfo[i], out[:64])
+        assert np.float32(metric) == dist[i]
+
+
+def test_find_frame_entry_point(cuda, oracle):
+    from sicc_gb300 import fec, ofdm
+    d = dict(np.load(os.path.join(GOLDEN, "ofdm_small.npz")))
+    t = ofdm.reference_tables(ofdm.OFDM_SMALL)
+    for i in range(d["iq"].shape[0]):
+        x = d["iq"][i]
+        start, peak, cfo = fec.find_frame(x.astype(np.complex128), t.preamble.astype(np.complex128),
+                                          t.cfg.pre_half_len, t.cfg.sync_threshold, t.cfg.sample_rate)
+        if d["sync"][i][0] == 1 and d["sync"][i][3] > t.cfg.sync_threshold + 0.02:
+            assert abs((start - 1) - int(d["sync"][i][1])) <= 1
+            assert cfo == pytest.approx(d["sync"][i][4], rel=1e-2, abs=20.0)
+
+
+def test_error_paths(cuda):
+    from sicc_gb300 import _lib, fec
+    code = codes.short_code()
+    dec = fec.StreamBpOsdDecoder(code, max_batch=16)
+    torch = cuda
+    d = torch.zeros((32, code.n), dtype=torch.float32, device="cuda")
+    o = torch.zeros((32, code.k), dtype=torch.uint8, device="cuda")
+    with pytest.raises(_lib.SiccError):
+        dec.decode_device_batch(d, o)  # more than max_batch
+    with pytest.raises(_lib.SiccError):
+        dec.set_osd_params(5, 64, 10)
