@@ -38,7 +38,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 EBN0 = (2.0, 3.0)
 BATCH = 65536
-RESIDENT_BATCHES = 4  # per Eb/N0: 8 x 33.5 MB of LLRs resident, > 129 MB of L2
+RESIDENT_BATCHES = 4  # per Eb/N0: 8 x 33.5 MB of LLRs resident, > 129 MB of L2 together
 ITERS, ALPHA = 20, 0.75
 OSD_ORDER, OSD_FLIP, OSD_TESTS = 2, 64, 4096
 WORKLOAD = "bp_osd_128_64"
@@ -238,9 +238,9 @@ def run_ours(args, rank, world):
     alg_bytes = BATCH * bytes_per_cw
     achieved = alg_bytes / (avg_bp_ms * 1e-3) / 1e9
     traffic = None
-    try:
+    try:  # dram bytes per codeword from one ncu capture, scaled to this launch's frames
         with open(TRAFFIC) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+            traffic = round(json.load(f)["dram_bytes_per_codeword"] * BATCH)
     except Exception:
         pass
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
@@ -325,7 +325,11 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch", type=int, default=BATCH, help="frames per batch (profiling runs only)")
+    ap.add_argument("--resident", type=int, default=RESIDENT_BATCHES, help="resident batches per Eb/N0")
     args = ap.parse_args()
+    globals()["BATCH"] = args.batch
+    globals()["RESIDENT_BATCHES"] = args.resident
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus if "RANK" in os.environ else 1))
     if args.impl == "reference":

@@ -266,7 +266,7 @@ def test_find_frame_entry_point(cuda, oracle):
 def test_error_paths(cuda):
     from sicc_gb300 import _lib, fec
     code = codes.short_code()
-    dec = fec.StreamBpOsdDecoder(code, max_batch=16)
+    dec = fec.StreamBpOsdDecoder(code, max_batch=16, min_batch=8)
     torch = cuda
     d = torch.zeros((32, code.n), dtype=torch.float32, device="cuda")
     o = torch.zeros((32, code.k), dtype=torch.uint8, device="cuda")
