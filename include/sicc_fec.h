@@ -200,6 +200,26 @@ SICC_API int sicc_fec_set_timing(unsigned long long handle, int enabled);
 SICC_API int sicc_fec_get_kernel_ms(unsigned long long handle, int* out_calls, float* out_bp_ms, float* out_osd_ms,
                                     long long* out_osd_codewords);
 
+/* Device-resident BP->OSD decode that allocates nothing.  It has no
+ * counterpart in the reference.  It is for callers that cannot allocate
+ * device memory when they decode: a receiver whose memory is fixed once it
+ * starts, or code recorded into a CUDA graph, where cudaMalloc is not
+ * permitted during stream capture.  The BP->OSD hand-off scratch lives in one
+ * static device array of the library (about 8.4 MB on every GPU that loads
+ * it, held until the process exits); batches hold at most
+ * SICC_FEC_STATIC_MAX_CODEWORDS codewords of n <= 256, independent of the
+ * decoder's max_batch_size, and larger batches are rejected with
+ * INVALID_ARGUMENT.  The first call on a device resolves the array's address
+ * there (set-up), so make that first call before any stream capture.  Every
+ * call shares the one array: calls whose work overlaps on the GPU (other
+ * streams, other handles, other threads) race and must be serialised by the
+ * caller.  Outputs match sicc_fec_decode_device bit for bit. */
+#define SICC_FEC_STATIC_MAX_CODEWORDS 8192
+SICC_API int sicc_fec_decode_device_static(unsigned long long handle, const float* device_llrs, int codewords,
+                                           unsigned char* device_info_bits, unsigned char* device_success,
+                                           unsigned char* device_used_osd, unsigned char* device_iterations,
+                                           void* cuda_stream);
+
 /* Launch shape of the persistent BP kernel for a stream or CSR handle (0 = default). */
 SICC_API int sicc_fec_set_launch_shape(unsigned long long handle, int slots_per_cta, int ctas);
 

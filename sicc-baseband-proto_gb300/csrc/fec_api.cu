@@ -594,6 +594,59 @@ void validate_stream_config(const cuda_osd_stream_config_t* c)
 }
 
 }  // namespace
+
+// Decodes with a stream decoder's code tables and settings, but with the
+// BP -> OSD hand-off scratch supplied by the caller (used by the entry point
+// whose scratch is a static device array).  Layout of `scratch`:
+// [0, 256) two int counters; [256, 256 + 4*cap) OSD index list;
+// then cap rows of n floats (256-byte aligned).
+int decode_with_caller_scratch(unsigned long long handle, const float* d_llr, int count, uint8_t* d_info,
+                               uint8_t* d_success, uint8_t* d_used_osd, uint8_t* d_iter,
+                               unsigned char* (*scratch_on_current_device)(), int cap, cudaStream_t st)
+{
+    auto d = lookup<StreamDecoder>(handle, Decoder::kStream);
+    std::lock_guard<std::mutex> lock(d->mu);
+    require(count > 0 && count <= cap, "codewords must be in 1..the static scratch capacity");
+    require(d->n <= 256, "the static scratch holds codes with n <= 256");
+    check_cuda(cudaSetDevice(d->device), "cudaSetDevice");
+    unsigned char* scratch = scratch_on_current_device();
+    int* counters = reinterpret_cast<int*>(scratch);
+    int* index = reinterpret_cast<int*>(scratch + 256);
+    float* rows = reinterpret_cast<float*>(scratch + 256 + ((static_cast<size_t>(cap) * 4 + 255) & ~size_t(255)));
+    BpIO io{};
+    io.llr = d_llr;
+    io.count = count;
+    io.out_bits = d_info;
+    io.out_len = d->k;
+    io.out_stride = d->k;
+    io.success = d_success;
+    io.iterations = d_iter;
+    io.used_osd = d_used_osd;
+    io.work_counter = counters + 1;
+    BpParams p = d->bp;
+    p.route_failures_to_osd = d->osd_enabled ? 1 : 0;
+    // both counters start at zero on every call: the array keeps the previous call's contents
+    check_cuda(cudaMemsetAsync(counters, 0, 2 * sizeof(int), st), "clear static scratch counters");
+    if (d->osd_enabled) {
+        io.osd_llr = rows;
+        io.osd_index = index;
+        io.osd_count = counters;
+    }
+    if (d->code->layered()) launch_bp_layered(d->code->layered_view(), p, io, d->shape, st);
+    else launch_bp_flooding(d->code->flood_view(), p, io, st);
+    if (d->osd_enabled) {
+        OsdIO oio{};
+        oio.llr = rows;
+        oio.index = index;
+        oio.count_ptr = counters;
+        oio.out_info = d_info;
+        oio.info_stride = d->k;
+        oio.used_osd = d_used_osd;
+        launch_osd(d->code->osd_view(), oio, count, st);
+    }
+    return CUDA_OSD_STATUS_OK;
+}
+
 }  // namespace sicc
 
 using namespace sicc;
