@@ -1,0 +1,109 @@
+/*
+ * sicc_pipe.h — C ABI of the GB300 OFDM receive pipeline (libsicc_gb300.so).
+ *
+ * A thin C layer under the C++ class usrp_gpu_pipeline_bridge::Pipeline
+ * (include/gpu_ofdm_pipeline.hpp), which keeps the signatures of the
+ * reference's bridge source/cpp_cuda/uhd_cpp/src/gpu_ofdm_pipeline.hpp:10-93
+ * ("PH").  Each entry point cites the PH member it serves.  Status codes and
+ * cuda_osd_get_last_error() follow include/sicc_fec.h.
+ *
+ * Complex samples are interleaved float32 (re, im), the layout of
+ * std::complex<float> / cuFloatComplex.
+ */
+#ifndef SICC_PIPE_H
+#define SICC_PIPE_H
+
+#include "sicc_fec.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* PH:12-34 (Config), plus two trailing fields the reference fixes internally. */
+typedef struct sicc_pipe_config_t {
+    int nfft;
+    int cp;
+    int preamble_len;
+    int pre_half_len;
+    int num_symbols;
+    int active_sc;
+    int bits_per_symbol;
+    int code_n;
+    int code_k;
+    int blocks_per_frame;
+    int max_rx_search_samples;
+    float sample_rate;
+    float sync_threshold;
+    float tx_amplitude;
+    float demod_noise_var;
+    int use_pilot_channel_est;
+    /* extensions: 0 = defaults */
+    int sync_radius;        /* fine-timing radius; 0 = min(16, cp) as the CPU receiver (L:5223) */
+    int max_batch_frames;   /* frames per batched call (sicc_pipe_demod_batch); 0 = 256 */
+} sicc_pipe_config_t;
+
+/* PH:37-57 (StaticTables), receive-side members. */
+typedef struct sicc_pipe_tables_t {
+    const int* used_indices;   /* [active_sc] shifted-grid subcarrier indices */
+    const int* pilot_symbols;  /* [pilot_count] */
+    int pilot_count;
+    const int* data_symbols;   /* [data_count] */
+    int data_count;
+    const int* interp_p0;      /* [data_count] */
+    const int* interp_p1;      /* [data_count] */
+    const float* interp_alpha; /* [data_count] */
+    const float* pilot_grid;   /* [pilot_count][active_sc] complex */
+    const float* preamble;     /* [preamble_len] complex */
+} sicc_pipe_tables_t;
+
+/* PH:59-63 */
+typedef struct sicc_pipe_sync_t {
+    int start;    /* -1 when no frame was found */
+    float metric;
+    float cfo_hz;
+} sicc_pipe_sync_t;
+
+SICC_API int sicc_pipe_create(const sicc_pipe_config_t* config, int slots, unsigned long long* out_handle); /* PH:67 */
+SICC_API int sicc_pipe_destroy(unsigned long long handle);                                                   /* PH:68 */
+SICC_API int sicc_pipe_upload_static_tables(unsigned long long handle, const sicc_pipe_tables_t* tables);   /* PH:73 */
+/* PH:83-84: frame search on host / device samples; synchronous. */
+SICC_API int sicc_pipe_find_frame(unsigned long long handle, int slot, const float* host_iq, int sample_count,
+                                  sicc_pipe_sync_t* out_sync);
+SICC_API int sicc_pipe_find_frame_device(unsigned long long handle, int slot, const float* device_iq,
+                                         int sample_count, sicc_pipe_sync_t* out_sync);
+/* PH:85: search a host frame of frame_samples() samples, demodulate it; the
+ * returned device LLRs [coded_bits_per_frame] belong to the slot. */
+SICC_API int sicc_pipe_demod_to_device(unsigned long long handle, int slot, const float* host_frame,
+                                       sicc_pipe_sync_t* out_sync, const float** out_device_llr);
+/* PH:86: demodulate a device frame that starts at sample 0 with the given CFO. */
+SICC_API int sicc_pipe_demod_device_to_device(unsigned long long handle, int slot, const float* device_frame,
+                                              const sicc_pipe_sync_t* sync, const float** out_device_llr);
+/* PH:87 */
+SICC_API int sicc_pipe_demod_to_host(unsigned long long handle, int slot, const float* host_frame, float* host_llr,
+                                     sicc_pipe_sync_t* out_sync);
+
+/* Per-frame search result of the batched extension (device memory layout). */
+typedef struct sicc_pipe_sync_record_t {
+    int found;         /* 1 found, 2 frame runs past the buffer, 0 not found */
+    int start;         /* refined start sample */
+    float coarse;      /* Schmidl-Cox metric at the coarse candidate */
+    float fine;        /* full-preamble correlation metric at the start */
+    float cfo_hz;
+    int coarse_start;
+} sicc_pipe_sync_record_t;
+
+/* Extension (no counterpart in the reference): search and demodulate `frames`
+ * device buffers at device_iq + f*stride (stride in complex samples, each
+ * holding sample_count samples) in one pair of launches on `cuda_stream`.
+ * LLRs go to device_llr + f*coded_bits_per_frame; per-frame search results to
+ * device_sync (device memory, may be null).  frames <= max_batch_frames. */
+SICC_API int sicc_pipe_demod_batch(unsigned long long handle, const float* device_iq, long long stride,
+                                   int sample_count, int frames, float* device_llr,
+                                   sicc_pipe_sync_record_t* device_sync, void* cuda_stream);
+/* Kernel durations (ms) of the last sicc_pipe_demod_batch call: sync, demod. */
+SICC_API int sicc_pipe_last_batch_ms(unsigned long long handle, float* out_sync_ms, float* out_demod_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -64,7 +64,7 @@ __device__ __forceinline__ int layered_syndrome(const LayeredView& cv, const int
 }  // namespace
 
 template <int D>
-__global__ void __launch_bounds__(kBpThreads)
+__global__ void __launch_bounds__(kBpThreads, 3)
 bp_layered_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int slot_floats, int track_best)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -367,7 +367,10 @@ size_t layered_smem_bytes(const LayeredView& cv, int slots, bool track_best, int
 {
     const int n_pad = (cv.n + 3) & ~3;
     const int mp = cv.num_layers * cv.width;
-    const int slot_floats = ((track_best ? 2 : 1) * n_pad + 3 * mp + 3) & ~3;
+    int slot_floats = ((track_best ? 2 : 1) * n_pad + 3 * mp + 3) & ~3;
+    // Groups that share a warp sit G banks apart (slot stride = G mod 32 words), so
+    // their simultaneous gathers of the same table column never collide.
+    if (cv.group < 32) slot_floats += ((cv.group - slot_floats % 32) + 32) % 32;
     if (slot_floats_out) *slot_floats_out = slot_floats;
     const int table = (cv.num_layers * cv.maxdeg * cv.width + 3) & ~3;
     return (static_cast<size_t>(table) + static_cast<size_t>(slots) * slot_floats) * sizeof(float);

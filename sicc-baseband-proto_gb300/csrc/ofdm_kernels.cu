@@ -35,6 +35,7 @@ constexpr int kSyncThreads = 256;
 constexpr int kSyncChunk = 17;
 constexpr int kSyncPass = kSyncThreads * kSyncChunk;
 constexpr int kMaxRefine = 1024;  // 2 * radius + 1
+constexpr int kMaxRadius = 511;
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
@@ -67,6 +68,10 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const int* __r
     float2* win = reinterpret_cast<float2*>(smem_raw);                 // [kSyncPass + pre_len]
     float* metric = reinterpret_cast<float*>(win + kSyncPass + p.pre_len);  // [kSyncPass]
     float4* chunk = reinterpret_cast<float4*>(metric + kSyncPass);     // [kSyncThreads] P.re, P.im, E1, E2
+    // fine (full-preamble) metric of every candidate of the pass and its
+    // refinement margins, computed at most once: consecutive threshold
+    // crossings share most of their refinement windows
+    float* memo = reinterpret_cast<float*>(chunk + kSyncThreads);       // [kSyncPass + 2 * kMaxRadius]
     __shared__ float red[4][kSyncThreads / 32];
     __shared__ float rmetric[kMaxRefine];
     __shared__ int s_best;
@@ -90,6 +95,7 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const int* __r
     for (int base = 0; !done && base < limit; base += kSyncPass) {
         const int span = min(kSyncPass + pre, avail - base);
         for (int i = tid; i < kSyncPass + pre; i += kSyncThreads) win[i] = (i < span) ? x[base + i] : make_float2(0.f, 0.f);
+        for (int i = tid; i < kSyncPass + 2 * kMaxRadius; i += kSyncThreads) memo[i] = -1.0f;
         __syncthreads();
         // window sums at chunk starts, one warp per chunk
         for (int t = warp; t < kSyncThreads; t += kSyncThreads / 32) {
@@ -178,7 +184,9 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const int* __r
             const int hi = min(avail - pre, cand + p.radius);
             if (tid == 0) { s_best = cand; s_bestm = 0.0f; }
             __syncthreads();
+            const int mbase = base - kMaxRadius;  // memo index of candidate dd is dd - mbase
             for (int dd = lo + warp; dd <= hi; dd += kSyncThreads / 32) {
+                if (memo[dd - mbase] >= 0.0f) continue;  // already evaluated for an earlier crossing
                 float cr = 0.f, ci = 0.f, eng = 0.f;
                 for (int i = lane; i < pre; i += 32) {
                     const float2 y = x[dd + i], q = preamble[i];
@@ -190,14 +198,14 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const int* __r
                 cr = warp_sum(cr);
                 ci = warp_sum(ci);
                 eng = warp_sum(eng);
-                if (lane == 0) rmetric[dd - lo] = (cr * cr + ci * ci) / fmaxf(eng * p.pre_energy, 1e-18f);
+                if (lane == 0) memo[dd - mbase] = (cr * cr + ci * ci) / fmaxf(eng * p.pre_energy, 1e-18f);
             }
             __syncthreads();
             if (tid == 0) {
                 float bm = 0.0f;
                 int bd = cand;
                 for (int dd = lo; dd <= hi; ++dd) {
-                    const float m = rmetric[dd - lo];
+                    const float m = memo[dd - mbase];
                     if (m > bm) { bm = m; bd = dd; }
                 }
                 s_best = bd;
@@ -265,7 +273,7 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const int* __r
         }
     }
 
-    if (res.found == 1) {
+    if (res.found == 1 || res.found == 2) {  // an incomplete frame also gets its CFO (for one-frame buffers)
         const int s0 = res.start;
         float ar = 0.f, ai = 0.f;
         for (int i = tid; i < L; i += kSyncThreads) {
@@ -295,9 +303,10 @@ void launch_sync(const float2* samples, long long stride, const int* counts, int
 {
     if (frames <= 0) return;
     const size_t smem = static_cast<size_t>(kSyncPass + p.pre_len) * sizeof(float2) +
-                        static_cast<size_t>(kSyncPass) * sizeof(float) + kSyncThreads * sizeof(float4);
+                        static_cast<size_t>(kSyncPass) * sizeof(float) + kSyncThreads * sizeof(float4) +
+                        static_cast<size_t>(kSyncPass + 2 * kMaxRadius) * sizeof(float);
     if (smem > 200 * 1024) throw InvalidArgument("preamble too long for the sync kernel");
-    if (2 * p.radius + 1 > kMaxRefine || p.radius < 0) throw InvalidArgument("refinement radius must be 0..511");
+    if (p.radius > kMaxRadius || p.radius < 0) throw InvalidArgument("refinement radius must be 0..511");
     check_cuda(cudaFuncSetAttribute(sync_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
                "cudaFuncSetAttribute(sync)");
     sync_kernel<<<frames, kSyncThreads, smem, st>>>(samples, stride, counts, count, preamble, p, out);
@@ -405,9 +414,8 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
         if (so.found != 1) {
             // no frame: zero LLRs (the caller sees found != 1 in the sync result)
             float* dst = llr + static_cast<long long>(f) * llr_stride;
-            for (int i = ds0 * v.active_sc * v.bits_per_symbol + threadIdx.x; i < ds1 * v.active_sc * v.bits_per_symbol;
-                 i += blockDim.x)
-                dst[i] = 0.0f;
+            const int hi = min(ds1 * v.active_sc * v.bits_per_symbol, v.kept_bits);
+            for (int i = ds0 * v.active_sc * v.bits_per_symbol + threadIdx.x; i < hi; i += blockDim.x) dst[i] = 0.0f;
             return;
         }
         start = so.start;
@@ -448,7 +456,8 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
         const int q0 = v.interp_p0[d] - pmin, q1 = v.interp_p1[d] - pmin;
         const float al = v.interp_alpha[d];
         const float w0 = __fsub_rn(1.0f, al);
-        for (int sc = threadIdx.x; sc < v.active_sc; sc += blockDim.x) {
+        const int sc_end = min(v.active_sc, v.kept_bits / bps - d * v.active_sc);  // REs of whole codewords
+        for (int sc = threadIdx.x; sc < sc_end; sc += blockDim.x) {
             const float2 y = Y[v.used_bins[sc]];
             float2 h = make_float2(1.0f, 0.0f);
             if (v.use_pilot_est) {
@@ -514,6 +523,8 @@ void launch_demod(const DemodView& v, const float2* samples, long long stride, c
     if (v.nfft < 4 || (v.nfft & (v.nfft - 1))) throw InvalidArgument("nfft must be a power of two >= 4");
     if (v.bits_per_symbol != 1 && v.bits_per_symbol != 2 && v.bits_per_symbol != 4 && v.bits_per_symbol != 6)
         throw InvalidArgument("bits_per_symbol must be 1, 2, 4 or 6");
+    if (v.kept_bits <= 0 || v.kept_bits > v.num_data * v.active_sc * v.bits_per_symbol || v.kept_bits % v.bits_per_symbol)
+        throw InvalidArgument("kept LLRs must be a positive multiple of bits_per_symbol within the frame");
     int spc = symbols_per_cta;
     if (spc <= 0) {
         const int groups = (v.num_data + 3) / 4;

@@ -41,6 +41,7 @@ struct DemodView {
     float sample_rate;
     float noise_var;
     int use_pilot_est;
+    int kept_bits;             // LLRs written per frame: the first kept_bits coded bits (whole codewords)
     const int* used_bins;      // [active_sc] natural FFT bin of each active subcarrier
     const int* pilot_symbols;  // [num_pilots]
     const int* data_symbols;   // [num_data]

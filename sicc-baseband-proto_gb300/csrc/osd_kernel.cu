@@ -27,7 +27,7 @@ constexpr int kOsdWarps = 8;
 
 template <int NW, int KR>
 struct OsdSmem {
-    uint32_t relbits[NW * 64];
+    unsigned long long keys[NW * 64];  // sort keys: (0x7fffffff - bits(|llr|)) << 32 | index
     float rel_sorted[NW * 64];
     int16_t perm[NW * 64];
     int16_t rowpiv[KR * 32];  // row id -> pivot index
@@ -42,6 +42,18 @@ __device__ __forceinline__ unsigned long long shfl_u64(unsigned long long v, int
     const unsigned lo = __shfl_sync(0xffffffffu, static_cast<unsigned>(v), src);
     const unsigned hi = __shfl_sync(0xffffffffu, static_cast<unsigned>(v >> 32), src);
     return (static_cast<unsigned long long>(hi) << 32) | lo;
+}
+
+// Word `w` of a register array, selected without dynamic indexing (which
+// would move the array to local memory).
+template <int NW>
+__device__ __forceinline__ unsigned long long pick(const unsigned long long (&a)[NW], int w)
+{
+    unsigned long long r = 0ull;
+#pragma unroll
+    for (int i = 0; i < NW; ++i)
+        if (i == w) r = a[i];
+    return r;
 }
 
 __device__ __forceinline__ unsigned long long shfl_xor_u64(unsigned long long v, int m)
@@ -69,23 +81,38 @@ osd_kernel(OsdView ov, OsdIO io)
     for (int item = blockIdx.x * kOsdWarps + warp; item < count; item += total_warps) {
         const int cw = io.index ? io.index[item] : item;
         const float* src = io.llr + static_cast<size_t>(item) * n;
-        // ---- 1. reliabilities, hard decisions, stable descending rank ----
-        for (int i = lane; i < NW * 64; i += 32) {
+        // ---- 1. reliabilities, hard decisions, stable descending sort ----
+        // Bitonic sort of 64-bit keys: ascending key = descending |llr|, ties by
+        // ascending index (the order of MATLAB's stable sort, cpu_bp_osd_decode.m:194).
+        constexpr int NP = NW * 64;
+        for (int i = lane; i < NP; i += 32) {
             const float x = (i < n) ? src[i] : 0.0f;
-            s.relbits[i] = (i < n) ? __float_as_uint(fabsf(x)) : 0u;
+            s.keys[i] = (i < n) ? ((static_cast<unsigned long long>(0x7fffffffu - __float_as_uint(fabsf(x))) << 32) |
+                                   static_cast<unsigned>(i))
+                                : ~0ull;
             const unsigned hb = __ballot_sync(0xffffffffu, (i < n) && (x < 0.0f));
             if (lane == 0) s.hard_orig[i >> 5] = hb;
         }
         __syncwarp();
-        for (int i = lane; i < n; i += 32) {
-            const uint32_t bi = s.relbits[i];
-            int r = 0;
-            for (int j = 0; j < n; ++j) {
-                const uint32_t bj = s.relbits[j];
-                r += (bj > bi) || (bj == bi && j < i);
+        for (int k2 = 2; k2 <= NP; k2 <<= 1) {
+            for (int j2 = k2 >> 1; j2 > 0; j2 >>= 1) {
+                for (int pr = lane; pr < NP / 2; pr += 32) {
+                    const int i = (pr / j2) * 2 * j2 + (pr % j2);
+                    const int ixj = i + j2;
+                    const bool asc = (i & k2) == 0;
+                    const unsigned long long a = s.keys[i], b = s.keys[ixj];
+                    if ((a > b) == asc) {
+                        s.keys[i] = b;
+                        s.keys[ixj] = a;
+                    }
+                }
+                __syncwarp();
             }
-            s.perm[r] = static_cast<int16_t>(i);
-            s.rel_sorted[r] = __uint_as_float(bi);
+        }
+        for (int r = lane; r < n; r += 32) {
+            const unsigned long long key = s.keys[r];
+            s.perm[r] = static_cast<int16_t>(key & 0xffffffffull);
+            s.rel_sorted[r] = __uint_as_float(0x7fffffffu - static_cast<unsigned>(key >> 32));
         }
         __syncwarp();
         // hard decisions in sorted order
@@ -146,7 +173,7 @@ osd_kernel(OsdView ov, OsdIO io)
 #pragma unroll
             for (int a = 0; a < KR; ++a) {
                 const int r = a * 32 + lane;
-                const bool cand = (r < k) && !((pivoted >> a) & 1u) && (rows[a][wj] & bj);
+                const bool cand = (r < k) && !((pivoted >> a) & 1u) && (pick<NW>(rows[a], wj) & bj);
                 const unsigned bal = __ballot_sync(0xffffffffu, cand);
                 if (ps < 0 && bal) {
                     ps = a;
@@ -166,7 +193,7 @@ osd_kernel(OsdView ov, OsdIO io)
 #pragma unroll
             for (int a = 0; a < KR; ++a) {
                 const bool is_p = (a == ps) && (lane == pl);
-                if (!is_p && (rows[a][wj] & bj)) {
+                if (!is_p && (pick<NW>(rows[a], wj) & bj)) {
 #pragma unroll
                     for (int w = 0; w < NW; ++w) rows[a][w] ^= pw[w];
                 }
@@ -195,7 +222,7 @@ osd_kernel(OsdView ov, OsdIO io)
 #pragma unroll
                 for (int w = 0; w < NW; ++w) s.rows[t][w] = rows[a][w];
                 const int pj = s.mrb_pos[t];
-                if ((hard_sorted[pj >> 6] >> (pj & 63)) & 1ull) {
+                if ((pick<NW>(hard_sorted, pj >> 6) >> (pj & 63)) & 1ull) {
 #pragma unroll
                     for (int w = 0; w < NW; ++w) acc[w] ^= rows[a][w];
                 }
@@ -219,36 +246,60 @@ osd_kernel(OsdView ov, OsdIO io)
         }
         __syncwarp();
         // ---- 6. all candidates in parallel ----
+        // A candidate's metric is a sum of non-negative terms in a fixed order, so
+        // its partial sums never decrease: once one exceeds the smallest metric
+        // already found the candidate cannot win and its sum stops.  Ties are not
+        // pruned (strict >), so the first minimum in test order still wins.
         unsigned long long best_key = ~0ull;
-        for (int q = lane; q < ov.num_tests; q += 32) {
-            unsigned long long d[NW];
+        float thr = INFINITY;
+        const int rounds = (ov.num_tests + 31) / 32;
+        for (int rd = 0; rd < rounds; ++rd) {
+            const int q = rd * 32 + lane;
+            if (q < ov.num_tests) {
+                unsigned long long d[NW];
 #pragma unroll
-            for (int w = 0; w < NW; ++w) d[w] = acc[w];
-            if (q > 0) {
-                const uint32_t cmb = ov.combos[q - 1];
+                for (int w = 0; w < NW; ++w) d[w] = acc[w];
+                if (q > 0) {
+                    const uint32_t cmb = ov.combos[q - 1];
 #pragma unroll
-                for (int f = 0; f < 3; ++f) {
-                    const uint32_t fi = (cmb >> (10 * f)) & 0x3FFu;
-                    if (fi != 0x3FFu) {
-                        const int t = s.flip[fi];
+                    for (int f = 0; f < 3; ++f) {
+                        const uint32_t fi = (cmb >> (10 * f)) & 0x3FFu;
+                        if (fi != 0x3FFu) {
+                            const int t = s.flip[fi];
 #pragma unroll
-                        for (int w = 0; w < NW; ++w) d[w] ^= s.rows[t][w];
+                            for (int w = 0; w < NW; ++w) d[w] ^= s.rows[t][w];
+                        }
+                    }
+                }
+                float metric = 0.0f;
+                bool pruned = false;
+#pragma unroll
+                for (int w = 0; w < NW; ++w) {
+                    unsigned long long bits = d[w];
+                    while (bits && !pruned) {
+                        const int b = __ffsll(static_cast<long long>(bits)) - 1;
+                        metric = __fadd_rn(metric, s.rel_sorted[w * 64 + b]);
+                        bits &= bits - 1;
+                        pruned = metric > thr;
+                    }
+                }
+                if (!pruned) {
+                    const unsigned long long key =
+                        (static_cast<unsigned long long>(__float_as_uint(metric)) << 32) | static_cast<unsigned>(q);
+                    if (key < best_key) {
+                        best_key = key;
+                        thr = fminf(thr, metric);
                     }
                 }
             }
-            float metric = 0.0f;
+            if (rd == 2 || (rd & 7) == 7) {  // share the best metric so far across the warp
 #pragma unroll
-            for (int w = 0; w < NW; ++w) {
-                unsigned long long bits = d[w];
-                while (bits) {
-                    const int b = __ffsll(static_cast<long long>(bits)) - 1;
-                    metric = __fadd_rn(metric, s.rel_sorted[w * 64 + b]);
-                    bits &= bits - 1;
+                for (int o = 16; o > 0; o >>= 1) {
+                    const unsigned long long other = shfl_xor_u64(best_key, o);
+                    best_key = other < best_key ? other : best_key;
                 }
+                if (best_key != ~0ull) thr = __uint_as_float(static_cast<unsigned>(best_key >> 32));
             }
-            const unsigned long long key = (static_cast<unsigned long long>(__float_as_uint(metric)) << 32) |
-                                           static_cast<unsigned>(q);
-            best_key = key < best_key ? key : best_key;
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -276,7 +327,7 @@ osd_kernel(OsdView ov, OsdIO io)
         for (int w = 0; w < NW; ++w) d[w] ^= hard_sorted[w];  // decoded codeword in sorted order
         for (int j = lane; j < n; j += 32) {
             const int o = s.perm[j];
-            const uint8_t bit = static_cast<uint8_t>((d[j >> 6] >> (j & 63)) & 1ull);
+            const uint8_t bit = static_cast<uint8_t>((pick<NW>(d, j >> 6) >> (j & 63)) & 1ull);
             if (io.out_info && o < k) io.out_info[static_cast<size_t>(cw) * io.info_stride + o] = bit;
             if (io.out_code) io.out_code[static_cast<size_t>(cw) * n + o] = bit;
         }

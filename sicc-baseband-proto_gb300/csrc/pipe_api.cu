@@ -1,0 +1,500 @@
+// C ABI of the OFDM receive pipeline (include/sicc_pipe.h): per-slot device
+// buffers and streams around the sync and demod kernels.  The slot model
+// follows the reference bridge (gpu_ofdm_pipeline.cu:1077-1247, 1472-1668):
+// a caller-managed ring of slots; every synchronous call waits for its slot's
+// stream before returning; returned device LLRs stay valid until the slot is
+// reused.
+#include "../../include/sicc_pipe.h"
+#include "ofdm_kernels.h"
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace sicc {
+namespace {
+
+static_assert(sizeof(sicc_pipe_sync_record_t) == sizeof(SyncOut), "sync record layout");
+
+template <class T>
+struct Buf {
+    T* p = nullptr;
+    void alloc(size_t n)
+    {
+        release();
+        if (n) check_cuda(cudaMalloc(&p, n * sizeof(T)), "cudaMalloc(pipeline)");
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+    ~Buf() { release(); }
+};
+
+template <class T>
+void upload(Buf<T>& b, const T* src, size_t n)
+{
+    b.alloc(n);
+    if (n) check_cuda(cudaMemcpy(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice), "upload pipeline table");
+}
+
+struct Slot {
+    Buf<float2> samples;
+    Buf<SyncOut> sync;
+    Buf<float> llr;
+    cudaStream_t stream = nullptr;
+    ~Slot()
+    {
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+struct Pipe {
+    sicc_pipe_config_t cfg{};
+    int device = 0;
+    int frame_samples = 0;
+    int coded_bits = 0;     // blocks_per_frame * code_n: LLRs kept per frame
+    int capacity_bits = 0;  // data REs * bits per symbol
+    int max_rx = 0;
+    int batch_frames = 256;
+    int symbols_per_cta = 0;  // data symbols per demod CTA; their pilots span at most 4
+    bool tables = false;
+    float pre_energy = 0.0f;
+    DemodView view{};
+    Buf<int> used_bins, pilot_syms, data_syms, p0, p1;
+    Buf<float> alpha, axis;
+    Buf<float2> pilot_grid, preamble, twiddle;
+    std::vector<std::unique_ptr<Slot>> slots;
+    Buf<SyncOut> batch_sync;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    bool batch_timed = false;
+    std::mutex mu;
+    ~Pipe()
+    {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+
+    SyncParams sync_params(int mode) const
+    {
+        SyncParams p{};
+        p.half_len = cfg.pre_half_len;
+        p.pre_len = cfg.preamble_len;
+        p.radius = cfg.sync_radius > 0 ? cfg.sync_radius : std::min(16, cfg.cp);
+        p.threshold = cfg.sync_threshold;
+        p.sample_rate = cfg.sample_rate;
+        p.mode = mode;
+        p.max_search = 0;
+        p.frame_len = frame_samples;
+        p.pre_energy = pre_energy;
+        return p;
+    }
+};
+
+std::mutex g_mu;
+std::map<unsigned long long, std::shared_ptr<Pipe>> g_pipes;
+unsigned long long g_next = 0x7100;
+
+std::shared_ptr<Pipe> get(unsigned long long h)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_pipes.find(h);
+    if (it == g_pipes.end()) throw InvalidArgument("invalid pipeline handle");
+    return it->second;
+}
+
+Slot& slot_of(Pipe& p, int slot)
+{
+    if (slot < 0 || slot >= static_cast<int>(p.slots.size())) throw InvalidArgument("invalid GPU pipeline slot");
+    return *p.slots[slot];
+}
+
+template <class F>
+int guarded(F&& f)
+{
+    try {
+        return f();
+    } catch (const InvalidArgument& e) {
+        set_last_error(e.what());
+        return CUDA_OSD_STATUS_INVALID_ARGUMENT;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return CUDA_OSD_STATUS_INTERNAL_ERROR;
+    }
+}
+
+void require_tables(const Pipe& p)
+{
+    if (!p.tables) throw InvalidArgument("upload_static_tables must run before receiving");
+}
+
+sicc_pipe_sync_t to_public(const SyncOut& s)
+{
+    sicc_pipe_sync_t r{};
+    r.start = (s.found == 1) ? s.start : -1;
+    r.metric = s.fine;
+    r.cfo_hz = (s.found == 1) ? s.cfo_hz : 0.0f;
+    return r;
+}
+
+// Search `count` samples already in device memory (slot stream); returns the result.
+SyncOut run_sync(Pipe& p, Slot& s, const float2* d_iq, int count)
+{
+    if (count < p.cfg.preamble_len) throw InvalidArgument("RX sample_count is shorter than the preamble");
+    const SyncParams sp = p.sync_params(0);
+    launch_sync(d_iq, 0, nullptr, count, 1, p.preamble.p, sp, s.sync.p, s.stream);
+    SyncOut out{};
+    check_cuda(cudaMemcpyAsync(&out, s.sync.p, sizeof(SyncOut), cudaMemcpyDeviceToHost, s.stream), "copy sync result");
+    check_cuda(cudaStreamSynchronize(s.stream), "synchronize sync");
+    return out;
+}
+
+}  // namespace
+}  // namespace sicc
+
+using namespace sicc;
+
+extern "C" {
+
+int sicc_pipe_create(const sicc_pipe_config_t* config, int slots, unsigned long long* out_handle)
+{
+    return guarded([&] {
+        if (!config || !out_handle) throw InvalidArgument("null argument");
+        *out_handle = 0;
+        const sicc_pipe_config_t& c = *config;
+        if (c.blocks_per_frame <= 0) throw InvalidArgument("blocks_per_frame must be set before constructing the pipeline");
+        if (c.nfft < 4 || (c.nfft & (c.nfft - 1))) throw InvalidArgument("nfft must be a power of two");
+        if (c.cp < 0 || c.cp >= c.nfft) throw InvalidArgument("cp must be in [0, nfft)");
+        if (c.active_sc <= 0 || c.active_sc >= c.nfft) throw InvalidArgument("active_sc must be in (0, nfft)");
+        if (c.preamble_len != 2 * c.pre_half_len || c.pre_half_len <= 0)
+            throw InvalidArgument("preamble_len must equal 2 * pre_half_len");
+        if (c.bits_per_symbol != 1 && c.bits_per_symbol != 2 && c.bits_per_symbol != 4 && c.bits_per_symbol != 6)
+            throw InvalidArgument("bits_per_symbol must be 1, 2, 4, or 6");
+        auto p = std::make_shared<Pipe>();
+        p->cfg = c;
+        check_cuda(cudaGetDevice(&p->device), "cudaGetDevice");
+        p->frame_samples = c.preamble_len + c.num_symbols * (c.nfft + c.cp);
+        p->coded_bits = c.blocks_per_frame * c.code_n;
+        p->max_rx = c.max_rx_search_samples > 0 ? c.max_rx_search_samples : p->frame_samples;
+        p->batch_frames = c.max_batch_frames > 0 ? c.max_batch_frames : 256;
+        const int n_slots = std::max(slots, 1);
+        for (int i = 0; i < n_slots; ++i) {
+            auto s = std::make_unique<Slot>();
+            check_cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate(slot)");
+            // twice the longest buffer, zero-filled: a frame found near the end of a one-frame
+            // buffer ("incomplete") is demodulated from defined memory (zeros past the samples)
+            const size_t cap = 2 * static_cast<size_t>(std::max(p->max_rx, p->frame_samples));
+            s->samples.alloc(cap);
+            check_cuda(cudaMemset(s->samples.p, 0, cap * sizeof(float2)), "zero slot samples");
+            s->sync.alloc(1);
+            s->llr.alloc(static_cast<size_t>(p->coded_bits));
+            p->slots.push_back(std::move(s));
+        }
+        p->batch_sync.alloc(static_cast<size_t>(p->batch_frames));
+        for (auto& e : p->ev) check_cuda(cudaEventCreate(&e), "cudaEventCreate(pipeline)");
+        std::lock_guard<std::mutex> lock(g_mu);
+        *out_handle = ++g_next;
+        g_pipes[*out_handle] = p;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_destroy(unsigned long long handle)
+{
+    return guarded([&] {
+        std::shared_ptr<Pipe> p;
+        {
+            std::lock_guard<std::mutex> lock(g_mu);
+            auto it = g_pipes.find(handle);
+            if (it == g_pipes.end()) throw InvalidArgument("invalid pipeline handle");
+            p = it->second;
+            g_pipes.erase(it);
+        }
+        cudaSetDevice(p->device);
+        for (auto& s : p->slots) cudaStreamSynchronize(s->stream);
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_upload_static_tables(unsigned long long handle, const sicc_pipe_tables_t* t)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        if (!t || !t->used_indices || !t->data_symbols || !t->interp_p0 || !t->interp_p1 || !t->interp_alpha ||
+            !t->preamble)
+            throw InvalidArgument("null table");
+        const auto& c = p->cfg;
+        if (t->data_count <= 0 || t->data_count > c.num_symbols) throw InvalidArgument("data_symbols has wrong size");
+        p->capacity_bits = t->data_count * c.active_sc * c.bits_per_symbol;
+        if (p->coded_bits > p->capacity_bits)
+            throw InvalidArgument("coded bits per frame exceed the data resource elements");
+        if (p->coded_bits % c.bits_per_symbol)
+            throw InvalidArgument("coded bits per frame must be a multiple of bits_per_symbol");
+        if (c.use_pilot_channel_est && (t->pilot_count <= 0 || !t->pilot_symbols || !t->pilot_grid))
+            throw InvalidArgument("pilot tables are required for pilot channel estimation");
+        check_cuda(cudaSetDevice(p->device), "cudaSetDevice");
+        std::vector<int> bins(c.active_sc);
+        for (int sc = 0; sc < c.active_sc; ++sc) {
+            const int u = t->used_indices[sc];
+            if (u < 0 || u >= c.nfft) throw InvalidArgument("used_indices out of range");
+            bins[sc] = (u + c.nfft / 2) % c.nfft;  // shifted grid -> natural bin (gpu_ofdm_pipeline.cu:124-127)
+        }
+        for (int d = 0; d < t->data_count; ++d) {
+            if (t->data_symbols[d] < 0 || t->data_symbols[d] >= c.num_symbols) throw InvalidArgument("data symbol index");
+            if (c.use_pilot_channel_est &&
+                (t->interp_p0[d] < 0 || t->interp_p0[d] >= t->pilot_count || t->interp_p1[d] < 0 ||
+                 t->interp_p1[d] >= t->pilot_count || std::abs(t->interp_p1[d] - t->interp_p0[d]) > 3))
+                throw InvalidArgument("interpolation pilot indices out of range");
+        }
+        // data symbols per CTA: about four, fewer when their interpolation pilots would span more than four
+        {
+            const int groups = (t->data_count + 3) / 4;
+            int spc = (t->data_count + groups - 1) / groups;
+            for (; spc > 1; --spc) {
+                bool ok = true;
+                for (int d0 = 0; d0 < t->data_count && ok; d0 += spc) {
+                    int lo = 1 << 30, hi = -1;
+                    for (int d = d0; d < std::min(t->data_count, d0 + spc); ++d) {
+                        lo = std::min(lo, std::min(t->interp_p0[d], t->interp_p1[d]));
+                        hi = std::max(hi, std::max(t->interp_p0[d], t->interp_p1[d]));
+                    }
+                    ok = !c.use_pilot_channel_est || hi - lo + 1 <= 4;
+                }
+                if (ok) break;
+            }
+            p->symbols_per_cta = spc;
+        }
+        upload(p->used_bins, bins.data(), bins.size());
+        upload(p->data_syms, t->data_symbols, t->data_count);
+        upload(p->p0, t->interp_p0, t->data_count);
+        upload(p->p1, t->interp_p1, t->data_count);
+        upload(p->alpha, t->interp_alpha, t->data_count);
+        if (t->pilot_count > 0) {
+            for (int q = 0; q < t->pilot_count; ++q)
+                if (t->pilot_symbols[q] < 0 || t->pilot_symbols[q] >= c.num_symbols) throw InvalidArgument("pilot symbol index");
+            upload(p->pilot_syms, t->pilot_symbols, t->pilot_count);
+            upload(p->pilot_grid, reinterpret_cast<const float2*>(t->pilot_grid),
+                   static_cast<size_t>(t->pilot_count) * c.active_sc);
+        }
+        upload(p->preamble, reinterpret_cast<const float2*>(t->preamble), c.preamble_len);
+        float e = 0.0f;
+        for (int i = 0; i < c.preamble_len; ++i)
+            e += t->preamble[2 * i] * t->preamble[2 * i] + t->preamble[2 * i + 1] * t->preamble[2 * i + 1];
+        p->pre_energy = e;
+        // twiddles exp(-2 pi i j / N), computed in double
+        std::vector<float2> tw(c.nfft);
+        for (int j = 0; j < c.nfft; ++j) {
+            const double a = -2.0 * 3.141592653589793238462643383279502884 * j / c.nfft;
+            tw[j] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
+        }
+        upload(p->twiddle, tw.data(), tw.size());
+        // axis amplitudes of Gray square QAM, scaled to unit average power as the
+        // reference constellation (uhd_ldpc_ofdm_link.cpp:2362-2414)
+        std::vector<float> lv;
+        const int bps = c.bits_per_symbol;
+        if (bps == 1) {
+            lv = {1.0f, -1.0f};
+        } else if (bps == 2) {
+            const float s = static_cast<float>(1.0 / std::sqrt(2.0));
+            lv = {s, -s};
+        } else {
+            const int ab = bps / 2, levels = 1 << ab;
+            double avg = 0.0;
+            auto g2b = [](int g) {
+                int b = 0;
+                for (; g; g >>= 1) b ^= g;
+                return b;
+            };
+            for (int i = 0; i < levels; ++i)
+                for (int q = 0; q < levels; ++q) {
+                    const double a = (levels - 1) - 2 * g2b(i), b = (levels - 1) - 2 * g2b(q);
+                    avg += a * a + b * b;
+                }
+            const float scale = static_cast<float>(1.0 / std::sqrt(avg / (levels * levels)));
+            for (int g = 0; g < levels; ++g) lv.push_back(static_cast<float>((levels - 1) - 2 * g2b(g)) * scale);
+        }
+        upload(p->axis, lv.data(), lv.size());
+        DemodView& v = p->view;
+        v.nfft = c.nfft;
+        v.cp = c.cp;
+        v.num_symbols = c.num_symbols;
+        v.active_sc = c.active_sc;
+        v.bits_per_symbol = c.bits_per_symbol;
+        v.pre_len = c.preamble_len;
+        v.num_pilots = t->pilot_count;
+        v.num_data = t->data_count;
+        v.sample_rate = c.sample_rate;
+        v.noise_var = c.demod_noise_var;
+        v.use_pilot_est = c.use_pilot_channel_est ? 1 : 0;
+        v.kept_bits = p->coded_bits;
+        v.used_bins = p->used_bins.p;
+        v.pilot_symbols = p->pilot_syms.p;
+        v.data_symbols = p->data_syms.p;
+        v.interp_p0 = p->p0.p;
+        v.interp_p1 = p->p1.p;
+        v.interp_alpha = p->alpha.p;
+        v.pilot_grid = p->pilot_grid.p;
+        v.twiddle = p->twiddle.p;
+        v.axis_levels = p->axis.p;
+        p->tables = true;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+static int find_frame_impl(unsigned long long handle, int slot, const float* iq, bool device, int count,
+                           sicc_pipe_sync_t* out)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        require_tables(*p);
+        if (!iq || !out) throw InvalidArgument("null argument");
+        Slot& s = slot_of(*p, slot);
+        check_cuda(cudaSetDevice(p->device), "cudaSetDevice");
+        if (count > p->max_rx) throw InvalidArgument("RX sample_count exceeds slot allocation");
+        const float2* d = reinterpret_cast<const float2*>(iq);
+        if (!device) {
+            check_cuda(cudaMemcpyAsync(s.samples.p, iq, static_cast<size_t>(count) * sizeof(float2),
+                                       cudaMemcpyHostToDevice, s.stream),
+                       "copy RX samples");
+            d = s.samples.p;
+        }
+        *out = to_public(run_sync(*p, s, d, count));
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_find_frame(unsigned long long handle, int slot, const float* host_iq, int sample_count,
+                         sicc_pipe_sync_t* out_sync)
+{
+    return find_frame_impl(handle, slot, host_iq, false, sample_count, out_sync);
+}
+
+int sicc_pipe_find_frame_device(unsigned long long handle, int slot, const float* device_iq, int sample_count,
+                                sicc_pipe_sync_t* out_sync)
+{
+    return find_frame_impl(handle, slot, device_iq, true, sample_count, out_sync);
+}
+
+int sicc_pipe_demod_to_device(unsigned long long handle, int slot, const float* host_frame, sicc_pipe_sync_t* out_sync,
+                              const float** out_device_llr)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        require_tables(*p);
+        if (!host_frame || !out_device_llr) throw InvalidArgument("null argument");
+        Slot& s = slot_of(*p, slot);
+        check_cuda(cudaSetDevice(p->device), "cudaSetDevice");
+        const int count = p->frame_samples;
+        check_cuda(cudaMemcpyAsync(s.samples.p, host_frame, static_cast<size_t>(count) * sizeof(float2),
+                                   cudaMemcpyHostToDevice, s.stream),
+                   "copy RX frame");
+        const SyncOut so = run_sync(*p, s, s.samples.p, count);
+        // frames that run past the buffer are demodulated as found (the buffer is one frame long)
+        SyncOut use = so;
+        if (so.found == 2) {
+            use.found = 1;
+            check_cuda(cudaMemcpyAsync(s.sync.p, &use, sizeof(SyncOut), cudaMemcpyHostToDevice, s.stream), "sync");
+        }
+        launch_demod(p->view, s.samples.p, 0, s.sync.p, 1, s.llr.p, p->coded_bits, s.stream, p->symbols_per_cta);
+        check_cuda(cudaStreamSynchronize(s.stream), "synchronize RX demod device LLR");
+        if (out_sync) *out_sync = to_public(so);
+        *out_device_llr = s.llr.p;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_demod_device_to_device(unsigned long long handle, int slot, const float* device_frame,
+                                     const sicc_pipe_sync_t* sync, const float** out_device_llr)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        require_tables(*p);
+        if (!device_frame || !sync || !out_device_llr) throw InvalidArgument("null argument");
+        Slot& s = slot_of(*p, slot);
+        check_cuda(cudaSetDevice(p->device), "cudaSetDevice");
+        SyncOut so{};
+        so.found = 1;
+        so.start = 0;  // the device frame starts at its first sample (gpu_ofdm_pipeline.cu:1230-1236)
+        so.fine = sync->metric;
+        so.cfo_hz = sync->cfo_hz;
+        check_cuda(cudaMemcpyAsync(s.sync.p, &so, sizeof(SyncOut), cudaMemcpyHostToDevice, s.stream), "copy sync");
+        launch_demod(p->view, reinterpret_cast<const float2*>(device_frame), 0, s.sync.p, 1, s.llr.p, p->coded_bits,
+                     s.stream, p->symbols_per_cta);
+        check_cuda(cudaStreamSynchronize(s.stream), "synchronize RX device-frame demod LLR");
+        *out_device_llr = s.llr.p;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_demod_to_host(unsigned long long handle, int slot, const float* host_frame, float* host_llr,
+                            sicc_pipe_sync_t* out_sync)
+{
+    const float* d_llr = nullptr;
+    sicc_pipe_sync_t so{};
+    int st = sicc_pipe_demod_to_device(handle, slot, host_frame, &so, &d_llr);
+    if (st != CUDA_OSD_STATUS_OK) return st;
+    return guarded([&] {
+        auto p = get(handle);
+        if (!host_llr) throw InvalidArgument("null host_llr");
+        Slot& s = slot_of(*p, slot);
+        check_cuda(cudaMemcpyAsync(host_llr, d_llr, static_cast<size_t>(p->coded_bits) * sizeof(float),
+                                   cudaMemcpyDeviceToHost, s.stream),
+                   "copy RX LLRs to host");
+        check_cuda(cudaStreamSynchronize(s.stream), "synchronize RX demod LLR copy");
+        if (out_sync) *out_sync = so;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_demod_batch(unsigned long long handle, const float* device_iq, long long stride, int sample_count,
+                          int frames, float* device_llr, sicc_pipe_sync_record_t* device_sync, void* cuda_stream)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        require_tables(*p);
+        if (!device_iq || !device_llr) throw InvalidArgument("null device pointer");
+        if (frames <= 0 || frames > p->batch_frames) throw InvalidArgument("frames must be in 1..max_batch_frames");
+        if (sample_count < p->cfg.preamble_len || stride < sample_count)
+            throw InvalidArgument("sample_count must cover the preamble and fit the stride");
+        check_cuda(cudaSetDevice(p->device), "cudaSetDevice");
+        cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+        SyncOut* so = device_sync ? reinterpret_cast<SyncOut*>(device_sync) : p->batch_sync.p;
+        check_cuda(cudaEventRecord(p->ev[0], st), "cudaEventRecord");
+        launch_sync(reinterpret_cast<const float2*>(device_iq), stride, nullptr, sample_count, frames, p->preamble.p,
+                    p->sync_params(0), so, st);
+        check_cuda(cudaEventRecord(p->ev[1], st), "cudaEventRecord");
+        launch_demod(p->view, reinterpret_cast<const float2*>(device_iq), stride, so, frames, device_llr, p->coded_bits,
+                     st, p->symbols_per_cta);
+        check_cuda(cudaEventRecord(p->ev[2], st), "cudaEventRecord");
+        p->batch_timed = true;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_last_batch_ms(unsigned long long handle, float* out_sync_ms, float* out_demod_ms)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        if (!p->batch_timed) throw InvalidArgument("no batch has run");
+        check_cuda(cudaEventSynchronize(p->ev[2]), "cudaEventSynchronize");
+        float a = 0.0f, b = 0.0f;
+        check_cuda(cudaEventElapsedTime(&a, p->ev[0], p->ev[1]), "cudaEventElapsedTime");
+        check_cuda(cudaEventElapsedTime(&b, p->ev[1], p->ev[2]), "cudaEventElapsedTime");
+        if (out_sync_ms) *out_sync_ms = a;
+        if (out_demod_ms) *out_demod_ms = b;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+}  // extern "C"
