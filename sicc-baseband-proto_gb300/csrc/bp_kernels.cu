@@ -18,6 +18,7 @@
 // Every floating-point step uses explicit round-to-nearest intrinsics so no
 // multiply-add contraction changes a result: the kernels reproduce the
 // single-precision oracle (oracle/sicc_oracle.c) bit for bit.
+#include "bp_device.cuh"
 #include "bp_kernels.h"
 
 #include <algorithm>
@@ -26,20 +27,6 @@
 namespace sicc {
 
 namespace {
-
-__device__ __forceinline__ float nms_mag(float alpha, float beta, float mn)
-{
-    const float a = __fmul_rn(alpha, mn);
-    if (beta == 0.0f) return a;
-    const float d = __fsub_rn(a, beta);
-    return d > 0.0f ? d : 0.0f;
-}
-
-__device__ __forceinline__ float rebuild(float m1, float m2, unsigned meta, int j)
-{
-    const float mag = (j == static_cast<int>(meta >> 27)) ? m2 : m1;
-    return ((meta >> j) & 1u) ? -mag : mag;
-}
 
 // Group-local syndrome weight of hard(app) under the layered tables.
 __device__ __forceinline__ int layered_syndrome(const LayeredView& cv, const int* s_vars, const float* app,

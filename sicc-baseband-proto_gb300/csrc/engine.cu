@@ -1,0 +1,579 @@
+// Mixed-code batched decoding (include/sicc_engine.h).
+//
+// One batch holds codewords of several codes.  prepare_kernel groups them by
+// code (a counting sort in the queue order: largest code first) and sizes the
+// work units; bp_mixed_kernel then runs persistently: each warp takes the next
+// unit — up to 32/G codewords of one code, G lanes each — from a device
+// counter, decodes it with that code's layered schedule (the same arithmetic
+// as bp_layered_kernel, so results are bit-exact with the single-code
+// decoders) and takes another unit until the queue is empty.  Codewords whose
+// syndrome fails go to one OSD launch that reads each item's code tables.
+#include "../../include/sicc_engine.h"
+#include "bp_device.cuh"
+#include "bp_kernels.h"
+#include "code_plan.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+namespace sicc {
+
+namespace {
+
+constexpr int kMaxCodes = 64;
+
+struct CodeDesc {
+    int n, k, num_layers, width, maxdeg, group, rows_per_lane, max_iter;
+    float alpha, beta;
+    int route_osd;
+    int slot_floats;  // shared-memory floats per codeword slot
+    const int* vars;  // [num_layers][maxdeg][width]
+};
+
+struct MixedIO {
+    const CodeDesc* codes;
+    const uint8_t* code_of;      // [count]
+    const float* llr;
+    const long long* llr_off;    // [count]
+    uint8_t* info;
+    const long long* info_off;   // [count]
+    uint8_t* success;
+    uint8_t* used_osd;
+    uint8_t* iterations;
+    const int* order;            // [count] codeword indices grouped by code, queue order
+    const int* q_code;           // [K] code id at queue position q
+    const int* q_start;          // [K+1] first entry of queue position q in `order`
+    const int* q_units;          // [K+1] first unit of queue position q
+    int K;
+    int* work;                   // unit counter
+    float* best;                 // [warps][4][n_max] best-syndrome posteriors (global scratch)
+    int n_max;
+    float* osd_llr;              // same layout as llr (llr_off)
+    int* osd_index;
+    int* osd_count;
+};
+
+// prepare: counts per code, queue-ordered starts, units, scatter into `order`.
+__global__ void __launch_bounds__(1024)
+prepare_kernel(const uint8_t* __restrict__ code_of, int count, const int* __restrict__ q_code, int K,
+               const int* __restrict__ per_warp, int* __restrict__ order, int* __restrict__ q_start,
+               int* __restrict__ q_units, int* __restrict__ work, int* __restrict__ osd_count)
+{
+    __shared__ int cnt[kMaxCodes], fill[kMaxCodes], pos_of_code[kMaxCodes];
+    for (int i = threadIdx.x; i < kMaxCodes; i += blockDim.x) {
+        cnt[i] = 0;
+        fill[i] = 0;
+    }
+    __syncthreads();
+    // codewords whose code id is not registered are left out (their outputs are not written)
+    for (int i = threadIdx.x; i < count; i += blockDim.x)
+        if (code_of[i] < K) atomicAdd(&cnt[code_of[i]], 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int s = 0, u = 0;
+        for (int q = 0; q < K; ++q) {
+            const int c = q_code[q];
+            pos_of_code[c] = s;
+            q_start[q] = s;
+            q_units[q] = u;
+            s += cnt[c];
+            u += (cnt[c] + per_warp[c] - 1) / per_warp[c];
+        }
+        q_start[K] = s;
+        q_units[K] = u;
+        *work = 0;
+        *osd_count = 0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < count; i += blockDim.x) {
+        const int c = code_of[i];
+        if (c < K) order[pos_of_code[c] + atomicAdd(&fill[c], 1)] = i;
+    }
+}
+
+__device__ __forceinline__ int mixed_syndrome(const CodeDesc& d, const float* app, int gl, int G, unsigned gmask)
+{
+    int cnt = 0;
+    for (int L = 0; L < d.num_layers; ++L) {
+        for (int rr = 0; rr < d.rows_per_lane; ++rr) {
+            const int rs = gl + rr * G;
+            const int* vp = d.vars + (L * d.maxdeg) * d.width + rs;
+            unsigned par = 0;
+            for (int j = 0; j < d.maxdeg; ++j) {
+                const int v = __ldg(vp + j * d.width);
+                if (v >= 0) par ^= (app[v] < 0.0f) ? 1u : 0u;
+            }
+            cnt += static_cast<int>(par);
+        }
+    }
+    return static_cast<int>(__reduce_add_sync(gmask, static_cast<unsigned>(cnt)));
+}
+
+template <int D>
+__global__ void __launch_bounds__(256)
+bp_mixed_kernel(MixedIO io, int warp_floats)
+{
+    extern __shared__ __align__(16) float smem_f[];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    float* wbase = smem_f + static_cast<size_t>(warp) * warp_floats;
+    const int gwarp = blockIdx.x * (blockDim.x >> 5) + warp;
+    const int total_units = io.q_units[io.K];
+
+    for (;;) {
+        int u = 0;
+        if (lane == 0) u = atomicAdd(io.work, 1);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= total_units) break;
+        int q = 0;
+        while (q + 1 < io.K && u >= io.q_units[q + 1]) ++q;
+        const CodeDesc d = io.codes[io.q_code[q]];
+        const int G = d.group;
+        const int per = 32 / G;
+        const int sub = lane / G;
+        const int gl = lane & (G - 1);
+        const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
+        const int local = (u - io.q_units[q]) * per + sub;
+        bool active = local < io.q_start[q + 1] - io.q_start[q];
+        const int cw = active ? io.order[io.q_start[q] + local] : 0;
+        const int n = d.n;
+        const int n_pad = (n + 3) & ~3;
+        const int mp = d.num_layers * d.width;
+        float* app = wbase + sub * d.slot_floats;
+        float* r1 = app + n_pad;
+        float* r2 = r1 + mp;
+        unsigned* meta = reinterpret_cast<unsigned*>(r2 + mp);
+        float* best = io.best + (static_cast<size_t>(gwarp) * 4 + sub) * io.n_max;
+        int iter = 0, best_w = 0;
+        if (active) {
+            const float* src = io.llr + io.llr_off[cw];
+            for (int i = gl; i < n; i += G) {
+                const float v = __ldcs(src + i);
+                app[i] = v;
+                if (d.route_osd) best[i] = v;
+            }
+            for (int r = gl; r < mp; r += G) {
+                r1[r] = 0.0f;
+                r2[r] = 0.0f;
+                meta[r] = 0u;
+            }
+            __syncwarp(gmask);
+            best_w = mixed_syndrome(d, app, gl, G, gmask);
+        }
+        while (__any_sync(0xffffffffu, active)) {
+            if (!active) continue;
+            for (int L = 0; L < d.num_layers; ++L) {
+                for (int rr = 0; rr < d.rows_per_lane; ++rr) {
+                    const int rs = gl + rr * G;
+                    const int ridx = L * d.width + rs;
+                    const float o1 = r1[ridx], o2 = r2[ridx];
+                    const unsigned om = meta[ridx];
+                    const int* vp = d.vars + (L * d.maxdeg) * d.width + rs;
+                    float qv[D];
+                    int v[D];
+                    float m1 = FLT_MAX, m2 = FLT_MAX;
+                    int idx = 0;
+                    unsigned neg = 0;
+#pragma unroll
+                    for (int j = 0; j < D; ++j) {
+                        v[j] = (j < d.maxdeg) ? __ldg(vp + j * d.width) : -1;
+                        qv[j] = 0.0f;
+                        if (v[j] >= 0) {
+                            const float qj = __fsub_rn(app[v[j]], rebuild(o1, o2, om, j));
+                            qv[j] = qj;
+                            neg |= (qj < 0.0f) ? (1u << j) : 0u;
+                            const float a = fabsf(qj);
+                            if (a < m1) {
+                                m2 = m1;
+                                m1 = a;
+                                idx = j;
+                            } else if (a < m2) {
+                                m2 = a;
+                            }
+                        }
+                    }
+                    const unsigned tot = static_cast<unsigned>(__popc(neg)) & 1u;
+                    const float n1 = nms_mag(d.alpha, d.beta, m1);
+                    const float n2 = nms_mag(d.alpha, d.beta, m2);
+                    unsigned nm = static_cast<unsigned>(idx) << 27;
+#pragma unroll
+                    for (int j = 0; j < D; ++j) {
+                        if (v[j] >= 0) {
+                            const unsigned s = tot ^ ((neg >> j) & 1u);
+                            const float mag = (j == idx) ? n2 : n1;
+                            nm |= s << j;
+                            app[v[j]] = __fadd_rn(qv[j], s ? -mag : mag);
+                        }
+                    }
+                    r1[ridx] = n1;
+                    r2[ridx] = n2;
+                    meta[ridx] = nm;
+                }
+                __syncwarp(gmask);
+            }
+            const int w = mixed_syndrome(d, app, gl, G, gmask);
+            ++iter;
+            if (d.route_osd && (w < best_w || w == 0)) {
+                for (int i = gl; i < n; i += G) best[i] = app[i];
+            }
+            if (w < best_w) best_w = w;
+            if (w == 0 || iter >= d.max_iter) {
+                const bool ok = (w == 0);
+                if (gl == 0) {
+                    if (io.success) io.success[cw] = ok ? 1 : 0;
+                    if (io.iterations) io.iterations[cw] = static_cast<uint8_t>(iter);
+                    if (io.used_osd) io.used_osd[cw] = 0;
+                }
+                uint8_t* dst = io.info + io.info_off[cw];
+                for (int i = gl; i < d.k; i += G) dst[i] = app[i] < 0.0f ? 1 : 0;
+                if (!ok && d.route_osd) {
+                    __syncwarp(gmask);  // best written by other lanes of the group
+                    float* o = io.osd_llr + io.llr_off[cw];
+                    for (int i = gl; i < n; i += G) o[i] = best[i];
+                    if (gl == 0) io.osd_index[atomicAdd(io.osd_count, 1)] = cw;
+                }
+                active = false;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+struct EngineCode {
+    std::unique_ptr<DeviceCode> code;
+    CodeDesc desc{};
+    bool osd = false;
+    long long cost = 0;
+};
+
+struct Engine {
+    sicc_engine_config_t cfg{};
+    int device = 0;
+    std::vector<EngineCode> codes;
+    int n_max = 0, k_max = 0, maxdeg = 0, osd_nmax = 0, osd_kmax = 0;
+    int warps_per_cta = 0, ctas = 0;
+    // device state
+    CodeDesc* d_codes = nullptr;
+    OsdView* d_views = nullptr;
+    int* d_per_warp = nullptr;
+    int* d_q_code = nullptr;
+    int* d_q_start = nullptr;
+    int* d_q_units = nullptr;
+    int* d_order = nullptr;
+    int* d_counters = nullptr;  // [0] work, [1] osd count
+    int* d_osd_index = nullptr;
+    float* d_osd_llr = nullptr;
+    float* d_best = nullptr;
+    size_t best_warps = 0;
+    bool dirty = true;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool timed = false;
+    std::mutex mu;
+    ~Engine()
+    {
+        for (void* p : {static_cast<void*>(d_codes), static_cast<void*>(d_views), static_cast<void*>(d_per_warp),
+                        static_cast<void*>(d_q_code), static_cast<void*>(d_q_start), static_cast<void*>(d_q_units),
+                        static_cast<void*>(d_order), static_cast<void*>(d_counters), static_cast<void*>(d_osd_index),
+                        static_cast<void*>(d_osd_llr), static_cast<void*>(d_best)})
+            if (p) cudaFree(p);
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+
+    int warp_floats() const
+    {
+        int w = 0;
+        for (const auto& c : codes) w = std::max(w, (32 / c.desc.group) * c.desc.slot_floats);
+        return w;
+    }
+
+    // Uploads the code descriptors and the queue order after codes change.
+    void commit()
+    {
+        if (!dirty) return;
+        const int K = static_cast<int>(codes.size());
+        std::vector<CodeDesc> descs(K);
+        std::vector<OsdView> views(K);
+        std::vector<int> per(K), qcode(K);
+        for (int c = 0; c < K; ++c) {
+            descs[c] = codes[c].desc;
+            per[c] = 32 / codes[c].desc.group;
+            views[c] = codes[c].osd ? codes[c].code->osd_view() : OsdView{};
+            qcode[c] = c;
+        }
+        // queue order: most expensive codes first, so the long codewords start early
+        std::stable_sort(qcode.begin(), qcode.end(), [&](int a, int b) { return codes[a].cost > codes[b].cost; });
+        auto up = [](auto*& dst, const auto& v) {
+            using T = std::remove_reference_t<decltype(v[0])>;
+            if (dst) cudaFree(dst);
+            check_cuda(cudaMalloc(&dst, std::max<size_t>(v.size(), 1) * sizeof(T)), "cudaMalloc(engine)");
+            check_cuda(cudaMemcpy(dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload(engine)");
+        };
+        up(d_codes, descs);
+        up(d_views, views);
+        up(d_per_warp, per);
+        up(d_q_code, qcode);
+        dirty = false;
+    }
+};
+
+std::mutex g_mu;
+std::map<unsigned long long, std::shared_ptr<Engine>> g_engines;
+unsigned long long g_next = 0x9100;
+
+std::shared_ptr<Engine> get(unsigned long long h)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_engines.find(h);
+    if (it == g_engines.end()) throw InvalidArgument("invalid engine handle");
+    return it->second;
+}
+
+template <class F>
+int guarded(F&& f)
+{
+    try {
+        return f();
+    } catch (const InvalidArgument& e) {
+        set_last_error(e.what());
+        return CUDA_OSD_STATUS_INVALID_ARGUMENT;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return CUDA_OSD_STATUS_INTERNAL_ERROR;
+    }
+}
+
+template <int D>
+void launch_mixed(Engine& e, const MixedIO& io, cudaStream_t st)
+{
+    const int wf = e.warp_floats();
+    int warps = e.warps_per_cta > 0 ? e.warps_per_cta : 8;
+    while (warps > 1 && static_cast<size_t>(warps) * wf * sizeof(float) > 200 * 1024) --warps;
+    const size_t smem = static_cast<size_t>(warps) * wf * sizeof(float);
+    if (smem > 227 * 1024) throw InvalidArgument("a registered code is too large for the mixed kernel");
+    check_cuda(cudaFuncSetAttribute(bp_mixed_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)),
+               "cudaFuncSetAttribute(bp_mixed)");
+    int ctas = e.ctas;
+    if (ctas <= 0) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bp_mixed_kernel<D>, warps * 32, smem) !=
+                cudaSuccess ||
+            per_sm <= 0)
+            per_sm = 1;
+        ctas = per_sm * device_sm_count();
+    }
+    const size_t need = static_cast<size_t>(ctas) * warps;
+    if (need > e.best_warps) {
+        if (e.d_best) cudaFree(e.d_best);
+        check_cuda(cudaMalloc(&e.d_best, need * 4 * static_cast<size_t>(e.n_max) * sizeof(float)), "cudaMalloc(best)");
+        e.best_warps = need;
+    }
+    MixedIO m = io;
+    m.best = e.d_best;
+    bp_mixed_kernel<D><<<ctas, warps * 32, smem, st>>>(m, wf);
+    check_cuda(cudaGetLastError(), "bp_mixed_kernel launch");
+}
+
+}  // namespace
+}  // namespace sicc
+
+using namespace sicc;
+
+extern "C" {
+
+int sicc_engine_create(const sicc_engine_config_t* config, unsigned long long* out_handle)
+{
+    return guarded([&] {
+        if (!config || !out_handle) throw InvalidArgument("null argument");
+        *out_handle = 0;
+        if (config->max_codewords <= 0 || config->max_llr_floats <= 0)
+            throw InvalidArgument("max_codewords and max_llr_floats must be positive");
+        if (config->max_codes <= 0 || config->max_codes > kMaxCodes) throw InvalidArgument("max_codes must be 1..64");
+        auto e = std::make_shared<Engine>();
+        e->cfg = *config;
+        check_cuda(cudaGetDevice(&e->device), "cudaGetDevice");
+        check_cuda(cudaMalloc(&e->d_order, sizeof(int) * config->max_codewords), "cudaMalloc(order)");
+        check_cuda(cudaMalloc(&e->d_q_start, sizeof(int) * (kMaxCodes + 1)), "cudaMalloc(q_start)");
+        check_cuda(cudaMalloc(&e->d_q_units, sizeof(int) * (kMaxCodes + 1)), "cudaMalloc(q_units)");
+        check_cuda(cudaMalloc(&e->d_counters, sizeof(int) * 2), "cudaMalloc(counters)");
+        check_cuda(cudaMalloc(&e->d_osd_index, sizeof(int) * config->max_codewords), "cudaMalloc(osd index)");
+        check_cuda(cudaMalloc(&e->d_osd_llr, sizeof(float) * config->max_llr_floats), "cudaMalloc(osd rows)");
+        for (auto& ev : e->ev) check_cuda(cudaEventCreate(&ev), "cudaEventCreate(engine)");
+        std::lock_guard<std::mutex> lock(g_mu);
+        *out_handle = ++g_next;
+        g_engines[*out_handle] = e;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_engine_destroy(unsigned long long handle)
+{
+    return guarded([&] {
+        std::shared_ptr<Engine> e;
+        {
+            std::lock_guard<std::mutex> lock(g_mu);
+            auto it = g_engines.find(handle);
+            if (it == g_engines.end()) throw InvalidArgument("invalid engine handle");
+            e = it->second;
+            g_engines.erase(it);
+        }
+        cudaSetDevice(e->device);
+        cudaDeviceSynchronize();
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_engine_add_code(unsigned long long handle, const sicc_engine_code_t* code, int* out_code_id)
+{
+    return guarded([&] {
+        auto e = get(handle);
+        std::lock_guard<std::mutex> lock(e->mu);
+        if (!code || !out_code_id || !code->row_ptr || !code->col_ind) throw InvalidArgument("null argument");
+        if (static_cast<int>(e->codes.size()) >= e->cfg.max_codes) throw InvalidArgument("engine holds max_codes codes");
+        if (code->max_iterations < 1 || code->max_iterations > 255) throw InvalidArgument("max_iterations must be 1..255");
+        check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+        const bool want_osd = code->osd_order >= 0;
+        OsdSettings os;
+        if (want_osd) {
+            os.order = code->osd_order;
+            os.max_flip_positions = code->osd_max_flip_positions;
+            os.max_tests = code->osd_max_tests;
+        }
+        EngineCode ec;
+        ec.code = std::make_unique<DeviceCode>(code->n, code->m, code->row_ptr, code->col_ind, kFlatLayered, nullptr,
+                                               0, want_osd, os);
+        const LayeredView& lv = ec.code->layered_view();
+        if (lv.maxdeg > 16) throw InvalidArgument("the mixed kernel supports row degree <= 16");
+        CodeDesc& d = ec.desc;
+        d.n = code->n;
+        d.k = ec.code->k();
+        d.num_layers = lv.num_layers;
+        d.width = lv.width;
+        d.maxdeg = lv.maxdeg;
+        d.group = lv.group;
+        d.rows_per_lane = lv.rows_per_lane;
+        d.max_iter = code->max_iterations;
+        d.alpha = code->normalization;
+        d.beta = code->offset;
+        d.route_osd = want_osd ? 1 : 0;
+        d.vars = lv.vars;
+        const int n_pad = (d.n + 3) & ~3;
+        int sf = (n_pad + 3 * d.num_layers * d.width + 3) & ~3;
+        if (d.group < 32) sf += ((d.group - sf % 32) + 32) % 32;  // groups of a warp G banks apart
+        d.slot_floats = sf;
+        ec.osd = want_osd;
+        ec.cost = static_cast<long long>(ec.code->edges()) * d.max_iter;
+        e->n_max = std::max(e->n_max, d.n);
+        e->k_max = std::max(e->k_max, d.k);
+        if (want_osd) {
+            e->osd_nmax = std::max(e->osd_nmax, d.n);
+            e->osd_kmax = std::max(e->osd_kmax, d.k);
+        }
+        e->codes.push_back(std::move(ec));
+        e->dirty = true;
+        *out_code_id = static_cast<int>(e->codes.size()) - 1;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_engine_set_launch_shape(unsigned long long handle, int warps_per_cta, int ctas)
+{
+    return guarded([&] {
+        auto e = get(handle);
+        std::lock_guard<std::mutex> lock(e->mu);
+        if (warps_per_cta < 0 || warps_per_cta > 8 || ctas < 0) throw InvalidArgument("warps_per_cta must be 0..8");
+        e->warps_per_cta = warps_per_cta;
+        e->ctas = ctas;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_engine_decode_device(unsigned long long handle, int codewords, const unsigned char* device_code_ids,
+                              const float* device_llr, const long long* device_llr_offsets, unsigned char* device_info,
+                              const long long* device_info_offsets, unsigned char* device_success,
+                              unsigned char* device_used_osd, unsigned char* device_iterations, void* cuda_stream)
+{
+    return guarded([&] {
+        auto e = get(handle);
+        std::lock_guard<std::mutex> lock(e->mu);
+        if (e->codes.empty()) throw InvalidArgument("no code registered");
+        if (codewords <= 0 || codewords > e->cfg.max_codewords) throw InvalidArgument("codewords must be in 1..max_codewords");
+        if (!device_code_ids || !device_llr || !device_llr_offsets || !device_info || !device_info_offsets)
+            throw InvalidArgument("null device pointer");
+        check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+        e->commit();
+        cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+        const int K = static_cast<int>(e->codes.size());
+        check_cuda(cudaEventRecord(e->ev[0], st), "cudaEventRecord");
+        prepare_kernel<<<1, 1024, 0, st>>>(device_code_ids, codewords, e->d_q_code, K, e->d_per_warp, e->d_order,
+                                           e->d_q_start, e->d_q_units, e->d_counters, e->d_counters + 1);
+        check_cuda(cudaGetLastError(), "prepare_kernel launch");
+        check_cuda(cudaEventRecord(e->ev[1], st), "cudaEventRecord");
+        MixedIO io{};
+        io.codes = e->d_codes;
+        io.code_of = device_code_ids;
+        io.llr = device_llr;
+        io.llr_off = device_llr_offsets;
+        io.info = device_info;
+        io.info_off = device_info_offsets;
+        io.success = device_success;
+        io.used_osd = device_used_osd;
+        io.iterations = device_iterations;
+        io.order = e->d_order;
+        io.q_code = e->d_q_code;
+        io.q_start = e->d_q_start;
+        io.q_units = e->d_q_units;
+        io.K = K;
+        io.work = e->d_counters;
+        io.n_max = e->n_max;
+        io.osd_llr = e->d_osd_llr;
+        io.osd_index = e->d_osd_index;
+        io.osd_count = e->d_counters + 1;
+        launch_mixed<16>(*e, io, st);
+        check_cuda(cudaEventRecord(e->ev[2], st), "cudaEventRecord");
+        if (e->osd_nmax > 0) {
+            OsdIO oio{};
+            oio.llr = e->d_osd_llr;
+            oio.index = e->d_osd_index;
+            oio.count_ptr = e->d_counters + 1;
+            oio.out_info = device_info;
+            oio.used_osd = device_used_osd;
+            oio.views = e->d_views;
+            oio.code_of = device_code_ids;
+            oio.llr_off = device_llr_offsets;
+            oio.info_off = device_info_offsets;
+            OsdView shape{};
+            shape.n = e->osd_nmax;
+            shape.k = e->osd_kmax;
+            launch_osd(shape, oio, codewords, st);
+        }
+        check_cuda(cudaEventRecord(e->ev[3], st), "cudaEventRecord");
+        e->timed = true;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_engine_last_ms(unsigned long long handle, float* out_prepare_ms, float* out_bp_ms, float* out_osd_ms)
+{
+    return guarded([&] {
+        auto e = get(handle);
+        std::lock_guard<std::mutex> lock(e->mu);
+        if (!e->timed) throw InvalidArgument("no decode has run");
+        check_cuda(cudaEventSynchronize(e->ev[3]), "cudaEventSynchronize");
+        float a = 0, b = 0, c = 0;
+        cudaEventElapsedTime(&a, e->ev[0], e->ev[1]);
+        cudaEventElapsedTime(&b, e->ev[1], e->ev[2]);
+        cudaEventElapsedTime(&c, e->ev[2], e->ev[3]);
+        if (out_prepare_ms) *out_prepare_ms = a;
+        if (out_bp_ms) *out_bp_ms = b;
+        if (out_osd_ms) *out_osd_ms = c;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+}  // extern "C"

@@ -67,20 +67,24 @@ __device__ __forceinline__ unsigned long long shfl_xor_u64(unsigned long long v,
 
 template <int NW, int KR>
 __global__ void __launch_bounds__(kOsdWarps * 32)
-osd_kernel(OsdView ov, OsdIO io)
+osd_kernel(OsdView ov0, OsdIO io)
 {
     constexpr int KW = (KR + 1) / 2;
     __shared__ OsdSmem<NW, KR> sm_all[kOsdWarps];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     OsdSmem<NW, KR>& s = sm_all[warp];
-    const int n = ov.n, k = ov.k;
     const int count = io.count_ptr ? *io.count_ptr : io.count;
     const int total_warps = gridDim.x * kOsdWarps;
 
     for (int item = blockIdx.x * kOsdWarps + warp; item < count; item += total_warps) {
         const int cw = io.index ? io.index[item] : item;
-        const float* src = io.llr + static_cast<size_t>(item) * n;
+        const OsdView ov = io.views ? io.views[io.code_of[cw]] : ov0;
+        const int n = ov.n, k = ov.k;
+        const float* src = io.llr_off ? io.llr + io.llr_off[cw] : io.llr + static_cast<size_t>(item) * n;
+        uint8_t* info_dst = io.out_info ? (io.info_off ? io.out_info + io.info_off[cw]
+                                                       : io.out_info + static_cast<size_t>(cw) * io.info_stride)
+                                        : nullptr;
         // ---- 1. reliabilities, hard decisions, stable descending sort ----
         // Bitonic sort of 64-bit keys: ascending key = descending |llr|, ties by
         // ascending index (the order of MATLAB's stable sort, cpu_bp_osd_decode.m:194).
@@ -328,7 +332,7 @@ osd_kernel(OsdView ov, OsdIO io)
         for (int j = lane; j < n; j += 32) {
             const int o = s.perm[j];
             const uint8_t bit = static_cast<uint8_t>((pick<NW>(d, j >> 6) >> (j & 63)) & 1ull);
-            if (io.out_info && o < k) io.out_info[static_cast<size_t>(cw) * io.info_stride + o] = bit;
+            if (info_dst && o < k) info_dst[o] = bit;
             if (io.out_code) io.out_code[static_cast<size_t>(cw) * n + o] = bit;
         }
         if (lane == 0) {
@@ -359,6 +363,7 @@ void launch_osd(const OsdView& ov, const OsdIO& io, int max_items, cudaStream_t 
 {
     (void)warps_per_cta;
     if (max_items <= 0) return;
+    // for a mixed-code batch `ov` carries the largest n and k of its codes
     const int nw = (ov.n + 63) / 64;
     const int kr = (ov.k + 31) / 32;
     const int NW = nw <= 1 ? 1 : (nw <= 2 ? 2 : 4);

@@ -108,6 +108,13 @@ struct OsdIO {
     uint8_t* out_code;       // [codewords][n] decoded codeword (optional)
     float* out_metric;       // [codewords] winning metric (optional)
     uint8_t* used_osd;       // [codewords] set to 1 (optional)
+    // mixed-code batches (all null for one code): per item its code's tables,
+    // its posterior row at llr + llr_off[codeword], its info bits at
+    // out_info + info_off[codeword]
+    const OsdView* views;
+    const uint8_t* code_of;  // [codewords] code id
+    const long long* llr_off;
+    const long long* info_off;
 };
 
 }  // namespace sicc

@@ -205,5 +205,6 @@ def gf2_parity_matrix(code: QcCode) -> np.ndarray:
 
 def encode(p_matrix: np.ndarray, info: np.ndarray) -> np.ndarray:
     """Systematic-front encode of info [B][k] (uint8) with P [k][n-k]."""
-    parity = (info.astype(np.int32) @ p_matrix.astype(np.int32)) & 1
+    # float32 products are exact here (sums of at most k <= 2^24 ones) and use BLAS
+    parity = (info.astype(np.float32) @ p_matrix.astype(np.float32)).astype(np.int64) & 1
     return np.concatenate([info.astype(np.uint8), parity.astype(np.uint8)], axis=1)
