@@ -452,29 +452,24 @@ def run_mixed(args, rank, world):
         sel = np.array([w.codes[c].n == n for c in w.code_of])
         fer_by_n[str(n)] = float(fe[sel].mean())
 
-    # plain form: one synchronous launch per request, one decoder per code (the reference's
-    # per-frame CudaBpOsdDecoder::decode_device / CudaBpDecoder::decode_device pattern)
+    # plain form, as the reference decodes a frame (uhd_ldpc_ofdm_link.cpp:3541-3628, 3744-3785): one
+    # decoder per code, one synchronous call per request with device LLRs in and host outputs
     decs = []
     for c in w.codes:
         if engine.osd_supported(c):
-            decs.append(fec.StreamBpOsdDecoder(c, max_batch=512, max_iter=engine.iteration_cap(c.n),
+            decs.append(fec.StreamBpOsdDecoder(c, max_batch=512, min_batch=1, max_iter=engine.iteration_cap(c.n),
                                                normalization=ALPHA, offset=0.0, damping=0.0, min_abs_llr_accept=0.0,
                                                osd_order=OSD_ORDER, osd_max_flip=OSD_FLIP, osd_max_tests=OSD_TESTS))
         else:
             decs.append(fec.CsrBpDecoder.for_code(c, max_batch=512, max_iter=engine.iteration_cap(c.n),
                                                   normalization=ALPHA))
-    d_bits = torch.zeros((512, 2048), dtype=torch.uint8, device="cuda")
 
     def plain_pass():
         for r, ci in enumerate(w.req_code):
             a, b = int(w.req_start[r]), int(w.req_start[r + 1])
-            llr_v = d_llr[int(w.llr_off[a]):]
-            if isinstance(decs[ci], fec.StreamBpOsdDecoder):
-                decs[ci].decode_device_batch(llr_v, d_info[int(w.info_off[a]):], d_ok[a:], d_used[a:], None,
-                                             stream=stream, count=b - a)
-            else:
-                decs[ci].decode_device_batch(llr_v, d_bits, d_ok[a:], None, None, stream=stream, count=b - a)
-            torch.cuda.synchronize()
+            n = w.codes[ci].n
+            llr_v = d_llr[int(w.llr_off[a]): int(w.llr_off[a]) + (b - a) * n].view(b - a, n)
+            decs[ci].decode(llr_v, device=True)  # submit + flush + poll / device-batch call, host outputs
 
     plain_pass()
     t0 = time.perf_counter()
@@ -494,7 +489,9 @@ def run_mixed(args, rank, world):
             "fer_by_length": fer_by_n, "fer": float(fe.mean()),
             "kernel_ms": {"prepare": round(prep_ms, 4), "bp_mixed": round(bp_ms, 4), "osd": round(osd_ms, 4)},
             "plain_one_code_per_launch": {"value": round(plain_mbps, 3), "unit": "Mbit/s",
-                                          "launches_per_pass": int(len(w.req_code)),
+                                          "calls_per_pass": int(len(w.req_code)),
+                                          "api": "per request: cuda_osd_submit_device_codewords+flush+poll_ready or "
+                                                 "cuda_osd_decode_bp_csr_device_batch (host outputs, synchronous)",
                                           "speedup_of_batched": round(value / plain_mbps, 2)},
             "gpu_launches": args.steps * 3, "clocks": clk,
             "roofline": {"bound": "hbm", "kernel": "bp_mixed_kernel<16>",
@@ -504,6 +501,149 @@ def run_mixed(args, rank, world):
                          "traffic": None, "peak_source": peak_kind,
                          "note": "issue-bound; HBM fraction shown per contract"},
             "e2e": None, "cpu_baseline": None}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ serving loop
+SERVE_LOADS = (0.1, 0.3, 0.5, 0.7, 0.8, 0.9, 1.0, 1.2)
+
+
+def run_serve(args, rank, world):
+    """Poisson arrivals of decode requests into the continuous-batching server.
+
+    Requests: bursts of U{1..512} codewords of one of the 15 mixed codes (Eb/N0 ~ U[1,5] dB per codeword),
+    or, with probability 0.3, U{1..17} frames of the 16-QAM OFDM workload (up to 510 codewords of the
+    (1024,512) code) as raw IQ that the server demodulates first.  Protection per request: BP only or
+    BP+OSD with probability 1/2 (OSD where the code has OSD tables: n <= 256, k <= 128).  The peak is the
+    throughput with every request offered at once; the sweep offers Poisson load at fractions of it.
+    Inputs and outputs live in pinned host memory; latency runs from the scheduled arrival to the results
+    on the host.
+    """
+    import torch
+    from sicc_gb300 import channel, codes, engine, ofdm
+    from sicc_gb300.server import Server
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(777 + rank)
+    mixed = codes.mixed_codes()
+    ocode = codes.ofdm_code()
+    t = ofdm.reference_tables(ofdm.OFDM_C3)
+    blocks = t.coded_bits // ocode.n
+
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+
+    # request pools (pinned): 512 codewords per code, 24 frames per SNR point
+    llr_pool, info_pool = [], []
+    for ci, c in enumerate(mixed):
+        info, _, llr = channel.awgn_llrs(c, 512, rng.uniform(1.0, 5.0, 512), seed=9000 + ci)
+        buf = pinned((512, c.n), torch.float32)
+        buf[:] = llr
+        llr_pool.append(buf)
+        info_pool.append(info)
+    iq_pool, iq_info = [], []
+    for i, snr in enumerate(OFDM_SNRS):
+        gen = ofdm.FrameGenerator(t, ocode, seed=600 + i)
+        b = gen.batch(24, snr_db=snr, cfo_subcarriers=0.1, max_offset=200, rayleigh_taps=6)
+        buf = pinned(b.iq.shape, torch.complex64)
+        buf[:] = b.iq
+        iq_pool.append((buf, float(np.float32(np.mean(b.noise_var)))))
+        iq_info.append(b.info)
+    stride = iq_pool[0][0].shape[1]
+
+    srv = Server(hbm_budget_bytes=40 << 30, max_batch_codewords=args.serve_batch,
+                 max_inflight_batches=args.serve_inflight, max_pending_requests=1 << 16)
+    ids = [srv.add_code(c, engine.iteration_cap(c.n), ALPHA, OSD_ORDER if engine.osd_supported(c) else -1,
+                        OSD_FLIP, OSD_TESTS) for c in mixed]
+    ocid = srv.add_code(ocode, OFDM_ITERS, ALPHA, -1)
+    phys = [srv.add_phy(t, ocid, blocks, nv, stride) for _, nv in iq_pool]
+    srv.start()
+
+    # one request list, reused at every load point (outputs are overwritten)
+    n_req = args.serve_requests
+    reqs, truth, info_bits, iq_reqs = [], [], 0, 0
+    for r in range(n_req):
+        prot = int(rng.integers(0, 2))
+        if rng.random() < 0.3:
+            s = int(rng.integers(0, len(OFDM_SNRS)))
+            f = int(rng.integers(1, 18))
+            a = int(rng.integers(0, 24 - f + 1))
+            out = pinned((f * blocks, ocode.k), torch.uint8)
+            reqs.append(srv.request(1, phys[s], iq_pool[s][0][a:a + f], prot, tag=r, out=out))
+            truth.append(iq_info[s][a:a + f].reshape(f * blocks, ocode.k))
+            info_bits += f * blocks * ocode.k
+            iq_reqs += 1
+        else:
+            ci = int(rng.integers(0, len(mixed)))
+            b = int(rng.integers(1, 513))
+            a = int(rng.integers(0, 512 - b + 1))
+            out = pinned((b, mixed[ci].k), torch.uint8)
+            reqs.append(srv.request(0, ids[ci], llr_pool[ci][a:a + b], prot, tag=r, out=out))
+            truth.append(info_pool[ci][a:a + b])
+            info_bits += b * mixed[ci].k
+    in_bytes = sum(int(q[1].nbytes) for q in reqs)
+    out_bytes = sum(int(q[2].nbytes) for q in reqs)
+    at_once = np.zeros(n_req)
+
+    for _ in range(args.warmup):
+        srv.replay(reqs, at_once)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    st0 = srv.stats()
+    walls = []
+    for _ in range(args.steps):
+        res, wall = srv.replay(reqs, at_once)
+        walls.append(wall)
+    st1 = srv.stats()
+    peak_s = statistics.median(walls) * 1e-6
+    peak_mbps = info_bits / peak_s / 1e6
+    fe = [int(np.any(q[2] != tr, axis=1).sum()) for q, tr in zip(reqs, truth)]
+    cw_total = sum(q[2].shape[0] for q in reqs)
+    sweep = []
+    for load in SERVE_LOADS:
+        rate = load * n_req / peak_s  # requests per second
+        gaps = rng.exponential(1.0 / rate, n_req)
+        arr = np.cumsum(gaps) * 1e6
+        arr -= arr[0]
+        b0 = srv.stats()
+        res, wall = srv.replay(reqs, arr)
+        b1 = srv.stats()
+        lat = np.array([d.latency_us for d in res]) * 1e-3
+        sweep.append({"load": load, "offered_mbps": round(load * peak_mbps, 2),
+                      "achieved_mbps": round(info_bits / (wall * 1e-6) / 1e6, 2),
+                      "p50_ms": round(float(np.percentile(lat, 50)), 4),
+                      "p99_ms": round(float(np.percentile(lat, 99)), 4),
+                      "p99_9_ms": round(float(np.percentile(lat, 99.9)), 4),
+                      "mean_batch_codewords": round((b1.codewords - b0.codewords) / max(b1.batches - b0.batches, 1), 1),
+                      "batches": int(b1.batches - b0.batches)})
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    p80 = next(x for x in sweep if x["load"] == 0.8)
+    launches = int(st1.batches - st0.batches) * 3 + args.steps * iq_reqs * 2
+    line = {"metric": "served info-bit Mbps (Poisson mixed-code + OFDM IQ requests), p50/p99/p99.9 latency",
+            "value": round(peak_mbps, 3), "unit": "Mbit/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(peak_s * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded BPSK/AWGN LLRs; seeded OFDM IQ: 6-tap Rayleigh, CFO 0.1 sc, SNR 8/12/16 dB)",
+            "config": {"workload": "serve_mixed", "requests": n_req, "iq_requests": iq_reqs,
+                       "codewords": cw_total, "info_bits": info_bits, "hbm_budget_gb": 40,
+                       "max_batch_codewords": args.serve_batch, "inflight_batches": args.serve_inflight,
+                       "burst": "U{1..512} codewords or U{1..17} OFDM frames (p=0.3)",
+                       "protection": "BP or BP+OSD (p=1/2); OSD order 2 on n <= 256, k <= 128",
+                       "step": "every request offered at once (peak); then one Poisson pass per load point",
+                       "l2": "inputs copied host->device every request (pinned host pools)"},
+            "fer": round(sum(fe) / cw_total, 5), "load_sweep": sweep,
+            "p99_ms_at_80pct_load": p80["p99_ms"],
+            "server": {"batches": int(st.batches), "busy_rejections": int(st.busy_rejections),
+                       "arena_peak_mb": round(st.arena_bytes_peak / 1e6, 1)},
+            "gpu_launches": launches, "clocks": clk, "roofline": None,
+            "e2e": {"value": round(peak_mbps, 3), "unit": "Mbit/s", "h2d_bytes_per_step": in_bytes,
+                    "d2h_bytes_per_step": out_bytes},
+            "cpu_baseline": None}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -554,7 +694,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=BATCH, help="frames per batch (profiling runs only)")
     ap.add_argument("--resident", type=int, default=RESIDENT_BATCHES, help="resident batches per Eb/N0")
-    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "ofdm_rx_1024_512", "mixed_100k"])
+    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "ofdm_rx_1024_512", "mixed_100k", "serve_mixed"])
+    ap.add_argument("--serve-requests", type=int, default=2500)
+    ap.add_argument("--serve-batch", type=int, default=16384, help="codewords per server launch")
+    ap.add_argument("--serve-inflight", type=int, default=2, help="batches overlapping on the device")
     ap.add_argument("--mixed-codewords", type=int, default=100_000)
     ap.add_argument("--ofdm-frames", type=int, default=OFDM_FRAMES)
     args = ap.parse_args()
@@ -568,6 +711,8 @@ def main():
         run_ofdm(args, rank, world)
     elif args.workload == "mixed_100k":
         run_mixed(args, rank, world)
+    elif args.workload == "serve_mixed":
+        run_serve(args, rank, world)
     else:
         run_ours(args, rank, world)
 

@@ -14,10 +14,10 @@
  * Codeword c of a batch: LLRs at llr + llr_offset[c] (n floats of its code),
  * information bits written at info + info_offset[c] (k bytes).  All batch
  * arrays are device memory; calls are asynchronous on the given stream.
- * LLR offsets must stay below max_llr_floats (the OSD hand-off rows use the
- * same offsets in the engine's scratch); codewords whose code id is not a
- * registered code are skipped and their outputs left untouched.  Calls on one
- * handle must not overlap on the GPU.
+ * max_llr_floats bounds the sum of n over a batch's codewords (the OSD
+ * hand-off scratch); codewords whose code id is not a registered code are
+ * skipped and their outputs left untouched.  Calls on one handle must not
+ * overlap on the GPU.
  */
 #ifndef SICC_ENGINE_H
 #define SICC_ENGINE_H
@@ -58,6 +58,16 @@ SICC_API int sicc_engine_decode_device(unsigned long long handle, int codewords,
                                        unsigned char* device_info, const long long* device_info_offsets,
                                        unsigned char* device_success, unsigned char* device_used_osd,
                                        unsigned char* device_iterations, void* cuda_stream);
+/* As sicc_engine_decode_device with a protection level per codeword
+ * (device_protection[c] = 1: a failed syndrome falls back to OSD when the
+ * code has OSD tables; 0: BP only). */
+SICC_API int sicc_engine_decode_device_protected(unsigned long long handle, int codewords,
+                                                 const unsigned char* device_code_ids,
+                                                 const unsigned char* device_protection, const float* device_llr,
+                                                 const long long* device_llr_offsets, unsigned char* device_info,
+                                                 const long long* device_info_offsets, unsigned char* device_success,
+                                                 unsigned char* device_used_osd, unsigned char* device_iterations,
+                                                 void* cuda_stream);
 /* Kernel durations (ms) of the last decode: prepare (sort), BP, OSD. */
 SICC_API int sicc_engine_last_ms(unsigned long long handle, float* out_prepare_ms, float* out_bp_ms,
                                  float* out_osd_ms);

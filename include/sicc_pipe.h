@@ -100,7 +100,16 @@ typedef struct sicc_pipe_sync_record_t {
 SICC_API int sicc_pipe_demod_batch(unsigned long long handle, const float* device_iq, long long stride,
                                    int sample_count, int frames, float* device_llr,
                                    sicc_pipe_sync_record_t* device_sync, void* cuda_stream);
-/* Kernel durations (ms) of the last sicc_pipe_demod_batch call: sync, demod. */
+/* As sicc_pipe_demod_batch for frames scattered in device memory: frame f is
+ * read from device_iq + 2*device_frame_offsets[f] (offsets in complex
+ * samples, each frame holding sample_count samples) and its LLRs written to
+ * device_llr + device_llr_offsets[f] (offsets in floats).  device_sync is
+ * required.  Used to demodulate the frames of many requests in one launch. */
+SICC_API int sicc_pipe_demod_gather(unsigned long long handle, const float* device_iq,
+                                    const long long* device_frame_offsets, int sample_count, int frames,
+                                    float* device_llr, const long long* device_llr_offsets,
+                                    sicc_pipe_sync_record_t* device_sync, void* cuda_stream);
+/* Kernel durations (ms) of the last sicc_pipe_demod_batch / _gather call: sync, demod. */
 SICC_API int sicc_pipe_last_batch_ms(unsigned long long handle, float* out_sync_ms, float* out_demod_ms);
 
 #ifdef __cplusplus

@@ -44,6 +44,7 @@ struct MixedIO {
     uint8_t* success;
     uint8_t* used_osd;
     uint8_t* iterations;
+    const uint8_t* protect;      // [count] 1 = OSD fallback allowed (null: every codeword of an OSD code)
     const int* order;            // [count] codeword indices grouped by code, queue order
     const int* q_code;           // [K] code id at queue position q
     const int* q_start;          // [K+1] first entry of queue position q in `order`
@@ -52,16 +53,19 @@ struct MixedIO {
     int* work;                   // unit counter
     float* best;                 // [warps][4][n_max] best-syndrome posteriors (global scratch)
     int n_max;
-    float* osd_llr;              // same layout as llr (llr_off)
-    int* osd_index;
+    float* osd_llr;              // compact rows of the codewords handed to OSD
+    int* osd_index;              // [items] codeword of each row
+    long long* osd_rowoff;       // [items] float offset of each row in osd_llr
     int* osd_count;
+    unsigned long long* osd_floats;  // row allocation counter
 };
 
 // prepare: counts per code, queue-ordered starts, units, scatter into `order`.
 __global__ void __launch_bounds__(1024)
 prepare_kernel(const uint8_t* __restrict__ code_of, int count, const int* __restrict__ q_code, int K,
                const int* __restrict__ per_warp, int* __restrict__ order, int* __restrict__ q_start,
-               int* __restrict__ q_units, int* __restrict__ work, int* __restrict__ osd_count)
+               int* __restrict__ q_units, int* __restrict__ work, int* __restrict__ osd_count,
+               unsigned long long* __restrict__ osd_floats)
 {
     __shared__ int cnt[kMaxCodes], fill[kMaxCodes], pos_of_code[kMaxCodes];
     for (int i = threadIdx.x; i < kMaxCodes; i += blockDim.x) {
@@ -87,6 +91,7 @@ prepare_kernel(const uint8_t* __restrict__ code_of, int count, const int* __rest
         q_units[K] = u;
         *work = 0;
         *osd_count = 0;
+        *osd_floats = 0ull;
     }
     __syncthreads();
     for (int i = threadIdx.x; i < count; i += blockDim.x) {
@@ -230,11 +235,18 @@ bp_mixed_kernel(MixedIO io, int warp_floats)
                 }
                 uint8_t* dst = io.info + io.info_off[cw];
                 for (int i = gl; i < d.k; i += G) dst[i] = app[i] < 0.0f ? 1 : 0;
-                if (!ok && d.route_osd) {
-                    __syncwarp(gmask);  // best written by other lanes of the group
-                    float* o = io.osd_llr + io.llr_off[cw];
+                if (!ok && d.route_osd && (io.protect == nullptr || io.protect[cw])) {
+                    unsigned long long off = 0ull;
+                    if (gl == 0) {
+                        const int it = atomicAdd(io.osd_count, 1);
+                        off = atomicAdd(io.osd_floats, static_cast<unsigned long long>(n));
+                        io.osd_index[it] = cw;
+                        io.osd_rowoff[it] = static_cast<long long>(off);
+                    }
+                    const unsigned lo = __shfl_sync(gmask, static_cast<unsigned>(off), sub * G);
+                    const unsigned hi = __shfl_sync(gmask, static_cast<unsigned>(off >> 32), sub * G);
+                    float* o = io.osd_llr + ((static_cast<unsigned long long>(hi) << 32) | lo);
                     for (int i = gl; i < n; i += G) o[i] = best[i];
-                    if (gl == 0) io.osd_index[atomicAdd(io.osd_count, 1)] = cw;
                 }
                 active = false;
             }
@@ -264,7 +276,8 @@ struct Engine {
     int* d_q_start = nullptr;
     int* d_q_units = nullptr;
     int* d_order = nullptr;
-    int* d_counters = nullptr;  // [0] work, [1] osd count
+    int* d_counters = nullptr;  // [0] work, [1] osd count, [2..3] osd float counter (64-bit)
+    long long* d_osd_rowoff = nullptr;
     int* d_osd_index = nullptr;
     float* d_osd_llr = nullptr;
     float* d_best = nullptr;
@@ -278,7 +291,7 @@ struct Engine {
         for (void* p : {static_cast<void*>(d_codes), static_cast<void*>(d_views), static_cast<void*>(d_per_warp),
                         static_cast<void*>(d_q_code), static_cast<void*>(d_q_start), static_cast<void*>(d_q_units),
                         static_cast<void*>(d_order), static_cast<void*>(d_counters), static_cast<void*>(d_osd_index),
-                        static_cast<void*>(d_osd_llr), static_cast<void*>(d_best)})
+                        static_cast<void*>(d_osd_llr), static_cast<void*>(d_best), static_cast<void*>(d_osd_rowoff)})
             if (p) cudaFree(p);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
@@ -400,7 +413,8 @@ int sicc_engine_create(const sicc_engine_config_t* config, unsigned long long* o
         check_cuda(cudaMalloc(&e->d_order, sizeof(int) * config->max_codewords), "cudaMalloc(order)");
         check_cuda(cudaMalloc(&e->d_q_start, sizeof(int) * (kMaxCodes + 1)), "cudaMalloc(q_start)");
         check_cuda(cudaMalloc(&e->d_q_units, sizeof(int) * (kMaxCodes + 1)), "cudaMalloc(q_units)");
-        check_cuda(cudaMalloc(&e->d_counters, sizeof(int) * 2), "cudaMalloc(counters)");
+        check_cuda(cudaMalloc(&e->d_counters, sizeof(int) * 4), "cudaMalloc(counters)");
+        check_cuda(cudaMalloc(&e->d_osd_rowoff, sizeof(long long) * config->max_codewords), "cudaMalloc(osd rows)");
         check_cuda(cudaMalloc(&e->d_osd_index, sizeof(int) * config->max_codewords), "cudaMalloc(osd index)");
         check_cuda(cudaMalloc(&e->d_osd_llr, sizeof(float) * config->max_llr_floats), "cudaMalloc(osd rows)");
         for (auto& ev : e->ev) check_cuda(cudaEventCreate(&ev), "cudaEventCreate(engine)");
@@ -493,10 +507,12 @@ int sicc_engine_set_launch_shape(unsigned long long handle, int warps_per_cta, i
     });
 }
 
-int sicc_engine_decode_device(unsigned long long handle, int codewords, const unsigned char* device_code_ids,
-                              const float* device_llr, const long long* device_llr_offsets, unsigned char* device_info,
-                              const long long* device_info_offsets, unsigned char* device_success,
-                              unsigned char* device_used_osd, unsigned char* device_iterations, void* cuda_stream)
+int sicc_engine_decode_device_protected(unsigned long long handle, int codewords, const unsigned char* device_code_ids,
+                                        const unsigned char* device_protection, const float* device_llr,
+                                        const long long* device_llr_offsets, unsigned char* device_info,
+                                        const long long* device_info_offsets, unsigned char* device_success,
+                                        unsigned char* device_used_osd, unsigned char* device_iterations,
+                                        void* cuda_stream)
 {
     return guarded([&] {
         auto e = get(handle);
@@ -511,7 +527,8 @@ int sicc_engine_decode_device(unsigned long long handle, int codewords, const un
         const int K = static_cast<int>(e->codes.size());
         check_cuda(cudaEventRecord(e->ev[0], st), "cudaEventRecord");
         prepare_kernel<<<1, 1024, 0, st>>>(device_code_ids, codewords, e->d_q_code, K, e->d_per_warp, e->d_order,
-                                           e->d_q_start, e->d_q_units, e->d_counters, e->d_counters + 1);
+                                           e->d_q_start, e->d_q_units, e->d_counters, e->d_counters + 1,
+                                           reinterpret_cast<unsigned long long*>(e->d_counters + 2));
         check_cuda(cudaGetLastError(), "prepare_kernel launch");
         check_cuda(cudaEventRecord(e->ev[1], st), "cudaEventRecord");
         MixedIO io{};
@@ -524,6 +541,7 @@ int sicc_engine_decode_device(unsigned long long handle, int codewords, const un
         io.success = device_success;
         io.used_osd = device_used_osd;
         io.iterations = device_iterations;
+        io.protect = device_protection;
         io.order = e->d_order;
         io.q_code = e->d_q_code;
         io.q_start = e->d_q_start;
@@ -533,7 +551,9 @@ int sicc_engine_decode_device(unsigned long long handle, int codewords, const un
         io.n_max = e->n_max;
         io.osd_llr = e->d_osd_llr;
         io.osd_index = e->d_osd_index;
+        io.osd_rowoff = e->d_osd_rowoff;
         io.osd_count = e->d_counters + 1;
+        io.osd_floats = reinterpret_cast<unsigned long long*>(e->d_counters + 2);
         launch_mixed<16>(*e, io, st);
         check_cuda(cudaEventRecord(e->ev[2], st), "cudaEventRecord");
         if (e->osd_nmax > 0) {
@@ -545,7 +565,7 @@ int sicc_engine_decode_device(unsigned long long handle, int codewords, const un
             oio.used_osd = device_used_osd;
             oio.views = e->d_views;
             oio.code_of = device_code_ids;
-            oio.llr_off = device_llr_offsets;
+            oio.row_off = e->d_osd_rowoff;
             oio.info_off = device_info_offsets;
             OsdView shape{};
             shape.n = e->osd_nmax;
@@ -556,6 +576,16 @@ int sicc_engine_decode_device(unsigned long long handle, int codewords, const un
         e->timed = true;
         return CUDA_OSD_STATUS_OK;
     });
+}
+
+int sicc_engine_decode_device(unsigned long long handle, int codewords, const unsigned char* device_code_ids,
+                              const float* device_llr, const long long* device_llr_offsets, unsigned char* device_info,
+                              const long long* device_info_offsets, unsigned char* device_success,
+                              unsigned char* device_used_osd, unsigned char* device_iterations, void* cuda_stream)
+{
+    return sicc_engine_decode_device_protected(handle, codewords, device_code_ids, nullptr, device_llr,
+                                               device_llr_offsets, device_info, device_info_offsets, device_success,
+                                               device_used_osd, device_iterations, cuda_stream);
 }
 
 int sicc_engine_last_ms(unsigned long long handle, float* out_prepare_ms, float* out_bp_ms, float* out_osd_ms)

@@ -1,6 +1,6 @@
 // OFDM receive kernels for sm_103a.
 //
-// sync_kernel (one CTA per frame) restates the CPU receiver's frame search
+// sync_kernel (one thread-block cluster per frame) restates the CPU receiver's frame search
 // (uhd_ldpc_ofdm_link.cpp:5123-5329): Schmidl-Cox metric
 //   P(d) = sum_{i<L} conj(x[d+i]) x[d+i+L],  E1 = sum |x[d+i]|^2,  E2 = sum |x[d+i+L]|^2,
 //   metric(d) = |P|^2 / max(E1*E2, 1e-18);
@@ -10,7 +10,8 @@
 // passes of 256 x 17 from a shared-memory copy of the samples: each pass
 // computes the window sums at 256 chunk starts warp-cooperatively and slides
 // them 17 candidates per thread (the odd chunk keeps shared-memory reads on
-// distinct banks).
+// distinct banks).  The passes of a frame are spread over the CTAs of its
+// cluster and resolved through distributed shared memory.
 //
 // demod_kernel (grid = frames x data-symbol groups) fuses the demodulator of
 // gpu_ofdm_pipeline.cu:566-672 / uhd_ldpc_ofdm_link.cpp:5350-5521: CFO
@@ -27,6 +28,10 @@
 #include <algorithm>
 #include <cfloat>
 
+#include <cooperative_groups.h>
+
+namespace cg = cooperative_groups;
+
 namespace sicc {
 
 namespace {
@@ -36,6 +41,7 @@ constexpr int kSyncChunk = 17;
 constexpr int kSyncPass = kSyncThreads * kSyncChunk;
 constexpr int kMaxRefine = 1024;  // 2 * radius + 1
 constexpr int kMaxRadius = 511;
+constexpr int kSyncMaxCluster = 8;  // portable cluster size
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
@@ -60,42 +66,86 @@ __device__ __forceinline__ float warp_sum(float v)
 
 }  // namespace
 
+// One search result per CTA, published to the cluster's rank 0 through
+// distributed shared memory.
+struct PassResult {
+    int key;      // mode 0: earliest successful candidate (INT_MAX: none); mode 1: position of the maximum (-1: none)
+    int start;    // mode 0: refined start
+    float fine;   // mode 0: refined metric; mode 1: the maximum coarse metric
+    float coarse; // mode 0: coarse metric at the candidate
+};
+
+// Full-preamble correlation metric of candidate dd, one warp: lane-strided
+// products summed per lane, then a butterfly sum.  Samples come from the
+// shared window when it covers them (win[i] = x[wbase + i]).
+__device__ __forceinline__ float fine_metric(const float2* __restrict__ x, const float2* win, int wbase, int wlen, int dd,
+                                             const float2* __restrict__ preamble, int pre, float pre_energy, int lane)
+{
+    float cr = 0.f, ci = 0.f, eng = 0.f;
+    const bool local = dd >= wbase && dd + pre <= wbase + wlen;
+    for (int i = lane; i < pre; i += 32) {
+        const float2 y = local ? win[dd - wbase + i] : x[dd + i];
+        const float2 q = preamble[i];
+        const float2 c = cmulconj(y, q);
+        cr += c.x;
+        ci += c.y;
+        eng += cnorm(y);
+    }
+    cr = warp_sum(cr);
+    ci = warp_sum(ci);
+    eng = warp_sum(eng);
+    return (cr * cr + ci * ci) / fmaxf(eng * pre_energy, 1e-18f);
+}
+
+// Frame search, one thread-block cluster per frame: CTA r of a cluster of C
+// scans passes r, r + C, ... of 4352 candidates each and stops at its first
+// pass holding a successful candidate; rank 0 then takes the earliest result
+// (mode 0) or the first global maximum (mode 1) over the cluster, refines it
+// (mode 1), computes the CFO and writes the record.  Within a pass every
+// threshold crossing is refined at once: the fine metric of each position
+// within +-radius of any crossing is computed once (one warp per position),
+// then each crossing takes the first maximum over its window (starting from
+// 0, strict >) and the earliest crossing whose maximum reaches the threshold
+// wins -- the outcome of the CPU receiver's sequential retry loop.
 __global__ void __launch_bounds__(kSyncThreads)
-sync_kernel(const float2* __restrict__ samples, long long stride, const int* __restrict__ counts, int count,
-            const float2* __restrict__ preamble, SyncParams p, SyncOut* __restrict__ out)
+sync_kernel(const float2* __restrict__ samples, long long stride, const long long* __restrict__ frame_off,
+            const int* __restrict__ counts, int count, const float2* __restrict__ preamble, SyncParams p,
+            SyncOut* __restrict__ out)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* win = reinterpret_cast<float2*>(smem_raw);                 // [kSyncPass + pre_len]
     float* metric = reinterpret_cast<float*>(win + kSyncPass + p.pre_len);  // [kSyncPass]
     float4* chunk = reinterpret_cast<float4*>(metric + kSyncPass);     // [kSyncThreads] P.re, P.im, E1, E2
-    // fine (full-preamble) metric of every candidate of the pass and its
-    // refinement margins, computed at most once: consecutive threshold
-    // crossings share most of their refinement windows
     float* memo = reinterpret_cast<float*>(chunk + kSyncThreads);       // [kSyncPass + 2 * kMaxRadius]
     __shared__ float red[4][kSyncThreads / 32];
     __shared__ float rmetric[kMaxRefine];
-    __shared__ int s_best;
-    __shared__ float s_bestm;
+    __shared__ int s_key[kSyncThreads / 32];
+    __shared__ PassResult s_res;
+    __shared__ PassResult s_final;
 
-    const int f = blockIdx.x;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int C = static_cast<int>(cluster.num_blocks());
+    const int rank = static_cast<int>(cluster.block_rank());
+    const int f = blockIdx.x / C;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const float2* x = samples + static_cast<long long>(f) * stride;
+    const float2* x = samples + (frame_off ? frame_off[f] : static_cast<long long>(f) * stride);
     const int avail = counts ? counts[f] : count;
-    const int L = p.half_len, pre = p.pre_len;
-    SyncOut res{0, -1, 0.0f, 0.0f, 0.0f, -1};
+    const int L = p.half_len, pre = p.pre_len, R = p.radius;
     int limit = avail - pre + 1;
     if (p.max_search > 0) limit = min(limit, p.max_search + 1);
 
-    float gbest_m = -1.0f;  // global-maximum mode
-    int gbest_d = -1;
-    int coarse = -1;
-    float coarse_m = 0.0f;
-    bool done = (limit <= 0);
+    if (tid == 0) {
+        s_res.key = p.mode == 1 ? -1 : 0x7fffffff;
+        s_res.start = -1;
+        s_res.fine = -1.0f;
+        s_res.coarse = 0.0f;
+    }
+    __syncthreads();
 
-    for (int base = 0; !done && base < limit; base += kSyncPass) {
+    for (int pass = rank; pass * kSyncPass < limit; pass += C) {
+        const int base = pass * kSyncPass;
         const int span = min(kSyncPass + pre, avail - base);
         for (int i = tid; i < kSyncPass + pre; i += kSyncThreads) win[i] = (i < span) ? x[base + i] : make_float2(0.f, 0.f);
-        for (int i = tid; i < kSyncPass + 2 * kMaxRadius; i += kSyncThreads) memo[i] = -1.0f;
         __syncthreads();
         // window sums at chunk starts, one warp per chunk
         for (int t = warp; t < kSyncThreads; t += kSyncThreads / 32) {
@@ -133,7 +183,7 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const int* __r
         }
         __syncthreads();
         if (p.mode == 1) {
-            // global maximum, first occurrence (strict >)
+            // maximum of the pass, first occurrence (strict >)
             float bm = -1.0f;
             int bd = 0x7fffffff;
             for (int c = 0; c < kSyncChunk; ++c) {
@@ -152,105 +202,107 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const int* __r
                 for (int w = 0; w < kSyncThreads / 32; ++w) {
                     const float m = red[0][w];
                     const int d = __float_as_int(red[1][w]);
-                    if (m > gbest_m || (m == gbest_m && base + d < gbest_d)) { gbest_m = m; gbest_d = base + d; }
+                    if (d == 0x7fffffff) continue;  // no valid candidate in that warp's chunks
+                    if (m > s_res.fine || (m == s_res.fine && base + d < s_res.key)) {
+                        s_res.fine = m;
+                        s_res.key = base + d;
+                    }
                 }
             }
             __syncthreads();
             continue;
         }
-        // earliest crossing in this pass; refine each crossing in order until one succeeds
-        int from = 0;
-        while (true) {
-            int first = 0x7fffffff;
-            for (int c = 0; c < kSyncChunk; ++c) {
-                const int d = tid * kSyncChunk + c;
-                if (d >= from && metric[d] >= p.threshold) { first = min(first, d); break; }
+        // positions within +-R of a crossing of this pass: memo index i <-> sample x = base - R + i
+        const int mspan = kSyncPass + 2 * R;
+        {
+            const int seg = (mspan + kSyncThreads - 1) / kSyncThreads;
+            const int i0 = tid * seg, i1 = min(mspan, i0 + seg);
+            auto crossing = [&](int y) -> int {  // memo index y holds candidate d = y - R
+                const int d = y - R;
+                return (d >= 0 && d < kSyncPass && metric[d] >= p.threshold) ? 1 : 0;
+            };
+            int cnt = 0;
+            if (i0 < i1)
+                for (int y = i0 - R; y <= i0 + R; ++y) cnt += crossing(y);
+            for (int i = i0; i < i1; ++i) {
+                const int xs = base - R + i;
+                memo[i] = (cnt > 0 && xs >= 0 && xs <= avail - pre) ? -2.0f : -1.0f;
+                cnt += crossing(i + R + 1) - crossing(i - R);
             }
-            first = __reduce_min_sync(0xffffffffu, static_cast<unsigned>(first));
-            if (lane == 0) red[0][warp] = __int_as_float(first);
-            __syncthreads();
-            if (tid == 0) {
-                int m = 0x7fffffff;
-                for (int w = 0; w < kSyncThreads / 32; ++w) m = min(m, __float_as_int(red[0][w]));
-                s_best = m;
-            }
-            __syncthreads();
-            const int d = s_best;
-            __syncthreads();
-            if (d == 0x7fffffff) break;  // next pass
-            // refine around base + d over [lo, hi]
-            const int cand = base + d;
-            const int lo = max(0, cand - p.radius);
-            const int hi = min(avail - pre, cand + p.radius);
-            if (tid == 0) { s_best = cand; s_bestm = 0.0f; }
-            __syncthreads();
-            const int mbase = base - kMaxRadius;  // memo index of candidate dd is dd - mbase
-            for (int dd = lo + warp; dd <= hi; dd += kSyncThreads / 32) {
-                if (memo[dd - mbase] >= 0.0f) continue;  // already evaluated for an earlier crossing
-                float cr = 0.f, ci = 0.f, eng = 0.f;
-                for (int i = lane; i < pre; i += 32) {
-                    const float2 y = x[dd + i], q = preamble[i];
-                    const float2 c = cmulconj(y, q);
-                    cr += c.x;
-                    ci += c.y;
-                    eng += cnorm(y);
-                }
-                cr = warp_sum(cr);
-                ci = warp_sum(ci);
-                eng = warp_sum(eng);
-                if (lane == 0) memo[dd - mbase] = (cr * cr + ci * ci) / fmaxf(eng * p.pre_energy, 1e-18f);
-            }
-            __syncthreads();
-            if (tid == 0) {
-                float bm = 0.0f;
-                int bd = cand;
-                for (int dd = lo; dd <= hi; ++dd) {
-                    const float m = memo[dd - mbase];
-                    if (m > bm) { bm = m; bd = dd; }
-                }
-                s_best = bd;
-                s_bestm = bm;
-            }
-            __syncthreads();
-            if (s_bestm >= p.threshold) {
-                coarse = cand;
-                coarse_m = metric[d] >= 0.0f ? metric[d] : 0.0f;
-                res.start = s_best;
-                res.fine = s_bestm;
-                res.found = (p.frame_len > 0 && s_best + p.frame_len > avail) ? 2 : 1;
-                done = true;
-                break;
-            }
-            from = d + 1;
         }
         __syncthreads();
+        for (int i = warp; i < mspan; i += kSyncThreads / 32) {
+            if (memo[i] != -2.0f) continue;
+            const float m = fine_metric(x, win, base, kSyncPass + pre, base - R + i, preamble, pre, p.pre_energy, lane);
+            if (lane == 0) memo[i] = m;
+        }
+        __syncthreads();
+        // earliest crossing of the pass whose window maximum reaches the threshold
+        int first = 0x7fffffff, fstart = -1;
+        float fbm = 0.0f;
+        for (int c = 0; c < kSyncChunk; ++c) {
+            const int d = tid * kSyncChunk + c;
+            if (!(metric[d] >= p.threshold)) continue;
+            const int cand = base + d;
+            const int lo = max(0, cand - R);
+            const int hi = min(avail - pre, cand + R);
+            float bm = 0.0f;
+            int bd = cand;
+            for (int dd = lo; dd <= hi; ++dd) {
+                const float m = memo[dd - base + R];
+                if (m > bm) { bm = m; bd = dd; }
+            }
+            if (bm >= p.threshold) { first = d; fstart = bd; fbm = bm; break; }
+        }
+        const int wmin = __reduce_min_sync(0xffffffffu, static_cast<unsigned>(first));
+        if (lane == 0) s_key[warp] = wmin;
+        __syncthreads();
+        int bmin = 0x7fffffff;
+        for (int w = 0; w < kSyncThreads / 32; ++w) bmin = min(bmin, s_key[w]);
+        if (bmin != 0x7fffffff && first == bmin) {
+            s_res.key = base + first;
+            s_res.start = fstart;
+            s_res.fine = fbm;
+            s_res.coarse = metric[first];
+        }
+        __syncthreads();
+        if (bmin != 0x7fffffff) break;  // later passes of this CTA come after
     }
 
-    if (p.mode == 1) {  // broadcast the global maximum found by thread 0
-        __syncthreads();
-        if (tid == 0) { s_best = gbest_d; s_bestm = gbest_m; }
-        __syncthreads();
-        gbest_d = s_best;
-        gbest_m = s_bestm;
-        __syncthreads();
-    }
-    if (p.mode == 1 && gbest_d >= 0 && gbest_m >= p.threshold) {
-        const int cand = gbest_d;
-        const int lo = max(0, cand - p.radius);
-        const int hi = min(limit - 1, cand + p.radius);
-        for (int dd = lo + warp; dd <= hi; dd += kSyncThreads / 32) {
-            float cr = 0.f, ci = 0.f, eng = 0.f;
-            for (int i = lane; i < pre; i += 32) {
-                const float2 y = x[dd + i], q = preamble[i];
-                const float2 c = cmulconj(y, q);
-                cr += c.x;
-                ci += c.y;
-                eng += cnorm(y);
+    // rank 0 gathers the cluster's results
+    cluster.sync();
+    if (rank == 0 && tid == 0) {
+        PassResult best = s_res;
+        for (int r = 1; r < C; ++r) {
+            const PassResult o = *cluster.map_shared_rank(&s_res, r);
+            if (p.mode == 1) {
+                if (o.key >= 0 && (o.fine > best.fine || (o.fine == best.fine && (best.key < 0 || o.key < best.key))))
+                    best = o;
+            } else if (o.key < best.key) {
+                best = o;
             }
-            cr = warp_sum(cr);
-            ci = warp_sum(ci);
-            eng = warp_sum(eng);
-            if (lane == 0) rmetric[dd - lo] = (cr * cr + ci * ci) / fmaxf(eng * p.pre_energy, 1e-18f);
+        }
+        s_final = best;
+    }
+    cluster.sync();  // remote shared memory stays valid until every read is done
+    if (rank != 0) return;
+
+    SyncOut res{0, -1, 0.0f, 0.0f, 0.0f, -1};
+    if (p.mode == 0) {
+        if (s_final.key != 0x7fffffff) {
+            res.coarse_start = s_final.key;
+            res.coarse = s_final.coarse >= 0.0f ? s_final.coarse : 0.0f;
+            res.start = s_final.start;
+            res.fine = s_final.fine;
+            res.found = (p.frame_len > 0 && res.start + p.frame_len > avail) ? 2 : 1;
+        }
+    } else if (s_final.key >= 0 && s_final.fine >= p.threshold) {
+        const int cand = s_final.key;
+        const int lo = max(0, cand - R);
+        const int hi = min(limit - 1, cand + R);
+        for (int dd = lo + warp; dd <= hi; dd += kSyncThreads / 32) {
+            const float m = fine_metric(x, win, 0, 0, dd, preamble, pre, p.pre_energy, lane);
+            if (lane == 0) rmetric[dd - lo] = m;
         }
         __syncthreads();
         if (tid == 0) {
@@ -258,18 +310,16 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const int* __r
             int bd = cand;
             for (int dd = lo; dd <= hi; ++dd)
                 if (rmetric[dd - lo] > bm) { bm = rmetric[dd - lo]; bd = dd; }
-            s_best = bd;
-            s_bestm = bm;
+            s_res.start = bd;
+            s_res.fine = bm;
         }
         __syncthreads();
-        coarse = cand;
-        coarse_m = gbest_m;
-        if (s_bestm >= p.threshold) {
-            res.start = s_best;
-            res.fine = s_bestm;
+        res.coarse_start = cand;
+        res.coarse = s_final.fine;
+        res.fine = s_res.fine;
+        if (s_res.fine >= p.threshold) {
+            res.start = s_res.start;
             res.found = 1;
-        } else {
-            res.fine = s_bestm;
         }
     }
 
@@ -291,15 +341,12 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const int* __r
             res.cfo_hz = atan2f(si, sr) * p.sample_rate / (2.0f * 3.14159265358979323846f * static_cast<float>(L));
         }
     }
-    if (tid == 0) {
-        res.coarse = coarse_m;
-        res.coarse_start = coarse;
-        out[f] = res;
-    }
+    if (tid == 0) out[f] = res;
 }
 
 void launch_sync(const float2* samples, long long stride, const int* counts, int count, int frames,
-                 const float2* preamble, const SyncParams& p, SyncOut* out, cudaStream_t st)
+                 const float2* preamble, const SyncParams& p, SyncOut* out, cudaStream_t st,
+                 const long long* frame_off)
 {
     if (frames <= 0) return;
     const size_t smem = static_cast<size_t>(kSyncPass + p.pre_len) * sizeof(float2) +
@@ -307,10 +354,28 @@ void launch_sync(const float2* samples, long long stride, const int* counts, int
                         static_cast<size_t>(kSyncPass + 2 * kMaxRadius) * sizeof(float);
     if (smem > 200 * 1024) throw InvalidArgument("preamble too long for the sync kernel");
     if (p.radius > kMaxRadius || p.radius < 0) throw InvalidArgument("refinement radius must be 0..511");
+    // passes of the longest search: frames hold at most `stride` samples
+    long long span = counts ? stride : std::min<long long>(count, stride);
+    long long limit = span - p.pre_len + 1;
+    if (p.max_search > 0) limit = std::min<long long>(limit, p.max_search + 1);
+    const long long passes = std::max<long long>(1, (limit + kSyncPass - 1) / kSyncPass);
+    const int cluster = static_cast<int>(std::min<long long>(kSyncMaxCluster, passes));
     check_cuda(cudaFuncSetAttribute(sync_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
                "cudaFuncSetAttribute(sync)");
-    sync_kernel<<<frames, kSyncThreads, smem, st>>>(samples, stride, counts, count, preamble, p, out);
-    check_cuda(cudaGetLastError(), "sync_kernel launch");
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(static_cast<unsigned>(frames) * cluster, 1, 1);
+    cfg.blockDim = dim3(kSyncThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    check_cuda(cudaLaunchKernelEx(&cfg, sync_kernel, samples, stride, frame_off, counts, count, preamble, p, out),
+               "sync_kernel launch");
 }
 
 // ---------------------------------------------------------------------------
@@ -395,7 +460,8 @@ __device__ __forceinline__ float sq_dist(float x, float c)
 
 __global__ void __launch_bounds__(kDemodThreads)
 demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, const SyncOut* __restrict__ sync,
-             float* __restrict__ llr, long long llr_stride, int symbols_per_cta)
+             float* __restrict__ llr, long long llr_stride, int symbols_per_cta, const long long* __restrict__ frame_off,
+             const long long* __restrict__ llr_off)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* buf0 = reinterpret_cast<float2*>(smem_raw);
@@ -413,7 +479,7 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
         const SyncOut so = sync[f];
         if (so.found != 1) {
             // no frame: zero LLRs (the caller sees found != 1 in the sync result)
-            float* dst = llr + static_cast<long long>(f) * llr_stride;
+            float* dst = llr + (llr_off ? llr_off[f] : static_cast<long long>(f) * llr_stride);
             const int hi = min(ds1 * v.active_sc * v.bits_per_symbol, v.kept_bits);
             for (int i = ds0 * v.active_sc * v.bits_per_symbol + threadIdx.x; i < hi; i += blockDim.x) dst[i] = 0.0f;
             return;
@@ -421,7 +487,7 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
         start = so.start;
         cfo = so.cfo_hz;
     }
-    const float2* x = samples + static_cast<long long>(f) * stride + start;
+    const float2* x = samples + (frame_off ? frame_off[f] : static_cast<long long>(f) * stride) + start;
     const float cfo_norm = cfo / v.sample_rate;
 
     // pilots referenced by this CTA's data symbols
@@ -449,7 +515,7 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
     const int bps = v.bits_per_symbol;
     const int abits = bps >> 1;
     const int levels = 1 << abits;
-    float* out = llr + static_cast<long long>(f) * llr_stride;
+    float* out = llr + (llr_off ? llr_off[f] : static_cast<long long>(f) * llr_stride);
     for (int d = ds0; d < ds1; ++d) {
         load_symbol(v, x, cfo_norm, v.data_symbols[d], buf0);
         const float2* Y = fft_stockham(buf0, buf1, v.nfft, v.twiddle);
@@ -517,7 +583,8 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
 }
 
 void launch_demod(const DemodView& v, const float2* samples, long long stride, const SyncOut* sync, int frames,
-                  float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta)
+                  float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta, const long long* frame_off,
+                  const long long* llr_off)
 {
     if (frames <= 0 || v.num_data <= 0) return;
     if (v.nfft < 4 || (v.nfft & (v.nfft - 1))) throw InvalidArgument("nfft must be a power of two >= 4");
@@ -535,7 +602,8 @@ void launch_demod(const DemodView& v, const float2* samples, long long stride, c
     check_cuda(cudaFuncSetAttribute(demod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
                "cudaFuncSetAttribute(demod)");
     const dim3 grid(frames, (v.num_data + spc - 1) / spc);
-    demod_kernel<<<grid, kDemodThreads, smem, st>>>(v, samples, stride, sync, llr, llr_stride, spc);
+    demod_kernel<<<grid, kDemodThreads, smem, st>>>(v, samples, stride, sync, llr, llr_stride, spc, frame_off,
+                                                    llr_off);
     check_cuda(cudaGetLastError(), "demod_kernel launch");
 }
 

@@ -29,10 +29,12 @@ struct SyncParams {
     float pre_energy;     // sum |preamble|^2
 };
 
-// One CTA per frame.  samples: frame f starts at samples + f*stride and holds
-// counts[f] (or `count` when counts is null) samples.
+// One cluster of up to 8 CTAs per frame.  samples: frame f starts at samples + f*stride (or
+// samples + frame_off[f], device offsets in complex samples) and holds counts[f] (or `count` when counts
+// is null) samples, at most `stride`.
 void launch_sync(const float2* samples, long long stride, const int* counts, int count, int frames,
-                 const float2* preamble, const SyncParams& p, SyncOut* out, cudaStream_t st);
+                 const float2* preamble, const SyncParams& p, SyncOut* out, cudaStream_t st,
+                 const long long* frame_off = nullptr);
 
 // Static demodulation tables resident on the device.
 struct DemodView {
@@ -56,8 +58,10 @@ struct DemodView {
 // Fused demodulator: CFO derotation + CP strip + FFT + LS pilot estimate +
 // interpolation + MMSE equalisation + max-log LLR.  Frame f's samples start at
 // samples + f*stride + sync[f].start (sync may be null: start 0, cfo 0 unless
-// `cfo_override` is used); LLRs go to llr + f*llr_stride.
+// `cfo_override` is used); LLRs go to llr + f*llr_stride.  With frame_off / llr_off (device offsets in
+// complex samples / floats) frame f is read from samples + frame_off[f] and written to llr + llr_off[f].
 void launch_demod(const DemodView& v, const float2* samples, long long stride, const SyncOut* sync, int frames,
-                  float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta = 0);
+                  float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta = 0,
+                  const long long* frame_off = nullptr, const long long* llr_off = nullptr);
 
 }  // namespace sicc

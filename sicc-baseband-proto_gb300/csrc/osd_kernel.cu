@@ -81,7 +81,9 @@ osd_kernel(OsdView ov0, OsdIO io)
         const int cw = io.index ? io.index[item] : item;
         const OsdView ov = io.views ? io.views[io.code_of[cw]] : ov0;
         const int n = ov.n, k = ov.k;
-        const float* src = io.llr_off ? io.llr + io.llr_off[cw] : io.llr + static_cast<size_t>(item) * n;
+        const float* src = io.row_off   ? io.llr + io.row_off[item]
+                           : io.llr_off ? io.llr + io.llr_off[cw]
+                                        : io.llr + static_cast<size_t>(item) * n;
         uint8_t* info_dst = io.out_info ? (io.info_off ? io.out_info + io.info_off[cw]
                                                        : io.out_info + static_cast<size_t>(cw) * io.info_stride)
                                         : nullptr;

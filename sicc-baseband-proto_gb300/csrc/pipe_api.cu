@@ -481,6 +481,34 @@ int sicc_pipe_demod_batch(unsigned long long handle, const float* device_iq, lon
     });
 }
 
+int sicc_pipe_demod_gather(unsigned long long handle, const float* device_iq, const long long* device_frame_offsets,
+                           int sample_count, int frames, float* device_llr, const long long* device_llr_offsets,
+                           sicc_pipe_sync_record_t* device_sync, void* cuda_stream)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        require_tables(*p);
+        if (!device_iq || !device_frame_offsets || !device_llr || !device_llr_offsets || !device_sync)
+            throw InvalidArgument("null device pointer");
+        if (frames <= 0 || frames > p->batch_frames) throw InvalidArgument("frames must be in 1..max_batch_frames");
+        if (sample_count < p->cfg.preamble_len) throw InvalidArgument("sample_count must cover the preamble");
+        check_cuda(cudaSetDevice(p->device), "cudaSetDevice");
+        cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+        SyncOut* so = reinterpret_cast<SyncOut*>(device_sync);
+        const float2* iq = reinterpret_cast<const float2*>(device_iq);
+        check_cuda(cudaEventRecord(p->ev[0], st), "cudaEventRecord");
+        launch_sync(iq, sample_count, nullptr, sample_count, frames, p->preamble.p, p->sync_params(0), so, st,
+                    device_frame_offsets);
+        check_cuda(cudaEventRecord(p->ev[1], st), "cudaEventRecord");
+        launch_demod(p->view, iq, 0, so, frames, device_llr, 0, st, p->symbols_per_cta, device_frame_offsets,
+                     device_llr_offsets);
+        check_cuda(cudaEventRecord(p->ev[2], st), "cudaEventRecord");
+        p->batch_timed = true;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
 int sicc_pipe_last_batch_ms(unsigned long long handle, float* out_sync_ms, float* out_demod_ms)
 {
     return guarded([&] {

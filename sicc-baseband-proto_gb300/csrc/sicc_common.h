@@ -109,12 +109,13 @@ struct OsdIO {
     float* out_metric;       // [codewords] winning metric (optional)
     uint8_t* used_osd;       // [codewords] set to 1 (optional)
     // mixed-code batches (all null for one code): per item its code's tables,
-    // its posterior row at llr + llr_off[codeword], its info bits at
-    // out_info + info_off[codeword]
+    // its posterior row at llr + row_off[item] (or llr + llr_off[codeword]),
+    // its info bits at out_info + info_off[codeword]
     const OsdView* views;
     const uint8_t* code_of;  // [codewords] code id
     const long long* llr_off;
     const long long* info_off;
+    const long long* row_off;
 };
 
 }  // namespace sicc

@@ -34,6 +34,7 @@ _SIGS = {
     "sicc_engine_add_code": (C.c_int, [C.c_ulonglong, C.POINTER(EngineCode), C.POINTER(C.c_int)]),
     "sicc_engine_set_launch_shape": (C.c_int, [C.c_ulonglong, C.c_int, C.c_int]),
     "sicc_engine_decode_device": (C.c_int, [C.c_ulonglong, C.c_int] + [C.c_void_p] * 9),
+    "sicc_engine_decode_device_protected": (C.c_int, [C.c_ulonglong, C.c_int] + [C.c_void_p] * 10),
     "sicc_engine_last_ms": (C.c_int, [C.c_ulonglong] + [C.POINTER(C.c_float)] * 3),
 }
 
@@ -87,12 +88,19 @@ class Engine:
         _lib.check(_fn("sicc_engine_set_launch_shape")(self.handle, warps_per_cta, ctas), "sicc_engine_set_launch_shape")
 
     def decode_device(self, count, d_code_ids, d_llr, d_llr_off, d_info, d_info_off, d_success=None, d_used=None,
-                      d_iter=None, stream=None):
+                      d_iter=None, stream=None, d_protection=None):
+        """One batch; with d_protection (uint8 per codeword) only codewords marked 1 may fall back to OSD."""
         st = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
         p = _lib.ptr
-        _lib.check(_fn("sicc_engine_decode_device")(self.handle, count, p(d_code_ids), p(d_llr), p(d_llr_off), p(d_info),
-                                                    p(d_info_off), p(d_success), p(d_used), p(d_iter), st),
-                   "sicc_engine_decode_device")
+        if d_protection is None:
+            _lib.check(_fn("sicc_engine_decode_device")(self.handle, count, p(d_code_ids), p(d_llr), p(d_llr_off),
+                                                        p(d_info), p(d_info_off), p(d_success), p(d_used), p(d_iter),
+                                                        st), "sicc_engine_decode_device")
+        else:
+            _lib.check(_fn("sicc_engine_decode_device_protected")(self.handle, count, p(d_code_ids), p(d_protection),
+                                                                  p(d_llr), p(d_llr_off), p(d_info), p(d_info_off),
+                                                                  p(d_success), p(d_used), p(d_iter), st),
+                       "sicc_engine_decode_device_protected")
 
     def last_ms(self):
         a, b, c = C.c_float(), C.c_float(), C.c_float()

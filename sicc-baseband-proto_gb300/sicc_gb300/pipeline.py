@@ -53,6 +53,8 @@ _SIGS = {
     "sicc_pipe_demod_to_host": (C.c_int, [C.c_ulonglong, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(PipeSync)]),
     "sicc_pipe_demod_batch": (C.c_int, [C.c_ulonglong, C.c_void_p, C.c_longlong, C.c_int, C.c_int, C.c_void_p,
                                         C.c_void_p, C.c_void_p]),
+    "sicc_pipe_demod_gather": (C.c_int, [C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]),
     "sicc_pipe_last_batch_ms": (C.c_int, [C.c_ulonglong, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
 }
 
@@ -66,37 +68,46 @@ def _sync_tuple(s: PipeSync):
     return s.start, s.metric, s.cfo_hz
 
 
+def pipe_structs(tables: Tables, code_n: int, code_k: int, blocks_per_frame: int, noise_var: float,
+                 max_rx_search_samples: int = 0, max_batch_frames: int = 256, sync_radius: int = 0,
+                 use_pilot_channel_est: bool = True):
+    """(PipeConfig, PipeTables, arrays the tables point into) for one PHY profile."""
+    cfg = tables.cfg
+    c = PipeConfig(nfft=cfg.nfft, cp=cfg.cp, preamble_len=2 * cfg.pre_half_len, pre_half_len=cfg.pre_half_len,
+                   num_symbols=cfg.num_symbols, active_sc=cfg.active_sc, bits_per_symbol=cfg.bits_per_symbol,
+                   code_n=code_n, code_k=code_k, blocks_per_frame=blocks_per_frame,
+                   max_rx_search_samples=max_rx_search_samples, sample_rate=cfg.sample_rate,
+                   sync_threshold=cfg.sync_threshold, tx_amplitude=cfg.amplitude, demod_noise_var=noise_var,
+                   use_pilot_channel_est=1 if use_pilot_channel_est else 0, sync_radius=sync_radius,
+                   max_batch_frames=max_batch_frames)
+    keep = dict(used=np.ascontiguousarray(tables.used_indices, np.int32),
+                pil=np.ascontiguousarray(tables.pilot_symbols, np.int32),
+                dat=np.ascontiguousarray(tables.data_symbols, np.int32),
+                p0=np.ascontiguousarray(tables.interp_p0, np.int32),
+                p1=np.ascontiguousarray(tables.interp_p1, np.int32),
+                al=np.ascontiguousarray(tables.interp_alpha, np.float32),
+                grid=np.ascontiguousarray(tables.pilot_grid, np.complex64),
+                pre=np.ascontiguousarray(tables.preamble, np.complex64))
+    t = PipeTables(used_indices=keep["used"].ctypes.data, pilot_symbols=keep["pil"].ctypes.data,
+                   pilot_count=len(keep["pil"]), data_symbols=keep["dat"].ctypes.data,
+                   data_count=len(keep["dat"]), interp_p0=keep["p0"].ctypes.data,
+                   interp_p1=keep["p1"].ctypes.data, interp_alpha=keep["al"].ctypes.data,
+                   pilot_grid=keep["grid"].ctypes.data, preamble=keep["pre"].ctypes.data)
+    return c, t, keep
+
+
 class RxPipeline:
     def __init__(self, tables: Tables, code_n: int, code_k: int, blocks_per_frame: int, noise_var: float,
                  slots: int = 3, max_rx_search_samples: int = 0, max_batch_frames: int = 256, sync_radius: int = 0,
                  use_pilot_channel_est: bool = True):
-        cfg = tables.cfg
-        c = PipeConfig(nfft=cfg.nfft, cp=cfg.cp, preamble_len=2 * cfg.pre_half_len, pre_half_len=cfg.pre_half_len,
-                       num_symbols=cfg.num_symbols, active_sc=cfg.active_sc, bits_per_symbol=cfg.bits_per_symbol,
-                       code_n=code_n, code_k=code_k, blocks_per_frame=blocks_per_frame,
-                       max_rx_search_samples=max_rx_search_samples, sample_rate=cfg.sample_rate,
-                       sync_threshold=cfg.sync_threshold, tx_amplitude=cfg.amplitude, demod_noise_var=noise_var,
-                       use_pilot_channel_est=1 if use_pilot_channel_est else 0, sync_radius=sync_radius,
-                       max_batch_frames=max_batch_frames)
+        c, t, keep = pipe_structs(tables, code_n, code_k, blocks_per_frame, noise_var, max_rx_search_samples,
+                                  max_batch_frames, sync_radius, use_pilot_channel_est)
         h = C.c_ulonglong(0)
         _lib.check(_fn("sicc_pipe_create")(C.byref(c), slots, C.byref(h)), "sicc_pipe_create")
         self.handle = h.value
         self.tables = tables
         self.coded_bits = blocks_per_frame * code_n
         self.frame_samples = tables.frame_len
-        keep = dict(used=np.ascontiguousarray(tables.used_indices, np.int32),
-                    pil=np.ascontiguousarray(tables.pilot_symbols, np.int32),
-                    dat=np.ascontiguousarray(tables.data_symbols, np.int32),
-                    p0=np.ascontiguousarray(tables.interp_p0, np.int32),
-                    p1=np.ascontiguousarray(tables.interp_p1, np.int32),
-                    al=np.ascontiguousarray(tables.interp_alpha, np.float32),
-                    grid=np.ascontiguousarray(tables.pilot_grid, np.complex64),
-                    pre=np.ascontiguousarray(tables.preamble, np.complex64))
-        t = PipeTables(used_indices=keep["used"].ctypes.data, pilot_symbols=keep["pil"].ctypes.data,
-                       pilot_count=len(keep["pil"]), data_symbols=keep["dat"].ctypes.data,
-                       data_count=len(keep["dat"]), interp_p0=keep["p0"].ctypes.data,
-                       interp_p1=keep["p1"].ctypes.data, interp_alpha=keep["al"].ctypes.data,
-                       pilot_grid=keep["grid"].ctypes.data, preamble=keep["pre"].ctypes.data)
         _lib.check(_fn("sicc_pipe_upload_static_tables")(self.handle, C.byref(t)), "upload_static_tables")
 
     def close(self):
@@ -149,6 +160,13 @@ class RxPipeline:
         st = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
         _lib.check(_fn("sicc_pipe_demod_batch")(self.handle, _lib.ptr(d_iq), stride, sample_count, frames,
                                                 _lib.ptr(d_llr), _lib.ptr(d_sync), st), "sicc_pipe_demod_batch")
+
+    def demod_gather(self, d_iq, d_frame_off, sample_count: int, frames: int, d_llr, d_llr_off, d_sync, stream=None):
+        """Frames at d_iq + frame_off[f] (complex samples) -> LLRs at d_llr + llr_off[f] (floats)."""
+        st = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+        p = _lib.ptr
+        _lib.check(_fn("sicc_pipe_demod_gather")(self.handle, p(d_iq), p(d_frame_off), sample_count, frames, p(d_llr),
+                                                 p(d_llr_off), p(d_sync), st), "sicc_pipe_demod_gather")
 
     def last_batch_ms(self):
         a, b = C.c_float(), C.c_float()

@@ -135,6 +135,43 @@ def test_batched_search_and_demod(cuda, oracle):
     assert sms > 0 and dms > 0
 
 
+def test_gathered_demod_matches_batched(cuda):
+    """Frames scattered in device memory (reversed, gaps) demodulate exactly as the strided batch."""
+    torch = cuda
+    from sicc_gb300.pipeline import SYNC_RECORD
+    t = ofdm.reference_tables(ofdm.OFDM_SMALL)
+    code = codes.short_code()
+    gen = ofdm.FrameGenerator(t, code, seed=41)
+    b = gen.batch(10, snr_db=9.0, cfo_subcarriers=0.2, max_offset=150)
+    L = b.iq.shape[1]
+    p = _pipe(t, float(np.float32(np.mean(b.noise_var))), max_batch_frames=16)
+    d_iq = torch.from_numpy(b.iq).cuda()
+    d_llr = torch.zeros((10, p.coded_bits), dtype=torch.float32, device="cuda")
+    d_sync = torch.zeros(10 * SYNC_RECORD.itemsize, dtype=torch.uint8, device="cuda")
+    p.demod_batch(d_iq, L, L, 10, d_llr, d_sync, torch.cuda.current_stream())
+    # gathered: frame f at slot 2*(9-f) of a buffer twice as long, LLRs reversed with a gap
+    big = torch.zeros((20, L), dtype=torch.complex64, device="cuda")
+    order = np.arange(10)[::-1].copy()
+    for f in range(10):
+        big[2 * order[f]] = d_iq[f]
+    f_off = torch.from_numpy((2 * order * L).astype(np.int64)).cuda()
+    gap = p.coded_bits + 64
+    l_off = torch.from_numpy((order * gap).astype(np.int64)).cuda()
+    g_llr = torch.full((10 * gap,), 7.0, dtype=torch.float32, device="cuda")
+    g_sync = torch.zeros(10 * SYNC_RECORD.itemsize, dtype=torch.uint8, device="cuda")
+    p.demod_gather(big, f_off, L, 10, g_llr, l_off, g_sync, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    ref_llr = d_llr.cpu().numpy()
+    ref_sync = d_sync.cpu().numpy().view(SYNC_RECORD)
+    got = g_llr.cpu().numpy()
+    got_sync = g_sync.cpu().numpy().view(SYNC_RECORD)
+    for f in range(10):
+        o = order[f] * gap
+        assert np.array_equal(got[o:o + p.coded_bits], ref_llr[f])
+        assert np.all(got[o + p.coded_bits:o + gap] == 7.0)
+        assert got_sync[f] == ref_sync[f]
+
+
 def test_ofdm_rx_workload_frames(cuda, oracle):
     """The 1024-point, 600-subcarrier 16-QAM workload: 30 codewords + 480 filler bits per frame."""
     torch = cuda
