@@ -586,6 +586,7 @@ def run_serve(args, rank, world):
     in_bytes = sum(int(q[1].nbytes) for q in reqs)
     out_bytes = sum(int(q[2].nbytes) for q in reqs)
     at_once = np.zeros(n_req)
+    is_iq = np.array([q[0].kind == 1 for q in reqs])
 
     for _ in range(args.warmup):
         srv.replay(reqs, at_once)
@@ -612,11 +613,18 @@ def run_serve(args, rank, world):
         res, wall = srv.replay(reqs, arr)
         b1 = srv.stats()
         lat = np.array([d.latency_us for d in res]) * 1e-3
+        wait = np.array([d.launch_us for d in res]) * 1e-3
+        gpu = np.array([d.batch_gpu_us for d in res]) * 1e-3
         sweep.append({"load": load, "offered_mbps": round(load * peak_mbps, 2),
                       "achieved_mbps": round(info_bits / (wall * 1e-6) / 1e6, 2),
                       "p50_ms": round(float(np.percentile(lat, 50)), 4),
                       "p99_ms": round(float(np.percentile(lat, 99)), 4),
                       "p99_9_ms": round(float(np.percentile(lat, 99.9)), 4),
+                      "p99_ms_llr_requests": round(float(np.percentile(lat[~is_iq], 99)), 4),
+                      "p99_ms_iq_requests": round(float(np.percentile(lat[is_iq], 99)), 4),
+                      "p50_wait_ms": round(float(np.percentile(wait, 50)), 4),
+                      "p50_batch_gpu_ms": round(float(np.percentile(gpu, 50)), 4),
+                      "p99_batch_gpu_ms": round(float(np.percentile(gpu, 99)), 4),
                       "mean_batch_codewords": round((b1.codewords - b0.codewords) / max(b1.batches - b0.batches, 1), 1),
                       "batches": int(b1.batches - b0.batches)})
     clk = clocks.stop()

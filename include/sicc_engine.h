@@ -42,7 +42,7 @@ typedef struct sicc_engine_code_t {
     int max_iterations;
     float normalization;
     float offset;
-    int osd_order;          /* -1: no OSD; 0..3 */
+    int osd_order;          /* -1: no OSD; 0..3 (n <= 256, k <= 128: warp kernel; else m <= 1024, n <= 4096) */
     int osd_max_flip_positions;
     int osd_max_tests;
 } sicc_engine_code_t;
@@ -68,6 +68,14 @@ SICC_API int sicc_engine_decode_device_protected(unsigned long long handle, int 
                                                  const long long* device_info_offsets, unsigned char* device_success,
                                                  unsigned char* device_used_osd, unsigned char* device_iterations,
                                                  void* cuda_stream);
+/* OSD alone on given soft values: codeword c's n values at device_llr +
+ * device_llr_offsets[c] go straight to its code's OSD (codes registered
+ * without OSD are skipped).  Outputs: information bits, used flag (set to 1),
+ * and the winning correlation discrepancy (device_metric, may be null). */
+SICC_API int sicc_engine_osd_device(unsigned long long handle, int codewords, const unsigned char* device_code_ids,
+                                    const float* device_llr, const long long* device_llr_offsets,
+                                    unsigned char* device_info, const long long* device_info_offsets,
+                                    unsigned char* device_used_osd, float* device_metric, void* cuda_stream);
 /* Kernel durations (ms) of the last decode: prepare (sort), BP, OSD. */
 SICC_API int sicc_engine_last_ms(unsigned long long handle, float* out_prepare_ms, float* out_bp_ms,
                                  float* out_osd_ms);

@@ -63,6 +63,8 @@ typedef struct sicc_completion_t {
     int osd_codewords;
     double latency_us;           /* submit -> results on the host */
     double queue_us;             /* submit -> admitted into the arena */
+    double launch_us;            /* submit -> its batch launched */
+    double batch_gpu_us;         /* device time of its batch (first copy to last copy back) */
 } sicc_completion_t;
 
 typedef struct sicc_server_stats_t {

@@ -1,5 +1,6 @@
 // Host-side code compilation: CSR parity-check matrix -> device tables.
 #include "code_plan.h"
+#include "bp_kernels.h"
 
 #include <algorithm>
 #include <cstring>
@@ -176,6 +177,7 @@ DeviceCode::~DeviceCode()
 {
     for (void* p : owned_) cudaFree(p);
     if (combos_buf_) cudaFree(combos_buf_);
+    if (combos_h_buf_) cudaFree(combos_h_buf_);
 }
 
 void DeviceCode::build_layered()
@@ -278,6 +280,45 @@ void DeviceCode::set_osd(const OsdSettings& s)
     osd_.pool = pool;
     osd_.num_tests = 1 + static_cast<int>(combos.size());
     osd_.combos = static_cast<const uint32_t*>(combos_buf_);
+}
+
+void DeviceCode::set_osd_h(const OsdSettings& s)
+{
+    if (s.order < 0 || s.order > 3) throw InvalidArgument("OSD order must be 0..3");
+    if (s.max_tests < 1) throw InvalidArgument("OSD max_tests must be >= 1");
+    if (m_ > 1024 || n_ > 4096) throw InvalidArgument("large-code OSD supports m <= 1024 and n <= 4096");
+    const int pool = std::min(k_, std::max(s.max_flip_positions, 0));
+    if (pool > 128) throw InvalidArgument("large-code OSD flip pool must be <= 128");
+    if (osd_h_smem_bytes(n_, m_, pool) > 227 * 1024) throw InvalidArgument("large-code OSD tables exceed shared memory");
+    if (osd_h_.n == 0) {
+        std::vector<int> col_ptr(n_ + 1, 0), col_rows(edges_);
+        for (int e = 0; e < edges_; ++e) ++col_ptr[col_ind_[e] + 1];
+        for (int v = 0; v < n_; ++v) col_ptr[v + 1] += col_ptr[v];
+        std::vector<int> fill(col_ptr.begin(), col_ptr.end() - 1);
+        for (int r = 0; r < m_; ++r)
+            for (int e = row_ptr_[r]; e < row_ptr_[r + 1]; ++e) col_rows[fill[col_ind_[e]]++] = r;
+        osd_h_.col_ptr = device_upload(col_ptr, owned_);
+        osd_h_.col_rows = device_upload(col_rows, owned_);
+        osd_h_.row_ptr = device_upload(row_ptr_, owned_);
+        osd_h_.col_ind = device_upload(col_ind_, owned_);
+    }
+    const auto combos = osd_combos(pool, s.order, s.max_tests);
+    if (combos_h_buf_) {
+        cudaFree(combos_h_buf_);
+        combos_h_buf_ = nullptr;
+    }
+    if (!combos.empty()) {
+        check_cuda(cudaMalloc(&combos_h_buf_, combos.size() * sizeof(uint32_t)), "cudaMalloc(osd combos)");
+        check_cuda(cudaMemcpy(combos_h_buf_, combos.data(), combos.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+                   "upload osd combos");
+    }
+    osd_h_.n = n_;
+    osd_h_.m = m_;
+    osd_h_.k = k_;
+    osd_h_.mw = (m_ + 31) / 32;
+    osd_h_.pool = pool;
+    osd_h_.num_tests = 1 + static_cast<int>(combos.size());
+    osd_h_.combos = static_cast<const uint32_t*>(combos_h_buf_);
 }
 
 }  // namespace sicc

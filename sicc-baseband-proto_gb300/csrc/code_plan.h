@@ -37,15 +37,20 @@ public:
     int schedule() const { return schedule_; }
     bool layered() const { return schedule_ == kColoredLayered || schedule_ == kFlatLayered; }
     bool has_osd() const { return osd_.pcols != nullptr; }
+    bool has_osd_h() const { return osd_h_.n != 0; }
 
     const LayeredView& layered_view() const { return lv_; }
     const FloodView& flood_view() const { return fv_; }
     const OsdView& osd_view() const { return osd_; }
+    const OsdHView& osd_h_view() const { return osd_h_; }
     const std::vector<int>& row_order() const { return row_order_; }
     const std::vector<uint64_t>& parity_table() const { return parity_; }
     int parity_words() const { return parity_words_; }
 
     void set_osd(const OsdSettings& s);
+    // Tables of the large-code OSD kernel (elimination on H): any full-rank
+    // code with m <= 1024, n <= 4096, flip pool <= 128.
+    void set_osd_h(const OsdSettings& s);
 
 private:
     void build_layered();
@@ -59,8 +64,10 @@ private:
     LayeredView lv_{};
     FloodView fv_{};
     OsdView osd_{};
+    OsdHView osd_h_{};
     std::vector<void*> owned_;
     void* combos_buf_ = nullptr;
+    void* combos_h_buf_ = nullptr;
 };
 
 // Front-systematic parity table [k][words] (bit p of row i = parity bit p of

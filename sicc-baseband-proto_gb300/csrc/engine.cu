@@ -258,7 +258,8 @@ bp_mixed_kernel(MixedIO io, int warp_floats)
 struct EngineCode {
     std::unique_ptr<DeviceCode> code;
     CodeDesc desc{};
-    bool osd = false;
+    bool osd = false;    // OSD by the warp kernel (n <= 256, k <= 128)
+    bool osd_h = false;  // OSD by the large-code kernel
     long long cost = 0;
 };
 
@@ -267,10 +268,12 @@ struct Engine {
     int device = 0;
     std::vector<EngineCode> codes;
     int n_max = 0, k_max = 0, maxdeg = 0, osd_nmax = 0, osd_kmax = 0;
+    int h_nmax = 0, h_mmax = 0, h_poolmax = 0;  // large-code OSD launch bounds
     int warps_per_cta = 0, ctas = 0;
     // device state
     CodeDesc* d_codes = nullptr;
     OsdView* d_views = nullptr;
+    OsdHView* d_hviews = nullptr;
     int* d_per_warp = nullptr;
     int* d_q_code = nullptr;
     int* d_q_start = nullptr;
@@ -288,7 +291,8 @@ struct Engine {
     std::mutex mu;
     ~Engine()
     {
-        for (void* p : {static_cast<void*>(d_codes), static_cast<void*>(d_views), static_cast<void*>(d_per_warp),
+        for (void* p : {static_cast<void*>(d_codes), static_cast<void*>(d_views), static_cast<void*>(d_hviews),
+                        static_cast<void*>(d_per_warp),
                         static_cast<void*>(d_q_code), static_cast<void*>(d_q_start), static_cast<void*>(d_q_units),
                         static_cast<void*>(d_order), static_cast<void*>(d_counters), static_cast<void*>(d_osd_index),
                         static_cast<void*>(d_osd_llr), static_cast<void*>(d_best), static_cast<void*>(d_osd_rowoff)})
@@ -311,11 +315,13 @@ struct Engine {
         const int K = static_cast<int>(codes.size());
         std::vector<CodeDesc> descs(K);
         std::vector<OsdView> views(K);
+        std::vector<OsdHView> hviews(K);
         std::vector<int> per(K), qcode(K);
         for (int c = 0; c < K; ++c) {
             descs[c] = codes[c].desc;
             per[c] = 32 / codes[c].desc.group;
             views[c] = codes[c].osd ? codes[c].code->osd_view() : OsdView{};
+            hviews[c] = codes[c].osd_h ? codes[c].code->osd_h_view() : OsdHView{};
             qcode[c] = c;
         }
         // queue order: most expensive codes first, so the long codewords start early
@@ -328,6 +334,7 @@ struct Engine {
         };
         up(d_codes, descs);
         up(d_views, views);
+        up(d_hviews, hviews);
         up(d_per_warp, per);
         up(d_q_code, qcode);
         dirty = false;
@@ -458,9 +465,18 @@ int sicc_engine_add_code(unsigned long long handle, const sicc_engine_code_t* co
             os.max_flip_positions = code->osd_max_flip_positions;
             os.max_tests = code->osd_max_tests;
         }
+        // short codes: the warp OSD kernel (generator tables); longer ones: the CTA kernel on H
+        const bool warp_osd = want_osd && code->n <= 256 && code->n - code->m <= 128;
         EngineCode ec;
         ec.code = std::make_unique<DeviceCode>(code->n, code->m, code->row_ptr, code->col_ind, kFlatLayered, nullptr,
-                                               0, want_osd, os);
+                                               0, warp_osd, os);
+        if (want_osd && !warp_osd) {
+            std::vector<uint64_t> parity;
+            int words = 0, kk = 0;
+            if (!systematic_parity(code->n, code->m, code->row_ptr, code->col_ind, parity, words, kk))
+                throw InvalidArgument("OSD needs a full-rank code with the information bits first (systematic-front)");
+            ec.code->set_osd_h(os);
+        }
         const LayeredView& lv = ec.code->layered_view();
         if (lv.maxdeg > 16) throw InvalidArgument("the mixed kernel supports row degree <= 16");
         CodeDesc& d = ec.desc;
@@ -480,13 +496,19 @@ int sicc_engine_add_code(unsigned long long handle, const sicc_engine_code_t* co
         int sf = (n_pad + 3 * d.num_layers * d.width + 3) & ~3;
         if (d.group < 32) sf += ((d.group - sf % 32) + 32) % 32;  // groups of a warp G banks apart
         d.slot_floats = sf;
-        ec.osd = want_osd;
+        ec.osd = warp_osd;
+        ec.osd_h = want_osd && !warp_osd;
         ec.cost = static_cast<long long>(ec.code->edges()) * d.max_iter;
         e->n_max = std::max(e->n_max, d.n);
         e->k_max = std::max(e->k_max, d.k);
-        if (want_osd) {
+        if (ec.osd) {
             e->osd_nmax = std::max(e->osd_nmax, d.n);
             e->osd_kmax = std::max(e->osd_kmax, d.k);
+        }
+        if (ec.osd_h) {
+            e->h_nmax = std::max(e->h_nmax, d.n);
+            e->h_mmax = std::max(e->h_mmax, code->m);
+            e->h_poolmax = std::max(e->h_poolmax, ec.code->osd_h_view().pool);
         }
         e->codes.push_back(std::move(ec));
         e->dirty = true;
@@ -556,7 +578,7 @@ int sicc_engine_decode_device_protected(unsigned long long handle, int codewords
         io.osd_floats = reinterpret_cast<unsigned long long*>(e->d_counters + 2);
         launch_mixed<16>(*e, io, st);
         check_cuda(cudaEventRecord(e->ev[2], st), "cudaEventRecord");
-        if (e->osd_nmax > 0) {
+        if (e->osd_nmax > 0 || e->h_nmax > 0) {
             OsdIO oio{};
             oio.llr = e->d_osd_llr;
             oio.index = e->d_osd_index;
@@ -564,16 +586,58 @@ int sicc_engine_decode_device_protected(unsigned long long handle, int codewords
             oio.out_info = device_info;
             oio.used_osd = device_used_osd;
             oio.views = e->d_views;
+            oio.hviews = e->d_hviews;
             oio.code_of = device_code_ids;
             oio.row_off = e->d_osd_rowoff;
             oio.info_off = device_info_offsets;
+            if (e->osd_nmax > 0) {  // short codes, one warp per codeword
+                OsdView shape{};
+                shape.n = e->osd_nmax;
+                shape.k = e->osd_kmax;
+                launch_osd(shape, oio, codewords, st);
+            }
+            if (e->h_nmax > 0)  // long codes, one CTA per codeword
+                launch_osd_h(OsdHView{}, e->h_nmax, e->h_mmax, e->h_poolmax, oio, codewords, st);
+        }
+        check_cuda(cudaEventRecord(e->ev[3], st), "cudaEventRecord");
+        e->timed = true;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_engine_osd_device(unsigned long long handle, int codewords, const unsigned char* device_code_ids,
+                           const float* device_llr, const long long* device_llr_offsets, unsigned char* device_info,
+                           const long long* device_info_offsets, unsigned char* device_used_osd, float* device_metric,
+                           void* cuda_stream)
+{
+    return guarded([&] {
+        auto e = get(handle);
+        std::lock_guard<std::mutex> lock(e->mu);
+        if (e->codes.empty()) throw InvalidArgument("no code registered");
+        if (codewords <= 0 || codewords > e->cfg.max_codewords) throw InvalidArgument("codewords must be in 1..max_codewords");
+        if (!device_code_ids || !device_llr || !device_llr_offsets || !device_info || !device_info_offsets)
+            throw InvalidArgument("null device pointer");
+        check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+        e->commit();
+        cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+        OsdIO oio{};
+        oio.llr = device_llr;
+        oio.count = codewords;
+        oio.out_info = device_info;
+        oio.out_metric = device_metric;
+        oio.used_osd = device_used_osd;
+        oio.views = e->d_views;
+        oio.hviews = e->d_hviews;
+        oio.code_of = device_code_ids;
+        oio.llr_off = device_llr_offsets;
+        oio.info_off = device_info_offsets;
+        if (e->osd_nmax > 0) {
             OsdView shape{};
             shape.n = e->osd_nmax;
             shape.k = e->osd_kmax;
             launch_osd(shape, oio, codewords, st);
         }
-        check_cuda(cudaEventRecord(e->ev[3], st), "cudaEventRecord");
-        e->timed = true;
+        if (e->h_nmax > 0) launch_osd_h(OsdHView{}, e->h_nmax, e->h_mmax, e->h_poolmax, oio, codewords, st);
         return CUDA_OSD_STATUS_OK;
     });
 }

@@ -80,6 +80,7 @@ osd_kernel(OsdView ov0, OsdIO io)
     for (int item = blockIdx.x * kOsdWarps + warp; item < count; item += total_warps) {
         const int cw = io.index ? io.index[item] : item;
         const OsdView ov = io.views ? io.views[io.code_of[cw]] : ov0;
+        if (ov.n == 0) continue;  // code without warp-kernel tables (uniform over the warp)
         const int n = ov.n, k = ov.k;
         const float* src = io.row_off   ? io.llr + io.row_off[item]
                            : io.llr_off ? io.llr + io.llr_off[cw]

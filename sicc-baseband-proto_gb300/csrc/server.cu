@@ -98,14 +98,14 @@ struct Req {
     int n = 0, k = 0;
     long long off = -1, bytes = 0;   // arena block
     long long in_off = 0, llr_off = 0, info_off = 0;  // offsets inside the arena
-    Clock::time_point t_submit, t_admit;
+    Clock::time_point t_submit, t_admit, t_launch;
     cudaEvent_t h2d = nullptr;
 };
 
 struct Slot {
     unsigned long long engine = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t done = nullptr;
+    cudaEvent_t start = nullptr, done = nullptr;
     bool busy = false;
     std::vector<std::shared_ptr<Req>> reqs;
     // per-codeword metadata: host staging (pinned) and device copies
@@ -160,6 +160,7 @@ struct Server {
             if (s.engine) sicc_engine_destroy(s.engine);
             if (s.stream) cudaStreamDestroy(s.stream);
             if (s.done) cudaEventDestroy(s.done);
+            if (s.start) cudaEventDestroy(s.start);
             for (void* p : {static_cast<void*>(s.h_code), static_cast<void*>(s.h_prot),
                             static_cast<void*>(s.h_llr_off), static_cast<void*>(s.h_info_off),
                             static_cast<void*>(s.h_ok), static_cast<void*>(s.h_used),
@@ -230,6 +231,9 @@ struct Server {
             admitted.pop_front();
         }
         if (s.reqs.empty()) return false;
+        const auto t_launch = Clock::now();
+        for (auto& r : s.reqs) r->t_launch = t_launch;
+        check_cuda(cudaEventRecord(s.start, s.stream), "cudaEventRecord(batch)");
         // demodulate the IQ requests into their LLR areas: one gathered sync + demod launch pair per profile
         std::vector<int> phy_first(phys.size() + 1, 0);
         int nf = 0;
@@ -312,6 +316,8 @@ struct Server {
         for (auto& s : slots) {
             if (!s.busy || cudaEventQuery(s.done) != cudaSuccess) continue;
             const auto now = Clock::now();
+            float gpu_ms = 0.0f;
+            cudaEventElapsedTime(&gpu_ms, s.start, s.done);
             int c = 0;
             for (auto& r : s.reqs) {
                 sicc_completion_t done{};
@@ -324,6 +330,8 @@ struct Server {
                 }
                 done.latency_us = us_between(r->t_submit, now);
                 done.queue_us = us_between(r->t_submit, r->t_admit);
+                done.launch_us = us_between(r->t_submit, r->t_launch);
+                done.batch_gpu_us = 1000.0 * gpu_ms;
                 arena->release(r->off, r->bytes);
                 if (r->h2d) cudaEventDestroy(r->h2d);
                 r->h2d = nullptr;
@@ -507,7 +515,8 @@ int sicc_server_start(unsigned long long handle)
                 if (sicc_engine_add_code(sl.engine, &spec, &id) != CUDA_OSD_STATUS_OK) throw InvalidArgument(last_error());
             }
             check_cuda(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking), "cudaStreamCreate(slot)");
-            check_cuda(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming), "cudaEventCreate(slot)");
+            check_cuda(cudaEventCreate(&sl.done), "cudaEventCreate(slot)");
+            check_cuda(cudaEventCreate(&sl.start), "cudaEventCreate(slot)");
             check_cuda(cudaMallocHost(&sl.h_code, N), "cudaMallocHost");
             check_cuda(cudaMallocHost(&sl.h_prot, N), "cudaMallocHost");
             check_cuda(cudaMallocHost(&sl.h_llr_off, N * sizeof(long long)), "cudaMallocHost");
@@ -656,6 +665,8 @@ int sicc_server_replay(unsigned long long handle, const sicc_request_t* requests
                     if (pos < 0) continue;
                     out_completions[pos] = buf[i];
                     out_completions[pos].latency_us += late[pos];
+                    out_completions[pos].queue_us += late[pos];
+                    out_completions[pos].launch_us += late[pos];
                     t_last = Clock::now();
                     done_count.fetch_add(1);
                 }

@@ -98,6 +98,20 @@ struct OsdView {
     const uint32_t* combos;// [num_tests-1]: flip-pool indices packed 3 x 10 bits (1023 = none)
 };
 
+// OSD tables of a code the warp kernel does not cover (n > 256 or k > 128):
+// elimination runs on H (m x n) instead of G, see osd_large.cu.
+struct OsdHView {
+    int n, m, k;           // n == 0: not handled by the large-code kernel
+    int mw;                // 32-bit words per row-operation row: ceil(m / 32)
+    const int* col_ptr;    // [n+1] columns of H
+    const int* col_rows;   // [nnz]
+    const int* row_ptr;    // [m+1] rows of H
+    const int* col_ind;    // [nnz]
+    int pool;              // flip-pool size min(k, max_flip_positions)
+    int num_tests;         // tests including the base
+    const uint32_t* combos;// [num_tests-1] packed flip-pool indices, as OsdView::combos
+};
+
 struct OsdIO {
     const float* llr;        // posterior rows, indexed by work item
     const int* index;        // [items] codeword index of each item (null: item i -> codeword i)
@@ -112,6 +126,7 @@ struct OsdIO {
     // its posterior row at llr + row_off[item] (or llr + llr_off[codeword]),
     // its info bits at out_info + info_off[codeword]
     const OsdView* views;
+    const OsdHView* hviews;  // large-code tables by code id (the large-code kernel)
     const uint8_t* code_of;  // [codewords] code id
     const long long* llr_off;
     const long long* info_off;

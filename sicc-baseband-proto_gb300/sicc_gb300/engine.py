@@ -35,6 +35,7 @@ _SIGS = {
     "sicc_engine_set_launch_shape": (C.c_int, [C.c_ulonglong, C.c_int, C.c_int]),
     "sicc_engine_decode_device": (C.c_int, [C.c_ulonglong, C.c_int] + [C.c_void_p] * 9),
     "sicc_engine_decode_device_protected": (C.c_int, [C.c_ulonglong, C.c_int] + [C.c_void_p] * 10),
+    "sicc_engine_osd_device": (C.c_int, [C.c_ulonglong, C.c_int] + [C.c_void_p] * 8),
     "sicc_engine_last_ms": (C.c_int, [C.c_ulonglong] + [C.POINTER(C.c_float)] * 3),
 }
 
@@ -47,6 +48,11 @@ def _fn(name):
 def osd_supported(code: QcCode) -> bool:
     """Codes the warp OSD kernel covers (n <= 256, k <= 128)."""
     return code.n <= 256 and code.k <= 128
+
+
+def osd_order_for(code: QcCode) -> int:
+    """OSD order of the mixed workload: 2 for n <= 256, 1 for longer codes."""
+    return 2 if code.n <= 256 else 1
 
 
 def iteration_cap(n: int) -> int:
@@ -101,6 +107,14 @@ class Engine:
                                                                   p(d_llr), p(d_llr_off), p(d_info), p(d_info_off),
                                                                   p(d_success), p(d_used), p(d_iter), st),
                        "sicc_engine_decode_device_protected")
+
+    def osd_device(self, count, d_code_ids, d_llr, d_llr_off, d_info, d_info_off, d_used=None, d_metric=None,
+                   stream=None):
+        """OSD alone on the given soft values (codes registered with an OSD order)."""
+        st = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+        p = _lib.ptr
+        _lib.check(_fn("sicc_engine_osd_device")(self.handle, count, p(d_code_ids), p(d_llr), p(d_llr_off), p(d_info),
+                                                 p(d_info_off), p(d_used), p(d_metric), st), "sicc_engine_osd_device")
 
     def last_ms(self):
         a, b, c = C.c_float(), C.c_float(), C.c_float()

@@ -38,7 +38,7 @@ class Request(C.Structure):
 class Completion(C.Structure):
     _fields_ = [("request_id", C.c_ulonglong), ("tag", C.c_ulonglong), ("status", C.c_int), ("codewords", C.c_int),
                 ("failed_codewords", C.c_int), ("osd_codewords", C.c_int), ("latency_us", C.c_double),
-                ("queue_us", C.c_double)]
+                ("queue_us", C.c_double), ("launch_us", C.c_double), ("batch_gpu_us", C.c_double)]
 
 
 class ServerStats(C.Structure):
@@ -78,11 +78,13 @@ class Done:
     osd_codewords: int
     latency_us: float
     queue_us: float
+    launch_us: float
+    batch_gpu_us: float
 
 
 def _done(c: Completion) -> Done:
     return Done(c.request_id, c.tag, c.status, c.codewords, c.failed_codewords, c.osd_codewords, c.latency_us,
-                c.queue_us)
+                c.queue_us, c.launch_us, c.batch_gpu_us)
 
 
 class Server:
