@@ -417,11 +417,8 @@ def run_mixed(args, rank, world):
     d_used = torch.zeros(w.count, dtype=torch.uint8, device="cuda")
     d_it = torch.zeros(w.count, dtype=torch.uint8, device="cuda")
     eng = engine.Engine(max_codewords=w.count, max_llr_floats=w.llr.size)
-    osd_codes = 0
-    for c in w.codes:
-        osd = engine.osd_supported(c)
-        osd_codes += osd
-        eng.add_code(c, engine.iteration_cap(c.n), ALPHA, 0.0, OSD_ORDER if osd else -1, OSD_FLIP, OSD_TESTS)
+    for c in w.codes:  # OSD order 2 for n <= 256, order 1 for the longer codes
+        eng.add_code(c, engine.iteration_cap(c.n), ALPHA, 0.0, engine.osd_order_for(c), OSD_FLIP, OSD_TESTS)
 
     def batched():
         eng.decode_device(w.count, d_code, d_llr, d_llr_off, d_info, d_info_off, d_ok, d_used, d_it, stream=stream)
@@ -453,7 +450,25 @@ def run_mixed(args, rank, world):
         fer_by_n[str(n)] = float(fe[sel].mean())
 
     # plain form, as the reference decodes a frame (uhd_ldpc_ofdm_link.cpp:3541-3628, 3744-3785): one
-    # decoder per code, one synchronous call per request with device LLRs in and host outputs
+    # decoder per code, one synchronous call per request with device LLRs in and host outputs.  Codes
+    # beyond the reference decoder's OSD limits (n <= 256, k <= 128) run BP + OSD through a one-code
+    # engine per request, so both forms do the same work.
+    class OneCodeEngine:
+        def __init__(self, c):
+            self.c = c
+            self.eng = engine.Engine(max_codewords=512, max_llr_floats=512 * c.n, max_codes=1)
+            self.eng.add_code(c, engine.iteration_cap(c.n), ALPHA, 0.0, engine.osd_order_for(c), OSD_FLIP, OSD_TESTS)
+            self.ids = torch.zeros(512, dtype=torch.uint8, device="cuda")
+            self.lo = torch.arange(512, dtype=torch.int64, device="cuda") * c.n
+            self.io = torch.arange(512, dtype=torch.int64, device="cuda") * c.k
+            self.info = torch.zeros(512 * c.k, dtype=torch.uint8, device="cuda")
+            self.ok = torch.zeros(512, dtype=torch.uint8, device="cuda")
+
+        def decode(self, llr_v, device=True):
+            b = llr_v.shape[0]
+            self.eng.decode_device(b, self.ids, llr_v, self.lo, self.info, self.io, self.ok, stream=stream)
+            return self.info[: b * self.c.k].cpu().numpy(), self.ok[:b].cpu().numpy()
+
     decs = []
     for c in w.codes:
         if engine.osd_supported(c):
@@ -461,8 +476,7 @@ def run_mixed(args, rank, world):
                                                normalization=ALPHA, offset=0.0, damping=0.0, min_abs_llr_accept=0.0,
                                                osd_order=OSD_ORDER, osd_max_flip=OSD_FLIP, osd_max_tests=OSD_TESTS))
         else:
-            decs.append(fec.CsrBpDecoder.for_code(c, max_batch=512, max_iter=engine.iteration_cap(c.n),
-                                                  normalization=ALPHA))
+            decs.append(OneCodeEngine(c))
 
     def plain_pass():
         for r, ci in enumerate(w.req_code):
@@ -484,14 +498,15 @@ def run_mixed(args, rank, world):
             "config": {"workload": "mixed_100k", "codewords": w.count, "requests": int(len(w.req_code)),
                        "lengths": [128, 256, 512, 1024, 2048], "rates": ["1/2", "11/16", "3/4"],
                        "bp": "layered NMS alpha 0.75, 20/25/30 iterations by length",
-                       "osd": f"order {OSD_ORDER} on {osd_codes} codes with n <= 256, k <= 128",
+                       "osd": "on failing codewords: order 2 (n <= 256), order 1 (n >= 512)",
                        "l2": f"{w.llr.nbytes / 1e6:.0f} MB of LLRs per step (> L2)"},
             "fer_by_length": fer_by_n, "fer": float(fe.mean()),
             "kernel_ms": {"prepare": round(prep_ms, 4), "bp_mixed": round(bp_ms, 4), "osd": round(osd_ms, 4)},
             "plain_one_code_per_launch": {"value": round(plain_mbps, 3), "unit": "Mbit/s",
                                           "calls_per_pass": int(len(w.req_code)),
-                                          "api": "per request: cuda_osd_submit_device_codewords+flush+poll_ready or "
-                                                 "cuda_osd_decode_bp_csr_device_batch (host outputs, synchronous)",
+                                          "api": "per request: cuda_osd_submit_device_codewords+flush+poll_ready "
+                                                 "(n <= 256, k <= 128) or a one-code engine call; host outputs, "
+                                                 "synchronous",
                                           "speedup_of_batched": round(value / plain_mbps, 2)},
             "gpu_launches": args.steps * 3, "clocks": clk,
             "roofline": {"bound": "hbm", "kernel": "bp_mixed_kernel<16>",
@@ -555,9 +570,9 @@ def run_serve(args, rank, world):
 
     srv = Server(hbm_budget_bytes=40 << 30, max_batch_codewords=args.serve_batch,
                  max_inflight_batches=args.serve_inflight, max_pending_requests=1 << 16)
-    ids = [srv.add_code(c, engine.iteration_cap(c.n), ALPHA, OSD_ORDER if engine.osd_supported(c) else -1,
+    ids = [srv.add_code(c, engine.iteration_cap(c.n), ALPHA, engine.osd_order_for(c),
                         OSD_FLIP, OSD_TESTS) for c in mixed]
-    ocid = srv.add_code(ocode, OFDM_ITERS, ALPHA, -1)
+    ocid = srv.add_code(ocode, OFDM_ITERS, ALPHA, engine.osd_order_for(ocode))
     phys = [srv.add_phy(t, ocid, blocks, nv, stride) for _, nv in iq_pool]
     srv.start()
 
@@ -641,7 +656,7 @@ def run_serve(args, rank, world):
                        "codewords": cw_total, "info_bits": info_bits, "hbm_budget_gb": 40,
                        "max_batch_codewords": args.serve_batch, "inflight_batches": args.serve_inflight,
                        "burst": "U{1..512} codewords or U{1..17} OFDM frames (p=0.3)",
-                       "protection": "BP or BP+OSD (p=1/2); OSD order 2 on n <= 256, k <= 128",
+                       "protection": "BP or BP+OSD (p=1/2); OSD order 2 (n <= 256), order 1 (n >= 512)",
                        "step": "every request offered at once (peak); then one Poisson pass per load point",
                        "l2": "inputs copied host->device every request (pinned host pools)"},
             "fer": round(sum(fe) / cw_total, 5), "load_sweep": sweep,

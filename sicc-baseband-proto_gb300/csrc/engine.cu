@@ -1,13 +1,20 @@
 // Mixed-code batched decoding (include/sicc_engine.h).
 //
 // One batch holds codewords of several codes.  prepare_kernel groups them by
-// code (a counting sort in the queue order: largest code first) and sizes the
-// work units; bp_mixed_kernel then runs persistently: each warp takes the next
-// unit — up to 32/G codewords of one code, G lanes each — from a device
-// counter, decodes it with that code's layered schedule (the same arithmetic
-// as bp_layered_kernel, so results are bit-exact with the single-code
-// decoders) and takes another unit until the queue is empty.  Codewords whose
-// syndrome fails go to one OSD launch that reads each item's code tables.
+// code (a counting sort in the queue order: widest layers, then largest cost
+// first) and sizes the work units; bp_mixed_kernel then runs persistently in
+// three phases, each unit decoded with its code's layered schedule (the same
+// arithmetic as bp_layered_kernel, so results are bit-exact with the
+// single-code decoders):
+//   1. groups of 4 warps take codewords of codes whose layers are >= 128 rows
+//      wide (one codeword per group, synchronised by a named barrier);
+//   2. groups of 2 warps take codes with 64-row layers;
+//   3. single warps take units of up to 32/G codewords of the narrower codes,
+//      G lanes each.
+// Wide codewords thus run on up to 128 lanes (a 2048-bit codeword is not
+// serialised on one warp) and every warp's shared-memory slot only has to
+// hold a quarter of the largest code's state.  Codewords whose syndrome fails
+// go to one OSD launch that reads each item's code tables.
 #include "../../include/sicc_engine.h"
 #include "bp_device.cuh"
 #include "bp_kernels.h"
@@ -28,6 +35,7 @@ constexpr int kMaxCodes = 64;
 
 struct CodeDesc {
     int n, k, num_layers, width, maxdeg, group, rows_per_lane, max_iter;
+    int warps;        // 4 or 2: decoded by a group of that many warps (group = 32 * warps); 1: narrow
     float alpha, beta;
     int route_osd;
     int slot_floats;  // shared-memory floats per codeword slot
@@ -50,7 +58,10 @@ struct MixedIO {
     const int* q_start;          // [K+1] first entry of queue position q in `order`
     const int* q_units;          // [K+1] first unit of queue position q
     int K;
-    int* work;                   // unit counter
+    int* work4;                  // unit counters of the three phases
+    int* work2;
+    int* work1;
+    const int* bounds;           // [2] end of the 4-warp units, end of the 2-warp units
     float* best;                 // [warps][4][n_max] best-syndrome posteriors (global scratch)
     int n_max;
     float* osd_llr;              // compact rows of the codewords handed to OSD
@@ -63,9 +74,8 @@ struct MixedIO {
 // prepare: counts per code, queue-ordered starts, units, scatter into `order`.
 __global__ void __launch_bounds__(1024)
 prepare_kernel(const uint8_t* __restrict__ code_of, int count, const int* __restrict__ q_code, int K,
-               const int* __restrict__ per_warp, int* __restrict__ order, int* __restrict__ q_start,
-               int* __restrict__ q_units, int* __restrict__ work, int* __restrict__ osd_count,
-               unsigned long long* __restrict__ osd_floats)
+               const int* __restrict__ per_warp, const int* __restrict__ q_warps, int* __restrict__ order,
+               int* __restrict__ q_start, int* __restrict__ q_units, int* __restrict__ counters)
 {
     __shared__ int cnt[kMaxCodes], fill[kMaxCodes], pos_of_code[kMaxCodes];
     for (int i = threadIdx.x; i < kMaxCodes; i += blockDim.x) {
@@ -78,7 +88,7 @@ prepare_kernel(const uint8_t* __restrict__ code_of, int count, const int* __rest
         if (code_of[i] < K) atomicAdd(&cnt[code_of[i]], 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-        int s = 0, u = 0;
+        int s = 0, u = 0, end4 = 0, end2 = 0;
         for (int q = 0; q < K; ++q) {
             const int c = q_code[q];
             pos_of_code[c] = s;
@@ -86,12 +96,19 @@ prepare_kernel(const uint8_t* __restrict__ code_of, int count, const int* __rest
             q_units[q] = u;
             s += cnt[c];
             u += (cnt[c] + per_warp[c] - 1) / per_warp[c];
+            if (q_warps[q] >= 4) end4 = u;  // the queue holds the 4-warp codes first, then the 2-warp ones
+            if (q_warps[q] >= 2) end2 = u;
         }
         q_start[K] = s;
         q_units[K] = u;
-        *work = 0;
-        *osd_count = 0;
-        *osd_floats = 0ull;
+        if (end2 < end4) end2 = end4;
+        counters[0] = 0;       // 4-warp unit counter
+        counters[1] = 0;       // OSD items
+        *reinterpret_cast<unsigned long long*>(counters + 2) = 0ull;  // OSD row floats
+        counters[4] = end4;    // 2-warp unit counter
+        counters[5] = end2;    // single-warp unit counter
+        counters[6] = end4;
+        counters[7] = end2;
     }
     __syncthreads();
     for (int i = threadIdx.x; i < count; i += blockDim.x) {
@@ -100,22 +117,268 @@ prepare_kernel(const uint8_t* __restrict__ code_of, int count, const int* __rest
     }
 }
 
-__device__ __forceinline__ int mixed_syndrome(const CodeDesc& d, const float* app, int gl, int G, unsigned gmask)
+// Variable of slot j of row rs in layer L.
+__device__ __forceinline__ int row_var(const CodeDesc& d, int L, int j, int rs)
+{
+    return __ldg(d.vars + (L * d.maxdeg + j) * d.width + rs);
+}
+
+// Unsatisfied checks among the rows gl, gl + G, ... of every layer.
+__device__ __forceinline__ int lane_syndrome(const CodeDesc& d, const float* app, int gl, int G)
 {
     int cnt = 0;
     for (int L = 0; L < d.num_layers; ++L) {
         for (int rr = 0; rr < d.rows_per_lane; ++rr) {
             const int rs = gl + rr * G;
-            const int* vp = d.vars + (L * d.maxdeg) * d.width + rs;
             unsigned par = 0;
             for (int j = 0; j < d.maxdeg; ++j) {
-                const int v = __ldg(vp + j * d.width);
+                const int v = row_var(d, L, j, rs);
                 if (v >= 0) par ^= (app[v] < 0.0f) ? 1u : 0u;
             }
             cnt += static_cast<int>(par);
         }
     }
-    return static_cast<int>(__reduce_add_sync(gmask, static_cast<unsigned>(cnt)));
+    return cnt;
+}
+
+__device__ __forceinline__ int mixed_syndrome(const CodeDesc& d, const float* app, int gl, int G, unsigned gmask)
+{
+    return static_cast<int>(__reduce_add_sync(gmask, static_cast<unsigned>(lane_syndrome(d, app, gl, G))));
+}
+
+// Layered normalized min-sum update of row rs of layer L: extrinsic inputs
+// from the posteriors and the row's compressed previous messages, new
+// (alpha*min1, alpha*min2, argmin, signs), posteriors updated in place.
+template <int D>
+__device__ __forceinline__ void update_row(const CodeDesc& d, float* app, float* r1, float* r2, unsigned* meta, int L,
+                                           int rs)
+{
+    const int ridx = L * d.width + rs;
+    const float o1 = r1[ridx], o2 = r2[ridx];
+    const unsigned om = meta[ridx];
+    float qv[D];
+    int v[D];
+    float m1 = FLT_MAX, m2 = FLT_MAX;
+    int idx = 0;
+    unsigned neg = 0;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+        v[j] = (j < d.maxdeg) ? row_var(d, L, j, rs) : -1;
+        qv[j] = 0.0f;
+        if (v[j] >= 0) {
+            const float qj = __fsub_rn(app[v[j]], rebuild(o1, o2, om, j));
+            qv[j] = qj;
+            neg |= (qj < 0.0f) ? (1u << j) : 0u;
+            const float a = fabsf(qj);
+            if (a < m1) {
+                m2 = m1;
+                m1 = a;
+                idx = j;
+            } else if (a < m2) {
+                m2 = a;
+            }
+        }
+    }
+    const unsigned tot = static_cast<unsigned>(__popc(neg)) & 1u;
+    const float n1 = nms_mag(d.alpha, d.beta, m1);
+    const float n2 = nms_mag(d.alpha, d.beta, m2);
+    unsigned nm = static_cast<unsigned>(idx) << 27;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+        if (v[j] >= 0) {
+            const unsigned sgn = tot ^ ((neg >> j) & 1u);
+            const float mag = (j == idx) ? n2 : n1;
+            nm |= sgn << j;
+            app[v[j]] = __fadd_rn(qv[j], sgn ? -mag : mag);
+        }
+    }
+    r1[ridx] = n1;
+    r2[ridx] = n2;
+    meta[ridx] = nm;
+}
+
+__device__ __forceinline__ void group_sync(int id, int threads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+// One codeword on a group of W warps (named barrier `bar`).
+template <int D, int W>
+__device__ __forceinline__ void wide_unit(const MixedIO& io, const CodeDesc& d, int cw, float* app, float* best, int g,
+                                          int gl, int bar, int* s_red, unsigned long long* s_off)
+{
+    constexpr int G = W * 32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = d.n;
+    const int mp = d.num_layers * d.width;
+    float* r1 = app + ((n + 3) & ~3);
+    float* r2 = r1 + mp;
+    unsigned* meta = reinterpret_cast<unsigned*>(r2 + mp);
+    const float* src = io.llr + io.llr_off[cw];
+    for (int i = gl; i < n; i += G) {
+        const float x = __ldcs(src + i);
+        app[i] = x;
+        if (d.route_osd) best[i] = x;
+    }
+    for (int r = gl; r < mp; r += G) {
+        r1[r] = 0.0f;
+        r2[r] = 0.0f;
+        meta[r] = 0u;
+    }
+    group_sync(bar, G);
+    auto syndrome = [&]() -> int {
+        const unsigned c = __reduce_add_sync(0xffffffffu, static_cast<unsigned>(lane_syndrome(d, app, gl, G)));
+        if (lane == 0) s_red[g * W + (warp % W)] = static_cast<int>(c);
+        group_sync(bar, G);
+        int tot = 0;
+#pragma unroll
+        for (int i = 0; i < W; ++i) tot += s_red[g * W + i];
+        return tot;
+    };
+    int best_w = syndrome();
+    int iter = 0;
+    for (;;) {
+        for (int L = 0; L < d.num_layers; ++L) {
+            for (int rr = 0; rr < d.rows_per_lane; ++rr) update_row<D>(d, app, r1, r2, meta, L, gl + rr * G);
+            group_sync(bar, G);
+        }
+        const int w = syndrome();
+        ++iter;
+        if (d.route_osd && (w < best_w || w == 0)) {
+            for (int i = gl; i < n; i += G) best[i] = app[i];
+            group_sync(bar, G);  // copied before the next layer rewrites the posteriors
+        }
+        if (w < best_w) best_w = w;
+        if (w == 0 || iter >= d.max_iter) {
+            const bool ok = (w == 0);
+            if (gl == 0) {
+                if (io.success) io.success[cw] = ok ? 1 : 0;
+                if (io.iterations) io.iterations[cw] = static_cast<uint8_t>(iter);
+                if (io.used_osd) io.used_osd[cw] = 0;
+            }
+            uint8_t* dst = io.info + io.info_off[cw];
+            for (int i = gl; i < d.k; i += G) dst[i] = app[i] < 0.0f ? 1 : 0;
+            if (!ok && d.route_osd && (io.protect == nullptr || io.protect[cw])) {
+                if (gl == 0) {
+                    const int it = atomicAdd(io.osd_count, 1);
+                    const unsigned long long off = atomicAdd(io.osd_floats, static_cast<unsigned long long>(n));
+                    io.osd_index[it] = cw;
+                    io.osd_rowoff[it] = static_cast<long long>(off);
+                    s_off[g] = off;
+                }
+                group_sync(bar, G);
+                float* o = io.osd_llr + s_off[g];
+                for (int i = gl; i < n; i += G) o[i] = best[i];
+            }
+            return;
+        }
+    }
+}
+
+// Phase of groups of W warps (W = 4: named barriers 1-2, W = 2: 3-6), one
+// codeword per group at a time from `counter`, up to unit `u_end`.
+template <int D, int W>
+__device__ void wide_phase(const MixedIO& io, float* smem_f, int warp_floats, int* counter, int u_end, int* s_unit,
+                           int* s_red, unsigned long long* s_off)
+{
+    constexpr int G = W * 32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = warp / W;
+    const int gl = (warp % W) * 32 + lane;
+    const int bar = (W == 4 ? 1 : 3) + g;
+    float* app = smem_f + static_cast<size_t>(g * W) * warp_floats;
+    const int gwarp0 = blockIdx.x * (blockDim.x >> 5) + g * W;
+    float* best = io.best + static_cast<size_t>(gwarp0) * 4 * io.n_max;
+    for (;;) {
+        if (gl == 0) s_unit[g] = atomicAdd(counter, 1);
+        group_sync(bar, G);
+        const int u = s_unit[g];
+        if (u >= u_end) break;  // the same value for the whole group
+        int q = 0;
+        while (q + 1 < io.K && u >= io.q_units[q + 1]) ++q;
+        const CodeDesc d = io.codes[io.q_code[q]];
+        const int cw = io.order[io.q_start[q] + (u - io.q_units[q])];
+        wide_unit<D, W>(io, d, cw, app, best, g, gl, bar, s_red, s_off);
+        group_sync(bar, G);  // the slot and s_unit are rewritten by the next unit
+    }
+}
+
+// Up to 32/G codewords of one code on one warp, G lanes each.
+template <int D>
+__device__ __forceinline__ void narrow_unit(const MixedIO& io, const CodeDesc& d, int q, int u, float* wbase, int gwarp)
+{
+    const int lane = threadIdx.x & 31;
+    const int G = d.group;
+    const int per = 32 / G;
+    const int sub = lane / G;
+    const int gl = lane & (G - 1);
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
+    const int local = (u - io.q_units[q]) * per + sub;
+    bool active = local < io.q_start[q + 1] - io.q_start[q];
+    const int cw = active ? io.order[io.q_start[q] + local] : 0;
+    const int n = d.n;
+    const int n_pad = (n + 3) & ~3;
+    const int mp = d.num_layers * d.width;
+    float* app = wbase + sub * d.slot_floats;
+    float* r1 = app + n_pad;
+    float* r2 = r1 + mp;
+    unsigned* meta = reinterpret_cast<unsigned*>(r2 + mp);
+    float* best = io.best + (static_cast<size_t>(gwarp) * 4 + sub) * io.n_max;
+    int iter = 0, best_w = 0;
+    if (active) {
+        const float* src = io.llr + io.llr_off[cw];
+        for (int i = gl; i < n; i += G) {
+            const float v = __ldcs(src + i);
+            app[i] = v;
+            if (d.route_osd) best[i] = v;
+        }
+        for (int r = gl; r < mp; r += G) {
+            r1[r] = 0.0f;
+            r2[r] = 0.0f;
+            meta[r] = 0u;
+        }
+        __syncwarp(gmask);
+        best_w = mixed_syndrome(d, app, gl, G, gmask);
+    }
+    while (__any_sync(0xffffffffu, active)) {
+        if (!active) continue;
+        for (int L = 0; L < d.num_layers; ++L) {
+            for (int rr = 0; rr < d.rows_per_lane; ++rr) update_row<D>(d, app, r1, r2, meta, L, gl + rr * G);
+            __syncwarp(gmask);
+        }
+        const int w = mixed_syndrome(d, app, gl, G, gmask);
+        ++iter;
+        if (d.route_osd && (w < best_w || w == 0)) {
+            for (int i = gl; i < n; i += G) best[i] = app[i];
+            __syncwarp(gmask);
+        }
+        if (w < best_w) best_w = w;
+        if (w == 0 || iter >= d.max_iter) {
+            const bool ok = (w == 0);
+            if (gl == 0) {
+                if (io.success) io.success[cw] = ok ? 1 : 0;
+                if (io.iterations) io.iterations[cw] = static_cast<uint8_t>(iter);
+                if (io.used_osd) io.used_osd[cw] = 0;
+            }
+            uint8_t* dst = io.info + io.info_off[cw];
+            for (int i = gl; i < d.k; i += G) dst[i] = app[i] < 0.0f ? 1 : 0;
+            if (!ok && d.route_osd && (io.protect == nullptr || io.protect[cw])) {
+                unsigned long long off = 0ull;
+                if (gl == 0) {
+                    const int it = atomicAdd(io.osd_count, 1);
+                    off = atomicAdd(io.osd_floats, static_cast<unsigned long long>(n));
+                    io.osd_index[it] = cw;
+                    io.osd_rowoff[it] = static_cast<long long>(off);
+                }
+                const unsigned lo = __shfl_sync(gmask, static_cast<unsigned>(off), sub * G);
+                const unsigned hi = __shfl_sync(gmask, static_cast<unsigned>(off >> 32), sub * G);
+                float* o = io.osd_llr + ((static_cast<unsigned long long>(hi) << 32) | lo);
+                for (int i = gl; i < n; i += G) o[i] = best[i];
+            }
+            active = false;
+        }
+    }
+    __syncwarp();
 }
 
 template <int D>
@@ -123,135 +386,29 @@ __global__ void __launch_bounds__(256)
 bp_mixed_kernel(MixedIO io, int warp_floats)
 {
     extern __shared__ __align__(16) float smem_f[];
+    __shared__ int s_unit[4];
+    __shared__ int s_red[8];
+    __shared__ unsigned long long s_off[4];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+
+    // phases 1 and 2: codewords of wide codes on groups of 4, then 2 warps
+    wide_phase<D, 4>(io, smem_f, warp_floats, io.work4, io.bounds[0], s_unit, s_red, s_off);
+    wide_phase<D, 2>(io, smem_f, warp_floats, io.work2, io.bounds[1], s_unit, s_red, s_off);
+
+    // phase 3: one warp per unit
     float* wbase = smem_f + static_cast<size_t>(warp) * warp_floats;
     const int gwarp = blockIdx.x * (blockDim.x >> 5) + warp;
     const int total_units = io.q_units[io.K];
-
     for (;;) {
         int u = 0;
-        if (lane == 0) u = atomicAdd(io.work, 1);
+        if (lane == 0) u = atomicAdd(io.work1, 1);
         u = __shfl_sync(0xffffffffu, u, 0);
         if (u >= total_units) break;
         int q = 0;
         while (q + 1 < io.K && u >= io.q_units[q + 1]) ++q;
         const CodeDesc d = io.codes[io.q_code[q]];
-        const int G = d.group;
-        const int per = 32 / G;
-        const int sub = lane / G;
-        const int gl = lane & (G - 1);
-        const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
-        const int local = (u - io.q_units[q]) * per + sub;
-        bool active = local < io.q_start[q + 1] - io.q_start[q];
-        const int cw = active ? io.order[io.q_start[q] + local] : 0;
-        const int n = d.n;
-        const int n_pad = (n + 3) & ~3;
-        const int mp = d.num_layers * d.width;
-        float* app = wbase + sub * d.slot_floats;
-        float* r1 = app + n_pad;
-        float* r2 = r1 + mp;
-        unsigned* meta = reinterpret_cast<unsigned*>(r2 + mp);
-        float* best = io.best + (static_cast<size_t>(gwarp) * 4 + sub) * io.n_max;
-        int iter = 0, best_w = 0;
-        if (active) {
-            const float* src = io.llr + io.llr_off[cw];
-            for (int i = gl; i < n; i += G) {
-                const float v = __ldcs(src + i);
-                app[i] = v;
-                if (d.route_osd) best[i] = v;
-            }
-            for (int r = gl; r < mp; r += G) {
-                r1[r] = 0.0f;
-                r2[r] = 0.0f;
-                meta[r] = 0u;
-            }
-            __syncwarp(gmask);
-            best_w = mixed_syndrome(d, app, gl, G, gmask);
-        }
-        while (__any_sync(0xffffffffu, active)) {
-            if (!active) continue;
-            for (int L = 0; L < d.num_layers; ++L) {
-                for (int rr = 0; rr < d.rows_per_lane; ++rr) {
-                    const int rs = gl + rr * G;
-                    const int ridx = L * d.width + rs;
-                    const float o1 = r1[ridx], o2 = r2[ridx];
-                    const unsigned om = meta[ridx];
-                    const int* vp = d.vars + (L * d.maxdeg) * d.width + rs;
-                    float qv[D];
-                    int v[D];
-                    float m1 = FLT_MAX, m2 = FLT_MAX;
-                    int idx = 0;
-                    unsigned neg = 0;
-#pragma unroll
-                    for (int j = 0; j < D; ++j) {
-                        v[j] = (j < d.maxdeg) ? __ldg(vp + j * d.width) : -1;
-                        qv[j] = 0.0f;
-                        if (v[j] >= 0) {
-                            const float qj = __fsub_rn(app[v[j]], rebuild(o1, o2, om, j));
-                            qv[j] = qj;
-                            neg |= (qj < 0.0f) ? (1u << j) : 0u;
-                            const float a = fabsf(qj);
-                            if (a < m1) {
-                                m2 = m1;
-                                m1 = a;
-                                idx = j;
-                            } else if (a < m2) {
-                                m2 = a;
-                            }
-                        }
-                    }
-                    const unsigned tot = static_cast<unsigned>(__popc(neg)) & 1u;
-                    const float n1 = nms_mag(d.alpha, d.beta, m1);
-                    const float n2 = nms_mag(d.alpha, d.beta, m2);
-                    unsigned nm = static_cast<unsigned>(idx) << 27;
-#pragma unroll
-                    for (int j = 0; j < D; ++j) {
-                        if (v[j] >= 0) {
-                            const unsigned s = tot ^ ((neg >> j) & 1u);
-                            const float mag = (j == idx) ? n2 : n1;
-                            nm |= s << j;
-                            app[v[j]] = __fadd_rn(qv[j], s ? -mag : mag);
-                        }
-                    }
-                    r1[ridx] = n1;
-                    r2[ridx] = n2;
-                    meta[ridx] = nm;
-                }
-                __syncwarp(gmask);
-            }
-            const int w = mixed_syndrome(d, app, gl, G, gmask);
-            ++iter;
-            if (d.route_osd && (w < best_w || w == 0)) {
-                for (int i = gl; i < n; i += G) best[i] = app[i];
-            }
-            if (w < best_w) best_w = w;
-            if (w == 0 || iter >= d.max_iter) {
-                const bool ok = (w == 0);
-                if (gl == 0) {
-                    if (io.success) io.success[cw] = ok ? 1 : 0;
-                    if (io.iterations) io.iterations[cw] = static_cast<uint8_t>(iter);
-                    if (io.used_osd) io.used_osd[cw] = 0;
-                }
-                uint8_t* dst = io.info + io.info_off[cw];
-                for (int i = gl; i < d.k; i += G) dst[i] = app[i] < 0.0f ? 1 : 0;
-                if (!ok && d.route_osd && (io.protect == nullptr || io.protect[cw])) {
-                    unsigned long long off = 0ull;
-                    if (gl == 0) {
-                        const int it = atomicAdd(io.osd_count, 1);
-                        off = atomicAdd(io.osd_floats, static_cast<unsigned long long>(n));
-                        io.osd_index[it] = cw;
-                        io.osd_rowoff[it] = static_cast<long long>(off);
-                    }
-                    const unsigned lo = __shfl_sync(gmask, static_cast<unsigned>(off), sub * G);
-                    const unsigned hi = __shfl_sync(gmask, static_cast<unsigned>(off >> 32), sub * G);
-                    float* o = io.osd_llr + ((static_cast<unsigned long long>(hi) << 32) | lo);
-                    for (int i = gl; i < n; i += G) o[i] = best[i];
-                }
-                active = false;
-            }
-        }
-        __syncwarp();
+        narrow_unit<D>(io, d, q, u, wbase, gwarp);
     }
 }
 
@@ -275,11 +432,14 @@ struct Engine {
     OsdView* d_views = nullptr;
     OsdHView* d_hviews = nullptr;
     int* d_per_warp = nullptr;
+    int* d_q_warps = nullptr;   // [K] warps per codeword of the code at each queue position
     int* d_q_code = nullptr;
     int* d_q_start = nullptr;
     int* d_q_units = nullptr;
     int* d_order = nullptr;
-    int* d_counters = nullptr;  // [0] work, [1] osd count, [2..3] osd float counter (64-bit)
+    // [0] 4-warp units, [1] OSD items, [2..3] OSD row floats (64-bit), [4] 2-warp units,
+    // [5] single-warp units, [6..7] ends of the 4-warp and 2-warp units
+    int* d_counters = nullptr;
     long long* d_osd_rowoff = nullptr;
     int* d_osd_index = nullptr;
     float* d_osd_llr = nullptr;
@@ -292,7 +452,7 @@ struct Engine {
     ~Engine()
     {
         for (void* p : {static_cast<void*>(d_codes), static_cast<void*>(d_views), static_cast<void*>(d_hviews),
-                        static_cast<void*>(d_per_warp),
+                        static_cast<void*>(d_per_warp), static_cast<void*>(d_q_warps),
                         static_cast<void*>(d_q_code), static_cast<void*>(d_q_start), static_cast<void*>(d_q_units),
                         static_cast<void*>(d_order), static_cast<void*>(d_counters), static_cast<void*>(d_osd_index),
                         static_cast<void*>(d_osd_llr), static_cast<void*>(d_best), static_cast<void*>(d_osd_rowoff)})
@@ -301,11 +461,17 @@ struct Engine {
             if (e) cudaEventDestroy(e);
     }
 
+    // shared-memory floats per warp: a narrow code's 32/G slots, or a W-warp
+    // group's slot spread over its W warps
     int warp_floats() const
     {
         int w = 0;
-        for (const auto& c : codes) w = std::max(w, (32 / c.desc.group) * c.desc.slot_floats);
-        return w;
+        for (const auto& c : codes) {
+            const int need = c.desc.warps > 1 ? (c.desc.slot_floats + c.desc.warps - 1) / c.desc.warps
+                                              : (32 / c.desc.group) * c.desc.slot_floats;
+            w = std::max(w, need);
+        }
+        return (w + 3) & ~3;
     }
 
     // Uploads the code descriptors and the queue order after codes change.
@@ -316,16 +482,20 @@ struct Engine {
         std::vector<CodeDesc> descs(K);
         std::vector<OsdView> views(K);
         std::vector<OsdHView> hviews(K);
-        std::vector<int> per(K), qcode(K);
+        std::vector<int> per(K), qcode(K), qwarps(K);
         for (int c = 0; c < K; ++c) {
             descs[c] = codes[c].desc;
-            per[c] = 32 / codes[c].desc.group;
+            per[c] = codes[c].desc.warps > 1 ? 1 : 32 / codes[c].desc.group;
             views[c] = codes[c].osd ? codes[c].code->osd_view() : OsdView{};
             hviews[c] = codes[c].osd_h ? codes[c].code->osd_h_view() : OsdHView{};
             qcode[c] = c;
         }
-        // queue order: most expensive codes first, so the long codewords start early
-        std::stable_sort(qcode.begin(), qcode.end(), [&](int a, int b) { return codes[a].cost > codes[b].cost; });
+        // queue order: 4-warp codes, 2-warp codes, then the rest; within each, most expensive first
+        std::stable_sort(qcode.begin(), qcode.end(), [&](int a, int b) {
+            if (codes[a].desc.warps != codes[b].desc.warps) return codes[a].desc.warps > codes[b].desc.warps;
+            return codes[a].cost > codes[b].cost;
+        });
+        for (int q = 0; q < K; ++q) qwarps[q] = codes[qcode[q]].desc.warps;
         auto up = [](auto*& dst, const auto& v) {
             using T = std::remove_reference_t<decltype(v[0])>;
             if (dst) cudaFree(dst);
@@ -336,6 +506,7 @@ struct Engine {
         up(d_views, views);
         up(d_hviews, hviews);
         up(d_per_warp, per);
+        up(d_q_warps, qwarps);
         up(d_q_code, qcode);
         dirty = false;
     }
@@ -371,8 +542,9 @@ template <int D>
 void launch_mixed(Engine& e, const MixedIO& io, cudaStream_t st)
 {
     const int wf = e.warp_floats();
-    int warps = e.warps_per_cta > 0 ? e.warps_per_cta : 8;
-    while (warps > 1 && static_cast<size_t>(warps) * wf * sizeof(float) > 200 * 1024) --warps;
+    // whole groups of 4 warps (the wide phases split a CTA into groups of 4 and 2 warps)
+    int warps = e.warps_per_cta == 4 ? 4 : 8;
+    if (static_cast<size_t>(warps) * wf * sizeof(float) > 200 * 1024) warps = 4;
     const size_t smem = static_cast<size_t>(warps) * wf * sizeof(float);
     if (smem > 227 * 1024) throw InvalidArgument("a registered code is too large for the mixed kernel");
     check_cuda(cudaFuncSetAttribute(bp_mixed_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -420,7 +592,7 @@ int sicc_engine_create(const sicc_engine_config_t* config, unsigned long long* o
         check_cuda(cudaMalloc(&e->d_order, sizeof(int) * config->max_codewords), "cudaMalloc(order)");
         check_cuda(cudaMalloc(&e->d_q_start, sizeof(int) * (kMaxCodes + 1)), "cudaMalloc(q_start)");
         check_cuda(cudaMalloc(&e->d_q_units, sizeof(int) * (kMaxCodes + 1)), "cudaMalloc(q_units)");
-        check_cuda(cudaMalloc(&e->d_counters, sizeof(int) * 4), "cudaMalloc(counters)");
+        check_cuda(cudaMalloc(&e->d_counters, sizeof(int) * 8), "cudaMalloc(counters)");
         check_cuda(cudaMalloc(&e->d_osd_rowoff, sizeof(long long) * config->max_codewords), "cudaMalloc(osd rows)");
         check_cuda(cudaMalloc(&e->d_osd_index, sizeof(int) * config->max_codewords), "cudaMalloc(osd index)");
         check_cuda(cudaMalloc(&e->d_osd_llr, sizeof(float) * config->max_llr_floats), "cudaMalloc(osd rows)");
@@ -487,6 +659,13 @@ int sicc_engine_add_code(unsigned long long handle, const sicc_engine_code_t* co
         d.maxdeg = lv.maxdeg;
         d.group = lv.group;
         d.rows_per_lane = lv.rows_per_lane;
+        d.warps = 1;
+        if (lv.width >= 128 && lv.width % 128 == 0) d.warps = 4;      // layers of >= 128 rows: 128 lanes
+        else if (lv.width >= 64 && lv.width % 64 == 0) d.warps = 2;   // 64-row layers: 64 lanes
+        if (d.warps > 1) {
+            d.group = 32 * d.warps;
+            d.rows_per_lane = lv.width / d.group;
+        }
         d.max_iter = code->max_iterations;
         d.alpha = code->normalization;
         d.beta = code->offset;
@@ -548,9 +727,8 @@ int sicc_engine_decode_device_protected(unsigned long long handle, int codewords
         cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
         const int K = static_cast<int>(e->codes.size());
         check_cuda(cudaEventRecord(e->ev[0], st), "cudaEventRecord");
-        prepare_kernel<<<1, 1024, 0, st>>>(device_code_ids, codewords, e->d_q_code, K, e->d_per_warp, e->d_order,
-                                           e->d_q_start, e->d_q_units, e->d_counters, e->d_counters + 1,
-                                           reinterpret_cast<unsigned long long*>(e->d_counters + 2));
+        prepare_kernel<<<1, 1024, 0, st>>>(device_code_ids, codewords, e->d_q_code, K, e->d_per_warp, e->d_q_warps,
+                                           e->d_order, e->d_q_start, e->d_q_units, e->d_counters);
         check_cuda(cudaGetLastError(), "prepare_kernel launch");
         check_cuda(cudaEventRecord(e->ev[1], st), "cudaEventRecord");
         MixedIO io{};
@@ -569,7 +747,10 @@ int sicc_engine_decode_device_protected(unsigned long long handle, int codewords
         io.q_start = e->d_q_start;
         io.q_units = e->d_q_units;
         io.K = K;
-        io.work = e->d_counters;
+        io.work4 = e->d_counters;
+        io.work2 = e->d_counters + 4;
+        io.work1 = e->d_counters + 5;
+        io.bounds = e->d_counters + 6;
         io.n_max = e->n_max;
         io.osd_llr = e->d_osd_llr;
         io.osd_index = e->d_osd_index;

@@ -14,8 +14,9 @@
 //     greedy scan gives the extreme basis in either order);
 //   * those m columns are found by Gauss-Jordan elimination on H: the
 //     accumulated row operations T (m x m bits, 128 KiB at m = 1024) live in
-//     shared memory, and column c's reduced form is T h_c, the XOR of the few
-//     columns of T that h_c selects (column weight <= 16);
+//     shared memory column-major, column c's reduced form is T h_c, the XOR
+//     of the few columns of T that h_c selects (column weight <= 16), and a
+//     pivot touches only the columns of T with a 1 in the pivot row;
 //   * with T H in reduced form on those columns, a candidate that keeps the
 //     hard decisions on the MRB except a flip set F differs from the hard
 //     decisions at the pivot positions selected by T s XOR (XOR over f in F of
@@ -39,25 +40,28 @@ struct OsdHLayout {
     int np;       // sort length: power of two >= the longest n
     int nmax;
     int mw;       // words per row of T for the largest m
-    int ts;       // row stride of T in words (odd: a warp reading one word of 32 rows hits 32 banks)
+    int ts;       // column stride of T in words (odd: a warp reading one word of 32 columns hits 32 banks)
     int poolmax;
 };
 
 struct OsdHSmem {
-    uint32_t* T;             // [32*mw][ts]
+    uint32_t* T;             // [32*mw][ts] column-major: column i of the row-operation matrix
     unsigned long long* keys;// [np]; reused as the flip-pool scratch after the sort
     float* rel;              // [nmax] |llr| by sorted position j
     int16_t* perm;           // [nmax] code position at sorted position j
-    int16_t* row_of_col;     // [nmax] pivot row of a code position, -1 for the MRB
+    int16_t* row_of_col;     // [nmax] pivot rank of a code position, -1 for the MRB
     uint32_t* hard;          // [nmax/32+1] hard decisions by code position
-    uint32_t* vw;            // [mw] reduced column of the position being scanned
+    uint32_t* wv;            // [2][32] v + e_p of the last two pivots
+    uint32_t* piv;           // [mw] pivoted rows
+    int16_t* order;          // [32*mw] row of the t-th pivot
+    uint32_t* vs;            // [poolmax+1][32] T s and T h_f by row (before reordering)
     uint32_t* syn;           // [mw] s = H * hard by row of H
-    int16_t* pivj;           // [32*mw] sorted position of each pivot row's column
-    float* relq;             // [32*mw] |llr| of each pivot row's column
+    int16_t* pivj;           // [32*mw] sorted position of the t-th pivot's column
+    float* relq;             // [32*mw] |llr| of the t-th pivot's column
     int16_t* mrb;            // [nmax] dependent positions met during the scan (descending j)
     int16_t* pool_j;         // [poolmax] flip pool (sorted positions, weakest first)
-    uint32_t* avec;          // [poolmax][mw] T h_f for the pool
-    uint32_t* aug;           // [mw] T s
+    uint32_t* avec;          // [poolmax][mw] T h_f for the pool, bit t = pivot rank t
+    uint32_t* aug;           // [mw] T s, bit t = pivot rank t
 };
 
 __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -78,7 +82,10 @@ __host__ __device__ inline size_t carve(const OsdHLayout& l, unsigned char* base
     t.perm = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nmax) * 2));
     t.row_of_col = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nmax) * 2));
     t.hard = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(l.nmax) / 32 + 1) * 4));
-    t.vw = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.mw) * 4));
+    t.wv = reinterpret_cast<uint32_t*>(take(64 * 4));
+    t.piv = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.mw) * 4));
+    t.order = reinterpret_cast<int16_t*>(take(rows * 2));
+    t.vs = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(l.poolmax) + 1) * 32 * 4));
     t.syn = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.mw) * 4));
     t.pivj = reinterpret_cast<int16_t*>(take(rows * 2));
     t.relq = reinterpret_cast<float*>(take(rows * 4));
@@ -92,14 +99,6 @@ __host__ __device__ inline size_t carve(const OsdHLayout& l, unsigned char* base
 
 __device__ __forceinline__ unsigned tbit(const uint32_t* row, int q) { return (row[q >> 5] >> (q & 31)) & 1u; }
 
-// Reduced column T h_c, bit of row r.
-__device__ __forceinline__ unsigned reduced_bit(const uint32_t* Trow, const int* __restrict__ col_rows, int e0, int e1)
-{
-    unsigned v = 0;
-    for (int e = e0; e < e1; ++e) v ^= tbit(Trow, col_rows[e]);
-    return v;
-}
-
 }  // namespace
 
 __global__ void __launch_bounds__(kOsdHThreads, 1)
@@ -108,7 +107,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     OsdHSmem s;
     carve(lay, smem_raw, &s);
-    __shared__ int s_piv[3];
+    __shared__ int s_p[2];
     __shared__ int s_nd;
     __shared__ unsigned long long s_best;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -162,10 +161,10 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             s.perm[j] = static_cast<int16_t>(key & 0xffffffffull);
             s.rel[j] = __uint_as_float(0x7fffffffu - static_cast<unsigned>(key >> 32));
         }
-        // ---- 2. T = identity, syndrome of the hard decisions ----
+        // ---- 2. T = identity (column-major), syndrome of the hard decisions ----
         for (int i = tid; i < rows * TS; i += kOsdHThreads) {
-            const int r = i / TS, w = i - r * TS;
-            s.T[i] = (r < m && w == (r >> 5)) ? (1u << (r & 31)) : 0u;
+            const int col = i / TS, w = i - col * TS;
+            s.T[i] = (col < m && w == (col >> 5)) ? (1u << (col & 31)) : 0u;
         }
         for (int r = tid; r < rows; r += kOsdHThreads) {
             unsigned par = 0;
@@ -174,66 +173,109 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             const unsigned b = __ballot_sync(0xffffffffu, par);
             if (lane == 0) s.syn[r >> 5] = b;
         }
-        if (tid == 0) {
-            s_piv[0] = s_piv[1] = s_piv[2] = INT_MAX;
-            s_nd = 0;
+        for (int w = tid; w < MW; w += kOsdHThreads) s.piv[w] = 0u;
+        // column of H at each sorted position: first edge << 8 | weight (the sort keys are dead)
+        int* colinfo = reinterpret_cast<int*>(s.keys);
+        for (int j = tid; j < n; j += kOsdHThreads) {
+            const int c = s.perm[j];
+            const int e0 = hv.col_ptr[c];
+            colinfo[j] = (e0 << 8) | (hv.col_ptr[c + 1] - e0);
         }
+        if (tid == 0) s_nd = 0;
         __syncthreads();
 
         // ---- 3. Gauss-Jordan scan of H's columns in increasing reliability ----
+        // Warp 0 forms the reduced column v = T h_c (XOR of the columns of T that
+        // h_c selects) and picks the lowest unpivoted row p with v_p = 1; then
+        // every column of T with a 1 in row p takes v + e_p (T <- (I + (v + e_p) e_p^T) T),
+        // which turns column c into e_p and leaves earlier pivot columns alone.
         int t = 0, jstop = -1, it = 0;
+        // warp 0 holds the rows of the next column, one per lane, loaded a column ahead
+        int nrow = -1, ncnt = 0, ne0 = 0;
+        if (warp == 0) {
+            const int ci = colinfo[n - 1];
+            ne0 = ci >> 8;
+            ncnt = ci & 255;
+            nrow = lane < ncnt ? hv.col_rows[ne0 + lane] : -1;
+        }
         for (int j = n - 1; j >= 0; --j, ++it) {
-            const int c = s.perm[j];
-            const int e0 = hv.col_ptr[c], e1 = hv.col_ptr[c + 1];
-            const int cur = it % 3;
-            for (int r = tid; r < rows; r += kOsdHThreads) {
-                const unsigned v = reduced_bit(s.T + static_cast<size_t>(r) * TS, hv.col_rows, e0, e1);
-                const unsigned b = __ballot_sync(0xffffffffu, v);
-                const int r0 = r & ~31;
-                unsigned cand = b;
-                if (r0 + 32 <= t) cand = 0u;
-                else if (r0 < t) cand &= ~0u << (t - r0);
-                if (lane == 0) {
-                    s.vw[r >> 5] = b;
-                    if (cand) atomicMin(&s_piv[cur], r0 + __ffs(cand) - 1);
-                }
-            }
-            __syncthreads();
-            const int p = s_piv[cur];
-            // buffer (it+2)%3 was last read before this iteration's barrier and is next
-            // written after the following one
-            if (tid == 0) s_piv[(it + 2) % 3] = INT_MAX;
-            if (p == INT_MAX) {  // dependent on the pivots so far: an MRB position
-                if (tid == 0) s.mrb[s_nd++] = static_cast<int16_t>(j);
-                continue;
-            }
+            const int buf = it & 1;  // double-buffered: read after this barrier, rewritten two barriers later
             if (warp == 0) {
-                if (p != t) {
-                    for (int w = lane; w < MW; w += 32) {
-                        const uint32_t a = s.T[static_cast<size_t>(t) * TS + w];
-                        s.T[static_cast<size_t>(t) * TS + w] = s.T[static_cast<size_t>(p) * TS + w];
-                        s.T[static_cast<size_t>(p) * TS + w] = a;
+                const int c = s.perm[j];
+                unsigned v = 0u;
+                const int cnt = ncnt, e0 = ne0, myrow = nrow;
+                // the column's rows in groups of 8, all loads of a group in flight together
+                for (int e = 0; e < cnt && e < 32; e += 8) {
+                    unsigned part[8];
+#pragma unroll
+                    for (int x = 0; x < 8; ++x) {
+                        const int q = __shfl_sync(0xffffffffu, myrow, (e + x) & 31);
+                        part[x] = (e + x < cnt && lane < MW) ? s.T[static_cast<size_t>(q) * TS + lane] : 0u;
                     }
+                    v ^= (part[0] ^ part[1]) ^ (part[2] ^ part[3]) ^ (part[4] ^ part[5]) ^ (part[6] ^ part[7]);
                 }
-                if (lane == 0) {
-                    // after the swap row t holds the pivot and row p the former row t
-                    const unsigned vt = (s.vw[t >> 5] >> (t & 31)) & 1u;
-                    s.vw[p >> 5] = (s.vw[p >> 5] & ~(1u << (p & 31))) | (vt << (p & 31));
-                    s.vw[t >> 5] &= ~(1u << (t & 31));
-                    s.row_of_col[c] = static_cast<int16_t>(t);
-                    s.pivj[t] = static_cast<int16_t>(j);
+                for (int e = 32; e < cnt; ++e)  // columns heavier than 32
+                    if (lane < MW) v ^= s.T[static_cast<size_t>(hv.col_rows[e0 + e]) * TS + lane];
+                if (j > 0) {  // prefetch the next column's rows
+                    const int ci = colinfo[j - 1];
+                    ne0 = ci >> 8;
+                    ncnt = ci & 255;
+                    nrow = lane < ncnt ? hv.col_rows[ne0 + lane] : -1;
                 }
+                const unsigned x = (lane < MW) ? (v & ~s.piv[lane]) : 0u;
+                const unsigned lanes = __ballot_sync(0xffffffffu, x != 0u);
+                int p = -1;
+                if (lanes) {
+                    const int l0 = __ffs(lanes) - 1;
+                    const unsigned x0 = __shfl_sync(0xffffffffu, x, l0);
+                    p = l0 * 32 + __ffs(x0) - 1;
+                    if (lane < MW) s.wv[buf * 32 + lane] = (lane == (p >> 5)) ? (v ^ (1u << (p & 31))) : v;
+                    if (lane == (p >> 5)) s.piv[lane] |= 1u << (p & 31);
+                    if (lane == 0) {
+                        s.order[t] = static_cast<int16_t>(p);
+                        s.row_of_col[c] = static_cast<int16_t>(t);
+                        s.pivj[t] = static_cast<int16_t>(j);
+                    }
+                } else if (lane == 0) {
+                    s.mrb[s_nd++] = static_cast<int16_t>(j);  // dependent: an MRB position
+                }
+                if (lane == 0) s_p[buf] = p;
             }
             __syncthreads();
+            const int p = s_p[buf];
+            if (p < 0) continue;
             {
-                const uint32_t* prow = s.T + static_cast<size_t>(t) * TS;
-                for (int q = warp; q < MW; q += kOsdHWarps) {
-                    unsigned bits = s.vw[q];
-                    while (bits) {
-                        const int b = __ffs(bits) - 1;
-                        bits &= bits - 1;
-                        uint32_t* row = s.T + static_cast<size_t>(q * 32 + b) * TS;
-                        for (int w = lane; w < MW; w += 32) row[w] ^= prow[w];
+                const unsigned wreg = (lane < MW) ? s.wv[buf * 32 + lane] : 0u;
+                const int pw = p >> 5;
+                const unsigned pb = 1u << (p & 31);
+                // the pivot-row bit of this warp's column chunks, loaded together
+                unsigned hits[(32 + kOsdHWarps - 1) / kOsdHWarps];
+#pragma unroll
+                for (int h = 0; h < (32 + kOsdHWarps - 1) / kOsdHWarps; ++h) {
+                    const int q = warp + h * kOsdHWarps;
+                    const bool in = q < MW && (s.T[static_cast<size_t>(q * 32 + lane) * TS + pw] & pb) != 0u;
+                    hits[h] = __ballot_sync(0xffffffffu, in);
+                }
+#pragma unroll
+                for (int h = 0; h < (32 + kOsdHWarps - 1) / kOsdHWarps; ++h) {
+                    const int q = warp + h * kOsdHWarps;
+                    unsigned hit = hits[h];
+                    while (hit) {  // two columns at a time: both loads in flight together
+                        const int b0 = __ffs(hit) - 1;
+                        hit &= hit - 1;
+                        uint32_t* c0 = s.T + static_cast<size_t>(q * 32 + b0) * TS;
+                        if (hit) {
+                            const int b1 = __ffs(hit) - 1;
+                            hit &= hit - 1;
+                            uint32_t* c1 = s.T + static_cast<size_t>(q * 32 + b1) * TS;
+                            if (lane < MW) {
+                                const uint32_t a0 = c0[lane], a1 = c1[lane];
+                                c0[lane] = a0 ^ wreg;
+                                c1[lane] = a1 ^ wreg;
+                            }
+                        } else if (lane < MW) {
+                            c0[lane] ^= wreg;
+                        }
                     }
                 }
             }
@@ -273,22 +315,39 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         }
         __syncthreads();
 
-        // ---- 5. T s and the reduced pool columns, by pivot row ----
+        // ---- 5. T s and the reduced pool columns, then in pivot order ----
         const int pool = hv.pool;
-        for (int r = tid; r < rows; r += kOsdHThreads) {
-            const uint32_t* Tr = s.T + static_cast<size_t>(r) * TS;
-            unsigned par = 0;
-            for (int w = 0; w < MW; ++w) par ^= __popc(Tr[w] & s.syn[w]);
-            unsigned b = __ballot_sync(0xffffffffu, par & 1u);
-            if (lane == 0) s.aug[r >> 5] = b;
-            for (int i = 0; i < pool; ++i) {
+        for (int i = tid; i < (pool + 1) * 32; i += kOsdHThreads) s.vs[i] = 0u;
+        __syncthreads();
+        {
+            // T s: XOR of the columns of T selected by s, spread over the warps
+            unsigned acc = 0u;
+            for (int q = warp; q < m; q += kOsdHWarps)
+                if (lane < MW && tbit(s.syn, q)) acc ^= s.T[static_cast<size_t>(q) * TS + lane];
+            if (lane < MW && acc) atomicXor(&s.vs[lane], acc);
+            // T h_f for the flip pool, one warp per column
+            for (int i = warp; i < pool; i += kOsdHWarps) {
                 const int c = s.perm[s.pool_j[i]];
-                const unsigned v = reduced_bit(Tr, hv.col_rows, hv.col_ptr[c], hv.col_ptr[c + 1]);
-                b = __ballot_sync(0xffffffffu, v);
-                if (lane == 0) s.avec[i * MW + (r >> 5)] = b;
+                unsigned v = 0u;
+                if (lane < MW)
+                    for (int e = hv.col_ptr[c]; e < hv.col_ptr[c + 1]; ++e)
+                        v ^= s.T[static_cast<size_t>(hv.col_rows[e]) * TS + lane];
+                if (lane < MW) s.vs[(i + 1) * 32 + lane] = v;
             }
-            s.relq[r] = r < m ? s.rel[s.pivj[r]] : 0.0f;
         }
+        __syncthreads();
+        // bit t of an ordered vector = bit order[t] of the row-indexed one
+        for (int vi = 0; vi <= pool; ++vi) {
+            const uint32_t* src_v = s.vs + vi * 32;
+            uint32_t* dst_v = vi == 0 ? s.aug : s.avec + (vi - 1) * MW;
+            for (int r = tid; r < rows; r += kOsdHThreads) {
+                const int q = r < m ? s.order[r] : -1;
+                const unsigned bit = q >= 0 ? tbit(src_v, q) : 0u;
+                const unsigned b = __ballot_sync(0xffffffffu, bit);
+                if (lane == 0) dst_v[r >> 5] = b;
+            }
+        }
+        for (int r = tid; r < rows; r += kOsdHThreads) s.relq[r] = r < m ? s.rel[s.pivj[r]] : 0.0f;
         __syncthreads();
 
         // ---- 6. candidates: metric in increasing sorted position, exact pruning ----
