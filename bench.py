@@ -603,8 +603,13 @@ def run_serve(args, rank, world):
     at_once = np.zeros(n_req)
     is_iq = np.array([q[0].kind == 1 for q in reqs])
 
+    def progress(msg):
+        print(f"[serve] {msg}", file=sys.stderr, flush=True)
+
+    progress(f"{n_req} requests, {info_bits} info bits; warm-up")
     for _ in range(args.warmup):
-        srv.replay(reqs, at_once)
+        _, wall = srv.replay(reqs, at_once)
+        progress(f"warm-up replay {wall * 1e-6:.3f} s")
     clocks = ClockSampler(dev)
     clocks.start()
     time.sleep(0.3)
@@ -616,6 +621,7 @@ def run_serve(args, rank, world):
     st1 = srv.stats()
     peak_s = statistics.median(walls) * 1e-6
     peak_mbps = info_bits / peak_s / 1e6
+    progress(f"peak {peak_mbps:.1f} Mbit/s ({peak_s:.3f} s per pass)")
     fe = [int(np.any(q[2] != tr, axis=1).sum()) for q, tr in zip(reqs, truth)]
     cw_total = sum(q[2].shape[0] for q in reqs)
     sweep = []
@@ -627,6 +633,7 @@ def run_serve(args, rank, world):
         b0 = srv.stats()
         res, wall = srv.replay(reqs, arr)
         b1 = srv.stats()
+        progress(f"load {load}: {wall * 1e-6:.3f} s")
         lat = np.array([d.latency_us for d in res]) * 1e-3
         wait = np.array([d.launch_us for d in res]) * 1e-3
         gpu = np.array([d.batch_gpu_us for d in res]) * 1e-3
@@ -718,7 +725,7 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH, help="frames per batch (profiling runs only)")
     ap.add_argument("--resident", type=int, default=RESIDENT_BATCHES, help="resident batches per Eb/N0")
     ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "ofdm_rx_1024_512", "mixed_100k", "serve_mixed"])
-    ap.add_argument("--serve-requests", type=int, default=2500)
+    ap.add_argument("--serve-requests", type=int, default=1500)
     ap.add_argument("--serve-batch", type=int, default=16384, help="codewords per server launch")
     ap.add_argument("--serve-inflight", type=int, default=2, help="batches overlapping on the device")
     ap.add_argument("--mixed-codewords", type=int, default=100_000)

@@ -28,7 +28,9 @@ namespace sicc {
 
 namespace {
 
-// Group-local syndrome weight of hard(app) under the layered tables.
+// Group-local syndrome weight of hard(app) under the layered tables; a row's
+// D slots are loaded together (no chain of dependent loads per slot).
+template <int D>
 __device__ __forceinline__ int layered_syndrome(const LayeredView& cv, const int* s_vars, const float* app,
                                                 int gl, int G, unsigned gmask)
 {
@@ -38,9 +40,17 @@ __device__ __forceinline__ int layered_syndrome(const LayeredView& cv, const int
             const int rs = gl + rr * G;
             const int* vp = s_vars + (L * cv.maxdeg) * cv.width + rs;
             unsigned par = 0;
-            for (int j = 0; j < cv.maxdeg; ++j) {
-                const int v = vp[j * cv.width];
-                if (v >= 0) par ^= (app[v] < 0.0f) ? 1u : 0u;
+#pragma unroll
+            for (int j0 = 0; j0 < D; j0 += 8) {  // groups of 8 slots bound the registers held
+                int v[8];
+#pragma unroll
+                for (int x = 0; x < 8; ++x) {
+                    const int j = j0 + x;
+                    v[x] = (j < D && j < cv.maxdeg) ? vp[j * cv.width] : -1;
+                }
+#pragma unroll
+                for (int x = 0; x < 8; ++x)
+                    if (v[x] >= 0) par ^= (app[v[x]] < 0.0f) ? 1u : 0u;
             }
             cnt += static_cast<int>(par);
         }
@@ -104,7 +114,7 @@ bp_layered_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int sl
             meta[r] = 0u;
         }
         __syncwarp(gmask);
-        best_w = layered_syndrome(cv, s_vars, app, gl, G, gmask);
+        best_w = layered_syndrome<D>(cv, s_vars, app, gl, G, gmask);
         iter = 0;
     };
 
@@ -162,7 +172,7 @@ bp_layered_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int sl
                 }
                 __syncwarp(gmask);
             }
-            const int w = layered_syndrome(cv, s_vars, app, gl, G, gmask);
+            const int w = layered_syndrome<D>(cv, s_vars, app, gl, G, gmask);
             ++iter;
             if (track_best && (w < best_w || (w == 0 && best_w == 0))) {
                 for (int i = gl; i < n; i += G) best[i] = app[i];

@@ -26,8 +26,8 @@ void launch_osd(const OsdView& ov, const OsdIO& io, int max_items, cudaStream_t 
                 int ctas = 0);
 
 // OSD of long codes, one CTA per codeword (io.hviews for mixed batches, else
-// `hv`); nmax/mmax/poolmax bound the codes of the launch.
-void launch_osd_h(const OsdHView& hv, int nmax, int mmax, int poolmax, const OsdIO& io, int max_items,
+// `hv`); nmax/mmax/poolmax/nnzmax (edges of H) bound the codes of the launch.
+void launch_osd_h(const OsdHView& hv, int nmax, int mmax, int poolmax, int nnzmax, const OsdIO& io, int max_items,
                   cudaStream_t st);
 size_t osd_h_smem_bytes(int nmax, int mmax, int poolmax);
 

@@ -123,7 +123,9 @@ __device__ __forceinline__ int row_var(const CodeDesc& d, int L, int j, int rs)
     return __ldg(d.vars + (L * d.maxdeg + j) * d.width + rs);
 }
 
-// Unsatisfied checks among the rows gl, gl + G, ... of every layer.
+// Unsatisfied checks among the rows gl, gl + G, ... of every layer; a row's
+// D slots are loaded together (no chain of dependent loads per slot).
+template <int D>
 __device__ __forceinline__ int lane_syndrome(const CodeDesc& d, const float* app, int gl, int G)
 {
     int cnt = 0;
@@ -131,9 +133,17 @@ __device__ __forceinline__ int lane_syndrome(const CodeDesc& d, const float* app
         for (int rr = 0; rr < d.rows_per_lane; ++rr) {
             const int rs = gl + rr * G;
             unsigned par = 0;
-            for (int j = 0; j < d.maxdeg; ++j) {
-                const int v = row_var(d, L, j, rs);
-                if (v >= 0) par ^= (app[v] < 0.0f) ? 1u : 0u;
+#pragma unroll
+            for (int j0 = 0; j0 < D; j0 += 8) {  // groups of 8 slots bound the registers held
+                int v[8];
+#pragma unroll
+                for (int x = 0; x < 8; ++x) {
+                    const int j = j0 + x;
+                    v[x] = (j < D && j < d.maxdeg) ? row_var(d, L, j, rs) : -1;
+                }
+#pragma unroll
+                for (int x = 0; x < 8; ++x)
+                    if (v[x] >= 0) par ^= (app[v[x]] < 0.0f) ? 1u : 0u;
             }
             cnt += static_cast<int>(par);
         }
@@ -141,9 +151,10 @@ __device__ __forceinline__ int lane_syndrome(const CodeDesc& d, const float* app
     return cnt;
 }
 
+template <int D>
 __device__ __forceinline__ int mixed_syndrome(const CodeDesc& d, const float* app, int gl, int G, unsigned gmask)
 {
-    return static_cast<int>(__reduce_add_sync(gmask, static_cast<unsigned>(lane_syndrome(d, app, gl, G))));
+    return static_cast<int>(__reduce_add_sync(gmask, static_cast<unsigned>(lane_syndrome<D>(d, app, gl, G))));
 }
 
 // Layered normalized min-sum update of row rs of layer L: extrinsic inputs
@@ -227,7 +238,7 @@ __device__ __forceinline__ void wide_unit(const MixedIO& io, const CodeDesc& d, 
     }
     group_sync(bar, G);
     auto syndrome = [&]() -> int {
-        const unsigned c = __reduce_add_sync(0xffffffffu, static_cast<unsigned>(lane_syndrome(d, app, gl, G)));
+        const unsigned c = __reduce_add_sync(0xffffffffu, static_cast<unsigned>(lane_syndrome<D>(d, app, gl, G)));
         if (lane == 0) s_red[g * W + (warp % W)] = static_cast<int>(c);
         group_sync(bar, G);
         int tot = 0;
@@ -276,7 +287,10 @@ __device__ __forceinline__ void wide_unit(const MixedIO& io, const CodeDesc& d, 
 }
 
 // Phase of groups of W warps (W = 4: named barriers 1-2, W = 2: 3-6), one
-// codeword per group at a time from `counter`, up to unit `u_end`.
+// codeword per group at a time from `counter`, up to unit `u_end`.  The
+// group scalars (s_unit, s_red, s_off) are the phase's own: a group of the
+// 2-warp phase can start while a 4-warp group of the same CTA is still
+// running, so the two phases must not share them.
 template <int D, int W>
 __device__ void wide_phase(const MixedIO& io, float* smem_f, int warp_floats, int* counter, int u_end, int* s_unit,
                            int* s_red, unsigned long long* s_off)
@@ -338,7 +352,7 @@ __device__ __forceinline__ void narrow_unit(const MixedIO& io, const CodeDesc& d
             meta[r] = 0u;
         }
         __syncwarp(gmask);
-        best_w = mixed_syndrome(d, app, gl, G, gmask);
+        best_w = mixed_syndrome<D>(d, app, gl, G, gmask);
     }
     while (__any_sync(0xffffffffu, active)) {
         if (!active) continue;
@@ -346,7 +360,7 @@ __device__ __forceinline__ void narrow_unit(const MixedIO& io, const CodeDesc& d
             for (int rr = 0; rr < d.rows_per_lane; ++rr) update_row<D>(d, app, r1, r2, meta, L, gl + rr * G);
             __syncwarp(gmask);
         }
-        const int w = mixed_syndrome(d, app, gl, G, gmask);
+        const int w = mixed_syndrome<D>(d, app, gl, G, gmask);
         ++iter;
         if (d.route_osd && (w < best_w || w == 0)) {
             for (int i = gl; i < n; i += G) best[i] = app[i];
@@ -386,15 +400,15 @@ __global__ void __launch_bounds__(256)
 bp_mixed_kernel(MixedIO io, int warp_floats)
 {
     extern __shared__ __align__(16) float smem_f[];
-    __shared__ int s_unit[4];
-    __shared__ int s_red[8];
-    __shared__ unsigned long long s_off[4];
+    __shared__ int s_unit4[2], s_unit2[4];
+    __shared__ int s_red4[8], s_red2[8];
+    __shared__ unsigned long long s_off4[2], s_off2[4];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
 
     // phases 1 and 2: codewords of wide codes on groups of 4, then 2 warps
-    wide_phase<D, 4>(io, smem_f, warp_floats, io.work4, io.bounds[0], s_unit, s_red, s_off);
-    wide_phase<D, 2>(io, smem_f, warp_floats, io.work2, io.bounds[1], s_unit, s_red, s_off);
+    wide_phase<D, 4>(io, smem_f, warp_floats, io.work4, io.bounds[0], s_unit4, s_red4, s_off4);
+    wide_phase<D, 2>(io, smem_f, warp_floats, io.work2, io.bounds[1], s_unit2, s_red2, s_off2);
 
     // phase 3: one warp per unit
     float* wbase = smem_f + static_cast<size_t>(warp) * warp_floats;
@@ -425,7 +439,7 @@ struct Engine {
     int device = 0;
     std::vector<EngineCode> codes;
     int n_max = 0, k_max = 0, maxdeg = 0, osd_nmax = 0, osd_kmax = 0;
-    int h_nmax = 0, h_mmax = 0, h_poolmax = 0;  // large-code OSD launch bounds
+    int h_nmax = 0, h_mmax = 0, h_poolmax = 0, h_nnzmax = 0;  // large-code OSD launch bounds
     int warps_per_cta = 0, ctas = 0;
     // device state
     CodeDesc* d_codes = nullptr;
@@ -688,6 +702,7 @@ int sicc_engine_add_code(unsigned long long handle, const sicc_engine_code_t* co
             e->h_nmax = std::max(e->h_nmax, d.n);
             e->h_mmax = std::max(e->h_mmax, code->m);
             e->h_poolmax = std::max(e->h_poolmax, ec.code->osd_h_view().pool);
+            e->h_nnzmax = std::max(e->h_nnzmax, ec.code->edges());
         }
         e->codes.push_back(std::move(ec));
         e->dirty = true;
@@ -778,7 +793,7 @@ int sicc_engine_decode_device_protected(unsigned long long handle, int codewords
                 launch_osd(shape, oio, codewords, st);
             }
             if (e->h_nmax > 0)  // long codes, one CTA per codeword
-                launch_osd_h(OsdHView{}, e->h_nmax, e->h_mmax, e->h_poolmax, oio, codewords, st);
+                launch_osd_h(OsdHView{}, e->h_nmax, e->h_mmax, e->h_poolmax, e->h_nnzmax, oio, codewords, st);
         }
         check_cuda(cudaEventRecord(e->ev[3], st), "cudaEventRecord");
         e->timed = true;
@@ -818,7 +833,7 @@ int sicc_engine_osd_device(unsigned long long handle, int codewords, const unsig
             shape.k = e->osd_kmax;
             launch_osd(shape, oio, codewords, st);
         }
-        if (e->h_nmax > 0) launch_osd_h(OsdHView{}, e->h_nmax, e->h_mmax, e->h_poolmax, oio, codewords, st);
+        if (e->h_nmax > 0) launch_osd_h(OsdHView{}, e->h_nmax, e->h_mmax, e->h_poolmax, e->h_nnzmax, oio, codewords, st);
         return CUDA_OSD_STATUS_OK;
     });
 }

@@ -42,6 +42,7 @@ struct OsdHLayout {
     int mw;       // words per row of T for the largest m
     int ts;       // column stride of T in words (odd: a warp reading one word of 32 columns hits 32 banks)
     int poolmax;
+    int nnzmax;   // > 0: the columns' row lists are staged in shared memory (16-bit rows)
 };
 
 struct OsdHSmem {
@@ -62,6 +63,7 @@ struct OsdHSmem {
     int16_t* pool_j;         // [poolmax] flip pool (sorted positions, weakest first)
     uint32_t* avec;          // [poolmax][mw] T h_f for the pool, bit t = pivot rank t
     uint32_t* aug;           // [mw] T s, bit t = pivot rank t
+    int16_t* rows;           // [nnzmax] rows of H's columns (when staged)
 };
 
 __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -93,11 +95,18 @@ __host__ __device__ inline size_t carve(const OsdHLayout& l, unsigned char* base
     t.pool_j = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.poolmax) * 2));
     t.avec = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.poolmax) * l.mw * 4));
     t.aug = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.mw) * 4));
+    t.rows = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nnzmax) * 2));
     if (s) *s = t;
     return o;
 }
 
 __device__ __forceinline__ unsigned tbit(const uint32_t* row, int q) { return (row[q >> 5] >> (q & 31)) & 1u; }
+
+// Slot of column q of T.  The columns a pivot touches come in runs of
+// consecutive rows (the parity part of these codes is a chain); a transposed
+// placement spreads a run over the 32-column chunks, hence over the warps
+// that apply the pivot, instead of loading one warp with the whole run.
+__device__ __forceinline__ int tslot(int q, int mw) { return (q & 31) * mw + (q >> 5); }
 
 }  // namespace
 
@@ -162,10 +171,10 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             s.rel[j] = __uint_as_float(0x7fffffffu - static_cast<unsigned>(key >> 32));
         }
         // ---- 2. T = identity (column-major), syndrome of the hard decisions ----
-        for (int i = tid; i < rows * TS; i += kOsdHThreads) {
-            const int col = i / TS, w = i - col * TS;
-            s.T[i] = (col < m && w == (col >> 5)) ? (1u << (col & 31)) : 0u;
-        }
+        for (int i = tid; i < rows * TS; i += kOsdHThreads) s.T[i] = 0u;
+        __syncthreads();
+        for (int col = tid; col < m; col += kOsdHThreads)
+            s.T[static_cast<size_t>(tslot(col, MW)) * TS + (col >> 5)] = 1u << (col & 31);
         for (int r = tid; r < rows; r += kOsdHThreads) {
             unsigned par = 0;
             if (r < m)
@@ -175,6 +184,9 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         }
         for (int w = tid; w < MW; w += kOsdHThreads) s.piv[w] = 0u;
         // column of H at each sorted position: first edge << 8 | weight (the sort keys are dead)
+        const bool staged = lay.nnzmax > 0;
+        if (staged)
+            for (int e = tid; e < hv.col_ptr[n]; e += kOsdHThreads) s.rows[e] = static_cast<int16_t>(hv.col_rows[e]);
         int* colinfo = reinterpret_cast<int*>(s.keys);
         for (int j = tid; j < n; j += kOsdHThreads) {
             const int c = s.perm[j];
@@ -190,38 +202,49 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         // every column of T with a 1 in row p takes v + e_p (T <- (I + (v + e_p) e_p^T) T),
         // which turns column c into e_p and leaves earlier pivot columns alone.
         int t = 0, jstop = -1, it = 0;
-        // warp 0 holds the rows of the next column, one per lane, loaded a column ahead
-        int nrow = -1, ncnt = 0, ne0 = 0;
+        // Warp 0 runs one column ahead: while it selects the pivot of column j
+        // it already reads the columns of T for column j-1 (T is not written
+        // between the two barriers), and once p_j is known it applies pivot
+        // j's row operation to that reduced column: u + u_{p_j} (v_j + e_{p_j}).
+        auto rows_of = [&](int jj, int& e0, int& cnt) -> int {  // one row of column jj per lane
+            const int ci = colinfo[jj];
+            e0 = ci >> 8;
+            cnt = ci & 255;
+            return lane < cnt ? (staged ? static_cast<int>(s.rows[e0 + lane]) : hv.col_rows[e0 + lane]) : -1;
+        };
+        auto reduce_column = [&](int myrow, int e0, int cnt) -> unsigned {  // T h_c, word `lane`
+            unsigned v = 0u;
+            for (int e = 0; e < cnt && e < 32; e += 8) {  // groups of 8 loads in flight together
+                unsigned part[8];
+#pragma unroll
+                for (int x = 0; x < 8; ++x) {
+                    const int q = __shfl_sync(0xffffffffu, myrow, (e + x) & 31);
+                    part[x] = (e + x < cnt && lane < MW) ? s.T[static_cast<size_t>(tslot(q, MW)) * TS + lane] : 0u;
+                }
+                v ^= (part[0] ^ part[1]) ^ (part[2] ^ part[3]) ^ (part[4] ^ part[5]) ^ (part[6] ^ part[7]);
+            }
+            for (int e = 32; e < cnt; ++e)  // columns heavier than 32
+                if (lane < MW) v ^= s.T[static_cast<size_t>(tslot(hv.col_rows[e0 + e], MW)) * TS + lane];
+            return v;
+        };
+        unsigned vcur = 0u;  // warp 0: T h_c of the column being scanned
         if (warp == 0) {
-            const int ci = colinfo[n - 1];
-            ne0 = ci >> 8;
-            ncnt = ci & 255;
-            nrow = lane < ncnt ? hv.col_rows[ne0 + lane] : -1;
+            int e0, cnt;
+            const int r = rows_of(n - 1, e0, cnt);
+            vcur = reduce_column(r, e0, cnt);
         }
         for (int j = n - 1; j >= 0; --j, ++it) {
             const int buf = it & 1;  // double-buffered: read after this barrier, rewritten two barriers later
             if (warp == 0) {
                 const int c = s.perm[j];
-                unsigned v = 0u;
-                const int cnt = ncnt, e0 = ne0, myrow = nrow;
-                // the column's rows in groups of 8, all loads of a group in flight together
-                for (int e = 0; e < cnt && e < 32; e += 8) {
-                    unsigned part[8];
-#pragma unroll
-                    for (int x = 0; x < 8; ++x) {
-                        const int q = __shfl_sync(0xffffffffu, myrow, (e + x) & 31);
-                        part[x] = (e + x < cnt && lane < MW) ? s.T[static_cast<size_t>(q) * TS + lane] : 0u;
-                    }
-                    v ^= (part[0] ^ part[1]) ^ (part[2] ^ part[3]) ^ (part[4] ^ part[5]) ^ (part[6] ^ part[7]);
+                // the next column against the current T (pivot j not applied yet)
+                unsigned unext = 0u;
+                if (j > 0) {
+                    int e0, cnt;
+                    const int r = rows_of(j - 1, e0, cnt);
+                    unext = reduce_column(r, e0, cnt);
                 }
-                for (int e = 32; e < cnt; ++e)  // columns heavier than 32
-                    if (lane < MW) v ^= s.T[static_cast<size_t>(hv.col_rows[e0 + e]) * TS + lane];
-                if (j > 0) {  // prefetch the next column's rows
-                    const int ci = colinfo[j - 1];
-                    ne0 = ci >> 8;
-                    ncnt = ci & 255;
-                    nrow = lane < ncnt ? hv.col_rows[ne0 + lane] : -1;
-                }
+                const unsigned v = vcur;
                 const unsigned x = (lane < MW) ? (v & ~s.piv[lane]) : 0u;
                 const unsigned lanes = __ballot_sync(0xffffffffu, x != 0u);
                 int p = -1;
@@ -229,16 +252,21 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                     const int l0 = __ffs(lanes) - 1;
                     const unsigned x0 = __shfl_sync(0xffffffffu, x, l0);
                     p = l0 * 32 + __ffs(x0) - 1;
-                    if (lane < MW) s.wv[buf * 32 + lane] = (lane == (p >> 5)) ? (v ^ (1u << (p & 31))) : v;
+                    const unsigned w = (lane == (p >> 5)) ? (v ^ (1u << (p & 31))) : v;
+                    if (lane < MW) s.wv[buf * 32 + lane] = w;
                     if (lane == (p >> 5)) s.piv[lane] |= 1u << (p & 31);
                     if (lane == 0) {
                         s.order[t] = static_cast<int16_t>(p);
                         s.row_of_col[c] = static_cast<int16_t>(t);
                         s.pivj[t] = static_cast<int16_t>(j);
                     }
+                    // pivot j's row operation on the next column
+                    const unsigned up = (__shfl_sync(0xffffffffu, unext, p >> 5) >> (p & 31)) & 1u;
+                    if (up) unext ^= w;
                 } else if (lane == 0) {
                     s.mrb[s_nd++] = static_cast<int16_t>(j);  // dependent: an MRB position
                 }
+                vcur = unext;
                 if (lane == 0) s_p[buf] = p;
             }
             __syncthreads();
@@ -260,22 +288,22 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                 for (int h = 0; h < (32 + kOsdHWarps - 1) / kOsdHWarps; ++h) {
                     const int q = warp + h * kOsdHWarps;
                     unsigned hit = hits[h];
-                    while (hit) {  // two columns at a time: both loads in flight together
-                        const int b0 = __ffs(hit) - 1;
-                        hit &= hit - 1;
-                        uint32_t* c0 = s.T + static_cast<size_t>(q * 32 + b0) * TS;
-                        if (hit) {
-                            const int b1 = __ffs(hit) - 1;
+                    // up to 8 columns per round: all loads before any store (a store followed by a
+                    // load of another column would otherwise serialise every column on the store)
+                    while (hit) {
+                        int bs[8];
+#pragma unroll
+                        for (int x = 0; x < 8; ++x) {
+                            bs[x] = hit ? __ffs(hit) - 1 : -1;
                             hit &= hit - 1;
-                            uint32_t* c1 = s.T + static_cast<size_t>(q * 32 + b1) * TS;
-                            if (lane < MW) {
-                                const uint32_t a0 = c0[lane], a1 = c1[lane];
-                                c0[lane] = a0 ^ wreg;
-                                c1[lane] = a1 ^ wreg;
-                            }
-                        } else if (lane < MW) {
-                            c0[lane] ^= wreg;
                         }
+                        uint32_t a[8];
+#pragma unroll
+                        for (int x = 0; x < 8; ++x)
+                            a[x] = (bs[x] >= 0 && lane < MW) ? s.T[static_cast<size_t>(q * 32 + bs[x]) * TS + lane] : 0u;
+#pragma unroll
+                        for (int x = 0; x < 8; ++x)
+                            if (bs[x] >= 0 && lane < MW) s.T[static_cast<size_t>(q * 32 + bs[x]) * TS + lane] = a[x] ^ wreg;
                     }
                 }
             }
@@ -323,7 +351,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             // T s: XOR of the columns of T selected by s, spread over the warps
             unsigned acc = 0u;
             for (int q = warp; q < m; q += kOsdHWarps)
-                if (lane < MW && tbit(s.syn, q)) acc ^= s.T[static_cast<size_t>(q) * TS + lane];
+                if (lane < MW && tbit(s.syn, q)) acc ^= s.T[static_cast<size_t>(tslot(q, MW)) * TS + lane];
             if (lane < MW && acc) atomicXor(&s.vs[lane], acc);
             // T h_f for the flip pool, one warp per column
             for (int i = warp; i < pool; i += kOsdHWarps) {
@@ -331,7 +359,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                 unsigned v = 0u;
                 if (lane < MW)
                     for (int e = hv.col_ptr[c]; e < hv.col_ptr[c + 1]; ++e)
-                        v ^= s.T[static_cast<size_t>(hv.col_rows[e]) * TS + lane];
+                        v ^= s.T[static_cast<size_t>(tslot(hv.col_rows[e], MW)) * TS + lane];
                 if (lane < MW) s.vs[(i + 1) * 32 + lane] = v;
             }
         }
@@ -431,7 +459,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
 }
 
 size_t osd_h_smem_bytes(int nmax, int mmax, int poolmax)
-{
+{  // without the staged row lists
     OsdHLayout l{};
     l.nmax = nmax;
     l.np = 1;
@@ -442,7 +470,7 @@ size_t osd_h_smem_bytes(int nmax, int mmax, int poolmax)
     return carve(l, nullptr, nullptr);
 }
 
-void launch_osd_h(const OsdHView& hv, int nmax, int mmax, int poolmax, const OsdIO& io, int max_items,
+void launch_osd_h(const OsdHView& hv, int nmax, int mmax, int poolmax, int nnzmax, const OsdIO& io, int max_items,
                   cudaStream_t st)
 {
     if (max_items <= 0) return;
@@ -454,8 +482,12 @@ void launch_osd_h(const OsdHView& hv, int nmax, int mmax, int poolmax, const Osd
     l.mw = (mmax + 31) / 32;
     l.ts = l.mw | 1;
     l.poolmax = std::max(poolmax, 1);
-    const size_t smem = carve(l, nullptr, nullptr);
+    l.nnzmax = 0;
+    size_t smem = carve(l, nullptr, nullptr);
     if (smem > 227 * 1024) throw InvalidArgument("large-code OSD tables exceed shared memory (m <= 1024, n <= 4096)");
+    l.nnzmax = nnzmax;  // stage the columns' row lists when they fit as well
+    if (nnzmax <= 0 || carve(l, nullptr, nullptr) > 227 * 1024) l.nnzmax = 0;
+    smem = carve(l, nullptr, nullptr);
     check_cuda(cudaFuncSetAttribute(osd_h_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
                "cudaFuncSetAttribute(osd_h)");
     int per_sm = 0;
