@@ -259,13 +259,27 @@ struct StreamDecoder : Decoder {
     std::vector<std::unique_ptr<Batch>> batches;  // ring
     int filling = 0;
     std::deque<int> flight;  // batch ids in launch order
-    struct Ready {
-        std::vector<uint8_t> info;
-        unsigned long long ts, id;
-        unsigned block;
-        uint8_t used_osd;
+    // Results of retired batches, handed out by poll in ranges.
+    struct ReadySeg {
+        std::vector<uint8_t> info, used;
+        std::vector<unsigned long long> ts, ids;
+        std::vector<unsigned> blocks;
+        size_t pos = 0;
     };
-    std::deque<Ready> ready;
+    std::deque<ReadySeg> ready;
+    // Submitted LLRs are copied on their own stream, so a submit returns once its copy is
+    // done (the caller's buffer is free) while earlier batches keep decoding.
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copied = nullptr;
+
+    ~StreamDecoder() override
+    {
+        if (copy_stream) {
+            cudaStreamSynchronize(copy_stream);
+            cudaStreamDestroy(copy_stream);
+        }
+        if (copied) cudaEventDestroy(copied);
+    }
     bool draining = false;
     cuda_osd_stream_stats_t stats{};
     uint64_t last_arrival_us = 0;
@@ -292,6 +306,8 @@ struct StreamDecoder : Decoder {
         bp.min_abs_accept = c.bp_min_abs_llr_accept;
         bp.max_iter = c.bp_max_iterations;
         scratch.alloc(max_batch, n, k);
+        check_cuda(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate(copy)");
+        check_cuda(cudaEventCreateWithFlags(&copied, cudaEventDisableTiming), "cudaEventCreate(copy)");
         for (int i = 0; i < 3; ++i) {
             auto b = std::make_unique<Batch>();
             b->llr.alloc(static_cast<size_t>(max_batch) * n);
@@ -303,6 +319,9 @@ struct StreamDecoder : Decoder {
             b->h_success.alloc(max_batch);
             check_cuda(cudaEventCreate(&b->done), "cudaEventCreate");
             check_cuda(cudaEventCreate(&b->start), "cudaEventCreate");
+            b->ts.reserve(max_batch);
+            b->ids.reserve(max_batch);
+            b->blocks.reserve(max_batch);
             batches.push_back(std::move(b));
         }
         stats.ewma_interarrival_us = static_cast<double>(c.default_interarrival_us);
@@ -312,6 +331,8 @@ struct StreamDecoder : Decoder {
     {
         Batch& b = *batches[filling];
         if (b.count == 0) return;
+        check_cuda(cudaEventRecord(copied, copy_stream), "cudaEventRecord(copy)");
+        check_cuda(cudaStreamWaitEvent(stream, copied, 0), "cudaStreamWaitEvent(copy)");
         check_cuda(cudaEventRecord(b.start, stream), "cudaEventRecord");
         run_bp_osd(*code, bp, shape, osd_enabled, b.llr.p, b.count, b.info.p, k, k, b.success.p, b.used_osd.p,
                    nullptr, nullptr, scratch, stream, &timing);
@@ -339,17 +360,17 @@ struct StreamDecoder : Decoder {
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, b.start, b.done);
         stats.total_decode_ms += ms;
+        ReadySeg sg;
+        sg.info.assign(b.h_info.p, b.h_info.p + static_cast<size_t>(b.count) * k);
+        sg.used.assign(b.h_used_osd.p, b.h_used_osd.p + b.count);
+        sg.ts.swap(b.ts);
+        sg.ids.swap(b.ids);
+        sg.blocks.swap(b.blocks);
         for (int i = 0; i < b.count; ++i) {
-            Ready r;
-            r.info.assign(b.h_info.p + static_cast<size_t>(i) * k, b.h_info.p + static_cast<size_t>(i + 1) * k);
-            r.ts = b.ts[i];
-            r.id = b.ids[i];
-            r.block = b.blocks[i];
-            r.used_osd = b.h_used_osd.p[i];
-            stats.osd_fallback_codewords += r.used_osd ? 1 : 0;
+            stats.osd_fallback_codewords += b.h_used_osd.p[i] ? 1 : 0;
             stats.bp_success_codewords += b.h_success.p[i] ? 1 : 0;
-            ready.push_back(std::move(r));
         }
+        ready.push_back(std::move(sg));
         stats.decoded_codewords += static_cast<unsigned long long>(b.count);
         stats.average_batch_size = static_cast<double>(stats.decoded_codewords) /
                                    static_cast<double>(std::max<unsigned long long>(stats.decoded_batches, 1));
@@ -358,6 +379,9 @@ struct StreamDecoder : Decoder {
         b.ts.clear();
         b.ids.clear();
         b.blocks.clear();
+        b.ts.reserve(max_batch);
+        b.ids.reserve(max_batch);
+        b.blocks.reserve(max_batch);
         flight.pop_front();
     }
 
@@ -416,7 +440,7 @@ struct StreamDecoder : Decoder {
             const size_t bytes = static_cast<size_t>(take) * n * sizeof(float);
             check_cuda(cudaMemcpyAsync(b.llr.p + static_cast<size_t>(b.count) * n,
                                        llrs + static_cast<size_t>(done) * n, bytes,
-                                       device_ptr ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream),
+                                       device_ptr ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, copy_stream),
                        "copy submitted LLRs");
             for (int i = 0; i < take; ++i) {
                 b.ts.push_back(ts ? ts[done + i] : now);
@@ -429,7 +453,8 @@ struct StreamDecoder : Decoder {
             if (b.count >= max_batch) launch_filling();
         }
         // the caller may reuse its buffer as soon as this returns
-        check_cuda(cudaStreamSynchronize(stream), "synchronize submit copy");
+        check_cuda(cudaEventRecord(copied, copy_stream), "cudaEventRecord(copy)");
+        check_cuda(cudaEventSynchronize(copied), "synchronize submit copy");
         stats.last_submit_timestamp_us = ts && count > 0 ? ts[count - 1] : now;
         stats.current_pending_codewords = pending();
         stats.max_pending_codewords = std::max(stats.max_pending_codewords, stats.current_pending_codewords);
@@ -450,14 +475,17 @@ struct StreamDecoder : Decoder {
         }
         int out = 0;
         while (out < max_cw && !ready.empty()) {
-            Ready& r = ready.front();
-            if (out_info) std::memcpy(out_info + static_cast<size_t>(out) * k, r.info.data(), static_cast<size_t>(k));
-            if (out_ts) out_ts[out] = r.ts;
-            if (out_ids) out_ids[out] = r.id;
-            if (out_blocks) out_blocks[out] = r.block;
-            if (out_used) out_used[out] = r.used_osd;
-            ready.pop_front();
-            ++out;
+            ReadySeg& sg = ready.front();
+            const size_t take = std::min<size_t>(sg.ts.size() - sg.pos, static_cast<size_t>(max_cw - out));
+            if (out_info)
+                std::memcpy(out_info + static_cast<size_t>(out) * k, sg.info.data() + sg.pos * k, take * k);
+            if (out_ts) std::copy(sg.ts.begin() + sg.pos, sg.ts.begin() + sg.pos + take, out_ts + out);
+            if (out_ids) std::copy(sg.ids.begin() + sg.pos, sg.ids.begin() + sg.pos + take, out_ids + out);
+            if (out_blocks) std::copy(sg.blocks.begin() + sg.pos, sg.blocks.begin() + sg.pos + take, out_blocks + out);
+            if (out_used) std::copy(sg.used.begin() + sg.pos, sg.used.begin() + sg.pos + take, out_used + out);
+            sg.pos += take;
+            out += static_cast<int>(take);
+            if (sg.pos == sg.ts.size()) ready.pop_front();
         }
         if (ready.empty() && flight.empty() && pending() == 0) draining = false;
         stats.current_pending_codewords = pending();

@@ -179,14 +179,19 @@ class StreamBpOsdDecoder:
     def flush(self):
         _lib.check(_lib.load().cuda_osd_flush(self.handle), "cuda_osd_flush")
 
-    def poll(self, max_codewords: int):
-        """Returns (info [r,k], timestamps, frame_ids, block_indices, used_osd) for r ready codewords."""
+    def poll_buffers(self, max_codewords: int):
+        """Output arrays for ``poll`` (info, timestamps, frame_ids, block_indices, used_osd)."""
+        return (np.zeros((max_codewords, self.k), np.uint8), np.zeros(max_codewords, np.uint64),
+                np.zeros(max_codewords, np.uint64), np.zeros(max_codewords, np.uint32),
+                np.zeros(max_codewords, np.uint8))
+
+    def poll(self, max_codewords: int, bufs=None):
+        """Returns (info [r,k], timestamps, frame_ids, block_indices, used_osd) for r ready codewords.
+
+        ``bufs`` (from ``poll_buffers``, at least max_codewords long) avoids allocating per call.
+        """
         L = _lib.load()
-        tmp = np.zeros((max_codewords, self.k), np.uint8)
-        o_ts = np.zeros(max_codewords, np.uint64)
-        o_ids = np.zeros(max_codewords, np.uint64)
-        o_blk = np.zeros(max_codewords, np.uint32)
-        o_used = np.zeros(max_codewords, np.uint8)
+        tmp, o_ts, o_ids, o_blk, o_used = bufs if bufs is not None else self.poll_buffers(max_codewords)
         ready = C.c_int(0)
         _lib.check(L.cuda_osd_poll_ready(self.handle, max_codewords, tmp.ctypes.data, o_ts.ctypes.data,
                                          o_ids.ctypes.data, o_blk.ctypes.data, o_used.ctypes.data, C.byref(ready)),

@@ -209,6 +209,37 @@ def test_stream_decoder_device_submit_and_async_window(cuda, oracle):
             assert np.array_equal(got[(f, b)], exp)
 
 
+def test_stream_decoder_host_submits_past_the_ring_and_odd_polls(cuda, oracle):
+    """Five full batches submitted before any poll (the ring holds three), then polled 7 at a time."""
+    from sicc_gb300 import fec
+    code = codes.short_code()
+    oc = oracle.code(code.n, code.m, code.row_ptr, code.col_ind)
+    table = oc.systematic_parity()
+    dec = fec.StreamBpOsdDecoder(code, max_batch=64, min_batch=64, max_iter=20, normalization=0.75, offset=0.0,
+                                 damping=0.0, min_abs_llr_accept=0.0)
+    frames = [channel.awgn_llrs(code, 64, 2.0, seed=140 + f)[2] for f in range(5)]
+    for f, x in enumerate(frames):
+        buf = np.array(x)  # overwritten after the call: a submit must have copied it
+        dec.submit(buf, np.full(64, f), np.arange(64))
+        buf[:] = 0.0
+    dec.flush()
+    got = {}
+    bufs = dec.poll_buffers(7)
+    while len(got) < 320:
+        info, ts, ids, blk, used = dec.poll(7, bufs)
+        assert 0 < len(info) <= 7
+        for r in range(len(info)):
+            key = (int(ids[r]), int(blk[r]))
+            assert key not in got
+            got[key] = info[r].copy()
+    for f, x in enumerate(frames):
+        for b in range(0, 64, 5):
+            exp, _ = _oracle_bp_osd(oracle, oc, table, code, x[b])
+            assert np.array_equal(got[(f, b)], exp)
+    st = dec.stats()
+    assert st["decoded_codewords"] == 320 and st["decoded_batches"] == 5
+
+
 def test_device_batch_entry_matches_stream_api(cuda, oracle):
     from sicc_gb300 import fec
     torch = cuda
