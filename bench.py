@@ -387,7 +387,9 @@ def run_ofdm(args, rank, world):
 
     peak, peak_kind = peaks()
     demod_bytes = frames * (8 * t.cfg.num_symbols * t.cfg.nfft + 4 * blocks * code.n)
-    kern = {"sync_kernel": sync_ms, "demod_kernel": demod_ms, "bp_layered_kernel<16>": bp_ms}
+    maxdeg = int(np.max(np.diff(code.row_ptr)))
+    bp_name = f"bp_layered_kernel<{8 if maxdeg <= 8 else 12 if maxdeg <= 12 else 16 if maxdeg <= 16 else 27}>"
+    kern = {"sync_kernel": sync_ms, "demod_kernel": demod_ms, bp_name: bp_ms}
     top = max(kern, key=kern.get)
     achieved = demod_bytes / (demod_ms / len(OFDM_SNRS) * 1e-3) / 1e9
     line = {"metric": "info-bit Mbps OFDM RX (sync+demod+decode), 16-QAM, (1024,512)", "value": round(value, 3),

@@ -415,7 +415,9 @@ void launch_bp_layered(const LayeredView& cv, const BpParams& p, const BpIO& io,
     if (layered_smem_bytes(cv, slots, track_best, nullptr) > 227 * 1024)
         throw InvalidArgument("code too large for the shared-memory layered kernel");
     check_cuda(cudaMemsetAsync(io.work_counter, 0, sizeof(int), st), "reset work counter");
+    // the row loops are unrolled to D slots: the closest D above the code's row degree
     if (cv.maxdeg <= 8) launch_layered_t<8>(cv, p, io, slots, shape.ctas, track_best, st);
+    else if (cv.maxdeg <= 12) launch_layered_t<12>(cv, p, io, slots, shape.ctas, track_best, st);
     else if (cv.maxdeg <= 16) launch_layered_t<16>(cv, p, io, slots, shape.ctas, track_best, st);
     else launch_layered_t<27>(cv, p, io, slots, shape.ctas, track_best, st);
 }
@@ -448,6 +450,7 @@ void launch_bp_flooding(const FloodView& cv, const BpParams& p, const BpIO& io, 
 }
 
 template __global__ void bp_layered_kernel<8>(LayeredView, BpParams, BpIO, int, int, int);
+template __global__ void bp_layered_kernel<12>(LayeredView, BpParams, BpIO, int, int, int);
 template __global__ void bp_layered_kernel<16>(LayeredView, BpParams, BpIO, int, int, int);
 template __global__ void bp_layered_kernel<27>(LayeredView, BpParams, BpIO, int, int, int);
 
