@@ -35,6 +35,7 @@ namespace {
 constexpr int kOsdHThreads = 512;
 constexpr int kOsdHWarps = kOsdHThreads / 32;
 constexpr int kOsdHMaxPool = 128;
+constexpr int kRound = 4;  // columns of H per elimination round
 
 struct OsdHLayout {
     int np;       // sort length: power of two >= the longest n
@@ -52,7 +53,7 @@ struct OsdHSmem {
     int16_t* perm;           // [nmax] code position at sorted position j
     int16_t* row_of_col;     // [nmax] pivot rank of a code position, -1 for the MRB
     uint32_t* hard;          // [nmax/32+1] hard decisions by code position
-    uint32_t* wv;            // [2][32] v + e_p of the last two pivots
+    uint32_t* wv;            // [kRound][32] v + e_p of the round's pivots
     uint32_t* piv;           // [mw] pivoted rows
     int16_t* order;          // [32*mw] row of the t-th pivot
     uint32_t* vs;            // [poolmax+1][32] T s and T h_f by row (before reordering)
@@ -84,7 +85,7 @@ __host__ __device__ inline size_t carve(const OsdHLayout& l, unsigned char* base
     t.perm = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nmax) * 2));
     t.row_of_col = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nmax) * 2));
     t.hard = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(l.nmax) / 32 + 1) * 4));
-    t.wv = reinterpret_cast<uint32_t*>(take(64 * 4));
+    t.wv = reinterpret_cast<uint32_t*>(take(kRound * 32 * 4));
     t.piv = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.mw) * 4));
     t.order = reinterpret_cast<int16_t*>(take(rows * 2));
     t.vs = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(l.poolmax) + 1) * 32 * 4));
@@ -116,8 +117,8 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     OsdHSmem s;
     carve(lay, smem_raw, &s);
-    __shared__ int s_p[2];
-    __shared__ int s_nd;
+    __shared__ int s_rp[kRound];
+    __shared__ int s_nd, s_np, s_used, s_jstop;
     __shared__ unsigned long long s_best;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int TS = lay.ts;
@@ -201,11 +202,12 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         // h_c selects) and picks the lowest unpivoted row p with v_p = 1; then
         // every column of T with a 1 in row p takes v + e_p (T <- (I + (v + e_p) e_p^T) T),
         // which turns column c into e_p and leaves earlier pivot columns alone.
-        int t = 0, jstop = -1, it = 0;
-        // Warp 0 runs one column ahead: while it selects the pivot of column j
-        // it already reads the columns of T for column j-1 (T is not written
-        // between the two barriers), and once p_j is known it applies pivot
-        // j's row operation to that reduced column: u + u_{p_j} (v_j + e_{p_j}).
+        // Columns are taken kRound at a time.  Warp 0 reduces the round's columns
+        // against T as it stands (all loads in flight together), then picks their
+        // pivots in order, applying each earlier pivot of the round to the later
+        // columns (u + u_p (v + e_p)).  Then every warp applies the round's pivots,
+        // in order, to its chunks of T: a column takes pivot r's row operation when
+        // its row-p_r bit is set after the previous ones.  Two barriers per round.
         auto rows_of = [&](int jj, int& e0, int& cnt) -> int {  // one row of column jj per lane
             const int ci = colinfo[jj];
             e0 = ci >> 8;
@@ -227,70 +229,100 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                 if (lane < MW) v ^= s.T[static_cast<size_t>(tslot(hv.col_rows[e0 + e], MW)) * TS + lane];
             return v;
         };
-        unsigned vcur = 0u;  // warp 0: T h_c of the column being scanned
-        if (warp == 0) {
-            int e0, cnt;
-            const int r = rows_of(n - 1, e0, cnt);
-            vcur = reduce_column(r, e0, cnt);
-        }
-        for (int j = n - 1; j >= 0; --j, ++it) {
-            const int buf = it & 1;  // double-buffered: read after this barrier, rewritten two barriers later
+        int t = 0, jstop = -1;
+        unsigned pivw = 0u;  // warp 0: pivoted rows, word `lane`
+        for (int j = n - 1; j >= 0 && t < m;) {
             if (warp == 0) {
-                const int c = s.perm[j];
-                // the next column against the current T (pivot j not applied yet)
-                unsigned unext = 0u;
-                if (j > 0) {
-                    int e0, cnt;
-                    const int r = rows_of(j - 1, e0, cnt);
-                    unext = reduce_column(r, e0, cnt);
-                }
-                const unsigned v = vcur;
-                const unsigned x = (lane < MW) ? (v & ~s.piv[lane]) : 0u;
-                const unsigned lanes = __ballot_sync(0xffffffffu, x != 0u);
-                int p = -1;
-                if (lanes) {
-                    const int l0 = __ffs(lanes) - 1;
-                    const unsigned x0 = __shfl_sync(0xffffffffu, x, l0);
-                    p = l0 * 32 + __ffs(x0) - 1;
-                    const unsigned w = (lane == (p >> 5)) ? (v ^ (1u << (p & 31))) : v;
-                    if (lane < MW) s.wv[buf * 32 + lane] = w;
-                    if (lane == (p >> 5)) s.piv[lane] |= 1u << (p & 31);
-                    if (lane == 0) {
-                        s.order[t] = static_cast<int16_t>(p);
-                        s.row_of_col[c] = static_cast<int16_t>(t);
-                        s.pivj[t] = static_cast<int16_t>(j);
+                unsigned u[kRound];
+#pragma unroll
+                for (int r = 0; r < kRound; ++r) {
+                    u[r] = 0u;
+                    if (j - r >= 0) {
+                        int e0, cnt;
+                        const int rw = rows_of(j - r, e0, cnt);
+                        u[r] = reduce_column(rw, e0, cnt);
                     }
-                    // pivot j's row operation on the next column
-                    const unsigned up = (__shfl_sync(0xffffffffu, unext, p >> 5) >> (p & 31)) & 1u;
-                    if (up) unext ^= w;
-                } else if (lane == 0) {
-                    s.mrb[s_nd++] = static_cast<int16_t>(j);  // dependent: an MRB position
                 }
-                vcur = unext;
-                if (lane == 0) s_p[buf] = p;
+                int pr[kRound];
+                unsigned wr[kRound];
+                int np = 0, used = 0, js = -1;
+#pragma unroll
+                for (int r = 0; r < kRound; ++r) {
+                    pr[r] = -1;
+                    wr[r] = 0u;
+                    if (j - r >= 0 && t + np < m) {
+                        unsigned v = u[r];
+#pragma unroll
+                        for (int q = 0; q < r; ++q) {  // earlier pivots of the round
+                            if (pr[q] >= 0) {
+                                const unsigned bit = (__shfl_sync(0xffffffffu, v, pr[q] >> 5) >> (pr[q] & 31)) & 1u;
+                                if (bit) v ^= wr[q];
+                            }
+                        }
+                        const unsigned x = (lane < MW) ? (v & ~pivw) : 0u;
+                        const unsigned lanes = __ballot_sync(0xffffffffu, x != 0u);
+                        const int c = s.perm[j - r];
+                        if (lanes) {
+                            const int l0 = __ffs(lanes) - 1;
+                            const unsigned x0 = __shfl_sync(0xffffffffu, x, l0);
+                            const int p = l0 * 32 + __ffs(x0) - 1;
+                            pr[r] = p;
+                            wr[r] = (lane == (p >> 5)) ? (v ^ (1u << (p & 31))) : v;
+                            if (lane == (p >> 5)) pivw |= 1u << (p & 31);
+                            if (lane == 0) {
+                                s.order[t + np] = static_cast<int16_t>(p);
+                                s.row_of_col[c] = static_cast<int16_t>(t + np);
+                                s.pivj[t + np] = static_cast<int16_t>(j - r);
+                            }
+                            ++np;
+                            if (t + np == m) js = j - r;
+                        } else if (lane == 0) {
+                            s.mrb[s_nd++] = static_cast<int16_t>(j - r);  // dependent: an MRB position
+                        }
+                        used = r + 1;
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < kRound; ++r) {
+                    if (lane == 0) s_rp[r] = pr[r];
+                    s.wv[r * 32 + lane] = wr[r];
+                }
+                if (lane == 0) {
+                    s_np = np;
+                    s_used = used;
+                    s_jstop = js;
+                }
             }
             __syncthreads();
-            const int p = s_p[buf];
-            if (p < 0) continue;
-            {
-                const unsigned wreg = (lane < MW) ? s.wv[buf * 32 + lane] : 0u;
-                const int pw = p >> 5;
-                const unsigned pb = 1u << (p & 31);
-                // the pivot-row bit of this warp's column chunks, loaded together
+            const int np = s_np;
+            const int used = s_used;
+            if (np > 0) {
+                int P[kRound];
+                unsigned W[kRound];
+#pragma unroll
+                for (int r = 0; r < kRound; ++r) {
+                    P[r] = s_rp[r];
+                    W[r] = s.wv[r * 32 + lane];
+                }
+                // the pivot-row bits of this warp's column chunks
                 unsigned hits[(32 + kOsdHWarps - 1) / kOsdHWarps];
 #pragma unroll
                 for (int h = 0; h < (32 + kOsdHWarps - 1) / kOsdHWarps; ++h) {
                     const int q = warp + h * kOsdHWarps;
-                    const bool in = q < MW && (s.T[static_cast<size_t>(q * 32 + lane) * TS + pw] & pb) != 0u;
+                    bool in = false;
+                    if (q < MW) {
+                        const uint32_t* col = s.T + static_cast<size_t>(q * 32 + lane) * TS;
+#pragma unroll
+                        for (int r = 0; r < kRound; ++r)
+                            if (P[r] >= 0) in |= ((col[P[r] >> 5] >> (P[r] & 31)) & 1u) != 0u;
+                    }
                     hits[h] = __ballot_sync(0xffffffffu, in);
                 }
 #pragma unroll
                 for (int h = 0; h < (32 + kOsdHWarps - 1) / kOsdHWarps; ++h) {
                     const int q = warp + h * kOsdHWarps;
                     unsigned hit = hits[h];
-                    // up to 8 columns per round: all loads before any store (a store followed by a
-                    // load of another column would otherwise serialise every column on the store)
-                    while (hit) {
+                    while (hit) {  // up to 8 columns per pass, loads before stores
                         int bs[8];
 #pragma unroll
                         for (int x = 0; x < 8; ++x) {
@@ -302,16 +334,24 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                         for (int x = 0; x < 8; ++x)
                             a[x] = (bs[x] >= 0 && lane < MW) ? s.T[static_cast<size_t>(q * 32 + bs[x]) * TS + lane] : 0u;
 #pragma unroll
+                        for (int r = 0; r < kRound; ++r) {  // the round's pivots in order
+                            if (P[r] < 0) continue;
+#pragma unroll
+                            for (int x = 0; x < 8; ++x) {
+                                const unsigned bit = (__shfl_sync(0xffffffffu, a[x], P[r] >> 5) >> (P[r] & 31)) & 1u;
+                                if (bit) a[x] ^= W[r];
+                            }
+                        }
+#pragma unroll
                         for (int x = 0; x < 8; ++x)
-                            if (bs[x] >= 0 && lane < MW) s.T[static_cast<size_t>(q * 32 + bs[x]) * TS + lane] = a[x] ^ wreg;
+                            if (bs[x] >= 0 && lane < MW) s.T[static_cast<size_t>(q * 32 + bs[x]) * TS + lane] = a[x];
                     }
                 }
             }
+            t += np;
+            if (t == m) jstop = s_jstop;
+            j -= used;
             __syncthreads();
-            if (++t == m) {
-                jstop = j;
-                break;
-            }
         }
         if (t < m) {  // H rank deficient: leave the BP decision in place
             __syncthreads();
