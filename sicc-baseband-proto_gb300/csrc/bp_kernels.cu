@@ -416,8 +416,11 @@ void launch_bp_layered(const LayeredView& cv, const BpParams& p, const BpIO& io,
         throw InvalidArgument("code too large for the shared-memory layered kernel");
     check_cuda(cudaMemsetAsync(io.work_counter, 0, sizeof(int), st), "reset work counter");
     // the row loops are unrolled to D slots: the closest D above the code's row degree
-    if (cv.maxdeg <= 8) launch_layered_t<8>(cv, p, io, slots, shape.ctas, track_best, st);
+    if (cv.maxdeg <= 6) launch_layered_t<6>(cv, p, io, slots, shape.ctas, track_best, st);
+    else if (cv.maxdeg <= 8) launch_layered_t<8>(cv, p, io, slots, shape.ctas, track_best, st);
+    else if (cv.maxdeg <= 10) launch_layered_t<10>(cv, p, io, slots, shape.ctas, track_best, st);
     else if (cv.maxdeg <= 12) launch_layered_t<12>(cv, p, io, slots, shape.ctas, track_best, st);
+    else if (cv.maxdeg <= 14) launch_layered_t<14>(cv, p, io, slots, shape.ctas, track_best, st);
     else if (cv.maxdeg <= 16) launch_layered_t<16>(cv, p, io, slots, shape.ctas, track_best, st);
     else launch_layered_t<27>(cv, p, io, slots, shape.ctas, track_best, st);
 }
@@ -449,8 +452,11 @@ void launch_bp_flooding(const FloodView& cv, const BpParams& p, const BpIO& io, 
     check_cuda(cudaGetLastError(), "bp_flooding_kernel launch");
 }
 
+template __global__ void bp_layered_kernel<6>(LayeredView, BpParams, BpIO, int, int, int);
 template __global__ void bp_layered_kernel<8>(LayeredView, BpParams, BpIO, int, int, int);
+template __global__ void bp_layered_kernel<10>(LayeredView, BpParams, BpIO, int, int, int);
 template __global__ void bp_layered_kernel<12>(LayeredView, BpParams, BpIO, int, int, int);
+template __global__ void bp_layered_kernel<14>(LayeredView, BpParams, BpIO, int, int, int);
 template __global__ void bp_layered_kernel<16>(LayeredView, BpParams, BpIO, int, int, int);
 template __global__ void bp_layered_kernel<27>(LayeredView, BpParams, BpIO, int, int, int);
 

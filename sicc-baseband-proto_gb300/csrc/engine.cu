@@ -313,7 +313,9 @@ __device__ void wide_phase(const MixedIO& io, float* smem_f, int warp_floats, in
         const CodeDesc d = io.codes[io.q_code[q]];
         const int cw = io.order[io.q_start[q] + (u - io.q_units[q])];
         // row loops unrolled to the closest D above the code's row degree
-        if (d.maxdeg <= 12) wide_unit<12, W>(io, d, cw, app, best, g, gl, bar, s_red, s_off);
+        if (d.maxdeg <= 10) wide_unit<10, W>(io, d, cw, app, best, g, gl, bar, s_red, s_off);
+        else if (d.maxdeg <= 12) wide_unit<12, W>(io, d, cw, app, best, g, gl, bar, s_red, s_off);
+        else if (d.maxdeg <= 14) wide_unit<14, W>(io, d, cw, app, best, g, gl, bar, s_red, s_off);
         else wide_unit<D, W>(io, d, cw, app, best, g, gl, bar, s_red, s_off);
         group_sync(bar, G);  // the slot and s_unit are rewritten by the next unit
     }
@@ -424,7 +426,9 @@ bp_mixed_kernel(MixedIO io, int warp_floats)
         int q = 0;
         while (q + 1 < io.K && u >= io.q_units[q + 1]) ++q;
         const CodeDesc d = io.codes[io.q_code[q]];
-        if (d.maxdeg <= 12) narrow_unit<12>(io, d, q, u, wbase, gwarp);
+        if (d.maxdeg <= 10) narrow_unit<10>(io, d, q, u, wbase, gwarp);
+        else if (d.maxdeg <= 12) narrow_unit<12>(io, d, q, u, wbase, gwarp);
+        else if (d.maxdeg <= 14) narrow_unit<14>(io, d, q, u, wbase, gwarp);
         else narrow_unit<D>(io, d, q, u, wbase, gwarp);
     }
 }
