@@ -618,6 +618,7 @@ def run_serve(args, rank, world):
     out_bytes = sum(int(q[2].nbytes) for q in reqs)
     at_once = np.zeros(n_req)
     is_iq = np.array([q[0].kind == 1 for q in reqs])
+    bp_only = np.array([q[0].protection == 0 for q in reqs])
 
     def progress(msg):
         print(f"[serve] {msg}", file=sys.stderr, flush=True)
@@ -660,6 +661,9 @@ def run_serve(args, rank, world):
                       "p99_9_ms": round(float(np.percentile(lat, 99.9)), 4),
                       "p99_ms_llr_requests": round(float(np.percentile(lat[~is_iq], 99)), 4),
                       "p99_ms_iq_requests": round(float(np.percentile(lat[is_iq], 99)), 4),
+                      "p50_ms_bp_only": round(float(np.percentile(lat[bp_only], 50)), 4),
+                      "p99_ms_bp_only": round(float(np.percentile(lat[bp_only], 99)), 4),
+                      "p99_ms_bp_osd": round(float(np.percentile(lat[~bp_only], 99)), 4),
                       "p50_wait_ms": round(float(np.percentile(wait, 50)), 4),
                       "p50_batch_gpu_ms": round(float(np.percentile(gpu, 50)), 4),
                       "p99_batch_gpu_ms": round(float(np.percentile(gpu, 99)), 4),

@@ -19,6 +19,7 @@
 #include "bp_device.cuh"
 #include "bp_kernels.h"
 #include "code_plan.h"
+#include "engine_internal.h"
 
 #include <algorithm>
 #include <cfloat>
@@ -730,13 +731,17 @@ int sicc_engine_set_launch_shape(unsigned long long handle, int warps_per_cta, i
     });
 }
 
-int sicc_engine_decode_device_protected(unsigned long long handle, int codewords, const unsigned char* device_code_ids,
-                                        const unsigned char* device_protection, const float* device_llr,
-                                        const long long* device_llr_offsets, unsigned char* device_info,
-                                        const long long* device_info_offsets, unsigned char* device_success,
-                                        unsigned char* device_used_osd, unsigned char* device_iterations,
-                                        void* cuda_stream)
+}  // extern "C"
+
+namespace sicc {
+
+int engine_decode(unsigned long long handle, int codewords, const unsigned char* device_code_ids,
+                  const unsigned char* device_protection, const float* device_llr, const long long* device_llr_offsets,
+                  unsigned char* device_info, const long long* device_info_offsets, unsigned char* device_success,
+                  unsigned char* device_used_osd, unsigned char* device_iterations, cudaStream_t stream,
+                  cudaEvent_t bp_done)
 {
+    void* cuda_stream = stream;
     return guarded([&] {
         auto e = get(handle);
         std::lock_guard<std::mutex> lock(e->mu);
@@ -781,6 +786,7 @@ int sicc_engine_decode_device_protected(unsigned long long handle, int codewords
         io.osd_floats = reinterpret_cast<unsigned long long*>(e->d_counters + 2);
         launch_mixed<16>(*e, io, st);
         check_cuda(cudaEventRecord(e->ev[2], st), "cudaEventRecord");
+        if (bp_done) check_cuda(cudaEventRecord(bp_done, st), "cudaEventRecord(bp done)");
         if (e->osd_nmax > 0 || e->h_nmax > 0) {
             OsdIO oio{};
             oio.llr = e->d_osd_llr;
@@ -806,6 +812,22 @@ int sicc_engine_decode_device_protected(unsigned long long handle, int codewords
         e->timed = true;
         return CUDA_OSD_STATUS_OK;
     });
+}
+
+}  // namespace sicc
+
+extern "C" {
+
+int sicc_engine_decode_device_protected(unsigned long long handle, int codewords, const unsigned char* device_code_ids,
+                                        const unsigned char* device_protection, const float* device_llr,
+                                        const long long* device_llr_offsets, unsigned char* device_info,
+                                        const long long* device_info_offsets, unsigned char* device_success,
+                                        unsigned char* device_used_osd, unsigned char* device_iterations,
+                                        void* cuda_stream)
+{
+    return engine_decode(handle, codewords, device_code_ids, device_protection, device_llr, device_llr_offsets,
+                         device_info, device_info_offsets, device_success, device_used_osd, device_iterations,
+                         static_cast<cudaStream_t>(cuda_stream), nullptr);
 }
 
 int sicc_engine_osd_device(unsigned long long handle, int codewords, const unsigned char* device_code_ids,

@@ -9,6 +9,7 @@
 // each slot with its own engine (the engine's scratch is per launch) and
 // staging buffers.
 #include "../../include/sicc_server.h"
+#include "engine_internal.h"
 #include "sicc_common.h"
 
 #include <algorithm>
@@ -99,14 +100,18 @@ struct Req {
     long long off = -1, bytes = 0;   // arena block
     long long in_off = 0, llr_off = 0, info_off = 0;  // offsets inside the arena
     Clock::time_point t_submit, t_admit, t_launch;
+    int first_cw = 0;        // its first codeword in the batch
+    bool completed = false;  // BP-only requests complete after BP, before the batch's OSD
     cudaEvent_t h2d = nullptr;
 };
 
 struct Slot {
     unsigned long long engine = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t start = nullptr, done = nullptr;
+    cudaStream_t early = nullptr;  // copies back the BP-only requests once BP is done
+    cudaEvent_t start = nullptr, done = nullptr, bp_done = nullptr, early_done = nullptr;
     bool busy = false;
+    bool early_pending = false;
     std::vector<std::shared_ptr<Req>> reqs;
     // per-codeword metadata: host staging (pinned) and device copies
     uint8_t* h_code = nullptr;
@@ -159,8 +164,12 @@ struct Server {
             if (s.stream) cudaStreamSynchronize(s.stream);
             if (s.engine) sicc_engine_destroy(s.engine);
             if (s.stream) cudaStreamDestroy(s.stream);
+            if (s.early) cudaStreamSynchronize(s.early);
             if (s.done) cudaEventDestroy(s.done);
             if (s.start) cudaEventDestroy(s.start);
+            if (s.bp_done) cudaEventDestroy(s.bp_done);
+            if (s.early_done) cudaEventDestroy(s.early_done);
+            if (s.early) cudaStreamDestroy(s.early);
             for (void* p : {static_cast<void*>(s.h_code), static_cast<void*>(s.h_prot),
                             static_cast<void*>(s.h_llr_off), static_cast<void*>(s.h_info_off),
                             static_cast<void*>(s.h_ok), static_cast<void*>(s.h_used),
@@ -270,6 +279,8 @@ struct Server {
         // per-codeword metadata of the batch
         int c = 0;
         for (auto& r : s.reqs) {
+            r->first_cw = c;
+            r->completed = false;
             const int cid = r->spec.kind == 0 ? r->spec.code_id : phys[r->spec.phy_id].code_id;
             for (int i = 0; i < r->codewords; ++i, ++c) {
                 s.h_code[c] = static_cast<uint8_t>(cid);
@@ -292,16 +303,34 @@ struct Server {
         check_cuda(cudaMemcpyAsync(d_info_off, s.h_info_off, s.count * sizeof(long long), cudaMemcpyHostToDevice,
                                    s.stream),
                    "copy meta");
-        const int st = sicc_engine_decode_device_protected(s.engine, s.count, d_code, d_prot,
-                                                           reinterpret_cast<const float*>(arena_base), d_llr_off,
-                                                           arena_base, d_info_off, d_ok, d_used, nullptr, s.stream);
+        const int st = engine_decode(s.engine, s.count, d_code, d_prot, reinterpret_cast<const float*>(arena_base),
+                                     d_llr_off, arena_base, d_info_off, d_ok, d_used, nullptr, s.stream, s.bp_done);
         if (st != CUDA_OSD_STATUS_OK) throw std::runtime_error(std::string("decode: ") + last_error());
-        check_cuda(cudaMemcpyAsync(s.h_ok, d_ok, s.count, cudaMemcpyDeviceToHost, s.stream), "copy flags");
+        // BP-only requests are final once BP is done: copy them back on the early stream while
+        // the batch's OSD runs (success flags are final after BP for every codeword)
+        bool any_early = false;
+        for (auto& r : s.reqs) any_early |= (r->spec.protection == 0);
+        if (any_early) {
+            check_cuda(cudaStreamWaitEvent(s.early, s.bp_done, 0), "cudaStreamWaitEvent(bp done)");
+            check_cuda(cudaMemcpyAsync(s.h_ok, d_ok, s.count, cudaMemcpyDeviceToHost, s.early), "copy flags");
+            for (auto& r : s.reqs)
+                if (r->spec.protection == 0)
+                    check_cuda(cudaMemcpyAsync(r->spec.host_info, arena_base + r->info_off,
+                                               static_cast<size_t>(r->codewords) * r->k, cudaMemcpyDeviceToHost,
+                                               s.early),
+                               "copy results");
+            check_cuda(cudaEventRecord(s.early_done, s.early), "cudaEventRecord(early)");
+            s.early_pending = true;
+        } else {
+            check_cuda(cudaMemcpyAsync(s.h_ok, d_ok, s.count, cudaMemcpyDeviceToHost, s.stream), "copy flags");
+        }
         check_cuda(cudaMemcpyAsync(s.h_used, d_used, s.count, cudaMemcpyDeviceToHost, s.stream), "copy flags");
         for (auto& r : s.reqs)
-            check_cuda(cudaMemcpyAsync(r->spec.host_info, arena_base + r->info_off,
-                                       static_cast<size_t>(r->codewords) * r->k, cudaMemcpyDeviceToHost, s.stream),
-                       "copy results");
+            if (r->spec.protection != 0)
+                check_cuda(cudaMemcpyAsync(r->spec.host_info, arena_base + r->info_off,
+                                           static_cast<size_t>(r->codewords) * r->k, cudaMemcpyDeviceToHost, s.stream),
+                           "copy results");
+        if (any_early) check_cuda(cudaStreamWaitEvent(s.stream, s.early_done, 0), "cudaStreamWaitEvent(early)");
         check_cuda(cudaEventRecord(s.done, s.stream), "cudaEventRecord(batch)");
         s.busy = true;
         stats.batches += 1;
@@ -310,34 +339,49 @@ struct Server {
         return true;
     }
 
+    // Completes request r of slot s (its results are on the host); with_used: the OSD flags are too.
+    void complete(Slot& s, Req& r, Clock::time_point now, cudaEvent_t until, bool with_used)
+    {
+        float gpu_ms = 0.0f;
+        cudaEventElapsedTime(&gpu_ms, s.start, until);
+        sicc_completion_t done{};
+        done.request_id = r.id;
+        done.tag = r.spec.tag;
+        done.codewords = r.codewords;
+        for (int i = 0; i < r.codewords; ++i) {
+            const int c = r.first_cw + i;
+            const bool used = with_used && s.h_used[c];
+            done.osd_codewords += used ? 1 : 0;
+            done.failed_codewords += (!s.h_ok[c] && !used) ? 1 : 0;
+        }
+        done.latency_us = us_between(r.t_submit, now);
+        done.queue_us = us_between(r.t_submit, r.t_admit);
+        done.launch_us = us_between(r.t_submit, r.t_launch);
+        done.batch_gpu_us = 1000.0 * gpu_ms;
+        arena->release(r.off, r.bytes);  // no later work of the batch touches this block
+        if (r.h2d) cudaEventDestroy(r.h2d);
+        r.h2d = nullptr;
+        r.completed = true;
+        completions.push_back(done);
+        stats.completed += 1;
+    }
+
     bool retire()
     {
         bool any = false;
         for (auto& s : slots) {
-            if (!s.busy || cudaEventQuery(s.done) != cudaSuccess) continue;
-            const auto now = Clock::now();
-            float gpu_ms = 0.0f;
-            cudaEventElapsedTime(&gpu_ms, s.start, s.done);
-            int c = 0;
-            for (auto& r : s.reqs) {
-                sicc_completion_t done{};
-                done.request_id = r->id;
-                done.tag = r->spec.tag;
-                done.codewords = r->codewords;
-                for (int i = 0; i < r->codewords; ++i, ++c) {
-                    done.osd_codewords += s.h_used[c] ? 1 : 0;
-                    done.failed_codewords += (!s.h_ok[c] && !s.h_used[c]) ? 1 : 0;
-                }
-                done.latency_us = us_between(r->t_submit, now);
-                done.queue_us = us_between(r->t_submit, r->t_admit);
-                done.launch_us = us_between(r->t_submit, r->t_launch);
-                done.batch_gpu_us = 1000.0 * gpu_ms;
-                arena->release(r->off, r->bytes);
-                if (r->h2d) cudaEventDestroy(r->h2d);
-                r->h2d = nullptr;
-                completions.push_back(done);
-                stats.completed += 1;
+            if (!s.busy) continue;
+            if (s.early_pending && cudaEventQuery(s.early_done) == cudaSuccess) {  // BP-only requests
+                const auto now = Clock::now();
+                for (auto& r : s.reqs)
+                    if (r->spec.protection == 0) complete(s, *r, now, s.early_done, false);
+                s.early_pending = false;
+                any = true;
             }
+            if (cudaEventQuery(s.done) != cudaSuccess) continue;
+            const auto now = Clock::now();
+            for (auto& r : s.reqs)
+                if (!r->completed) complete(s, *r, now, s.done, true);
             s.reqs.clear();
             s.busy = false;
             any = true;
@@ -517,6 +561,9 @@ int sicc_server_start(unsigned long long handle)
             check_cuda(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking), "cudaStreamCreate(slot)");
             check_cuda(cudaEventCreate(&sl.done), "cudaEventCreate(slot)");
             check_cuda(cudaEventCreate(&sl.start), "cudaEventCreate(slot)");
+            check_cuda(cudaEventCreate(&sl.early_done), "cudaEventCreate(slot)");
+            check_cuda(cudaEventCreateWithFlags(&sl.bp_done, cudaEventDisableTiming), "cudaEventCreate(slot)");
+            check_cuda(cudaStreamCreateWithFlags(&sl.early, cudaStreamNonBlocking), "cudaStreamCreate(slot)");
             check_cuda(cudaMallocHost(&sl.h_code, N), "cudaMallocHost");
             check_cuda(cudaMallocHost(&sl.h_prot, N), "cudaMallocHost");
             check_cuda(cudaMallocHost(&sl.h_llr_off, N * sizeof(long long)), "cudaMallocHost");
