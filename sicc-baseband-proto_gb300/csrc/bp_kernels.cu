@@ -144,25 +144,23 @@ bp_layered_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int sl
                             q[j] = qj;
                             neg |= (qj < 0.0f) ? (1u << j) : 0u;
                             const float a = fabsf(qj);
-                            if (a < m1) {
-                                m2 = m1;
-                                m1 = a;
-                                idx = j;
-                            } else if (a < m2) {
-                                m2 = a;
-                            }
+                            // first strict minimum and second minimum (magnitudes are >= +0)
+                            idx = (a < m1) ? j : idx;
+                            m2 = fminf(m2, fmaxf(m1, a));
+                            m1 = fminf(m1, a);
                         }
                     }
                     const unsigned tot = static_cast<unsigned>(__popc(neg)) & 1u;
                     const float n1 = nms_mag(p.alpha, p.beta, m1);
                     const float n2 = nms_mag(p.alpha, p.beta, m2);
-                    unsigned nm = static_cast<unsigned>(idx) << 27;
+                    // new message signs (tot ^ sign of the input) for every slot in one step; bits of
+                    // empty slots are never read back
+                    const unsigned nm = ((neg ^ (0u - tot)) & 0x07FFFFFFu) | (static_cast<unsigned>(idx) << 27);
 #pragma unroll
                     for (int j = 0; j < D; ++j) {
                         if (v[j] >= 0) {
-                            const unsigned s = tot ^ ((neg >> j) & 1u);
+                            const unsigned s = (nm >> j) & 1u;
                             const float mag = (j == idx) ? n2 : n1;
-                            nm |= s << j;
                             app[v[j]] = __fadd_rn(q[j], s ? -mag : mag);
                         }
                     }
