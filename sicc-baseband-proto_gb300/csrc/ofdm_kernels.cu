@@ -1,6 +1,6 @@
 // OFDM receive kernels for sm_103a.
 //
-// sync_kernel (one thread-block cluster per frame) restates the CPU receiver's frame search
+// sync_kernel (one CTA per frame and pass of 4352 candidates) restates the CPU receiver's frame search
 // (uhd_ldpc_ofdm_link.cpp:5123-5329): Schmidl-Cox metric
 //   P(d) = sum_{i<L} conj(x[d+i]) x[d+i+L],  E1 = sum |x[d+i]|^2,  E2 = sum |x[d+i+L]|^2,
 //   metric(d) = |P|^2 / max(E1*E2, 1e-18);
@@ -10,8 +10,8 @@
 // passes of 256 x 17 from a shared-memory copy of the samples: each pass
 // computes the window sums at 256 chunk starts warp-cooperatively and slides
 // them 17 candidates per thread (the odd chunk keeps shared-memory reads on
-// distinct banks).  The passes of a frame are spread over the CTAs of its
-// cluster and resolved through distributed shared memory.
+// distinct banks).  Every pass publishes its result to global scratch and the
+// last pass of a frame to finish resolves the frame.
 //
 // demod_kernel (grid = frames x data-symbol groups) fuses the demodulator of
 // gpu_ofdm_pipeline.cu:566-672 / uhd_ldpc_ofdm_link.cpp:5350-5521: CFO
@@ -28,9 +28,8 @@
 #include <algorithm>
 #include <cfloat>
 
-#include <cooperative_groups.h>
-
-namespace cg = cooperative_groups;
+#include <cstdint>
+#include <mutex>
 
 namespace sicc {
 
@@ -41,7 +40,6 @@ constexpr int kSyncChunk = 17;
 constexpr int kSyncPass = kSyncThreads * kSyncChunk;
 constexpr int kMaxRefine = 1024;  // 2 * radius + 1
 constexpr int kMaxRadius = 511;
-constexpr int kSyncMaxCluster = 8;  // portable cluster size
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
@@ -66,8 +64,8 @@ __device__ __forceinline__ float warp_sum(float v)
 
 }  // namespace
 
-// One search result per CTA, published to the cluster's rank 0 through
-// distributed shared memory.
+// One search result per pass, published to global scratch for the CTA that
+// resolves the frame.
 struct PassResult {
     int key;      // mode 0: earliest successful candidate (INT_MAX: none); mode 1: position of the maximum (-1: none)
     int start;    // mode 0: refined start
@@ -97,20 +95,23 @@ __device__ __forceinline__ float fine_metric(const float2* __restrict__ x, const
     return (cr * cr + ci * ci) / fmaxf(eng * pre_energy, 1e-18f);
 }
 
-// Frame search, one thread-block cluster per frame: CTA r of a cluster of C
-// scans passes r, r + C, ... of 4352 candidates each and stops at its first
-// pass holding a successful candidate; rank 0 then takes the earliest result
-// (mode 0) or the first global maximum (mode 1) over the cluster, refines it
-// (mode 1), computes the CFO and writes the record.  Within a pass every
-// threshold crossing is refined at once: the fine metric of each position
-// within +-radius of any crossing is computed once (one warp per position),
-// then each crossing takes the first maximum over its window (starting from
-// 0, strict >) and the earliest crossing whose maximum reaches the threshold
-// wins -- the outcome of the CPU receiver's sequential retry loop.
+// Frame search, one CTA per (pass, frame): pass q scans candidates
+// [4352 q, 4352 (q + 1)).  Within a pass every threshold crossing is refined
+// at once: the fine metric of each position within +-radius of any crossing is
+// computed once (one warp per position), then each crossing takes the first
+// maximum over its window (starting from 0, strict >) and the earliest
+// crossing whose maximum reaches the threshold wins -- the outcome of the CPU
+// receiver's sequential retry loop.  Mode 0 wants the earliest success, so a
+// pass that starts after an earlier pass of its frame succeeded skips its
+// scan (`ticket[frames + f]` holds passes - earliest successful pass, 0 for
+// none).  Each pass stores its result in `pres`, and the CTA that takes the
+// frame's last ticket (`ticket[f]`) takes the earliest result (mode 0) or the
+// first global maximum (mode 1), refines it (mode 1), computes the CFO and
+// writes the record.  `ticket` starts zeroed.
 __global__ void __launch_bounds__(kSyncThreads)
 sync_kernel(const float2* __restrict__ samples, long long stride, const long long* __restrict__ frame_off,
-            const int* __restrict__ counts, int count, const float2* __restrict__ preamble, SyncParams p,
-            SyncOut* __restrict__ out)
+            const int* __restrict__ counts, int count, int frames, int passes, const float2* __restrict__ preamble,
+            SyncParams p, PassResult* __restrict__ pres, int* __restrict__ ticket, SyncOut* __restrict__ out)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* win = reinterpret_cast<float2*>(smem_raw);                 // [kSyncPass + pre_len]
@@ -121,29 +122,31 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const long lon
     __shared__ float rmetric[kMaxRefine];
     __shared__ int s_key[kSyncThreads / 32];
     __shared__ PassResult s_res;
-    __shared__ PassResult s_final;
+    __shared__ int s_flag;
 
-    cg::cluster_group cluster = cg::this_cluster();
-    const int C = static_cast<int>(cluster.num_blocks());
-    const int rank = static_cast<int>(cluster.block_rank());
-    const int f = blockIdx.x / C;
+    // pass-major order: the first passes of all frames run first, so later
+    // passes of a frame found early skip their scans
+    const int pass = blockIdx.x / frames;
+    const int f = blockIdx.x - pass * frames;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const float2* x = samples + (frame_off ? frame_off[f] : static_cast<long long>(f) * stride);
     const int avail = counts ? counts[f] : count;
     const int L = p.half_len, pre = p.pre_len, R = p.radius;
     int limit = avail - pre + 1;
     if (p.max_search > 0) limit = min(limit, p.max_search + 1);
+    int* done = ticket + frames;
 
     if (tid == 0) {
         s_res.key = p.mode == 1 ? -1 : 0x7fffffff;
         s_res.start = -1;
         s_res.fine = -1.0f;
         s_res.coarse = 0.0f;
+        s_flag = p.mode == 0 && *reinterpret_cast<volatile int*>(done + f) > passes - pass;
     }
     __syncthreads();
 
-    for (int pass = rank; pass * kSyncPass < limit; pass += C) {
-        const int base = pass * kSyncPass;
+    const int base = pass * kSyncPass;
+    if (!s_flag && base < limit) {
         const int span = min(kSyncPass + pre, avail - base);
         for (int i = tid; i < kSyncPass + pre; i += kSyncThreads) win[i] = (i < span) ? x[base + i] : make_float2(0.f, 0.f);
         __syncthreads();
@@ -209,72 +212,87 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const long lon
                     }
                 }
             }
+        } else {
+            // positions within +-R of a crossing of this pass: memo index i <-> sample x = base - R + i
+            const int mspan = kSyncPass + 2 * R;
+            {
+                const int seg = (mspan + kSyncThreads - 1) / kSyncThreads;
+                const int i0 = tid * seg, i1 = min(mspan, i0 + seg);
+                auto crossing = [&](int y) -> int {  // memo index y holds candidate d = y - R
+                    const int d = y - R;
+                    return (d >= 0 && d < kSyncPass && metric[d] >= p.threshold) ? 1 : 0;
+                };
+                int cnt = 0;
+                if (i0 < i1)
+                    for (int y = i0 - R; y <= i0 + R; ++y) cnt += crossing(y);
+                for (int i = i0; i < i1; ++i) {
+                    const int xs = base - R + i;
+                    memo[i] = (cnt > 0 && xs >= 0 && xs <= avail - pre) ? -2.0f : -1.0f;
+                    cnt += crossing(i + R + 1) - crossing(i - R);
+                }
+            }
             __syncthreads();
-            continue;
-        }
-        // positions within +-R of a crossing of this pass: memo index i <-> sample x = base - R + i
-        const int mspan = kSyncPass + 2 * R;
-        {
-            const int seg = (mspan + kSyncThreads - 1) / kSyncThreads;
-            const int i0 = tid * seg, i1 = min(mspan, i0 + seg);
-            auto crossing = [&](int y) -> int {  // memo index y holds candidate d = y - R
-                const int d = y - R;
-                return (d >= 0 && d < kSyncPass && metric[d] >= p.threshold) ? 1 : 0;
-            };
-            int cnt = 0;
-            if (i0 < i1)
-                for (int y = i0 - R; y <= i0 + R; ++y) cnt += crossing(y);
-            for (int i = i0; i < i1; ++i) {
-                const int xs = base - R + i;
-                memo[i] = (cnt > 0 && xs >= 0 && xs <= avail - pre) ? -2.0f : -1.0f;
-                cnt += crossing(i + R + 1) - crossing(i - R);
+            for (int i = warp; i < mspan; i += kSyncThreads / 32) {
+                if (memo[i] != -2.0f) continue;
+                const float m = fine_metric(x, win, base, kSyncPass + pre, base - R + i, preamble, pre, p.pre_energy, lane);
+                if (lane == 0) memo[i] = m;
+            }
+            __syncthreads();
+            // earliest crossing of the pass whose window maximum reaches the threshold
+            int first = 0x7fffffff, fstart = -1;
+            float fbm = 0.0f;
+            for (int c = 0; c < kSyncChunk; ++c) {
+                const int d = tid * kSyncChunk + c;
+                if (!(metric[d] >= p.threshold)) continue;
+                const int cand = base + d;
+                const int lo = max(0, cand - R);
+                const int hi = min(avail - pre, cand + R);
+                float bm = 0.0f;
+                int bd = cand;
+                for (int dd = lo; dd <= hi; ++dd) {
+                    const float m = memo[dd - base + R];
+                    if (m > bm) { bm = m; bd = dd; }
+                }
+                if (bm >= p.threshold) { first = d; fstart = bd; fbm = bm; break; }
+            }
+            const int wmin = __reduce_min_sync(0xffffffffu, static_cast<unsigned>(first));
+            if (lane == 0) s_key[warp] = wmin;
+            __syncthreads();
+            int bmin = 0x7fffffff;
+            for (int w = 0; w < kSyncThreads / 32; ++w) bmin = min(bmin, s_key[w]);
+            if (bmin != 0x7fffffff && first == bmin) {
+                s_res.key = base + first;
+                s_res.start = fstart;
+                s_res.fine = fbm;
+                s_res.coarse = metric[first];
+                atomicMax(done + f, passes - pass);
             }
         }
-        __syncthreads();
-        for (int i = warp; i < mspan; i += kSyncThreads / 32) {
-            if (memo[i] != -2.0f) continue;
-            const float m = fine_metric(x, win, base, kSyncPass + pre, base - R + i, preamble, pre, p.pre_energy, lane);
-            if (lane == 0) memo[i] = m;
-        }
-        __syncthreads();
-        // earliest crossing of the pass whose window maximum reaches the threshold
-        int first = 0x7fffffff, fstart = -1;
-        float fbm = 0.0f;
-        for (int c = 0; c < kSyncChunk; ++c) {
-            const int d = tid * kSyncChunk + c;
-            if (!(metric[d] >= p.threshold)) continue;
-            const int cand = base + d;
-            const int lo = max(0, cand - R);
-            const int hi = min(avail - pre, cand + R);
-            float bm = 0.0f;
-            int bd = cand;
-            for (int dd = lo; dd <= hi; ++dd) {
-                const float m = memo[dd - base + R];
-                if (m > bm) { bm = m; bd = dd; }
-            }
-            if (bm >= p.threshold) { first = d; fstart = bd; fbm = bm; break; }
-        }
-        const int wmin = __reduce_min_sync(0xffffffffu, static_cast<unsigned>(first));
-        if (lane == 0) s_key[warp] = wmin;
-        __syncthreads();
-        int bmin = 0x7fffffff;
-        for (int w = 0; w < kSyncThreads / 32; ++w) bmin = min(bmin, s_key[w]);
-        if (bmin != 0x7fffffff && first == bmin) {
-            s_res.key = base + first;
-            s_res.start = fstart;
-            s_res.fine = fbm;
-            s_res.coarse = metric[first];
-        }
-        __syncthreads();
-        if (bmin != 0x7fffffff) break;  // later passes of this CTA come after
     }
+    __syncthreads();
 
-    // rank 0 gathers the cluster's results
-    cluster.sync();
-    if (rank == 0 && tid == 0) {
-        PassResult best = s_res;
-        for (int r = 1; r < C; ++r) {
-            const PassResult o = *cluster.map_shared_rank(&s_res, r);
+    // publish this pass; the frame's last pass to finish resolves it
+    if (tid == 0) {
+        pres[static_cast<long long>(f) * passes + pass] = s_res;
+        __threadfence();
+        s_flag = atomicAdd(ticket + f, 1) == passes - 1;
+    }
+    __syncthreads();
+    if (!s_flag) return;
+    __threadfence();
+    if (tid == 0) {
+        const PassResult* fr = pres + static_cast<long long>(f) * passes;
+        PassResult best;
+        best.key = __ldcg(&fr[0].key);
+        best.start = __ldcg(&fr[0].start);
+        best.fine = __ldcg(&fr[0].fine);
+        best.coarse = __ldcg(&fr[0].coarse);
+        for (int q = 1; q < passes; ++q) {
+            PassResult o;
+            o.key = __ldcg(&fr[q].key);
+            o.start = __ldcg(&fr[q].start);
+            o.fine = __ldcg(&fr[q].fine);
+            o.coarse = __ldcg(&fr[q].coarse);
             if (p.mode == 1) {
                 if (o.key >= 0 && (o.fine > best.fine || (o.fine == best.fine && (best.key < 0 || o.key < best.key))))
                     best = o;
@@ -282,22 +300,22 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const long lon
                 best = o;
             }
         }
-        s_final = best;
+        s_res = best;
     }
-    cluster.sync();  // remote shared memory stays valid until every read is done
-    if (rank != 0) return;
+    __syncthreads();
+    const PassResult fin = s_res;
 
     SyncOut res{0, -1, 0.0f, 0.0f, 0.0f, -1};
     if (p.mode == 0) {
-        if (s_final.key != 0x7fffffff) {
-            res.coarse_start = s_final.key;
-            res.coarse = s_final.coarse >= 0.0f ? s_final.coarse : 0.0f;
-            res.start = s_final.start;
-            res.fine = s_final.fine;
+        if (fin.key != 0x7fffffff) {
+            res.coarse_start = fin.key;
+            res.coarse = fin.coarse >= 0.0f ? fin.coarse : 0.0f;
+            res.start = fin.start;
+            res.fine = fin.fine;
             res.found = (p.frame_len > 0 && res.start + p.frame_len > avail) ? 2 : 1;
         }
-    } else if (s_final.key >= 0 && s_final.fine >= p.threshold) {
-        const int cand = s_final.key;
+    } else if (fin.key >= 0 && fin.fine >= p.threshold) {
+        const int cand = fin.key;
         const int lo = max(0, cand - R);
         const int hi = min(limit - 1, cand + R);
         for (int dd = lo + warp; dd <= hi; dd += kSyncThreads / 32) {
@@ -315,7 +333,7 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const long lon
         }
         __syncthreads();
         res.coarse_start = cand;
-        res.coarse = s_final.fine;
+        res.coarse = fin.fine;
         res.fine = s_res.fine;
         if (s_res.fine >= p.threshold) {
             res.start = s_res.start;
@@ -344,6 +362,32 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const long lon
     if (tid == 0) out[f] = res;
 }
 
+namespace {
+
+// Stream-ordered pool for the sync scratch (pass results and tickets), one per
+// device; freed blocks stay in the pool for the next launch.
+cudaMemPool_t sync_pool(int device)
+{
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    std::lock_guard<std::mutex> lock(mu);
+    if (device < 0 || device >= 64) throw InvalidArgument("device ordinal out of range");
+    if (!pools[device]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        cudaMemPool_t pool = nullptr;
+        check_cuda(cudaMemPoolCreate(&pool, &props), "cudaMemPoolCreate(sync)");
+        uint64_t keep = UINT64_MAX;
+        check_cuda(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
+        pools[device] = pool;
+    }
+    return pools[device];
+}
+
+}  // namespace
+
 void launch_sync(const float2* samples, long long stride, const int* counts, int count, int frames,
                  const float2* preamble, const SyncParams& p, SyncOut* out, cudaStream_t st,
                  const long long* frame_off)
@@ -359,23 +403,27 @@ void launch_sync(const float2* samples, long long stride, const int* counts, int
     long long limit = span - p.pre_len + 1;
     if (p.max_search > 0) limit = std::min<long long>(limit, p.max_search + 1);
     const long long passes = std::max<long long>(1, (limit + kSyncPass - 1) / kSyncPass);
-    const int cluster = static_cast<int>(std::min<long long>(kSyncMaxCluster, passes));
-    check_cuda(cudaFuncSetAttribute(sync_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
-               "cudaFuncSetAttribute(sync)");
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(static_cast<unsigned>(frames) * cluster, 1, 1);
-    cfg.blockDim = dim3(kSyncThreads, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = cluster;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    check_cuda(cudaLaunchKernelEx(&cfg, sync_kernel, samples, stride, frame_off, counts, count, preamble, p, out),
-               "sync_kernel launch");
+    if (passes * frames > 0x7fffffffLL) throw InvalidArgument("sync grid too large");
+    int device = 0;
+    check_cuda(cudaGetDevice(&device), "cudaGetDevice");
+    const size_t res_bytes = static_cast<size_t>(frames) * passes * sizeof(PassResult);
+    const size_t ticket_bytes = static_cast<size_t>(2) * frames * sizeof(int);
+    void* scratch = nullptr;
+    check_cuda(cudaMallocFromPoolAsync(&scratch, res_bytes + ticket_bytes, sync_pool(device), st),
+               "cudaMallocFromPoolAsync(sync)");
+    PassResult* pres = static_cast<PassResult*>(scratch);
+    int* ticket = reinterpret_cast<int*>(static_cast<unsigned char*>(scratch) + res_bytes);
+    cudaError_t err = cudaMemsetAsync(ticket, 0, ticket_bytes, st);
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(sync_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (err == cudaSuccess) {
+        sync_kernel<<<static_cast<unsigned>(passes * frames), kSyncThreads, smem, st>>>(
+            samples, stride, frame_off, counts, count, frames, static_cast<int>(passes), preamble, p, pres, ticket, out);
+        err = cudaGetLastError();
+    }
+    const cudaError_t ferr = cudaFreeAsync(scratch, st);
+    check_cuda(err, "sync_kernel launch");
+    check_cuda(ferr, "cudaFreeAsync(sync)");
 }
 
 // ---------------------------------------------------------------------------

@@ -29,7 +29,7 @@ struct SyncParams {
     float pre_energy;     // sum |preamble|^2
 };
 
-// One cluster of up to 8 CTAs per frame.  samples: frame f starts at samples + f*stride (or
+// One CTA per frame and pass of 4352 candidates, with stream-ordered scratch.  samples: frame f starts at samples + f*stride (or
 // samples + frame_off[f], device offsets in complex samples) and holds counts[f] (or `count` when counts
 // is null) samples, at most `stride`.
 void launch_sync(const float2* samples, long long stride, const int* counts, int count, int frames,
