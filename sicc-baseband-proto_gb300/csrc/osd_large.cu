@@ -15,8 +15,11 @@
 //   * those m columns are found by Gauss-Jordan elimination on H: the
 //     accumulated row operations T (m x m bits, 128 KiB at m = 1024) live in
 //     shared memory column-major, column c's reduced form is T h_c, the XOR
-//     of the few columns of T that h_c selects (column weight <= 16), and a
-//     pivot touches only the columns of T with a 1 in the pivot row;
+//     of the few columns of T that h_c selects (column weight <= 16).  The
+//     pivots are taken 8 at a time; their combined row operation is linear in
+//     a column's 8 pivot-row bits, so it is tabulated (two 16-entry tables of
+//     m-bit vectors) and each column of T with a nonzero index takes one
+//     table-lookup XOR per round;
 //   * with T H in reduced form on those columns, a candidate that keeps the
 //     hard decisions on the MRB except a flip set F differs from the hard
 //     decisions at the pivot positions selected by T s XOR (XOR over f in F of
@@ -35,7 +38,8 @@ namespace {
 constexpr int kOsdHThreads = 512;
 constexpr int kOsdHWarps = kOsdHThreads / 32;
 constexpr int kOsdHMaxPool = 128;
-constexpr int kRound = 4;  // columns of H per elimination round
+constexpr int kRound = 8;  // columns of H per elimination round
+constexpr int kTabStride = 33;  // words per table entry (odd: groups of lanes reading different entries spread over banks)
 
 struct OsdHLayout {
     int np;       // sort length: power of two >= the longest n
@@ -47,13 +51,16 @@ struct OsdHLayout {
 };
 
 struct OsdHSmem {
-    uint32_t* T;             // [32*mw][ts] column-major: column i of the row-operation matrix
+    uint32_t* T;             // [32*mw + 2*kRound][ts] column-major: column i of the row-operation matrix,
+                             // then two buffers of kRound reduced candidate columns
     unsigned long long* keys;// [np]; reused as the flip-pool scratch after the sort
     float* rel;              // [nmax] |llr| by sorted position j
     int16_t* perm;           // [nmax] code position at sorted position j
     int16_t* row_of_col;     // [nmax] pivot rank of a code position, -1 for the MRB
     uint32_t* hard;          // [nmax/32+1] hard decisions by code position
-    uint32_t* wv;            // [kRound][32] v + e_p of the round's pivots
+    uint32_t* wv;            // [kRound][32] the round's basis vectors U_r (0 for a dependent candidate)
+    uint32_t* tab;           // [32][kTabStride] XOR of U_0..3 (entries 0..15) and of U_4..7 (16..31) by index nibble
+    uint32_t* hits;          // [32*mw + kRound] slot << 8 | pivot-row index of the columns a round changes
     uint32_t* piv;           // [mw] pivoted rows
     int16_t* order;          // [32*mw] row of the t-th pivot
     uint32_t* vs;            // [poolmax+1][32] T s and T h_f by row (before reordering)
@@ -79,13 +86,15 @@ __host__ __device__ inline size_t carve(const OsdHLayout& l, unsigned char* base
     };
     const size_t rows = 32 * static_cast<size_t>(l.mw);
     OsdHSmem t{};
-    t.T = reinterpret_cast<uint32_t*>(take(rows * l.ts * 4));
+    t.T = reinterpret_cast<uint32_t*>(take((rows + 2 * kRound) * l.ts * 4));
     t.keys = reinterpret_cast<unsigned long long*>(take(static_cast<size_t>(l.np) * 8));
     t.rel = reinterpret_cast<float*>(take(static_cast<size_t>(l.nmax) * 4));
     t.perm = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nmax) * 2));
     t.row_of_col = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nmax) * 2));
     t.hard = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(l.nmax) / 32 + 1) * 4));
     t.wv = reinterpret_cast<uint32_t*>(take(kRound * 32 * 4));
+    t.tab = reinterpret_cast<uint32_t*>(take(32 * kTabStride * 4));
+    t.hits = reinterpret_cast<uint32_t*>(take((rows + kRound) * 4));
     t.piv = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.mw) * 4));
     t.order = reinterpret_cast<int16_t*>(take(rows * 2));
     t.vs = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(l.poolmax) + 1) * 32 * 4));
@@ -118,7 +127,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
     OsdHSmem s;
     carve(lay, smem_raw, &s);
     __shared__ int s_rp[kRound];
-    __shared__ int s_nd, s_np, s_used, s_jstop;
+    __shared__ int s_nd, s_np, s_used, s_jstop, s_nhits;
     __shared__ unsigned long long s_best;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int TS = lay.ts;
@@ -198,16 +207,21 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         __syncthreads();
 
         // ---- 3. Gauss-Jordan scan of H's columns in increasing reliability ----
-        // Warp 0 forms the reduced column v = T h_c (XOR of the columns of T that
-        // h_c selects) and picks the lowest unpivoted row p with v_p = 1; then
-        // every column of T with a 1 in row p takes v + e_p (T <- (I + (v + e_p) e_p^T) T),
-        // which turns column c into e_p and leaves earlier pivot columns alone.
-        // Columns are taken kRound at a time.  Warp 0 reduces the round's columns
-        // against T as it stands (all loads in flight together), then picks their
-        // pivots in order, applying each earlier pivot of the round to the later
-        // columns (u + u_p (v + e_p)).  Then every warp applies the round's pivots,
-        // in order, to its chunks of T: a column takes pivot r's row operation when
-        // its row-p_r bit is set after the previous ones.  Two barriers per round.
+        // A column c's reduced form is v = T h_c (the XOR of the columns of T that
+        // h_c selects); its pivot is the lowest unpivoted row p with v_p = 1, and
+        // the pivot's row operation T <- (I + W e_p^T) T, W = v + e_p, turns
+        // column c into e_p and leaves earlier pivot columns alone.
+        // Columns are taken kRound at a time.  Step A: warp 0 takes the round's
+        // candidates, already reduced against T as it stands, and picks their
+        // pivots in order, applying the round's earlier pivots to each later
+        // candidate; it keeps the round's combined operation as a basis:
+        //   a -> a + sum_r a_{p_r} U_r,  U_r <- U_r + U_r[p] W for a new pivot p,
+        // (a_{p_r} the column's bits before the round, U_r = 0 for a dependent
+        // candidate).  Meanwhile warps 1..kRound reduce the next round's
+        // candidates against the same T.  Step B: the two nibble tables of the
+        // basis, and one thread per column of T (and per next-round candidate)
+        // gathers its pivot-row bits into an index, listing the nonzero ones.
+        // Step C: every listed column takes its two table entries.
         auto rows_of = [&](int jj, int& e0, int& cnt) -> int {  // one row of column jj per lane
             const int ci = colinfo[jj];
             e0 = ci >> 8;
@@ -229,36 +243,44 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                 if (lane < MW) v ^= s.T[static_cast<size_t>(tslot(hv.col_rows[e0 + e], MW)) * TS + lane];
             return v;
         };
-        int t = 0, jstop = -1;
+        // candidate slot r of buffer b: rows + b * kRound + r
+        auto reduce_candidate = [&](int jj, int slot) {
+            unsigned v = 0u;
+            if (jj >= 0) {
+                int e0, cnt;
+                const int rw = rows_of(jj, e0, cnt);
+                v = reduce_column(rw, e0, cnt);
+            }
+            if (lane < MW) s.T[static_cast<size_t>(slot) * TS + lane] = v;
+        };
+        if (warp < kRound) reduce_candidate(n - 1 - warp, rows + warp);
+        if (tid == 0) s_nhits = 0;
+        __syncthreads();
+        // step C: G = 32 / 2^lg columns per warp instruction, MW words each
+        const int lg = MW <= 1 ? 0 : 32 - __clz(MW - 1);
+        const int G = 32 >> lg, grp = lane >> lg, wd = lane & ((1 << lg) - 1);
+        int t = 0, jstop = -1, buf = 0;
         unsigned pivw = 0u;  // warp 0: pivoted rows, word `lane`
         for (int j = n - 1; j >= 0 && t < m;) {
             if (warp == 0) {
-                unsigned u[kRound];
-#pragma unroll
-                for (int r = 0; r < kRound; ++r) {
-                    u[r] = 0u;
-                    if (j - r >= 0) {
-                        int e0, cnt;
-                        const int rw = rows_of(j - r, e0, cnt);
-                        u[r] = reduce_column(rw, e0, cnt);
-                    }
-                }
-                int pr[kRound];
-                unsigned wr[kRound];
+                unsigned U[kRound];
+                int P[kRound];
                 int np = 0, used = 0, js = -1;
 #pragma unroll
                 for (int r = 0; r < kRound; ++r) {
-                    pr[r] = -1;
-                    wr[r] = 0u;
+                    U[r] = 0u;
+                    P[r] = -1;
                     if (j - r >= 0 && t + np < m) {
-                        unsigned v = u[r];
+                        unsigned v = lane < MW ? s.T[static_cast<size_t>(rows + buf * kRound + r) * TS + lane] : 0u;
+                        // the round's earlier pivots: v + sum_i v_{p_i} U_i
+                        unsigned mk = 0u;
 #pragma unroll
-                        for (int q = 0; q < r; ++q) {  // earlier pivots of the round
-                            if (pr[q] >= 0) {
-                                const unsigned bit = (__shfl_sync(0xffffffffu, v, pr[q] >> 5) >> (pr[q] & 31)) & 1u;
-                                if (bit) v ^= wr[q];
-                            }
-                        }
+                        for (int i = 0; i < r; ++i)
+                            if (P[i] >= 0 && (P[i] >> 5) == lane) mk |= ((v >> (P[i] & 31)) & 1u) << i;
+                        mk = __reduce_or_sync(0xffffffffu, mk);
+#pragma unroll
+                        for (int i = 0; i < r; ++i)
+                            if ((mk >> i) & 1u) v ^= U[i];
                         const unsigned x = (lane < MW) ? (v & ~pivw) : 0u;
                         const unsigned lanes = __ballot_sync(0xffffffffu, x != 0u);
                         const int c = s.perm[j - r];
@@ -266,9 +288,17 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                             const int l0 = __ffs(lanes) - 1;
                             const unsigned x0 = __shfl_sync(0xffffffffu, x, l0);
                             const int p = l0 * 32 + __ffs(x0) - 1;
-                            pr[r] = p;
-                            wr[r] = (lane == (p >> 5)) ? (v ^ (1u << (p & 31))) : v;
-                            if (lane == (p >> 5)) pivw |= 1u << (p & 31);
+                            const unsigned W = (lane == l0) ? (v ^ (1u << (p & 31))) : v;
+                            unsigned mb = 0u;
+#pragma unroll
+                            for (int i = 0; i < r; ++i) mb |= ((U[i] >> (p & 31)) & 1u) << i;
+                            mb = __shfl_sync(0xffffffffu, mb, l0);
+#pragma unroll
+                            for (int i = 0; i < r; ++i)
+                                if ((mb >> i) & 1u) U[i] ^= W;
+                            U[r] = W;
+                            P[r] = p;
+                            if (lane == l0) pivw |= 1u << (p & 31);
                             if (lane == 0) {
                                 s.order[t + np] = static_cast<int16_t>(p);
                                 s.row_of_col[c] = static_cast<int16_t>(t + np);
@@ -284,74 +314,76 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                 }
 #pragma unroll
                 for (int r = 0; r < kRound; ++r) {
-                    if (lane == 0) s_rp[r] = pr[r];
-                    s.wv[r * 32 + lane] = wr[r];
+                    if (lane == 0) s_rp[r] = P[r];
+                    s.wv[r * 32 + lane] = U[r];
                 }
                 if (lane == 0) {
                     s_np = np;
                     s_used = used;
                     s_jstop = js;
                 }
+            } else if (warp <= kRound) {
+                reduce_candidate(j - kRound - (warp - 1), rows + (buf ^ 1) * kRound + (warp - 1));
             }
             __syncthreads();
             const int np = s_np;
             const int used = s_used;
             if (np > 0) {
-                int P[kRound];
-                unsigned W[kRound];
+                for (int i = tid; i < 32 * 32; i += kOsdHThreads) {
+                    const int e = i >> 5, w = i & 31, half = e >> 4;
+                    unsigned acc = 0u;
 #pragma unroll
-                for (int r = 0; r < kRound; ++r) {
-                    P[r] = s_rp[r];
-                    W[r] = s.wv[r * 32 + lane];
+                    for (int q = 0; q < 4; ++q)
+                        if ((e >> q) & 1) acc ^= s.wv[(half * 4 + q) * 32 + w];
+                    s.tab[e * kTabStride + w] = acc;
                 }
-                // the pivot-row bits of this warp's column chunks
-                unsigned hits[(32 + kOsdHWarps - 1) / kOsdHWarps];
+                int P[kRound];
 #pragma unroll
-                for (int h = 0; h < (32 + kOsdHWarps - 1) / kOsdHWarps; ++h) {
-                    const int q = warp + h * kOsdHWarps;
-                    bool in = false;
-                    if (q < MW) {
-                        const uint32_t* col = s.T + static_cast<size_t>(q * 32 + lane) * TS;
+                for (int r = 0; r < kRound; ++r) P[r] = s_rp[r];
+                const int nslots = rows + kRound;
+                for (int b0 = warp * 32; b0 < nslots; b0 += kOsdHThreads) {
+                    const int si = b0 + lane;
+                    const int slot = si < rows ? si : rows + (buf ^ 1) * kRound + (si - rows);
+                    unsigned idx = 0u;
+                    if (si < nslots) {
+                        const uint32_t* col = s.T + static_cast<size_t>(slot) * TS;
 #pragma unroll
                         for (int r = 0; r < kRound; ++r)
-                            if (P[r] >= 0) in |= ((col[P[r] >> 5] >> (P[r] & 31)) & 1u) != 0u;
+                            if (P[r] >= 0) idx |= ((col[P[r] >> 5] >> (P[r] & 31)) & 1u) << r;
                     }
-                    hits[h] = __ballot_sync(0xffffffffu, in);
+                    const unsigned bal = __ballot_sync(0xffffffffu, idx != 0u);
+                    int off = 0;
+                    if (lane == 0 && bal) off = atomicAdd(&s_nhits, __popc(bal));
+                    off = __shfl_sync(0xffffffffu, off, 0);
+                    if (idx) s.hits[off + __popc(bal & ((1u << lane) - 1u))] = (static_cast<unsigned>(slot) << 8) | idx;
                 }
+            }
+            __syncthreads();
+            if (np > 0) {
+                const int nh = s_nhits;
+                const int stepw = kOsdHWarps * G;
+                for (int h0 = warp * G + grp; h0 < nh; h0 += 4 * stepw) {
+                    unsigned e[4], a[4];
 #pragma unroll
-                for (int h = 0; h < (32 + kOsdHWarps - 1) / kOsdHWarps; ++h) {
-                    const int q = warp + h * kOsdHWarps;
-                    unsigned hit = hits[h];
-                    while (hit) {  // up to 8 columns per pass, loads before stores
-                        int bs[8];
+                    for (int u = 0; u < 4; ++u) {
+                        const int h = h0 + u * stepw;
+                        e[u] = (h < nh && wd < MW) ? s.hits[h] : 0u;
+                        a[u] = e[u] ? s.T[static_cast<size_t>(e[u] >> 8) * TS + wd] : 0u;
+                    }
 #pragma unroll
-                        for (int x = 0; x < 8; ++x) {
-                            bs[x] = hit ? __ffs(hit) - 1 : -1;
-                            hit &= hit - 1;
-                        }
-                        uint32_t a[8];
-#pragma unroll
-                        for (int x = 0; x < 8; ++x)
-                            a[x] = (bs[x] >= 0 && lane < MW) ? s.T[static_cast<size_t>(q * 32 + bs[x]) * TS + lane] : 0u;
-#pragma unroll
-                        for (int r = 0; r < kRound; ++r) {  // the round's pivots in order
-                            if (P[r] < 0) continue;
-#pragma unroll
-                            for (int x = 0; x < 8; ++x) {
-                                const unsigned bit = (__shfl_sync(0xffffffffu, a[x], P[r] >> 5) >> (P[r] & 31)) & 1u;
-                                if (bit) a[x] ^= W[r];
-                            }
-                        }
-#pragma unroll
-                        for (int x = 0; x < 8; ++x)
-                            if (bs[x] >= 0 && lane < MW) s.T[static_cast<size_t>(q * 32 + bs[x]) * TS + lane] = a[x];
+                    for (int u = 0; u < 4; ++u) {
+                        if (!e[u]) continue;
+                        a[u] ^= s.tab[(e[u] & 15u) * kTabStride + wd] ^ s.tab[(16u + ((e[u] >> 4) & 15u)) * kTabStride + wd];
+                        s.T[static_cast<size_t>(e[u] >> 8) * TS + wd] = a[u];
                     }
                 }
             }
             t += np;
             if (t == m) jstop = s_jstop;
             j -= used;
+            buf ^= 1;
             __syncthreads();
+            if (tid == 0) s_nhits = 0;  // read by every warp before the barrier; next used after the next one
         }
         if (t < m) {  // H rank deficient: leave the BP decision in place
             __syncthreads();
