@@ -17,9 +17,9 @@
 //     shared memory column-major, column c's reduced form is T h_c, the XOR
 //     of the few columns of T that h_c selects (column weight <= 16).  The
 //     pivots are taken 8 at a time; their combined row operation is linear in
-//     a column's 8 pivot-row bits, so it is tabulated (two 16-entry tables of
-//     m-bit vectors) and each column of T with a nonzero index takes one
-//     table-lookup XOR per round;
+//     a column's 8 pivot-row bits (a -> a + sum_r a_{p_r} U_r), so each
+//     column of T takes it in one pass, and one warp picks the next round's
+//     pivots while the others apply the current round to T;
 //   * with T H in reduced form on those columns, a candidate that keeps the
 //     hard decisions on the MRB except a flip set F differs from the hard
 //     decisions at the pivot positions selected by T s XOR (XOR over f in F of
@@ -39,7 +39,8 @@ constexpr int kOsdHThreads = 512;
 constexpr int kOsdHWarps = kOsdHThreads / 32;
 constexpr int kOsdHMaxPool = 128;
 constexpr int kRound = 8;  // columns of H per elimination round
-constexpr int kTabStride = 33;  // words per table entry (odd: groups of lanes reading different entries spread over banks)
+constexpr int kHitsPerWarp = 96;  // columns of T a worker owns: 32 * ceil(1024 / (32 * 15)) (m <= 1024)
+constexpr int kTabStride = 33;  // words per table entry: lanes reading different entries hit different banks
 
 struct OsdHLayout {
     int np;       // sort length: power of two >= the longest n
@@ -58,9 +59,12 @@ struct OsdHSmem {
     int16_t* perm;           // [nmax] code position at sorted position j
     int16_t* row_of_col;     // [nmax] pivot rank of a code position, -1 for the MRB
     uint32_t* hard;          // [nmax/32+1] hard decisions by code position
-    uint32_t* wv;            // [kRound][32] the round's basis vectors U_r (0 for a dependent candidate)
-    uint32_t* tab;           // [32][kTabStride] XOR of U_0..3 (entries 0..15) and of U_4..7 (16..31) by index nibble
-    uint32_t* hits;          // [32*mw + kRound] slot << 8 | pivot-row index of the columns a round changes
+    uint32_t* tab;           // [2][32][kTabStride] by round parity: entry g < 16 the XOR of U_0..3 selected by g, entry
+                             // 16 + g that of U_4..7; aliases vs..relq, which are first written after the
+                             // elimination
+    uint32_t* wv;            // [2][kRound][32] by round parity: the round's basis U_r (0 for a dependent candidate)
+    uint32_t* hits;          // [warps][kHitsPerWarp] per warp: the columns a round changes, word offset in T
+                             // (16 bits) | pivot-row index << 16
     uint32_t* piv;           // [mw] pivoted rows
     int16_t* order;          // [32*mw] row of the t-th pivot
     uint32_t* vs;            // [poolmax+1][32] T s and T h_f by row (before reordering)
@@ -92,19 +96,27 @@ __host__ __device__ inline size_t carve(const OsdHLayout& l, unsigned char* base
     t.perm = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nmax) * 2));
     t.row_of_col = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nmax) * 2));
     t.hard = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(l.nmax) / 32 + 1) * 4));
-    t.wv = reinterpret_cast<uint32_t*>(take(kRound * 32 * 4));
-    t.tab = reinterpret_cast<uint32_t*>(take(32 * kTabStride * 4));
-    t.hits = reinterpret_cast<uint32_t*>(take((rows + kRound) * 4));
+    t.wv = reinterpret_cast<uint32_t*>(take(2 * kRound * 32 * 4));
+    t.hits = reinterpret_cast<uint32_t*>(take(kOsdHWarps * kHitsPerWarp * 4));
     t.piv = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.mw) * 4));
     t.order = reinterpret_cast<int16_t*>(take(rows * 2));
-    t.vs = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(l.poolmax) + 1) * 32 * 4));
     t.syn = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.mw) * 4));
     t.pivj = reinterpret_cast<int16_t*>(take(rows * 2));
-    t.relq = reinterpret_cast<float*>(take(rows * 4));
     t.mrb = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nmax) * 2));
     t.pool_j = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.poolmax) * 2));
-    t.avec = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.poolmax) * l.mw * 4));
-    t.aug = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.mw) * 4));
+    {  // the tables of the elimination, then the vectors of the candidate search
+        const size_t b_vs = a16((static_cast<size_t>(l.poolmax) + 1) * 32 * 4);
+        const size_t b_avec = a16(static_cast<size_t>(l.poolmax) * l.mw * 4);
+        const size_t b_aug = a16(static_cast<size_t>(l.mw) * 4);
+        const size_t b_relq = a16(rows * 4);
+        const size_t b_vec = b_vs + b_avec + b_aug + b_relq, b_tab = 2 * 32 * 33 * 4;
+        unsigned char* g = take(b_vec > b_tab ? b_vec : b_tab);
+        t.tab = reinterpret_cast<uint32_t*>(g);
+        t.vs = reinterpret_cast<uint32_t*>(g);
+        t.avec = reinterpret_cast<uint32_t*>(g ? g + b_vs : nullptr);
+        t.aug = reinterpret_cast<uint32_t*>(g ? g + b_vs + b_avec : nullptr);
+        t.relq = reinterpret_cast<float*>(g ? g + b_vs + b_avec + b_aug : nullptr);
+    }
     t.rows = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nnzmax) * 2));
     if (s) *s = t;
     return o;
@@ -126,8 +138,9 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     OsdHSmem s;
     carve(lay, smem_raw, &s);
-    __shared__ int s_rp[kRound];
-    __shared__ int s_nd, s_np, s_used, s_jstop, s_nhits;
+    __shared__ int s_rp[2][kRound];
+    __shared__ int s_np[2], s_used[2], s_jstop[2];
+    __shared__ int s_nd;
     __shared__ unsigned long long s_best;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int TS = lay.ts;
@@ -211,17 +224,24 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         // h_c selects); its pivot is the lowest unpivoted row p with v_p = 1, and
         // the pivot's row operation T <- (I + W e_p^T) T, W = v + e_p, turns
         // column c into e_p and leaves earlier pivot columns alone.
-        // Columns are taken kRound at a time.  Step A: warp 0 takes the round's
-        // candidates, already reduced against T as it stands, and picks their
-        // pivots in order, applying the round's earlier pivots to each later
-        // candidate; it keeps the round's combined operation as a basis:
-        //   a -> a + sum_r a_{p_r} U_r,  U_r <- U_r + U_r[p] W for a new pivot p,
-        // (a_{p_r} the column's bits before the round, U_r = 0 for a dependent
-        // candidate).  Meanwhile warps 1..kRound reduce the next round's
-        // candidates against the same T.  Step B: the two nibble tables of the
-        // basis, and one thread per column of T (and per next-round candidate)
-        // gathers its pivot-row bits into an index, listing the nonzero ones.
-        // Step C: every listed column takes its two table entries.
+        // Columns are taken kRound at a time, in rounds pipelined over one
+        // barrier each.  In the barrier interval of round k:
+        //   * warp 0 takes round k's candidates (reduced against T before
+        //     round k-1), applies round k-1's operation to them, and picks
+        //     their pivots in order; each pivot's operation is applied at once
+        //     to the later candidates and to the round's basis,
+        //       a -> a + sum_r a_{p_r} U_r,  U_r <- U_r + U_r[p] W for a new pivot p
+        //     (a_{p_r} a column's bits before the round, U_r = 0 for a dependent
+        //     candidate);
+        //   * warps 1..15 tabulate round k-1's basis by index nibble, and the
+        //     worker warps apply round k-1's operation to the columns of T they
+        //     own (the pivot-row bits of a column form its index; columns with a
+        //     nonzero index take its two table entries), meet on a named
+        //     barrier, and kRound of them reduce round k+1's candidates against
+        //     T.  The workers are warps 1..15 when m > 512 (the update bounds
+        //     the round); for smaller m, where the selection does, warp 0 keeps
+        //     its scheduler (warps w = 0 mod 4) to itself and the workers are
+        //     the 12 warps w != 0 mod 4.
         auto rows_of = [&](int jj, int& e0, int& cnt) -> int {  // one row of column jj per lane
             const int ci = colinfo[jj];
             e0 = ci >> 8;
@@ -254,137 +274,204 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             if (lane < MW) s.T[static_cast<size_t>(slot) * TS + lane] = v;
         };
         if (warp < kRound) reduce_candidate(n - 1 - warp, rows + warp);
-        if (tid == 0) s_nhits = 0;
         __syncthreads();
-        // step C: G = 32 / 2^lg columns per warp instruction, MW words each
-        const int lg = MW <= 1 ? 0 : 32 - __clz(MW - 1);
-        const int G = 32 >> lg, grp = lane >> lg, wd = lane & ((1 << lg) - 1);
-        int t = 0, jstop = -1, buf = 0;
+        const int lg = MW <= 1 ? 0 : 32 - __clz(MW - 1);  // table words per entry: 2^lg >= MW
+        uint32_t* seg = s.hits + warp * kHitsPerWarp;
+        const bool narrow = m <= 512;
+        const int nworkers = narrow ? kOsdHWarps - kOsdHWarps / 4 : kOsdHWarps - 1;
+        const bool worker = warp != 0 && (!narrow || (warp & 3) != 0);
+        const int wi = narrow ? warp - (warp >> 2) - 1 : warp - 1;  // worker index
+        int t = 0, j = n - 1, nd = 0, jstop = -1;          // after the rounds selected so far
+        int pt = 0, pj = 0, pnd = 0, pnp = 0, pused = 0;   // the round whose update is pending
+        bool pending = false;
         unsigned pivw = 0u;  // warp 0: pivoted rows, word `lane`
-        for (int j = n - 1; j >= 0 && t < m;) {
-            if (warp == 0) {
-                unsigned U[kRound];
-                int P[kRound];
-                int np = 0, used = 0, js = -1;
+        unsigned Up[kRound];  // warp 0: the pending round's basis, and its pivot rows as word offset + bit
+        int pwo[kRound];
+        unsigned pwb[kRound];
 #pragma unroll
-                for (int r = 0; r < kRound; ++r) {
-                    U[r] = 0u;
-                    P[r] = -1;
-                    if (j - r >= 0 && t + np < m) {
-                        unsigned v = lane < MW ? s.T[static_cast<size_t>(rows + buf * kRound + r) * TS + lane] : 0u;
-                        // the round's earlier pivots: v + sum_i v_{p_i} U_i
-                        unsigned mk = 0u;
-#pragma unroll
-                        for (int i = 0; i < r; ++i)
-                            if (P[i] >= 0 && (P[i] >> 5) == lane) mk |= ((v >> (P[i] & 31)) & 1u) << i;
-                        mk = __reduce_or_sync(0xffffffffu, mk);
-#pragma unroll
-                        for (int i = 0; i < r; ++i)
-                            if ((mk >> i) & 1u) v ^= U[i];
-                        const unsigned x = (lane < MW) ? (v & ~pivw) : 0u;
-                        const unsigned lanes = __ballot_sync(0xffffffffu, x != 0u);
-                        const int c = s.perm[j - r];
-                        if (lanes) {
-                            const int l0 = __ffs(lanes) - 1;
-                            const unsigned x0 = __shfl_sync(0xffffffffu, x, l0);
-                            const int p = l0 * 32 + __ffs(x0) - 1;
-                            const unsigned W = (lane == l0) ? (v ^ (1u << (p & 31))) : v;
-                            unsigned mb = 0u;
-#pragma unroll
-                            for (int i = 0; i < r; ++i) mb |= ((U[i] >> (p & 31)) & 1u) << i;
-                            mb = __shfl_sync(0xffffffffu, mb, l0);
-#pragma unroll
-                            for (int i = 0; i < r; ++i)
-                                if ((mb >> i) & 1u) U[i] ^= W;
-                            U[r] = W;
-                            P[r] = p;
-                            if (lane == l0) pivw |= 1u << (p & 31);
-                            if (lane == 0) {
-                                s.order[t + np] = static_cast<int16_t>(p);
-                                s.row_of_col[c] = static_cast<int16_t>(t + np);
-                                s.pivj[t + np] = static_cast<int16_t>(j - r);
-                            }
-                            ++np;
-                            if (t + np == m) js = j - r;
-                        } else if (lane == 0) {
-                            s.mrb[s_nd++] = static_cast<int16_t>(j - r);  // dependent: an MRB position
-                        }
-                        used = r + 1;
-                    }
-                }
-#pragma unroll
-                for (int r = 0; r < kRound; ++r) {
-                    if (lane == 0) s_rp[r] = P[r];
-                    s.wv[r * 32 + lane] = U[r];
-                }
-                if (lane == 0) {
-                    s_np = np;
-                    s_used = used;
-                    s_jstop = js;
-                }
-            } else if (warp <= kRound) {
-                reduce_candidate(j - kRound - (warp - 1), rows + (buf ^ 1) * kRound + (warp - 1));
-            }
-            __syncthreads();
-            const int np = s_np;
-            const int used = s_used;
-            if (np > 0) {
-                for (int i = tid; i < 32 * 32; i += kOsdHThreads) {
-                    const int e = i >> 5, w = i & 31, half = e >> 4;
-                    unsigned acc = 0u;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q)
-                        if ((e >> q) & 1) acc ^= s.wv[(half * 4 + q) * 32 + w];
-                    s.tab[e * kTabStride + w] = acc;
-                }
-                int P[kRound];
-#pragma unroll
-                for (int r = 0; r < kRound; ++r) P[r] = s_rp[r];
-                const int nslots = rows + kRound;
-                for (int b0 = warp * 32; b0 < nslots; b0 += kOsdHThreads) {
-                    const int si = b0 + lane;
-                    const int slot = si < rows ? si : rows + (buf ^ 1) * kRound + (si - rows);
-                    unsigned idx = 0u;
-                    if (si < nslots) {
-                        const uint32_t* col = s.T + static_cast<size_t>(slot) * TS;
-#pragma unroll
-                        for (int r = 0; r < kRound; ++r)
-                            if (P[r] >= 0) idx |= ((col[P[r] >> 5] >> (P[r] & 31)) & 1u) << r;
-                    }
-                    const unsigned bal = __ballot_sync(0xffffffffu, idx != 0u);
-                    int off = 0;
-                    if (lane == 0 && bal) off = atomicAdd(&s_nhits, __popc(bal));
-                    off = __shfl_sync(0xffffffffu, off, 0);
-                    if (idx) s.hits[off + __popc(bal & ((1u << lane) - 1u))] = (static_cast<unsigned>(slot) << 8) | idx;
-                }
-            }
-            __syncthreads();
-            if (np > 0) {
-                const int nh = s_nhits;
-                const int stepw = kOsdHWarps * G;
-                for (int h0 = warp * G + grp; h0 < nh; h0 += 4 * stepw) {
-                    unsigned e[4], a[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int h = h0 + u * stepw;
-                        e[u] = (h < nh && wd < MW) ? s.hits[h] : 0u;
-                        a[u] = e[u] ? s.T[static_cast<size_t>(e[u] >> 8) * TS + wd] : 0u;
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        if (!e[u]) continue;
-                        a[u] ^= s.tab[(e[u] & 15u) * kTabStride + wd] ^ s.tab[(16u + ((e[u] >> 4) & 15u)) * kTabStride + wd];
-                        s.T[static_cast<size_t>(e[u] >> 8) * TS + wd] = a[u];
-                    }
-                }
-            }
-            t += np;
-            if (t == m) jstop = s_jstop;
-            j -= used;
-            buf ^= 1;
-            __syncthreads();
-            if (tid == 0) s_nhits = 0;  // read by every warp before the barrier; next used after the next one
+        for (int r = 0; r < kRound; ++r) {
+            Up[r] = 0u;
+            pwo[r] = 0;
+            pwb[r] = 0u;
         }
+        for (int k = 0;; ++k) {
+            const bool select = j >= 0 && t < m;
+            if (!select && !pending) break;
+            const int cb = k & 1;
+            if (warp == 0) {
+                if (select) {
+                    // branch-free, so that the loads and the candidates' chains overlap
+                    unsigned v[kRound], U[kRound];
+                    int P[kRound];
+#pragma unroll
+                    for (int r = 0; r < kRound; ++r) {
+                        v[r] = lane < MW ? s.T[static_cast<size_t>(rows + cb * kRound + r) * TS + lane] : 0u;
+                        U[r] = 0u;
+                        P[r] = -1;
+                    }
+                    {  // the previous round's operation, not yet in the reduced candidates (a no-op in round 0)
+                        // lane l: candidate l mod kRound's bits at that round's pivot rows
+                        const uint32_t* col = s.T + static_cast<size_t>(rows + cb * kRound + (lane & (kRound - 1))) * TS;
+                        unsigned idx = 0u;
+#pragma unroll
+                        for (int i = 0; i < kRound; ++i)
+                            if (col[pwo[i]] & pwb[i]) idx |= 1u << i;
+#pragma unroll
+                        for (int r = 0; r < kRound; ++r) {
+                            const unsigned ir = __shfl_sync(0xffffffffu, idx, r);
+#pragma unroll
+                            for (int i = 0; i < kRound; ++i) v[r] ^= ((ir >> i) & 1u) ? Up[i] : 0u;
+                        }
+                    }
+                    int np = 0, used = 0, js = -1;
+#pragma unroll
+                    for (int r = 0; r < kRound; ++r) {
+                        const bool valid = j - r >= 0 && t + np < m;  // warp-uniform
+                        // each lane: its lowest unpivoted set row (as a mask), and the later
+                        // candidates (bits r+1..) and the basis (bits ..r-1) at that row; the
+                        // lowest lane's wins
+                        const unsigned x = valid ? (v[r] & ~pivw) : 0u;
+                        const unsigned lb = x & (0u - x);
+                        unsigned mkl = 0u;
+#pragma unroll
+                        for (int c = 0; c < kRound; ++c) {
+                            if (c > r && (v[c] & lb)) mkl |= 1u << c;
+                            if (c < r && (U[c] & lb)) mkl |= 1u << c;
+                        }
+                        const unsigned lanes = __ballot_sync(0xffffffffu, x != 0u);
+                        const int l0 = (__ffs(lanes) - 1) & 31;
+                        const unsigned pb = lanes ? __shfl_sync(0xffffffffu, lb, l0) : 0u;
+                        const unsigned mk = lanes ? __shfl_sync(0xffffffffu, mkl, l0) : 0u;
+                        const unsigned W = lane == l0 ? (v[r] ^ pb) : v[r];
+#pragma unroll
+                        for (int c = 0; c < kRound; ++c) {
+                            if (c > r) v[c] ^= ((mk >> c) & 1u) ? W : 0u;
+                            if (c < r) U[c] ^= ((mk >> c) & 1u) ? W : 0u;
+                        }
+                        U[r] = pb ? W : 0u;
+                        P[r] = pb ? l0 * 32 + __ffs(pb) - 1 : -1;
+                        pivw |= lane == l0 ? pb : 0u;
+                        np += pb ? 1 : 0;
+                        js = (pb && t + np == m) ? j - r : js;
+                        used = valid ? r + 1 : used;
+                    }
+#pragma unroll
+                    for (int r = 0; r < kRound; ++r) {  // every lane stores (same values): no divergence
+                        s.wv[(cb * kRound + r) * 32 + lane] = U[r];
+                        s_rp[cb][r] = P[r];
+                        Up[r] = U[r];
+                        pwo[r] = P[r] >= 0 ? P[r] >> 5 : 0;
+                        pwb[r] = P[r] >= 0 ? 1u << (P[r] & 31) : 0u;
+                    }
+                    s_np[cb] = np;
+                    s_used[cb] = used;
+                    s_jstop[cb] = js;
+                }
+            } else {
+                if (pending) {
+                    const int pb = cb ^ 1;
+                    if (pnp > 0) {  // tables of the pending round's basis (entries 0 and 16 are 0)
+                        uint32_t* tb = s.tab + pb * 32 * kTabStride;
+                        const uint32_t* U = s.wv + pb * kRound * 32;
+                        for (int q = tid - 32; q < (32 << lg); q += kOsdHThreads - 32) {
+                            const int e = q >> lg, w = q & ((1 << lg) - 1), h = (e >> 4) * 4;
+                            unsigned acc = 0u;
+#pragma unroll
+                            for (int b = 0; b < 4; ++b)
+                                if ((e >> b) & 1) acc ^= U[(h + b) * 32 + w];
+                            tb[e * kTabStride + w] = acc;
+                        }
+                        asm volatile("bar.sync 1, %0;" ::"r"(kOsdHThreads - 32) : "memory");
+                    }
+                    int P[kRound];
+#pragma unroll
+                    for (int r = 0; r < kRound; ++r) P[r] = s_rp[pb][r];
+                    if (warp == kOsdHWarps - 1 && lane < pused) {  // pivot ranks and dependent positions
+                        int bp = 0, bd = 0, pr = -1;
+#pragma unroll
+                        for (int r = 0; r < kRound; ++r) {
+                            if (r < lane) {
+                                if (P[r] >= 0) ++bp;
+                                else ++bd;
+                            }
+                            if (r == lane) pr = P[r];
+                        }
+                        if (pr >= 0) {
+                            s.order[pt + bp] = static_cast<int16_t>(pr);
+                            s.row_of_col[s.perm[pj - lane]] = static_cast<int16_t>(pt + bp);
+                            s.pivj[pt + bp] = static_cast<int16_t>(pj - lane);
+                        } else {
+                            s.mrb[pnd + bd] = static_cast<int16_t>(pj - lane);  // dependent: an MRB position
+                        }
+                    }
+                    if (pnp > 0 && worker) {
+                        // gather: one thread per owned column, the touched ones listed; then one
+                        // thread per listed column walks its MW words (three loads, one store each)
+                        const uint32_t* tb = s.tab + pb * 32 * kTabStride;
+                        int woff[kRound];
+                        unsigned wbit[kRound];
+#pragma unroll
+                        for (int r = 0; r < kRound; ++r) {
+                            woff[r] = P[r] >= 0 ? P[r] >> 5 : 0;
+                            wbit[r] = P[r] >= 0 ? 1u << (P[r] & 31) : 0u;
+                        }
+                        int nh = 0;
+                        for (int b0 = wi * 32; b0 < rows; b0 += nworkers * 32) {
+                            const int slot = b0 + lane;
+                            unsigned idx = 0u;
+                            if (slot < rows) {
+                                const uint32_t* col = s.T + slot * TS;
+#pragma unroll
+                                for (int r = 0; r < kRound; ++r)
+                                    if (col[woff[r]] & wbit[r]) idx |= 1u << r;
+                            }
+                            const unsigned bal = __ballot_sync(0xffffffffu, idx != 0u);
+                            if (idx) seg[nh + __popc(bal & ((1u << lane) - 1u))] = static_cast<unsigned>(slot * TS) | (idx << 16);
+                            nh += __popc(bal);
+                        }
+                        __syncwarp();
+                        for (int h = lane; h < nh; h += 32) {
+                            const unsigned e = seg[h];
+                            uint32_t* c = s.T + (e & 0xffffu);
+                            const unsigned idx = e >> 16;
+                            const uint32_t* lo = tb + (idx & 15u) * kTabStride;
+                            const uint32_t* hi = tb + (16u + (idx >> 4)) * kTabStride;
+                            int w = 0;
+                            for (; w + 4 <= MW; w += 4) {
+                                const unsigned a0 = c[w] ^ lo[w] ^ hi[w];
+                                const unsigned a1 = c[w + 1] ^ lo[w + 1] ^ hi[w + 1];
+                                const unsigned a2 = c[w + 2] ^ lo[w + 2] ^ hi[w + 2];
+                                const unsigned a3 = c[w + 3] ^ lo[w + 3] ^ hi[w + 3];
+                                c[w] = a0;
+                                c[w + 1] = a1;
+                                c[w + 2] = a2;
+                                c[w + 3] = a3;
+                            }
+                            for (; w < MW; ++w) c[w] ^= lo[w] ^ hi[w];
+                        }
+                        __syncwarp();  // the list is rewritten in the next round
+                    }
+                }
+                // T is final for the pending round before the next candidates read it
+                asm volatile("bar.sync 1, %0;" ::"r"(kOsdHThreads - 32) : "memory");
+                if (select && worker && wi < kRound)
+                    reduce_candidate(j - kRound - wi, rows + (cb ^ 1) * kRound + wi);
+            }
+            __syncthreads();
+            pending = select;
+            if (select) {
+                pnp = s_np[cb];
+                pused = s_used[cb];
+                pt = t;
+                pj = j;
+                pnd = nd;
+                t += pnp;
+                if (t == m) jstop = s_jstop[cb];
+                nd += pused - pnp;
+                j -= pused;
+            }
+        }
+        if (tid == 0) s_nd = nd;
         if (t < m) {  // H rank deficient: leave the BP decision in place
             __syncthreads();
             continue;
@@ -547,6 +634,7 @@ void launch_osd_h(const OsdHView& hv, int nmax, int mmax, int poolmax, int nnzma
 {
     if (max_items <= 0) return;
     if (nmax > 32767 || poolmax > kOsdHMaxPool) throw InvalidArgument("large-code OSD: n <= 32767, pool <= 128");
+    if (mmax > 1024) throw InvalidArgument("large-code OSD: m <= 1024 (one warp holds a column of T)");
     OsdHLayout l{};
     l.nmax = nmax;
     l.np = 1;
