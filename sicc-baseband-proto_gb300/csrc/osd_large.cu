@@ -54,7 +54,7 @@ struct OsdHLayout {
 struct OsdHSmem {
     uint32_t* T;             // [32*mw + 2*kRound][ts] column-major: column i of the row-operation matrix,
                              // then two buffers of kRound reduced candidate columns
-    unsigned long long* keys;// [np]; reused as the flip-pool scratch after the sort
+    unsigned long long* keys;// [np]; holds the column lists of the sorted positions during the scan
     float* rel;              // [nmax] |llr| by sorted position j
     int16_t* perm;           // [nmax] code position at sorted position j
     int16_t* row_of_col;     // [nmax] pivot rank of a code position, -1 for the MRB
@@ -173,8 +173,30 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         }
         for (int i = tid; i < n; i += kOsdHThreads) s.row_of_col[i] = -1;
         __syncthreads();
-        for (int k2 = 2; k2 <= np; k2 <<= 1) {
-            for (int j2 = k2 >> 1; j2 > 0; j2 >>= 1) {
+        // bitonic sort (np >= 32): compare-exchange distances j2 >= 32 through shared memory, one
+        // barrier each; the distances below 32 of each merge level on registers within a warp
+        // (lane = element index mod 32), one barrier per level
+        auto warp_stages = [&](int k2lo, int k2hi, int j2top) {
+            for (int b0 = warp * 32; b0 < np; b0 += kOsdHThreads) {
+                const int i = b0 + lane;
+                unsigned long long v = s.keys[i];
+                for (int k2 = k2lo; k2 <= k2hi; k2 <<= 1) {
+                    const bool asc = (i & k2) == 0;
+                    for (int j2 = min(k2 >> 1, j2top); j2 > 0; j2 >>= 1) {
+                        const unsigned long long o =
+                            (static_cast<unsigned long long>(__shfl_xor_sync(0xffffffffu, static_cast<unsigned>(v >> 32), j2)) << 32) |
+                            __shfl_xor_sync(0xffffffffu, static_cast<unsigned>(v), j2);
+                        const bool take_min = ((i & j2) == 0) == asc;
+                        v = take_min ? (o < v ? o : v) : (o > v ? o : v);
+                    }
+                }
+                s.keys[i] = v;
+            }
+            __syncthreads();
+        };
+        warp_stages(2, 32, 16);
+        for (int k2 = 64; k2 <= np; k2 <<= 1) {
+            for (int j2 = k2 >> 1; j2 >= 32; j2 >>= 1) {
                 for (int pr = tid; pr < np / 2; pr += kOsdHThreads) {
                     const int i = (pr / j2) * 2 * j2 + (pr % j2);
                     const int ixj = i + j2;
@@ -187,6 +209,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                 }
                 __syncthreads();
             }
+            warp_stages(k2, k2, 16);
         }
         for (int j = tid; j < n; j += kOsdHThreads) {
             const unsigned long long key = s.keys[j];
@@ -324,37 +347,43 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                         }
                     }
                     int np = 0, used = 0, js = -1;
+                    int pl[kRound];  // the pivot's position on its lane, -1 elsewhere
 #pragma unroll
                     for (int r = 0; r < kRound; ++r) {
                         const bool valid = j - r >= 0 && t + np < m;  // warp-uniform
                         // each lane: its lowest unpivoted set row (as a mask), and the later
                         // candidates (bits r+1..) and the basis (bits ..r-1) at that row; the
-                        // lowest lane's wins
+                        // lowest such lane holds the pivot
                         const unsigned x = valid ? (v[r] & ~pivw) : 0u;
                         const unsigned lb = x & (0u - x);
-                        unsigned mkl = 0u;
+                        unsigned mv = 0u, mu = 0u;
 #pragma unroll
                         for (int c = 0; c < kRound; ++c) {
-                            if (c > r && (v[c] & lb)) mkl |= 1u << c;
-                            if (c < r && (U[c] & lb)) mkl |= 1u << c;
+                            if (c > r && (v[c] & lb)) mv |= 1u << c;
+                            if (c < r && (U[c] & lb)) mu |= 1u << c;
                         }
-                        const unsigned lanes = __ballot_sync(0xffffffffu, x != 0u);
-                        const int l0 = (__ffs(lanes) - 1) & 31;
-                        const unsigned pb = lanes ? __shfl_sync(0xffffffffu, lb, l0) : 0u;
-                        const unsigned mk = lanes ? __shfl_sync(0xffffffffu, mkl, l0) : 0u;
-                        const unsigned W = lane == l0 ? (v[r] ^ pb) : v[r];
+                        const unsigned l0u = __reduce_min_sync(0xffffffffu, x ? static_cast<unsigned>(lane) : 32u);
+                        const bool piv = l0u < 32u;
+                        const int l0 = static_cast<int>(l0u & 31u);
+                        const unsigned mk = piv ? __shfl_sync(0xffffffffu, mv, l0) : 0u;   // on the chain
+                        const unsigned mkU = piv ? __shfl_sync(0xffffffffu, mu, l0) : 0u;  // off it
+                        const bool me = piv && lane == l0;
+                        const unsigned W = me ? (v[r] ^ lb) : v[r];
 #pragma unroll
                         for (int c = 0; c < kRound; ++c) {
                             if (c > r) v[c] ^= ((mk >> c) & 1u) ? W : 0u;
-                            if (c < r) U[c] ^= ((mk >> c) & 1u) ? W : 0u;
+                            if (c < r) U[c] ^= ((mkU >> c) & 1u) ? W : 0u;
                         }
-                        U[r] = pb ? W : 0u;
-                        P[r] = pb ? l0 * 32 + __ffs(pb) - 1 : -1;
-                        pivw |= lane == l0 ? pb : 0u;
-                        np += pb ? 1 : 0;
-                        js = (pb && t + np == m) ? j - r : js;
+                        U[r] = piv ? W : 0u;
+                        pl[r] = me ? lane * 32 + __ffs(lb) - 1 : -1;
+                        pivw |= me ? lb : 0u;
+                        np += piv ? 1 : 0;
+                        js = (piv && t + np == m) ? j - r : js;
                         used = valid ? r + 1 : used;
                     }
+#pragma unroll
+                    for (int r = 0; r < kRound; ++r)
+                        P[r] = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(pl[r] + 1))) - 1;
 #pragma unroll
                     for (int r = 0; r < kRound; ++r) {  // every lane stores (same values): no divergence
                         s.wv[(cb * kRound + r) * 32 + lane] = U[r];
@@ -478,27 +507,32 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         }
 
         // ---- 4. flip pool: the weakest MRB positions, (|llr| ascending, position ascending) ----
-        if (tid == 0) {
-            int16_t* taken = reinterpret_cast<int16_t*>(s.keys);
+        // The MRB positions in descending sorted position -- the dependent ones met during the
+        // scan, then jstop-1 .. 0 -- come in ascending |llr|; ties come in descending position,
+        // so the pool entry i is taken from the mirror image of i within its run of equal |llr|
+        // (the runs found by binary search: |llr| is non-decreasing along that order).
+        {
             const int nd = s_nd, total = nd + jstop, want = hv.pool;
-            int cnt = 0;
-            while (cnt < total) {
-                const int jj = cnt < nd ? s.mrb[cnt] : jstop - 1 - (cnt - nd);  // descending position
-                if (cnt >= want && (cnt == 0 || s.rel[jj] != s.rel[taken[cnt - 1]])) break;
-                taken[cnt++] = static_cast<int16_t>(jj);
-            }
-            for (int a = 0; a < cnt;) {  // runs of equal |llr| come in descending position: reverse them
-                int b = a + 1;
-                while (b < cnt && s.rel[taken[b]] == s.rel[taken[a]]) ++b;
-                for (int x = a, y = b - 1; x < y; ++x, --y) {
-                    const int16_t z = taken[x];
-                    taken[x] = taken[y];
-                    taken[y] = z;
+            auto mrb_at = [&](int c) -> int { return c < nd ? s.mrb[c] : jstop - 1 - (c - nd); };
+            for (int i = tid; i < want; i += kOsdHThreads) {
+                const float ri = s.rel[mrb_at(i)];
+                int lo = 0, hi = i;  // first index with |llr| >= ri
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s.rel[mrb_at(mid)] < ri) lo = mid + 1;
+                    else hi = mid;
                 }
-                a = b;
+                const int a = lo;
+                lo = i + 1;
+                hi = total;  // first index with |llr| > ri
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s.rel[mrb_at(mid)] > ri) hi = mid;
+                    else lo = mid + 1;
+                }
+                s.pool_j[i] = static_cast<int16_t>(mrb_at(a + lo - 1 - i));
             }
-            for (int i = 0; i < want; ++i) s.pool_j[i] = taken[i];
-            s_best = ~0ull;
+            if (tid == 0) s_best = ~0ull;
         }
         __syncthreads();
 
