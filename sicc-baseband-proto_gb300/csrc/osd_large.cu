@@ -557,57 +557,106 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             }
         }
         __syncthreads();
-        // bit t of an ordered vector = bit order[t] of the row-indexed one
-        for (int vi = 0; vi <= pool; ++vi) {
-            const uint32_t* src_v = s.vs + vi * 32;
-            uint32_t* dst_v = vi == 0 ? s.aug : s.avec + (vi - 1) * MW;
-            for (int r = tid; r < rows; r += kOsdHThreads) {
-                const int q = r < m ? s.order[r] : -1;
-                const unsigned bit = q >= 0 ? tbit(src_v, q) : 0u;
-                const unsigned b = __ballot_sync(0xffffffffu, bit);
-                if (lane == 0) dst_v[r >> 5] = b;
+        // bit t of an ordered vector = bit order[t] of the row-indexed one (8 vectors' loads in flight)
+        for (int r = tid; r < rows; r += kOsdHThreads) {
+            const int q = r < m ? s.order[r] : -1;
+            const int qw = q >= 0 ? q >> 5 : 0;
+            const unsigned qb = q >= 0 ? 1u << (q & 31) : 0u;
+            for (int v0 = 0; v0 <= pool; v0 += 8) {
+                unsigned bits[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) bits[u] = v0 + u <= pool ? s.vs[(v0 + u) * 32 + qw] & qb : 0u;
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const unsigned b = __ballot_sync(0xffffffffu, bits[u] != 0u);
+                    const int vi = v0 + u;
+                    if (lane == 0 && vi <= pool) (vi == 0 ? s.aug : s.avec + (vi - 1) * MW)[r >> 5] = b;
+                }
             }
         }
         for (int r = tid; r < rows; r += kOsdHThreads) s.relq[r] = r < m ? s.rel[s.pivj[r]] : 0.0f;
         __syncthreads();
 
         // ---- 6. candidates: metric in increasing sorted position, exact pruning ----
+        // Bit t of T s (+ T h_f) marks a differing pivot position; pivot ranks in descending
+        // order hold the positions in ascending order, so the metric walks the bits from the
+        // top.  A flipped position f joins the sum before the first rank t < cut(f), the
+        // number of pivots after it.  Four set bits are taken at a time, their |llr| loaded
+        // together; the additions stay in order.
         for (int ti = tid; ti < hv.num_tests; ti += kOsdHThreads) {
-            int fl[3], fj[3], nf = 0;
+            int fa = -1, fb = -1, fc = -1;  // pool indices of the flips
             if (ti > 0) {
                 const uint32_t pk = hv.combos[ti - 1];
-                for (int q = 0; q < 3; ++q) {
-                    const int f = (pk >> (10 * q)) & 1023;
-                    if (f != 1023) fl[nf++] = f;
-                }
+                const int f0 = pk & 1023, f1 = (pk >> 10) & 1023, f2 = (pk >> 20) & 1023;
+                fa = f0 != 1023 ? f0 : -1;
+                fb = f1 != 1023 ? f1 : -1;
+                fc = f2 != 1023 ? f2 : -1;
             }
-            for (int q = 0; q < nf; ++q) fj[q] = s.pool_j[fl[q]];
-            for (int a = 1; a < nf; ++a)  // flip positions ascending
-                for (int b = a; b > 0 && fj[b - 1] > fj[b]; --b) {
-                    const int z = fj[b];
-                    fj[b] = fj[b - 1];
-                    fj[b - 1] = z;
+            // flip positions ascending (absent: INT_MAX), their |llr| and cuts
+            int j0 = fa >= 0 ? s.pool_j[fa] : INT_MAX, j1 = fb >= 0 ? s.pool_j[fb] : INT_MAX,
+                j2 = fc >= 0 ? s.pool_j[fc] : INT_MAX;
+            if (j0 > j1) { const int z = j0; j0 = j1; j1 = z; }
+            if (j1 > j2) { const int z = j1; j1 = j2; j2 = z; }
+            if (j0 > j1) { const int z = j0; j0 = j1; j1 = z; }
+            auto cut_of = [&](int jf) -> int {  // pivots at positions above jf (pivj decreases with rank)
+                if (jf == INT_MAX) return -1;
+                int lo = 0, hi = m;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s.pivj[mid] > jf) lo = mid + 1;
+                    else hi = mid;
                 }
+                return lo;
+            };
+            const int c0 = cut_of(j0), c1 = cut_of(j1), c2 = cut_of(j2);
+            const float r0 = j0 != INT_MAX ? s.rel[j0] : 0.0f, r1 = j1 != INT_MAX ? s.rel[j1] : 0.0f,
+                        r2 = j2 != INT_MAX ? s.rel[j2] : 0.0f;
+            int fi = 0;  // flips added so far
+            int ncut = c0;
+            float nrel = r0;
+            const uint32_t* va = fa >= 0 ? s.avec + fa * MW : nullptr;
+            const uint32_t* vb = fb >= 0 ? s.avec + fb * MW : nullptr;
+            const uint32_t* vc = fc >= 0 ? s.avec + fc * MW : nullptr;
             float acc = 0.0f;
-            int fi = 0;
             bool pruned = false;
-            // pivot rows in descending index hold the pivot positions in ascending order
             for (int w = MW - 1; w >= 0 && !pruned; --w) {
                 unsigned word = s.aug[w];
-                for (int q = 0; q < nf; ++q) word ^= s.avec[fl[q] * MW + w];
+                if (va) word ^= va[w];
+                if (vb) word ^= vb[w];
+                if (vc) word ^= vc[w];
                 while (word) {
-                    const int b = 31 - __clz(word);
-                    word &= ~(1u << b);
-                    const int r = w * 32 + b;
-                    const int jr = s.pivj[r];
-                    while (fi < nf && fj[fi] < jr) acc = __fadd_rn(acc, s.rel[fj[fi++]]);
-                    acc = __fadd_rn(acc, s.relq[r]);
+                    int bq[4];
+                    float rq[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        bq[u] = word ? 31 - __clz(word) : -1;
+                        if (bq[u] >= 0) word &= ~(1u << bq[u]);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) rq[u] = bq[u] >= 0 ? s.relq[w * 32 + bq[u]] : 0.0f;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        if (bq[u] < 0) break;
+                        const int t = w * 32 + bq[u];
+                        while (t < ncut) {  // flipped positions below this pivot's
+                            acc = __fadd_rn(acc, nrel);
+                            ++fi;
+                            ncut = fi == 1 ? c1 : fi == 2 ? c2 : -1;
+                            nrel = fi == 1 ? r1 : r2;
+                        }
+                        acc = __fadd_rn(acc, rq[u]);
+                    }
                 }
                 const unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(&s_best);
                 if (cur != ~0ull && acc > __uint_as_float(static_cast<unsigned>(cur >> 32))) pruned = true;
             }
             if (pruned) continue;
-            while (fi < nf) acc = __fadd_rn(acc, s.rel[fj[fi++]]);
+            while (ncut >= 0) {  // flipped positions above every differing pivot position
+                acc = __fadd_rn(acc, nrel);
+                ++fi;
+                ncut = fi == 1 ? c1 : fi == 2 ? c2 : -1;
+                nrel = fi == 1 ? r1 : r2;
+            }
             atomicMin(&s_best, (static_cast<unsigned long long>(__float_as_uint(acc)) << 32) | static_cast<unsigned>(ti));
         }
         __syncthreads();
