@@ -27,8 +27,18 @@ void launch_osd(const OsdView& ov, const OsdIO& io, int max_items, cudaStream_t 
 
 // OSD of long codes, one CTA per codeword (io.hviews for mixed batches, else
 // `hv`); nmax/mmax/poolmax/nnzmax (edges of H) bound the codes of the launch.
-void launch_osd_h(const OsdHView& hv, int nmax, int mmax, int poolmax, int nnzmax, const OsdIO& io, int max_items,
-                  cudaStream_t st);
+// Launch bounds of the large-code OSD over a set of codes.
+struct OsdHBounds {
+    int nmax = 0, mmax = 0, poolmax = 0, nnzmax = 0;
+    void add(int n, int m, int pool, int nnz);
+    bool empty() const { return nmax == 0; }
+};
+constexpr int kOsdHNarrowM = 512;  // codes with m <= 512 form the narrow class
+// Large-code OSD over the items of io: the narrow class (m <= 512) on 256-thread CTAs, two per SM, the
+// wide class on 512-thread CTAs.  With both classes present and a side stream given, the narrow launch
+// runs on `side`, forked from `st` and joined back to it through the two events.
+void launch_osd_h(const OsdHBounds& narrow, const OsdHBounds& wide, const OsdIO& io, int max_items, cudaStream_t st,
+                  cudaStream_t side = nullptr, cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 size_t osd_h_smem_bytes(int nmax, int mmax, int poolmax);
 
 }  // namespace sicc

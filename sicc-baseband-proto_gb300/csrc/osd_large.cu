@@ -35,11 +35,14 @@ namespace sicc {
 
 namespace {
 
-constexpr int kOsdHThreads = 512;
-constexpr int kOsdHWarps = kOsdHThreads / 32;
+// Codes with m <= kOsdHNarrowM run on CTAs of kOsdHNarrowThreads (two per SM: their serial pivot
+// selections overlap), the others on CTAs of kOsdHWideThreads (one per SM: their T fills it).
+constexpr int kOsdHWideThreads = 512;
+constexpr int kOsdHNarrowThreads = 256;
 constexpr int kOsdHMaxPool = 128;
 constexpr int kRound = 8;  // columns of H per elimination round
-constexpr int kHitsPerWarp = 96;  // columns of T a worker owns: 32 * ceil(1024 / (32 * 15)) (m <= 1024)
+constexpr int kHitsPerWarp = 96;  // columns of T a worker owns: 32 * ceil(1024 / (32 * 15)) (m <= 1024,
+                                  // 512 threads) and 32 * ceil(512 / (32 * 6)) (m <= 512, 256 threads)
 constexpr int kTabStride = 33;  // words per table entry: lanes reading different entries hit different banks
 
 struct OsdHLayout {
@@ -49,6 +52,8 @@ struct OsdHLayout {
     int ts;       // column stride of T in words (odd: a warp reading one word of 32 columns hits 32 banks)
     int poolmax;
     int nnzmax;   // > 0: the columns' row lists are staged in shared memory (16-bit rows)
+    int warps;    // warps per CTA
+    int mlo, mhi; // the launch decodes the items of codes with mlo < m <= mhi
 };
 
 struct OsdHSmem {
@@ -97,7 +102,7 @@ __host__ __device__ inline size_t carve(const OsdHLayout& l, unsigned char* base
     t.row_of_col = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nmax) * 2));
     t.hard = reinterpret_cast<uint32_t*>(take((static_cast<size_t>(l.nmax) / 32 + 1) * 4));
     t.wv = reinterpret_cast<uint32_t*>(take(2 * kRound * 32 * 4));
-    t.hits = reinterpret_cast<uint32_t*>(take(kOsdHWarps * kHitsPerWarp * 4));
+    t.hits = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.warps) * kHitsPerWarp * 4));
     t.piv = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.mw) * 4));
     t.order = reinterpret_cast<int16_t*>(take(rows * 2));
     t.syn = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(l.mw) * 4));
@@ -132,9 +137,11 @@ __device__ __forceinline__ int tslot(int q, int mw) { return (q & 31) * mw + (q 
 
 }  // namespace
 
-__global__ void __launch_bounds__(kOsdHThreads, 1)
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads, kThreads == kOsdHNarrowThreads ? 2 : 1)
 osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
 {
+    constexpr int kWarps = kThreads / 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     OsdHSmem s;
     carve(lay, smem_raw, &s);
@@ -149,7 +156,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
     for (int item = blockIdx.x; item < count; item += gridDim.x) {
         const int cw = io.index ? io.index[item] : item;
         const OsdHView hv = io.hviews ? io.hviews[io.code_of[cw]] : hv0;
-        if (hv.n == 0) continue;  // not a large-code item (uniform over the CTA)
+        if (hv.n == 0 || hv.m <= lay.mlo || hv.m > lay.mhi) continue;  // another kernel's item (uniform over the CTA)
         const int n = hv.n, m = hv.m, k = hv.k, MW = hv.mw, rows = 32 * hv.mw;
         const float* src = io.row_off   ? io.llr + io.row_off[item]
                            : io.llr_off ? io.llr + io.llr_off[cw]
@@ -160,24 +167,24 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
 
         // ---- 1. sort keys (descending |llr|, ties by position), hard decisions ----
         const int np = 1 << (32 - __clz(n - 1));
-        for (int i = tid; i < np; i += kOsdHThreads) {
+        for (int i = tid; i < np; i += kThreads) {
             const float x = (i < n) ? src[i] : 0.0f;
             s.keys[i] = (i < n) ? ((static_cast<unsigned long long>(0x7fffffffu - __float_as_uint(fabsf(x))) << 32) |
                                    static_cast<unsigned>(i))
                                 : ~0ull;
         }
-        for (int i = tid; i < ((n + 31) & ~31); i += kOsdHThreads) {
+        for (int i = tid; i < ((n + 31) & ~31); i += kThreads) {
             const bool neg = (i < n) && (src[i] < 0.0f);
             const unsigned b = __ballot_sync(0xffffffffu, neg);
             if (lane == 0) s.hard[i >> 5] = b;
         }
-        for (int i = tid; i < n; i += kOsdHThreads) s.row_of_col[i] = -1;
+        for (int i = tid; i < n; i += kThreads) s.row_of_col[i] = -1;
         __syncthreads();
         // bitonic sort (np >= 32): compare-exchange distances j2 >= 32 through shared memory, one
         // barrier each; the distances below 32 of each merge level on registers within a warp
         // (lane = element index mod 32), one barrier per level
         auto warp_stages = [&](int k2lo, int k2hi, int j2top) {
-            for (int b0 = warp * 32; b0 < np; b0 += kOsdHThreads) {
+            for (int b0 = warp * 32; b0 < np; b0 += kThreads) {
                 const int i = b0 + lane;
                 unsigned long long v = s.keys[i];
                 for (int k2 = k2lo; k2 <= k2hi; k2 <<= 1) {
@@ -197,7 +204,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         warp_stages(2, 32, 16);
         for (int k2 = 64; k2 <= np; k2 <<= 1) {
             for (int j2 = k2 >> 1; j2 >= 32; j2 >>= 1) {
-                for (int pr = tid; pr < np / 2; pr += kOsdHThreads) {
+                for (int pr = tid; pr < np / 2; pr += kThreads) {
                     const int i = (pr / j2) * 2 * j2 + (pr % j2);
                     const int ixj = i + j2;
                     const bool asc = (i & k2) == 0;
@@ -211,30 +218,30 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             }
             warp_stages(k2, k2, 16);
         }
-        for (int j = tid; j < n; j += kOsdHThreads) {
+        for (int j = tid; j < n; j += kThreads) {
             const unsigned long long key = s.keys[j];
             s.perm[j] = static_cast<int16_t>(key & 0xffffffffull);
             s.rel[j] = __uint_as_float(0x7fffffffu - static_cast<unsigned>(key >> 32));
         }
         // ---- 2. T = identity (column-major), syndrome of the hard decisions ----
-        for (int i = tid; i < rows * TS; i += kOsdHThreads) s.T[i] = 0u;
+        for (int i = tid; i < rows * TS; i += kThreads) s.T[i] = 0u;
         __syncthreads();
-        for (int col = tid; col < m; col += kOsdHThreads)
+        for (int col = tid; col < m; col += kThreads)
             s.T[static_cast<size_t>(tslot(col, MW)) * TS + (col >> 5)] = 1u << (col & 31);
-        for (int r = tid; r < rows; r += kOsdHThreads) {
+        for (int r = tid; r < rows; r += kThreads) {
             unsigned par = 0;
             if (r < m)
                 for (int e = hv.row_ptr[r]; e < hv.row_ptr[r + 1]; ++e) par ^= tbit(s.hard, hv.col_ind[e]);
             const unsigned b = __ballot_sync(0xffffffffu, par);
             if (lane == 0) s.syn[r >> 5] = b;
         }
-        for (int w = tid; w < MW; w += kOsdHThreads) s.piv[w] = 0u;
+        for (int w = tid; w < MW; w += kThreads) s.piv[w] = 0u;
         // column of H at each sorted position: first edge << 8 | weight (the sort keys are dead)
         const bool staged = lay.nnzmax > 0;
         if (staged)
-            for (int e = tid; e < hv.col_ptr[n]; e += kOsdHThreads) s.rows[e] = static_cast<int16_t>(hv.col_rows[e]);
+            for (int e = tid; e < hv.col_ptr[n]; e += kThreads) s.rows[e] = static_cast<int16_t>(hv.col_rows[e]);
         int* colinfo = reinterpret_cast<int*>(s.keys);
-        for (int j = tid; j < n; j += kOsdHThreads) {
+        for (int j = tid; j < n; j += kThreads) {
             const int c = s.perm[j];
             const int e0 = hv.col_ptr[c];
             colinfo[j] = (e0 << 8) | (hv.col_ptr[c + 1] - e0);
@@ -296,12 +303,12 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             }
             if (lane < MW) s.T[static_cast<size_t>(slot) * TS + lane] = v;
         };
-        if (warp < kRound) reduce_candidate(n - 1 - warp, rows + warp);
+        for (int c = warp; c < kRound; c += kWarps) reduce_candidate(n - 1 - c, rows + c);
         __syncthreads();
         const int lg = MW <= 1 ? 0 : 32 - __clz(MW - 1);  // table words per entry: 2^lg >= MW
         uint32_t* seg = s.hits + warp * kHitsPerWarp;
         const bool narrow = m <= 512;
-        const int nworkers = narrow ? kOsdHWarps - kOsdHWarps / 4 : kOsdHWarps - 1;
+        const int nworkers = narrow ? kWarps - kWarps / 4 : kWarps - 1;
         const bool worker = warp != 0 && (!narrow || (warp & 3) != 0);
         const int wi = narrow ? warp - (warp >> 2) - 1 : warp - 1;  // worker index
         int t = 0, j = n - 1, nd = 0, jstop = -1;          // after the rounds selected so far
@@ -402,7 +409,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                     if (pnp > 0) {  // tables of the pending round's basis (entries 0 and 16 are 0)
                         uint32_t* tb = s.tab + pb * 32 * kTabStride;
                         const uint32_t* U = s.wv + pb * kRound * 32;
-                        for (int q = tid - 32; q < (32 << lg); q += kOsdHThreads - 32) {
+                        for (int q = tid - 32; q < (32 << lg); q += kThreads - 32) {
                             const int e = q >> lg, w = q & ((1 << lg) - 1), h = (e >> 4) * 4;
                             unsigned acc = 0u;
 #pragma unroll
@@ -410,12 +417,12 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                                 if ((e >> b) & 1) acc ^= U[(h + b) * 32 + w];
                             tb[e * kTabStride + w] = acc;
                         }
-                        asm volatile("bar.sync 1, %0;" ::"r"(kOsdHThreads - 32) : "memory");
+                        asm volatile("bar.sync 1, %0;" ::"r"(kThreads - 32) : "memory");
                     }
                     int P[kRound];
 #pragma unroll
                     for (int r = 0; r < kRound; ++r) P[r] = s_rp[pb][r];
-                    if (warp == kOsdHWarps - 1 && lane < pused) {  // pivot ranks and dependent positions
+                    if (warp == kWarps - 1 && lane < pused) {  // pivot ranks and dependent positions
                         int bp = 0, bd = 0, pr = -1;
 #pragma unroll
                         for (int r = 0; r < kRound; ++r) {
@@ -482,9 +489,10 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                     }
                 }
                 // T is final for the pending round before the next candidates read it
-                asm volatile("bar.sync 1, %0;" ::"r"(kOsdHThreads - 32) : "memory");
-                if (select && worker && wi < kRound)
-                    reduce_candidate(j - kRound - wi, rows + (cb ^ 1) * kRound + wi);
+                asm volatile("bar.sync 1, %0;" ::"r"(kThreads - 32) : "memory");
+                if (select && worker)
+                    for (int c = wi; c < kRound; c += nworkers)
+                        reduce_candidate(j - kRound - c, rows + (cb ^ 1) * kRound + c);
             }
             __syncthreads();
             pending = select;
@@ -514,7 +522,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         {
             const int nd = s_nd, total = nd + jstop, want = hv.pool;
             auto mrb_at = [&](int c) -> int { return c < nd ? s.mrb[c] : jstop - 1 - (c - nd); };
-            for (int i = tid; i < want; i += kOsdHThreads) {
+            for (int i = tid; i < want; i += kThreads) {
                 const float ri = s.rel[mrb_at(i)];
                 int lo = 0, hi = i;  // first index with |llr| >= ri
                 while (lo < hi) {
@@ -538,16 +546,16 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
 
         // ---- 5. T s and the reduced pool columns, then in pivot order ----
         const int pool = hv.pool;
-        for (int i = tid; i < (pool + 1) * 32; i += kOsdHThreads) s.vs[i] = 0u;
+        for (int i = tid; i < (pool + 1) * 32; i += kThreads) s.vs[i] = 0u;
         __syncthreads();
         {
             // T s: XOR of the columns of T selected by s, spread over the warps
             unsigned acc = 0u;
-            for (int q = warp; q < m; q += kOsdHWarps)
+            for (int q = warp; q < m; q += kWarps)
                 if (lane < MW && tbit(s.syn, q)) acc ^= s.T[static_cast<size_t>(tslot(q, MW)) * TS + lane];
             if (lane < MW && acc) atomicXor(&s.vs[lane], acc);
             // T h_f for the flip pool, one warp per column
-            for (int i = warp; i < pool; i += kOsdHWarps) {
+            for (int i = warp; i < pool; i += kWarps) {
                 const int c = s.perm[s.pool_j[i]];
                 unsigned v = 0u;
                 if (lane < MW)
@@ -558,7 +566,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         }
         __syncthreads();
         // bit t of an ordered vector = bit order[t] of the row-indexed one (8 vectors' loads in flight)
-        for (int r = tid; r < rows; r += kOsdHThreads) {
+        for (int r = tid; r < rows; r += kThreads) {
             const int q = r < m ? s.order[r] : -1;
             const int qw = q >= 0 ? q >> 5 : 0;
             const unsigned qb = q >= 0 ? 1u << (q & 31) : 0u;
@@ -574,7 +582,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                 }
             }
         }
-        for (int r = tid; r < rows; r += kOsdHThreads) s.relq[r] = r < m ? s.rel[s.pivj[r]] : 0.0f;
+        for (int r = tid; r < rows; r += kThreads) s.relq[r] = r < m ? s.rel[s.pivj[r]] : 0.0f;
         __syncthreads();
 
         // ---- 6. candidates: metric in increasing sorted position, exact pruning ----
@@ -583,7 +591,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         // top.  A flipped position f joins the sum before the first rank t < cut(f), the
         // number of pivots after it.  Four set bits are taken at a time, their |llr| loaded
         // together; the additions stay in order.
-        for (int ti = tid; ti < hv.num_tests; ti += kOsdHThreads) {
+        for (int ti = tid; ti < hv.num_tests; ti += kThreads) {
             int fa = -1, fb = -1, fc = -1;  // pool indices of the flips
             if (ti > 0) {
                 const uint32_t pk = hv.combos[ti - 1];
@@ -689,9 +697,9 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             return static_cast<uint8_t>(bit);
         };
         if (info_dst)
-            for (int i = tid; i < k; i += kOsdHThreads) info_dst[i] = bit_at(i);
+            for (int i = tid; i < k; i += kThreads) info_dst[i] = bit_at(i);
         if (io.out_code)
-            for (int i = tid; i < n; i += kOsdHThreads) io.out_code[static_cast<size_t>(cw) * n + i] = bit_at(i);
+            for (int i = tid; i < n; i += kThreads) io.out_code[static_cast<size_t>(cw) * n + i] = bit_at(i);
         if (tid == 0) {
             if (io.used_osd) io.used_osd[cw] = 1;
             if (io.out_metric) io.out_metric[cw] = __uint_as_float(static_cast<unsigned>(best >> 32));
@@ -700,46 +708,84 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
     }
 }
 
-size_t osd_h_smem_bytes(int nmax, int mmax, int poolmax)
-{  // without the staged row lists
+namespace {
+
+OsdHLayout osd_h_layout(const OsdHBounds& bd, int threads, int mlo, int mhi)
+{
     OsdHLayout l{};
-    l.nmax = nmax;
+    l.nmax = bd.nmax;
     l.np = 1;
-    while (l.np < nmax) l.np <<= 1;
-    l.mw = (mmax + 31) / 32;
+    while (l.np < bd.nmax) l.np <<= 1;
+    l.mw = (bd.mmax + 31) / 32;
     l.ts = l.mw | 1;
-    l.poolmax = std::max(poolmax, 1);
-    return carve(l, nullptr, nullptr);
+    l.poolmax = std::max(bd.poolmax, 1);
+    l.warps = threads / 32;
+    l.mlo = mlo;
+    l.mhi = mhi;
+    l.nnzmax = 0;
+    return l;
 }
 
-void launch_osd_h(const OsdHView& hv, int nmax, int mmax, int poolmax, int nnzmax, const OsdIO& io, int max_items,
-                  cudaStream_t st)
+template <int kThreads>
+void launch_osd_h_class(const OsdHBounds& bd, int mlo, int mhi, const OsdIO& io, int max_items, cudaStream_t st)
 {
-    if (max_items <= 0) return;
-    if (nmax > 32767 || poolmax > kOsdHMaxPool) throw InvalidArgument("large-code OSD: n <= 32767, pool <= 128");
-    if (mmax > 1024) throw InvalidArgument("large-code OSD: m <= 1024 (one warp holds a column of T)");
-    OsdHLayout l{};
-    l.nmax = nmax;
-    l.np = 1;
-    while (l.np < nmax) l.np <<= 1;
-    l.mw = (mmax + 31) / 32;
-    l.ts = l.mw | 1;
-    l.poolmax = std::max(poolmax, 1);
-    l.nnzmax = 0;
+    OsdHLayout l = osd_h_layout(bd, kThreads, mlo, mhi);
     size_t smem = carve(l, nullptr, nullptr);
     if (smem > 227 * 1024) throw InvalidArgument("large-code OSD tables exceed shared memory (m <= 1024, n <= 4096)");
-    l.nnzmax = nnzmax;  // stage the columns' row lists when they fit as well
-    if (nnzmax <= 0 || carve(l, nullptr, nullptr) > 227 * 1024) l.nnzmax = 0;
+    l.nnzmax = bd.nnzmax;  // stage the columns' row lists when they fit as well
+    if (bd.nnzmax <= 0 || carve(l, nullptr, nullptr) > 227 * 1024) l.nnzmax = 0;
     smem = carve(l, nullptr, nullptr);
-    check_cuda(cudaFuncSetAttribute(osd_h_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+    check_cuda(cudaFuncSetAttribute(osd_h_kernel<kThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)),
                "cudaFuncSetAttribute(osd_h)");
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, osd_h_kernel, kOsdHThreads, smem) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, osd_h_kernel<kThreads>, kThreads, smem) != cudaSuccess ||
         per_sm <= 0)
         per_sm = 1;
     const int ctas = std::max(1, std::min(max_items, per_sm * device_sm_count()));
-    osd_h_kernel<<<ctas, kOsdHThreads, smem, st>>>(hv, l, io);
+    osd_h_kernel<kThreads><<<ctas, kThreads, smem, st>>>(OsdHView{}, l, io);
     check_cuda(cudaGetLastError(), "osd_h_kernel launch");
+}
+
+}  // namespace
+
+void OsdHBounds::add(int n, int m, int pool, int nnz)
+{
+    nmax = std::max(nmax, n);
+    mmax = std::max(mmax, m);
+    poolmax = std::max(poolmax, pool);
+    nnzmax = std::max(nnzmax, nnz);
+}
+
+size_t osd_h_smem_bytes(int nmax, int mmax, int poolmax)
+{  // without the staged row lists
+    OsdHBounds bd;
+    bd.add(nmax, mmax, poolmax, 0);
+    const int threads = mmax <= kOsdHNarrowM ? kOsdHNarrowThreads : kOsdHWideThreads;
+    const OsdHLayout l = osd_h_layout(bd, threads, 0, 1024);
+    return carve(l, nullptr, nullptr);
+}
+
+void launch_osd_h(const OsdHBounds& narrow, const OsdHBounds& wide, const OsdIO& io, int max_items, cudaStream_t st,
+                  cudaStream_t side, cudaEvent_t fork, cudaEvent_t join)
+{
+    if (max_items <= 0 || (narrow.empty() && wide.empty())) return;
+    for (const OsdHBounds* bd : {&narrow, &wide})
+        if (bd->nmax > 32767 || bd->poolmax > kOsdHMaxPool) throw InvalidArgument("large-code OSD: n <= 32767, pool <= 128");
+    if (narrow.mmax > kOsdHNarrowM || wide.mmax > 1024)
+        throw InvalidArgument("large-code OSD: m <= 1024 (one warp holds a column of T)");
+    const bool both = !narrow.empty() && !wide.empty() && side && fork && join;
+    if (both) {  // the two classes run side by side
+        check_cuda(cudaEventRecord(fork, st), "cudaEventRecord(osd fork)");
+        check_cuda(cudaStreamWaitEvent(side, fork, 0), "cudaStreamWaitEvent(osd fork)");
+    }
+    if (!narrow.empty())
+        launch_osd_h_class<kOsdHNarrowThreads>(narrow, 0, kOsdHNarrowM, io, max_items, both ? side : st);
+    if (!wide.empty()) launch_osd_h_class<kOsdHWideThreads>(wide, kOsdHNarrowM, 1024, io, max_items, st);
+    if (both) {
+        check_cuda(cudaEventRecord(join, side), "cudaEventRecord(osd join)");
+        check_cuda(cudaStreamWaitEvent(st, join, 0), "cudaStreamWaitEvent(osd join)");
+    }
 }
 
 }  // namespace sicc
