@@ -33,12 +33,17 @@ struct OsdHBounds {
     void add(int n, int m, int pool, int nnz);
     bool empty() const { return nmax == 0; }
 };
-constexpr int kOsdHNarrowM = 512;  // codes with m <= 512 form the narrow class
-// Large-code OSD over the items of io: the narrow class (m <= 512) on 256-thread CTAs, two per SM, the
-// wide class on 512-thread CTAs.  With both classes present and a side stream given, the narrow launch
-// runs on `side`, forked from `st` and joined back to it through the two events.
-void launch_osd_h(const OsdHBounds& narrow, const OsdHBounds& wide, const OsdIO& io, int max_items, cudaStream_t st,
-                  cudaStream_t side = nullptr, cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
+// The large-code OSD runs in classes by m: m <= 512 and m <= 640 on 256-thread CTAs (two per SM:
+// their serial pivot selections overlap; the second without staged column lists), m <= 1024 on
+// 512-thread CTAs (one per SM: T fills it).
+constexpr int kOsdHClasses = 3;
+constexpr int kOsdHClassMaxM[kOsdHClasses] = {512, 640, 1024};
+inline int osd_h_class(int m) { return m <= 512 ? 0 : m <= 640 ? 1 : 2; }
+// Large-code OSD over the items of io, one launch per class present in cls[kOsdHClasses]; with more
+// than one class and side streams given (kOsdHClasses - 1 of them, and as many join events), the
+// classes run side by side, forked from `st` and joined back to it.
+void launch_osd_h(const OsdHBounds* cls, const OsdIO& io, int max_items, cudaStream_t st,
+                  const cudaStream_t* side = nullptr, cudaEvent_t fork = nullptr, const cudaEvent_t* join = nullptr);
 size_t osd_h_smem_bytes(int nmax, int mmax, int poolmax);
 
 }  // namespace sicc

@@ -445,7 +445,7 @@ struct Engine {
     int device = 0;
     std::vector<EngineCode> codes;
     int n_max = 0, k_max = 0, maxdeg = 0, osd_nmax = 0, osd_kmax = 0;
-    OsdHBounds h_narrow, h_wide;  // large-code OSD launch bounds, by class (m <= 512, m > 512)
+    OsdHBounds h_cls[kOsdHClasses];  // large-code OSD launch bounds, by class
     int warps_per_cta = 0, ctas = 0;
     // device state
     CodeDesc* d_codes = nullptr;
@@ -467,8 +467,8 @@ struct Engine {
     size_t best_warps = 0;
     bool dirty = true;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    cudaStream_t side = nullptr;  // the narrow large-code OSD class, beside the wide one
-    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaStream_t side[kOsdHClasses - 1] = {};  // large-code OSD classes beside the first
+    cudaEvent_t fork = nullptr, join[kOsdHClasses - 1] = {};
     bool timed = false;
     std::mutex mu;
     ~Engine()
@@ -482,10 +482,17 @@ struct Engine {
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
-        if (join) cudaEventDestroy(join);
-        if (side) cudaStreamDestroy(side);
+        for (auto& e : join)
+            if (e) cudaEventDestroy(e);
+        for (auto& q : side)
+            if (q) cudaStreamDestroy(q);
     }
-    bool has_osd_h() const { return !h_narrow.empty() || !h_wide.empty(); }
+    bool has_osd_h() const
+    {
+        for (const auto& c : h_cls)
+            if (!c.empty()) return true;
+        return false;
+    }
 
     // shared-memory floats per warp: a narrow code's 32/G slots, or a W-warp
     // group's slot spread over its W warps
@@ -623,9 +630,9 @@ int sicc_engine_create(const sicc_engine_config_t* config, unsigned long long* o
         check_cuda(cudaMalloc(&e->d_osd_index, sizeof(int) * config->max_codewords), "cudaMalloc(osd index)");
         check_cuda(cudaMalloc(&e->d_osd_llr, sizeof(float) * config->max_llr_floats), "cudaMalloc(osd rows)");
         for (auto& ev : e->ev) check_cuda(cudaEventCreate(&ev), "cudaEventCreate(engine)");
-        check_cuda(cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking), "cudaStreamCreate(engine side)");
+        for (auto& q : e->side) check_cuda(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking), "cudaStreamCreate(engine side)");
         check_cuda(cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming), "cudaEventCreate(engine fork)");
-        check_cuda(cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming), "cudaEventCreate(engine join)");
+        for (auto& ev : e->join) check_cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate(engine join)");
         std::lock_guard<std::mutex> lock(g_mu);
         *out_handle = ++g_next;
         g_engines[*out_handle] = e;
@@ -713,9 +720,7 @@ int sicc_engine_add_code(unsigned long long handle, const sicc_engine_code_t* co
             e->osd_nmax = std::max(e->osd_nmax, d.n);
             e->osd_kmax = std::max(e->osd_kmax, d.k);
         }
-        if (ec.osd_h)
-            (code->m <= kOsdHNarrowM ? e->h_narrow : e->h_wide)
-                .add(d.n, code->m, ec.code->osd_h_view().pool, ec.code->edges());
+        if (ec.osd_h) e->h_cls[osd_h_class(code->m)].add(d.n, code->m, ec.code->osd_h_view().pool, ec.code->edges());
         e->codes.push_back(std::move(ec));
         e->dirty = true;
         *out_code_id = static_cast<int>(e->codes.size()) - 1;
@@ -810,7 +815,7 @@ int engine_decode(unsigned long long handle, int codewords, const unsigned char*
                 launch_osd(shape, oio, codewords, st);
             }
             if (e->has_osd_h())  // long codes, one CTA per codeword
-                launch_osd_h(e->h_narrow, e->h_wide, oio, codewords, st, e->side, e->fork, e->join);
+                launch_osd_h(e->h_cls, oio, codewords, st, e->side, e->fork, e->join);
         }
         check_cuda(cudaEventRecord(e->ev[3], st), "cudaEventRecord");
         e->timed = true;
@@ -866,7 +871,7 @@ int sicc_engine_osd_device(unsigned long long handle, int codewords, const unsig
             shape.k = e->osd_kmax;
             launch_osd(shape, oio, codewords, st);
         }
-        if (e->has_osd_h()) launch_osd_h(e->h_narrow, e->h_wide, oio, codewords, st, e->side, e->fork, e->join);
+        if (e->has_osd_h()) launch_osd_h(e->h_cls, oio, codewords, st, e->side, e->fork, e->join);
         return CUDA_OSD_STATUS_OK;
     });
 }

@@ -35,14 +35,10 @@ namespace sicc {
 
 namespace {
 
-// Codes with m <= kOsdHNarrowM run on CTAs of kOsdHNarrowThreads (two per SM: their serial pivot
-// selections overlap), the others on CTAs of kOsdHWideThreads (one per SM: their T fills it).
-constexpr int kOsdHWideThreads = 512;
-constexpr int kOsdHNarrowThreads = 256;
+constexpr int kOsdHClassThreads[kOsdHClasses] = {256, 256, 512};  // CTA size by class
 constexpr int kOsdHMaxPool = 128;
 constexpr int kRound = 8;  // columns of H per elimination round
-constexpr int kHitsPerWarp = 96;  // columns of T a worker owns: 32 * ceil(1024 / (32 * 15)) (m <= 1024,
-                                  // 512 threads) and 32 * ceil(512 / (32 * 6)) (m <= 512, 256 threads)
+constexpr int kHitsPerWarp = 96;  // a worker's list of touched columns (applied whenever it fills)
 constexpr int kTabStride = 33;  // words per table entry: lanes reading different entries hit different banks
 
 struct OsdHLayout {
@@ -59,7 +55,8 @@ struct OsdHLayout {
 struct OsdHSmem {
     uint32_t* T;             // [32*mw + 2*kRound][ts] column-major: column i of the row-operation matrix,
                              // then two buffers of kRound reduced candidate columns
-    unsigned long long* keys;// [np]; holds the column lists of the sorted positions during the scan
+    unsigned long long* keys;// [np] sort keys; shares T's space
+    int* colinfo;            // [nmax] first edge << 8 | weight of the column at each sorted position
     float* rel;              // [nmax] |llr| by sorted position j
     int16_t* perm;           // [nmax] code position at sorted position j
     int16_t* row_of_col;     // [nmax] pivot rank of a code position, -1 for the MRB
@@ -95,8 +92,13 @@ __host__ __device__ inline size_t carve(const OsdHLayout& l, unsigned char* base
     };
     const size_t rows = 32 * static_cast<size_t>(l.mw);
     OsdHSmem t{};
-    t.T = reinterpret_cast<uint32_t*>(take((rows + 2 * kRound) * l.ts * 4));
-    t.keys = reinterpret_cast<unsigned long long*>(take(static_cast<size_t>(l.np) * 8));
+    {  // the sort keys, then T (the keys are dead once the sorted order is extracted)
+        const size_t bt = (rows + 2 * kRound) * l.ts * 4, bk = static_cast<size_t>(l.np) * 8;
+        unsigned char* g = take(bt > bk ? bt : bk);
+        t.T = reinterpret_cast<uint32_t*>(g);
+        t.keys = reinterpret_cast<unsigned long long*>(g);
+    }
+    t.colinfo = reinterpret_cast<int*>(take(static_cast<size_t>(l.nmax) * 4));
     t.rel = reinterpret_cast<float*>(take(static_cast<size_t>(l.nmax) * 4));
     t.perm = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nmax) * 2));
     t.row_of_col = reinterpret_cast<int16_t*>(take(static_cast<size_t>(l.nmax) * 2));
@@ -138,7 +140,7 @@ __device__ __forceinline__ int tslot(int q, int mw) { return (q & 31) * mw + (q 
 }  // namespace
 
 template <int kThreads>
-__global__ void __launch_bounds__(kThreads, kThreads == kOsdHNarrowThreads ? 2 : 1)
+__global__ void __launch_bounds__(kThreads, kThreads == 256 ? 2 : 1)
 osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
 {
     constexpr int kWarps = kThreads / 32;
@@ -223,6 +225,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             s.perm[j] = static_cast<int16_t>(key & 0xffffffffull);
             s.rel[j] = __uint_as_float(0x7fffffffu - static_cast<unsigned>(key >> 32));
         }
+        __syncthreads();  // T overwrites the keys
         // ---- 2. T = identity (column-major), syndrome of the hard decisions ----
         for (int i = tid; i < rows * TS; i += kThreads) s.T[i] = 0u;
         __syncthreads();
@@ -236,11 +239,11 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             if (lane == 0) s.syn[r >> 5] = b;
         }
         for (int w = tid; w < MW; w += kThreads) s.piv[w] = 0u;
-        // column of H at each sorted position: first edge << 8 | weight (the sort keys are dead)
+        // column of H at each sorted position: first edge << 8 | weight
         const bool staged = lay.nnzmax > 0;
         if (staged)
             for (int e = tid; e < hv.col_ptr[n]; e += kThreads) s.rows[e] = static_cast<int16_t>(hv.col_rows[e]);
-        int* colinfo = reinterpret_cast<int*>(s.keys);
+        int* colinfo = s.colinfo;
         for (int j = tid; j < n; j += kThreads) {
             const int c = s.perm[j];
             const int e0 = hv.col_ptr[c];
@@ -268,10 +271,10 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         //     own (the pivot-row bits of a column form its index; columns with a
         //     nonzero index take its two table entries), meet on a named
         //     barrier, and kRound of them reduce round k+1's candidates against
-        //     T.  The workers are warps 1..15 when m > 512 (the update bounds
-        //     the round); for smaller m, where the selection does, warp 0 keeps
-        //     its scheduler (warps w = 0 mod 4) to itself and the workers are
-        //     the 12 warps w != 0 mod 4.
+        //     T.  In 512-thread CTAs (m > 640, the update bounds the round) the
+        //     workers are warps 1..15; in 256-thread CTAs (the selection bounds
+        //     it) warp 0 keeps its scheduler (warps w = 0 mod 4) to itself and
+        //     the workers are the warps w != 0 mod 4.
         auto rows_of = [&](int jj, int& e0, int& cnt) -> int {  // one row of column jj per lane
             const int ci = colinfo[jj];
             e0 = ci >> 8;
@@ -307,7 +310,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         __syncthreads();
         const int lg = MW <= 1 ? 0 : 32 - __clz(MW - 1);  // table words per entry: 2^lg >= MW
         uint32_t* seg = s.hits + warp * kHitsPerWarp;
-        const bool narrow = m <= 512;
+        constexpr bool narrow = kThreads < 512;  // the small-T classes: selection-bound
         const int nworkers = narrow ? kWarps - kWarps / 4 : kWarps - 1;
         const bool worker = warp != 0 && (!narrow || (warp & 3) != 0);
         const int wi = narrow ? warp - (warp >> 2) - 1 : warp - 1;  // worker index
@@ -451,8 +454,35 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                             woff[r] = P[r] >= 0 ? P[r] >> 5 : 0;
                             wbit[r] = P[r] >= 0 ? 1u << (P[r] & 31) : 0u;
                         }
+                        auto walk = [&](int nh) {
+                            __syncwarp();
+                            for (int h = lane; h < nh; h += 32) {
+                                const unsigned e = seg[h];
+                                uint32_t* c = s.T + (e & 0xffffu);
+                                const unsigned idx = e >> 16;
+                                const uint32_t* lo = tb + (idx & 15u) * kTabStride;
+                                const uint32_t* hi = tb + (16u + (idx >> 4)) * kTabStride;
+                                int w = 0;
+                                for (; w + 4 <= MW; w += 4) {
+                                    const unsigned a0 = c[w] ^ lo[w] ^ hi[w];
+                                    const unsigned a1 = c[w + 1] ^ lo[w + 1] ^ hi[w + 1];
+                                    const unsigned a2 = c[w + 2] ^ lo[w + 2] ^ hi[w + 2];
+                                    const unsigned a3 = c[w + 3] ^ lo[w + 3] ^ hi[w + 3];
+                                    c[w] = a0;
+                                    c[w + 1] = a1;
+                                    c[w + 2] = a2;
+                                    c[w + 3] = a3;
+                                }
+                                for (; w < MW; ++w) c[w] ^= lo[w] ^ hi[w];
+                            }
+                            __syncwarp();  // the list is rewritten next
+                        };
                         int nh = 0;
                         for (int b0 = wi * 32; b0 < rows; b0 += nworkers * 32) {
+                            if (nh > kHitsPerWarp - 32) {  // the list is full: apply it first
+                                walk(nh);
+                                nh = 0;
+                            }
                             const int slot = b0 + lane;
                             unsigned idx = 0u;
                             if (slot < rows) {
@@ -465,27 +495,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                             if (idx) seg[nh + __popc(bal & ((1u << lane) - 1u))] = static_cast<unsigned>(slot * TS) | (idx << 16);
                             nh += __popc(bal);
                         }
-                        __syncwarp();
-                        for (int h = lane; h < nh; h += 32) {
-                            const unsigned e = seg[h];
-                            uint32_t* c = s.T + (e & 0xffffu);
-                            const unsigned idx = e >> 16;
-                            const uint32_t* lo = tb + (idx & 15u) * kTabStride;
-                            const uint32_t* hi = tb + (16u + (idx >> 4)) * kTabStride;
-                            int w = 0;
-                            for (; w + 4 <= MW; w += 4) {
-                                const unsigned a0 = c[w] ^ lo[w] ^ hi[w];
-                                const unsigned a1 = c[w + 1] ^ lo[w + 1] ^ hi[w + 1];
-                                const unsigned a2 = c[w + 2] ^ lo[w + 2] ^ hi[w + 2];
-                                const unsigned a3 = c[w + 3] ^ lo[w + 3] ^ hi[w + 3];
-                                c[w] = a0;
-                                c[w + 1] = a1;
-                                c[w + 2] = a2;
-                                c[w + 3] = a3;
-                            }
-                            for (; w < MW; ++w) c[w] ^= lo[w] ^ hi[w];
-                        }
-                        __syncwarp();  // the list is rewritten in the next round
+                        walk(nh);
                     }
                 }
                 // T is final for the pending round before the next candidates read it
@@ -732,8 +742,10 @@ void launch_osd_h_class(const OsdHBounds& bd, int mlo, int mhi, const OsdIO& io,
     OsdHLayout l = osd_h_layout(bd, kThreads, mlo, mhi);
     size_t smem = carve(l, nullptr, nullptr);
     if (smem > 227 * 1024) throw InvalidArgument("large-code OSD tables exceed shared memory (m <= 1024, n <= 4096)");
-    l.nnzmax = bd.nnzmax;  // stage the columns' row lists when they fit as well
-    if (bd.nnzmax <= 0 || carve(l, nullptr, nullptr) > 227 * 1024) l.nnzmax = 0;
+    // stage the columns' row lists when they fit as well, and keep the class's CTAs per SM
+    const size_t per_sm_bytes = kThreads == 512 ? 227 * 1024 : 112 * 1024;  // two 256-thread CTAs per SM
+    l.nnzmax = bd.nnzmax;
+    if (bd.nnzmax <= 0 || carve(l, nullptr, nullptr) > (smem <= per_sm_bytes ? per_sm_bytes : 227 * 1024)) l.nnzmax = 0;
     smem = carve(l, nullptr, nullptr);
     check_cuda(cudaFuncSetAttribute(osd_h_kernel<kThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     static_cast<int>(smem)),
@@ -761,30 +773,43 @@ size_t osd_h_smem_bytes(int nmax, int mmax, int poolmax)
 {  // without the staged row lists
     OsdHBounds bd;
     bd.add(nmax, mmax, poolmax, 0);
-    const int threads = mmax <= kOsdHNarrowM ? kOsdHNarrowThreads : kOsdHWideThreads;
-    const OsdHLayout l = osd_h_layout(bd, threads, 0, 1024);
+    const int c = osd_h_class(mmax);
+    const OsdHLayout l = osd_h_layout(bd, kOsdHClassThreads[c], 0, 1024);
     return carve(l, nullptr, nullptr);
 }
 
-void launch_osd_h(const OsdHBounds& narrow, const OsdHBounds& wide, const OsdIO& io, int max_items, cudaStream_t st,
-                  cudaStream_t side, cudaEvent_t fork, cudaEvent_t join)
+void launch_osd_h(const OsdHBounds* cls, const OsdIO& io, int max_items, cudaStream_t st, const cudaStream_t* side,
+                  cudaEvent_t fork, const cudaEvent_t* join)
 {
-    if (max_items <= 0 || (narrow.empty() && wide.empty())) return;
-    for (const OsdHBounds* bd : {&narrow, &wide})
-        if (bd->nmax > 32767 || bd->poolmax > kOsdHMaxPool) throw InvalidArgument("large-code OSD: n <= 32767, pool <= 128");
-    if (narrow.mmax > kOsdHNarrowM || wide.mmax > 1024)
-        throw InvalidArgument("large-code OSD: m <= 1024 (one warp holds a column of T)");
-    const bool both = !narrow.empty() && !wide.empty() && side && fork && join;
-    if (both) {  // the two classes run side by side
-        check_cuda(cudaEventRecord(fork, st), "cudaEventRecord(osd fork)");
-        check_cuda(cudaStreamWaitEvent(side, fork, 0), "cudaStreamWaitEvent(osd fork)");
+    if (max_items <= 0) return;
+    int present = 0;
+    for (int c = 0; c < kOsdHClasses; ++c) {
+        if (cls[c].empty()) continue;
+        ++present;
+        if (cls[c].nmax > 32767 || cls[c].poolmax > kOsdHMaxPool)
+            throw InvalidArgument("large-code OSD: n <= 32767, pool <= 128");
+        if (cls[c].mmax > kOsdHClassMaxM[c]) throw InvalidArgument("large-code OSD: code in the wrong class (m <= 1024)");
     }
-    if (!narrow.empty())
-        launch_osd_h_class<kOsdHNarrowThreads>(narrow, 0, kOsdHNarrowM, io, max_items, both ? side : st);
-    if (!wide.empty()) launch_osd_h_class<kOsdHWideThreads>(wide, kOsdHNarrowM, 1024, io, max_items, st);
-    if (both) {
-        check_cuda(cudaEventRecord(join, side), "cudaEventRecord(osd join)");
-        check_cuda(cudaStreamWaitEvent(st, join, 0), "cudaStreamWaitEvent(osd join)");
+    if (present == 0) return;
+    // the classes run side by side: the first present one on st, the others on side streams
+    const bool fan = present > 1 && side && fork && join;
+    if (fan) check_cuda(cudaEventRecord(fork, st), "cudaEventRecord(osd fork)");
+    int used = 0;
+    for (int c = kOsdHClasses - 1; c >= 0; --c) {
+        if (cls[c].empty()) continue;
+        cudaStream_t cs = st;
+        if (fan && used > 0) {
+            cs = side[used - 1];
+            check_cuda(cudaStreamWaitEvent(cs, fork, 0), "cudaStreamWaitEvent(osd fork)");
+        }
+        const int mlo = c == 0 ? 0 : kOsdHClassMaxM[c - 1];
+        if (kOsdHClassThreads[c] == 256) launch_osd_h_class<256>(cls[c], mlo, kOsdHClassMaxM[c], io, max_items, cs);
+        else launch_osd_h_class<512>(cls[c], mlo, kOsdHClassMaxM[c], io, max_items, cs);
+        if (fan && used > 0) {
+            check_cuda(cudaEventRecord(join[used - 1], cs), "cudaEventRecord(osd join)");
+            check_cuda(cudaStreamWaitEvent(st, join[used - 1], 0), "cudaStreamWaitEvent(osd join)");
+        }
+        ++used;
     }
 }
 
