@@ -242,13 +242,26 @@ osd_kernel(OsdView ov0, OsdIO io)
             acc[w] ^= hard_sorted[w];  // base difference from the hard decision
         }
         // ---- 5. flip pool: basis positions, weakest first (stable) ----
+        // Pivots come in sorted-position order, so |llr| does not increase with the pivot
+        // index t: t's rank is the count of later runs plus its place in its run of equal
+        // |llr| (the run found by binary search).
         for (int t = lane; t < k; t += 32) {
-            const uint32_t bt = __float_as_uint(s.rel_sorted[s.mrb_pos[t]]);
-            int r = 0;
-            for (int u = 0; u < k; ++u) {
-                const uint32_t bu = __float_as_uint(s.rel_sorted[s.mrb_pos[u]]);
-                r += (bu < bt) || (bu == bt && u < t);
+            const float bt = s.rel_sorted[s.mrb_pos[t]];
+            int lo = 0, hi = t;  // first index with |llr| <= bt
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (s.rel_sorted[s.mrb_pos[mid]] > bt) lo = mid + 1;
+                else hi = mid;
             }
+            const int a = lo;
+            lo = t + 1;
+            hi = k;  // first index with |llr| < bt
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (s.rel_sorted[s.mrb_pos[mid]] < bt) hi = mid;
+                else lo = mid + 1;
+            }
+            const int r = (k - lo) + (t - a);
             if (r < ov.pool) s.flip[r] = static_cast<int16_t>(t);
         }
         __syncwarp();
@@ -281,11 +294,12 @@ osd_kernel(OsdView ov0, OsdIO io)
                 float metric = 0.0f;
                 bool pruned = false;
 #pragma unroll
-                for (int w = 0; w < NW; ++w) {
-                    unsigned long long bits = d[w];
+                for (int h = 0; h < 2 * NW; ++h) {
+                    unsigned bits = static_cast<unsigned>(d[h >> 1] >> ((h & 1) * 32));
+                    const float* rel = s.rel_sorted + h * 32;
                     while (bits && !pruned) {
-                        const int b = __ffsll(static_cast<long long>(bits)) - 1;
-                        metric = __fadd_rn(metric, s.rel_sorted[w * 64 + b]);
+                        const int b = __ffs(bits) - 1;
+                        metric = __fadd_rn(metric, rel[b]);
                         bits &= bits - 1;
                         pruned = metric > thr;
                     }
@@ -299,7 +313,7 @@ osd_kernel(OsdView ov0, OsdIO io)
                     }
                 }
             }
-            if (rd == 2 || (rd & 7) == 7) {  // share the best metric so far across the warp
+            if (rd & 1) {  // share the best metric so far across the warp
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
                     const unsigned long long other = shfl_xor_u64(best_key, o);
