@@ -27,7 +27,6 @@ constexpr int kOsdWarps = 8;
 
 template <int NW, int KR>
 struct OsdSmem {
-    unsigned long long keys[NW * 64];  // sort keys: (0x7fffffff - bits(|llr|)) << 32 | index
     float rel_sorted[NW * 64];
     int16_t perm[NW * 64];
     int16_t rowpiv[KR * 32];  // row id -> pivot index
@@ -89,37 +88,55 @@ osd_kernel(OsdView ov0, OsdIO io)
                                                        : io.out_info + static_cast<size_t>(cw) * io.info_stride)
                                         : nullptr;
         // ---- 1. reliabilities, hard decisions, stable descending sort ----
-        // Bitonic sort of 64-bit keys: ascending key = descending |llr|, ties by
-        // ascending index (the order of MATLAB's stable sort, cpu_bp_osd_decode.m:194).
-        constexpr int NP = NW * 64;
-        for (int i = lane; i < NP; i += 32) {
+        // Bitonic sort of 64-bit keys in registers (element q*32 + lane in v[q]):
+        // ascending key = descending |llr|, ties by ascending index (the order of
+        // MATLAB's stable sort, cpu_bp_osd_decode.m:194).
+        constexpr int NP = NW * 64, KPL = NP / 32;
+        unsigned long long v[KPL];
+#pragma unroll
+        for (int q = 0; q < KPL; ++q) {
+            const int i = q * 32 + lane;
             const float x = (i < n) ? src[i] : 0.0f;
-            s.keys[i] = (i < n) ? ((static_cast<unsigned long long>(0x7fffffffu - __float_as_uint(fabsf(x))) << 32) |
-                                   static_cast<unsigned>(i))
-                                : ~0ull;
+            v[q] = (i < n) ? ((static_cast<unsigned long long>(0x7fffffffu - __float_as_uint(fabsf(x))) << 32) |
+                              static_cast<unsigned>(i))
+                           : ~0ull;
             const unsigned hb = __ballot_sync(0xffffffffu, (i < n) && (x < 0.0f));
-            if (lane == 0) s.hard_orig[i >> 5] = hb;
+            if (lane == 0) s.hard_orig[q] = hb;
         }
-        __syncwarp();
+#pragma unroll
         for (int k2 = 2; k2 <= NP; k2 <<= 1) {
+#pragma unroll
             for (int j2 = k2 >> 1; j2 > 0; j2 >>= 1) {
-                for (int pr = lane; pr < NP / 2; pr += 32) {
-                    const int i = (pr / j2) * 2 * j2 + (pr % j2);
-                    const int ixj = i + j2;
-                    const bool asc = (i & k2) == 0;
-                    const unsigned long long a = s.keys[i], b = s.keys[ixj];
-                    if ((a > b) == asc) {
-                        s.keys[i] = b;
-                        s.keys[ixj] = a;
+                if (j2 >= 32) {  // partner in this lane
+#pragma unroll
+                    for (int q = 0; q < KPL; ++q) {
+                        if (q & (j2 >> 5)) continue;
+                        const int q2 = q | (j2 >> 5);
+                        const bool asc = ((q * 32 + lane) & k2) == 0;
+                        const unsigned long long a = v[q], b = v[q2];
+                        if ((a > b) == asc) {
+                            v[q] = b;
+                            v[q2] = a;
+                        }
+                    }
+                } else {  // partner in lane ^ j2
+#pragma unroll
+                    for (int q = 0; q < KPL; ++q) {
+                        const unsigned long long o = shfl_xor_u64(v[q], j2);
+                        const bool asc = ((q * 32 + lane) & k2) == 0;
+                        const bool take_min = ((lane & j2) == 0) == asc;
+                        v[q] = take_min ? (o < v[q] ? o : v[q]) : (o > v[q] ? o : v[q]);
                     }
                 }
-                __syncwarp();
             }
         }
-        for (int r = lane; r < n; r += 32) {
-            const unsigned long long key = s.keys[r];
-            s.perm[r] = static_cast<int16_t>(key & 0xffffffffull);
-            s.rel_sorted[r] = __uint_as_float(0x7fffffffu - static_cast<unsigned>(key >> 32));
+#pragma unroll
+        for (int q = 0; q < KPL; ++q) {
+            const int r = q * 32 + lane;
+            if (r < n) {
+                s.perm[r] = static_cast<int16_t>(v[q] & 0xffffffffull);
+                s.rel_sorted[r] = __uint_as_float(0x7fffffffu - static_cast<unsigned>(v[q] >> 32));
+            }
         }
         __syncwarp();
         // hard decisions in sorted order
@@ -160,14 +177,19 @@ osd_kernel(OsdView ov0, OsdIO io)
                     for (int x = 0; x < KW; ++x) col[x] = ov.pcols[static_cast<size_t>(o - k) * ov.kw + x];
                 }
             }
+            // 32 x 32 bit transposes (butterfly over lane ^ j): lane j's bits a*32.. of its
+            // column become lane r's bits q*32.. of row a*32 + r
 #pragma unroll
             for (int a = 0; a < KR; ++a) {
-                for (int rl = 0; rl < 32; ++rl) {
-                    const int r = a * 32 + rl;
-                    const unsigned b = __ballot_sync(0xffffffffu, (r < k) && ((col[r >> 6] >> (r & 63)) & 1ull));
-                    if (lane == rl)
-                        rows[a][q >> 1] |= static_cast<unsigned long long>(b) << ((q & 1) * 32);
+                unsigned x = static_cast<unsigned>(col[a >> 1] >> ((a & 1) * 32));
+                unsigned msk = 0x0000FFFFu;
+#pragma unroll
+                for (int jj = 16; jj > 0; jj >>= 1) {
+                    const unsigned y = __shfl_xor_sync(0xffffffffu, x, jj);
+                    x = (lane & jj) ? ((x & ~msk) | ((y & ~msk) >> jj)) : ((x & msk) | ((y & msk) << jj));
+                    msk ^= msk << (jj >> 1);
                 }
+                if (a * 32 + lane < k) rows[a][q >> 1] |= static_cast<unsigned long long>(x) << ((q & 1) * 32);
             }
         }
         // ---- 3. column-scan elimination: pivots = most reliable basis ----

@@ -207,7 +207,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         for (int k2 = 64; k2 <= np; k2 <<= 1) {
             for (int j2 = k2 >> 1; j2 >= 32; j2 >>= 1) {
                 for (int pr = tid; pr < np / 2; pr += kThreads) {
-                    const int i = (pr / j2) * 2 * j2 + (pr % j2);
+                    const int i = ((pr & ~(j2 - 1)) << 1) | (pr & (j2 - 1));  // j2 is a power of two
                     const int ixj = i + j2;
                     const bool asc = (i & k2) == 0;
                     const unsigned long long a = s.keys[i], b = s.keys[ixj];
