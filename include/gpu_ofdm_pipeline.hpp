@@ -5,8 +5,9 @@
 // GpuRxSyncExtractor / GpuRxDemodChain (uhd_ldpc_ofdm_link.cpp:6831-7182)
 // compile unchanged.  Implemented in libsicc_gb300.so over the C ABI of
 // include/sicc_pipe.h.  Errors are std::runtime_error, as in the reference
-// (gpu_ofdm_pipeline.cu:31-43).  The transmit members belong to the TX chain,
-// which this library does not provide: they throw.
+// (gpu_ofdm_pipeline.cu:31-43).  The transmit members run the GB300 TX chain
+// (encode, resource grid, channel and noise, inverse FFT, frame) over the
+// sicc_pipe_tx_* entry points.
 #pragma once
 
 #include <complex>

@@ -109,6 +109,41 @@ SICC_API int sicc_pipe_demod_gather(unsigned long long handle, const float* devi
                                     const long long* device_frame_offsets, int sample_count, int frames,
                                     float* device_llr, const long long* device_llr_offsets,
                                     sicc_pipe_sync_record_t* device_sync, void* cuda_stream);
+/* PH:37-57 (StaticTables), transmit-side members: the encoder and the channel
+ * tables of the TX chain (gpu_ofdm_pipeline.cu:854-920).  The grid tables
+ * (subcarriers, pilots, preamble) come from sicc_pipe_upload_static_tables. */
+typedef struct sicc_pipe_tx_tables_t {
+    const unsigned char* generator_kn; /* [code_k][code_n] 0/1, row-major; null with dvb_s2_accumulator */
+    int dvb_s2_accumulator;            /* 1: systematic + accumulator encoder */
+    const int* row_info_offsets;       /* [code_n - code_k + 1] starts of each parity row in row_info_cols */
+    const int* row_info_cols;          /* information columns of each parity row */
+    const float* precomp_h;            /* [num_symbols][active_sc] complex, or null */
+    const float* actual_h;             /* [num_symbols][active_sc] complex, or null */
+} sicc_pipe_tx_tables_t;
+
+SICC_API int sicc_pipe_upload_tx_tables(unsigned long long handle, const sicc_pipe_tx_tables_t* tables); /* PH:73 */
+/* PH:76-81 (submit_tx_frame_device_async): encode and modulate one frame of
+ * host info bits [info_bits_per_frame] (bytes 0/1) on the slot's stream,
+ * asynchronously; *out_device_frame ([frame_samples] complex) belongs to the
+ * slot.  With add_frequency_noise and frequency_noise_var > 0, complex
+ * Gaussian noise of that variance is added to the data resource elements. */
+SICC_API int sicc_pipe_tx_frame_device(unsigned long long handle, int slot, const unsigned char* host_info_bits,
+                                       float frequency_noise_var, unsigned long long noise_seed,
+                                       int add_frequency_noise, const float** out_device_frame);
+/* PH:75 (submit_tx_frame_async): as above without noise, then the frame is
+ * copied to host_frame ([frame_samples] complex; pinned memory overlaps). */
+SICC_API int sicc_pipe_tx_frame(unsigned long long handle, int slot, const unsigned char* host_info_bits,
+                                float* host_frame);
+/* PH:82 (synchronize_tx): wait for the slot's last TX frame. */
+SICC_API int sicc_pipe_tx_synchronize(unsigned long long handle, int slot);
+/* Extension: `frames` frames of device info bits ([frames][info_bits_per_frame])
+ * into device frames ([frames][frame_samples] complex) on cuda_stream in two
+ * launches; frame f's noise is seeded with noise_seed + f (no noise when
+ * frequency_noise_var <= 0).  frames <= max_batch_frames. */
+SICC_API int sicc_pipe_tx_batch(unsigned long long handle, const unsigned char* device_info_bits, int frames,
+                                float* device_frames, float frequency_noise_var, unsigned long long noise_seed,
+                                void* cuda_stream);
+
 /* Kernel durations (ms) of the last sicc_pipe_demod_batch / _gather call: sync, demod. */
 SICC_API int sicc_pipe_last_batch_ms(unsigned long long handle, float* out_sync_ms, float* out_demod_ms);
 

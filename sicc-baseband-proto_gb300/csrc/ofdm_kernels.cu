@@ -364,7 +364,7 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const long lon
 
 namespace {
 
-// Stream-ordered pool for the sync scratch (pass results and tickets), one per
+// Stream-ordered pool for kernel scratch (sync pass results and tickets, TX coded bits), one per
 // device; freed blocks stay in the pool for the next launch.
 cudaMemPool_t sync_pool(int device)
 {
@@ -653,6 +653,236 @@ void launch_demod(const DemodView& v, const float2* samples, long long stride, c
     demod_kernel<<<grid, kDemodThreads, smem, st>>>(v, samples, stride, sync, llr, llr_stride, spc, frame_off,
                                                     llr_off);
     check_cuda(cudaGetLastError(), "demod_kernel launch");
+}
+
+// ---------------------------------------------------------------------------
+// transmitter
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr int kTxThreads = 256;
+constexpr int kEncWarps = 8;
+
+// Gray square QAM, bits MSB-first per axis (gpu_ofdm_pipeline.cu:84-109).
+__device__ __forceinline__ float2 qam_from_bits(const uint8_t* bits, int bps)
+{
+    if (bps == 1) return make_float2(bits[0] ? -1.0f : 1.0f, 0.0f);
+    if (bps == 2) {
+        constexpr float s = 0.7071067811865475f;
+        return make_float2(bits[0] ? -s : s, bits[1] ? -s : s);
+    }
+    const int ab = bps / 2, levels = 1 << ab;
+    int gi = 0, gq = 0;
+    for (int i = 0; i < ab; ++i) {
+        gi = (gi << 1) | (bits[i] != 0);
+        gq = (gq << 1) | (bits[ab + i] != 0);
+    }
+    int bi = 0, bq = 0;  // Gray -> binary
+    for (; gi; gi >>= 1) bi ^= gi;
+    for (; gq; gq >>= 1) bq ^= gq;
+    const float scale = (bps == 4) ? 0.3162277660168379f : 0.1543033499620919f;
+    return make_float2(__fmul_rn(static_cast<float>((levels - 1) - 2 * bi), scale),
+                       __fmul_rn(static_cast<float>((levels - 1) - 2 * bq), scale));
+}
+
+// Counter-based normal deviates for the frequency-domain noise: a 32-bit
+// integer hash (xor-shift / multiply, "lowbias32") of seed ^ (index * golden
+// ratio) gives a uniform in (0, 1], and Box-Muller turns two of them into a
+// normal deviate (gpu_ofdm_pipeline.cu:259-280).
+__device__ __forceinline__ uint32_t hash32(uint32_t x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+__device__ __forceinline__ float uniform_open0(uint32_t seed, uint32_t idx)
+{
+    const uint32_t h = hash32(seed ^ (idx * 0x9e3779b9u));
+    return __fmul_rn(__fadd_rn(__uint2float_rn(h), 1.0f), 2.3283064365386963e-10f);
+}
+
+__device__ __forceinline__ float normal_dev(uint32_t seed, uint32_t idx)
+{
+    const float u1 = fmaxf(uniform_open0(seed, idx * 2u), 1.0e-7f);
+    const float u2 = uniform_open0(seed, idx * 2u + 1u);
+    return __fmul_rn(sqrtf(__fmul_rn(-2.0f, logf(u1))), cosf(__fmul_rn(__fmul_rn(2.0f, 3.14159265358979323846f), u2)));
+}
+
+// four bits -> four bytes (0/1)
+__device__ __forceinline__ uint32_t spread4(uint32_t x)
+{
+    return (x & 1u) | ((x & 2u) << 7) | ((x & 4u) << 14) | ((x & 8u) << 21);
+}
+
+}  // namespace
+
+// c = u G over GF(2): one warp per codeword, the set information bits select
+// bit-packed generator rows, 4 words of the codeword per lane per pass.
+__global__ void __launch_bounds__(kEncWarps * 32)
+tx_encode_generator_kernel(TxView v, const uint8_t* __restrict__ info, uint8_t* __restrict__ coded, int count)
+{
+    const int lane = threadIdx.x & 31;
+    const int n = v.code_n, k = v.code_k, gw = v.gen_stride;
+    for (int cw = blockIdx.x * kEncWarps + (threadIdx.x >> 5); cw < count; cw += gridDim.x * kEncWarps) {
+        const uint8_t* u = info + static_cast<size_t>(cw) * k;
+        uint8_t* c = coded + static_cast<size_t>(cw) * n;
+        for (int w0 = 0; w0 < (n + 31) / 32; w0 += 128) {
+            uint32_t acc[4] = {0u, 0u, 0u, 0u};
+            for (int i0 = 0; i0 < k; i0 += 32) {
+                unsigned bits = __ballot_sync(0xffffffffu, i0 + lane < k && (u[i0 + lane] & 1u));
+                while (bits) {
+                    const int b = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    const uint32_t* row = v.gen_words + static_cast<size_t>(i0 + b) * gw;
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) {
+                        const int w = w0 + r * 32 + lane;
+                        if (w < gw) acc[r] ^= __ldg(row + w);
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int w = w0 + r * 32 + lane;
+                if (w * 32 >= n) continue;
+                if (w * 32 + 32 <= n && (n & 3) == 0) {  // 32 bytes as 8 words
+                    uint32_t* dst = reinterpret_cast<uint32_t*>(c + w * 32);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) dst[q] = spread4((acc[r] >> (4 * q)) & 15u);
+                } else {
+                    for (int b = 0; b < 32 && w * 32 + b < n; ++b) c[w * 32 + b] = static_cast<uint8_t>((acc[r] >> b) & 1u);
+                }
+            }
+        }
+    }
+}
+
+// Systematic + accumulator encoder (gpu_ofdm_pipeline.cu:152-214): c[i] = u[i]
+// for i < k, then parity r = sum of u over row r's information columns, XOR the
+// previous parity: a prefix XOR over the rows, 32 rows per ballot.
+__global__ void __launch_bounds__(kEncWarps * 32)
+tx_encode_accumulator_kernel(TxView v, const uint8_t* __restrict__ info, uint8_t* __restrict__ coded, int count)
+{
+    const int lane = threadIdx.x & 31;
+    const int n = v.code_n, k = v.code_k, m = n - k;
+    for (int cw = blockIdx.x * kEncWarps + (threadIdx.x >> 5); cw < count; cw += gridDim.x * kEncWarps) {
+        const uint8_t* u = info + static_cast<size_t>(cw) * k;
+        uint8_t* c = coded + static_cast<size_t>(cw) * n;
+        for (int i = lane; i < k; i += 32) c[i] = u[i] & 1u;
+        unsigned carry = 0u;
+        for (int r0 = 0; r0 < m; r0 += 32) {
+            const int r = r0 + lane;
+            unsigned s = 0u;
+            if (r < m)
+                for (int q = v.acc_offsets[r]; q < v.acc_offsets[r + 1]; ++q) s ^= u[v.acc_cols[q]] & 1u;
+            unsigned y = __ballot_sync(0xffffffffu, s != 0u);
+            y ^= y << 1;
+            y ^= y << 2;
+            y ^= y << 4;
+            y ^= y << 8;
+            y ^= y << 16;
+            if (r < m) c[k + r] = static_cast<uint8_t>(((y >> lane) & 1u) ^ carry);
+            carry ^= (y >> 31) & 1u;
+        }
+    }
+}
+
+// One CTA per (OFDM symbol, frame); blockIdx.x == num_symbols writes the preamble.
+// The symbol's grid row is built in shared memory (gpu_ofdm_pipeline.cu:216-257,
+// 282-314), inverse-transformed as conj(FFT(conj(X))) (unnormalised, as cuFFT's
+// inverse) and written with its cyclic prefix, scaled by amplitude / nfft
+// (gpu_ofdm_pipeline.cu:316-342).
+__global__ void __launch_bounds__(kTxThreads)
+tx_symbol_kernel(TxView v, const uint8_t* __restrict__ coded, float2* __restrict__ out, float noise_var,
+                 unsigned long long noise_seed)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* buf0 = reinterpret_cast<float2*>(smem_raw);
+    float2* buf1 = buf0 + v.nfft;
+    const int sym = blockIdx.x, f = blockIdx.y;
+    float2* frame = out + static_cast<size_t>(f) * v.frame_samples;
+    if (sym == v.num_symbols) {
+        for (int i = threadIdx.x; i < v.pre_len; i += blockDim.x) {
+            const float2 p = v.preamble[i];
+            frame[i] = make_float2(__fmul_rn(p.x, v.amplitude), __fmul_rn(p.y, v.amplitude));
+        }
+        return;
+    }
+    for (int i = threadIdx.x; i < v.nfft; i += blockDim.x) buf0[i] = make_float2(0.0f, 0.0f);
+    __syncthreads();
+    const int pidx = v.pilot_of_symbol[sym], didx = v.data_of_symbol[sym];
+    const int coded_bits = v.blocks * v.code_n;
+    const uint8_t* bits = coded + static_cast<size_t>(f) * coded_bits;
+    const unsigned long long fs = noise_seed + static_cast<unsigned long long>(f);
+    const uint32_t seed = static_cast<uint32_t>(fs ^ (fs >> 32));
+    const float sigma = sqrtf(__fmul_rn(fmaxf(noise_var, 0.0f), 0.5f));
+    for (int sc = threadIdx.x; sc < v.active_sc; sc += blockDim.x) {
+        const int re = sym * v.active_sc + sc;
+        float2 value = make_float2(0.0f, 0.0f);
+        if (pidx >= 0) {
+            value = v.pilot_grid[static_cast<size_t>(pidx) * v.active_sc + sc];
+        } else if (didx >= 0) {
+            const int b0 = (didx * v.active_sc + sc) * v.bits_per_symbol;
+            uint8_t q[6] = {0, 0, 0, 0, 0, 0};  // bits past the coded bits are filler zeros
+            for (int i = 0; i < v.bits_per_symbol; ++i) q[i] = b0 + i < coded_bits ? bits[b0 + i] : 0;
+            value = qam_from_bits(q, v.bits_per_symbol);
+        }
+        if (v.precomp_h) {
+            const float2 h = v.precomp_h[re];
+            const float s = __fdiv_rn(1.0f, fmaxf(cnorm(h), 1.0e-10f));
+            value = cmul(value, make_float2(__fmul_rn(h.x, s), __fmul_rn(-h.y, s)));
+        }
+        if (v.actual_h) value = cmul(value, v.actual_h[re]);
+        if (noise_var > 0.0f && didx >= 0)
+            value = make_float2(__fadd_rn(value.x, __fmul_rn(sigma, normal_dev(seed, static_cast<uint32_t>(re)))),
+                                __fadd_rn(value.y, __fmul_rn(sigma, normal_dev(seed ^ 0xa5a5a5a5u, static_cast<uint32_t>(re)))));
+        buf0[v.used_bins[sc]] = make_float2(value.x, -value.y);  // conjugated for the inverse transform
+    }
+    __syncthreads();
+    const float2* Y = fft_stockham(buf0, buf1, v.nfft, v.twiddle);
+    const float scale = v.amplitude / static_cast<float>(v.nfft);
+    const int sym_len = v.nfft + v.cp;
+    float2* dst = frame + v.pre_len + static_cast<size_t>(sym) * sym_len;
+    for (int pos = threadIdx.x; pos < sym_len; pos += blockDim.x) {
+        const float2 y = Y[pos < v.cp ? v.nfft - v.cp + pos : pos - v.cp];
+        dst[pos] = make_float2(__fmul_rn(y.x, scale), __fmul_rn(-y.y, scale));
+    }
+}
+
+void launch_tx(const TxView& v, const uint8_t* info_bits, int frames, float2* frames_out, float noise_var,
+               unsigned long long noise_seed, cudaStream_t st)
+{
+    if (frames <= 0) return;
+    const size_t smem = 2 * static_cast<size_t>(v.nfft) * sizeof(float2);
+    if (smem > 200 * 1024) throw InvalidArgument("nfft too large for the TX kernel");
+    const int codewords = frames * v.blocks;
+    int device = 0;
+    check_cuda(cudaGetDevice(&device), "cudaGetDevice");
+    void* coded = nullptr;
+    check_cuda(cudaMallocFromPoolAsync(&coded, static_cast<size_t>(codewords) * v.code_n, sync_pool(device), st),
+               "cudaMallocFromPoolAsync(tx)");
+    uint8_t* cb = static_cast<uint8_t*>(coded);
+    const int ctas = std::max(1, std::min((codewords + kEncWarps - 1) / kEncWarps, 8 * device_sm_count()));
+    if (v.acc_offsets)
+        tx_encode_accumulator_kernel<<<ctas, kEncWarps * 32, 0, st>>>(v, info_bits, cb, codewords);
+    else
+        tx_encode_generator_kernel<<<ctas, kEncWarps * 32, 0, st>>>(v, info_bits, cb, codewords);
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(tx_symbol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (err == cudaSuccess) {
+        tx_symbol_kernel<<<dim3(v.num_symbols + 1, frames), kTxThreads, smem, st>>>(v, cb, frames_out, noise_var,
+                                                                                    noise_seed);
+        err = cudaGetLastError();
+    }
+    const cudaError_t ferr = cudaFreeAsync(coded, st);
+    check_cuda(err, "tx launch");
+    check_cuda(ferr, "cudaFreeAsync(tx)");
 }
 
 }  // namespace sicc

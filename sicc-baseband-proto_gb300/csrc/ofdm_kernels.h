@@ -64,4 +64,32 @@ void launch_demod(const DemodView& v, const float2* samples, long long stride, c
                   float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta = 0,
                   const long long* frame_off = nullptr, const long long* llr_off = nullptr);
 
+// Transmit tables resident on the device (the TX chain of gpu_ofdm_pipeline.cu:129-343, 922-1075).
+struct TxView {
+    int nfft, cp, num_symbols, active_sc, bits_per_symbol, pre_len;
+    int code_n, code_k, blocks;  // codewords per frame
+    int frame_samples;
+    float amplitude;
+    const int* used_bins;        // [active_sc] natural FFT bin of each active subcarrier
+    const int* pilot_of_symbol;  // [num_symbols] pilot index of the symbol, -1 for none
+    const int* data_of_symbol;   // [num_symbols] data index of the symbol, -1 for none
+    const float2* pilot_grid;    // [pilots][active_sc]
+    const float2* preamble;      // [pre_len]
+    const float2* precomp_h;     // [num_symbols][active_sc] or null
+    const float2* actual_h;      // [num_symbols][active_sc] or null
+    const float2* twiddle;       // [nfft] exp(-2 pi i j / nfft)
+    const uint32_t* gen_words;   // [code_k][gen_stride] bit-packed generator rows (bit j of word w: column 32w + j)
+    int gen_stride;
+    const int* acc_offsets;      // accumulator encoder: [m + 1] row starts in acc_cols (null: generator encoder)
+    const int* acc_cols;         // information columns of each parity row
+};
+
+// Encode and modulate `frames` frames of info bits (bytes, [frames][blocks * code_k]) into
+// complex frames at frames_out + f * frame_samples: c = u G (or the accumulator encoder),
+// resource grid, optional precompensation, channel and frequency-domain noise (noise_var > 0:
+// frame f seeded with noise_seed + f), inverse FFT, cyclic prefix, preamble, amplitude.  The
+// coded bits live in stream-ordered scratch.
+void launch_tx(const TxView& v, const uint8_t* info_bits, int frames, float2* frames_out, float noise_var,
+               unsigned long long noise_seed, cudaStream_t st);
+
 }  // namespace sicc

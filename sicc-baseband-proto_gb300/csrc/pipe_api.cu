@@ -47,9 +47,13 @@ struct Slot {
     Buf<float2> samples;
     Buf<SyncOut> sync;
     Buf<float> llr;
+    Buf<uint8_t> tx_info;  // TX: one frame's info bits
+    Buf<float2> tx_frame;
     cudaStream_t stream = nullptr;
+    cudaEvent_t tx_done = nullptr;
     ~Slot()
     {
+        if (tx_done) cudaEventDestroy(tx_done);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -71,6 +75,13 @@ struct Pipe {
     Buf<float2> pilot_grid, preamble, twiddle;
     std::vector<std::unique_ptr<Slot>> slots;
     Buf<SyncOut> batch_sync;
+    // transmitter
+    bool tx_tables = false;
+    TxView txv{};
+    Buf<int> pilot_of_sym, data_of_sym;
+    Buf<uint32_t> gen;
+    Buf<int> acc_off, acc_cols;
+    Buf<float2> precomp, actual;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     bool batch_timed = false;
     std::mutex mu;
@@ -131,6 +142,18 @@ int guarded(F&& f)
 void require_tables(const Pipe& p)
 {
     if (!p.tables) throw InvalidArgument("upload_static_tables must run before receiving");
+}
+
+void require_tx(const Pipe& p)
+{
+    if (!p.tables) throw InvalidArgument("upload_static_tables must run before transmitting");
+    if (!p.tx_tables) throw InvalidArgument("GPU TX requested before uploading a generator matrix");
+}
+
+// One frame of device info bits -> a device frame, on the slot's stream.
+void tx_one(Pipe& p, Slot& s, float noise_var, unsigned long long seed)
+{
+    launch_tx(p.txv, s.tx_info.p, 1, s.tx_frame.p, noise_var, seed, s.stream);
 }
 
 sicc_pipe_sync_t to_public(const SyncOut& s)
@@ -342,6 +365,30 @@ int sicc_pipe_upload_static_tables(unsigned long long handle, const sicc_pipe_ta
         v.pilot_grid = p->pilot_grid.p;
         v.twiddle = p->twiddle.p;
         v.axis_levels = p->axis.p;
+        // per-symbol pilot / data indices for the transmitter's resource grid
+        std::vector<int> pos(c.num_symbols, -1), dos(c.num_symbols, -1);
+        for (int q = 0; q < t->pilot_count; ++q) pos[t->pilot_symbols[q]] = q;
+        for (int d = 0; d < t->data_count; ++d) dos[t->data_symbols[d]] = d;
+        upload(p->pilot_of_sym, pos.data(), pos.size());
+        upload(p->data_of_sym, dos.data(), dos.size());
+        TxView& x = p->txv;
+        x.nfft = c.nfft;
+        x.cp = c.cp;
+        x.num_symbols = c.num_symbols;
+        x.active_sc = c.active_sc;
+        x.bits_per_symbol = c.bits_per_symbol;
+        x.pre_len = c.preamble_len;
+        x.code_n = c.code_n;
+        x.code_k = c.code_k;
+        x.blocks = c.blocks_per_frame;
+        x.frame_samples = p->frame_samples;
+        x.amplitude = c.tx_amplitude;
+        x.used_bins = p->used_bins.p;
+        x.pilot_of_symbol = p->pilot_of_sym.p;
+        x.data_of_symbol = p->data_of_sym.p;
+        x.pilot_grid = p->pilot_grid.p;
+        x.preamble = p->preamble.p;
+        x.twiddle = p->twiddle.p;
         p->tables = true;
         return CUDA_OSD_STATUS_OK;
     });
@@ -505,6 +552,142 @@ int sicc_pipe_demod_gather(unsigned long long handle, const float* device_iq, co
                      device_llr_offsets);
         check_cuda(cudaEventRecord(p->ev[2], st), "cudaEventRecord");
         p->batch_timed = true;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_upload_tx_tables(unsigned long long handle, const sicc_pipe_tx_tables_t* t)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        if (!t) throw InvalidArgument("null table");
+        const auto& c = p->cfg;
+        const int n = c.code_n, k = c.code_k, m = n - k;
+        if (k <= 0 || m <= 0) throw InvalidArgument("code dimensions must satisfy 0 < code_k < code_n");
+        check_cuda(cudaSetDevice(p->device), "cudaSetDevice");
+        TxView& x = p->txv;
+        if (t->dvb_s2_accumulator) {
+            if (!t->row_info_offsets) throw InvalidArgument("row_info_offsets has wrong size");
+            const int nnz = t->row_info_offsets[m];
+            if (t->row_info_offsets[0] != 0 || nnz < 0 || (nnz > 0 && !t->row_info_cols))
+                throw InvalidArgument("row_info_offsets has wrong size");
+            for (int r = 0; r < m; ++r)
+                if (t->row_info_offsets[r + 1] < t->row_info_offsets[r]) throw InvalidArgument("row_info_offsets must not decrease");
+            for (int q = 0; q < nnz; ++q)
+                if (t->row_info_cols[q] < 0 || t->row_info_cols[q] >= k) throw InvalidArgument("row_info_cols out of range");
+            upload(p->acc_off, t->row_info_offsets, static_cast<size_t>(m) + 1);
+            if (nnz > 0) upload(p->acc_cols, t->row_info_cols, static_cast<size_t>(nnz));
+            else p->acc_cols.alloc(1);
+            p->gen.release();
+            x.acc_offsets = p->acc_off.p;
+            x.acc_cols = p->acc_cols.p;
+            x.gen_words = nullptr;
+            x.gen_stride = 0;
+        } else {
+            if (!t->generator_kn) throw InvalidArgument("GPU TX requested before uploading a generator matrix");
+            const int gw = (n + 31) / 32;
+            std::vector<uint32_t> words(static_cast<size_t>(k) * gw, 0u);  // bit-packed rows
+            for (int r = 0; r < k; ++r)
+                for (int j = 0; j < n; ++j)
+                    if (t->generator_kn[static_cast<size_t>(r) * n + j] & 1u) words[static_cast<size_t>(r) * gw + j / 32] |= 1u << (j % 32);
+            upload(p->gen, words.data(), words.size());
+            p->acc_off.release();
+            p->acc_cols.release();
+            x.gen_words = p->gen.p;
+            x.gen_stride = gw;
+            x.acc_offsets = nullptr;
+            x.acc_cols = nullptr;
+        }
+        const size_t re = static_cast<size_t>(c.num_symbols) * c.active_sc;
+        if (t->precomp_h) upload(p->precomp, reinterpret_cast<const float2*>(t->precomp_h), re);
+        else p->precomp.release();
+        if (t->actual_h) upload(p->actual, reinterpret_cast<const float2*>(t->actual_h), re);
+        else p->actual.release();
+        x.precomp_h = p->precomp.p;
+        x.actual_h = p->actual.p;
+        const size_t info_bits = static_cast<size_t>(c.blocks_per_frame) * k;
+        for (auto& sl : p->slots) {
+            if (!sl->tx_info.p) {
+                sl->tx_info.alloc(info_bits);
+                sl->tx_frame.alloc(static_cast<size_t>(p->frame_samples));
+                check_cuda(cudaEventCreateWithFlags(&sl->tx_done, cudaEventDisableTiming), "cudaEventCreate(tx)");
+            }
+        }
+        p->tx_tables = true;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_tx_frame_device(unsigned long long handle, int slot, const unsigned char* host_info_bits,
+                              float frequency_noise_var, unsigned long long noise_seed, int add_frequency_noise,
+                              const float** out_device_frame)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        require_tx(*p);
+        if (!host_info_bits || !out_device_frame) throw InvalidArgument("null argument");
+        Slot& s = slot_of(*p, slot);
+        check_cuda(cudaSetDevice(p->device), "cudaSetDevice");
+        const size_t info_bits = static_cast<size_t>(p->cfg.blocks_per_frame) * p->cfg.code_k;
+        check_cuda(cudaMemcpyAsync(s.tx_info.p, host_info_bits, info_bits, cudaMemcpyHostToDevice, s.stream),
+                   "copy TX info bits");
+        tx_one(*p, s, add_frequency_noise ? frequency_noise_var : 0.0f, noise_seed);
+        check_cuda(cudaEventRecord(s.tx_done, s.stream), "record tx_done");
+        *out_device_frame = reinterpret_cast<const float*>(s.tx_frame.p);
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_tx_frame(unsigned long long handle, int slot, const unsigned char* host_info_bits, float* host_frame)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        require_tx(*p);
+        if (!host_info_bits || !host_frame) throw InvalidArgument("null argument");
+        Slot& s = slot_of(*p, slot);
+        check_cuda(cudaSetDevice(p->device), "cudaSetDevice");
+        const size_t info_bits = static_cast<size_t>(p->cfg.blocks_per_frame) * p->cfg.code_k;
+        check_cuda(cudaMemcpyAsync(s.tx_info.p, host_info_bits, info_bits, cudaMemcpyHostToDevice, s.stream),
+                   "copy TX info bits");
+        tx_one(*p, s, 0.0f, 0ull);
+        check_cuda(cudaMemcpyAsync(host_frame, s.tx_frame.p, static_cast<size_t>(p->frame_samples) * sizeof(float2),
+                                   cudaMemcpyDeviceToHost, s.stream),
+                   "copy TX frame to host");
+        check_cuda(cudaEventRecord(s.tx_done, s.stream), "record tx_done");
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_tx_synchronize(unsigned long long handle, int slot)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        Slot* s = nullptr;
+        {
+            std::lock_guard<std::mutex> lock(p->mu);
+            s = &slot_of(*p, slot);
+        }
+        if (s->tx_done) check_cuda(cudaEventSynchronize(s->tx_done), "synchronize tx_done");  // no TX yet: nothing to wait for
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_tx_batch(unsigned long long handle, const unsigned char* device_info_bits, int frames,
+                       float* device_frames, float frequency_noise_var, unsigned long long noise_seed, void* cuda_stream)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        require_tx(*p);
+        if (!device_info_bits || !device_frames) throw InvalidArgument("null device pointer");
+        if (frames <= 0 || frames > p->batch_frames) throw InvalidArgument("frames must be in 1..max_batch_frames");
+        check_cuda(cudaSetDevice(p->device), "cudaSetDevice");
+        cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+        launch_tx(p->txv, device_info_bits, frames, reinterpret_cast<float2*>(device_frames), frequency_noise_var,
+                  noise_seed, st);
         return CUDA_OSD_STATUS_OK;
     });
 }

@@ -88,21 +88,45 @@ void Pipeline::upload_static_tables(const StaticTables& t)
     ct.pilot_grid = reinterpret_cast<const float*>(t.pilot_grid.data());
     ct.preamble = reinterpret_cast<const float*>(t.preamble.data());
     check(sicc_pipe_upload_static_tables(impl_->handle, &ct), "upload_static_tables");
+    // transmit-side members (gpu_ofdm_pipeline.cu:854-920)
+    if (!t.generator_kn.empty() || t.dvb_s2_accumulator) {
+        const size_t re = static_cast<size_t>(c.num_symbols) * c.active_sc;
+        if (!t.generator_kn.empty())
+            require_size(t.generator_kn.size(), static_cast<size_t>(c.code_k) * c.code_n, "generator_kn");
+        if (t.dvb_s2_accumulator)
+            require_size(t.row_info_offsets.size(), static_cast<size_t>(c.code_n - c.code_k) + 1, "row_info_offsets");
+        if (!t.precomp_h.empty()) require_size(t.precomp_h.size(), re, "precomp_h");
+        if (!t.actual_h.empty()) require_size(t.actual_h.size(), re, "actual_h");
+        sicc_pipe_tx_tables_t tx{};
+        tx.generator_kn = t.generator_kn.empty() ? nullptr : t.generator_kn.data();
+        tx.dvb_s2_accumulator = t.dvb_s2_accumulator ? 1 : 0;
+        tx.row_info_offsets = t.row_info_offsets.empty() ? nullptr : t.row_info_offsets.data();
+        tx.row_info_cols = t.row_info_cols.empty() ? nullptr : t.row_info_cols.data();
+        tx.precomp_h = t.precomp_h.empty() ? nullptr : reinterpret_cast<const float*>(t.precomp_h.data());
+        tx.actual_h = t.actual_h.empty() ? nullptr : reinterpret_cast<const float*>(t.actual_h.data());
+        check(sicc_pipe_upload_tx_tables(impl_->handle, &tx), "upload_static_tables");
+    }
 }
 
-void Pipeline::submit_tx_frame_async(int, const uint8_t*, Complex32*)
+void Pipeline::submit_tx_frame_async(int slot, const uint8_t* h_info_bits, Complex32* h_tx_frame)
 {
-    throw std::runtime_error("the GB300 receive library has no TX chain (submit_tx_frame_async)");
+    check(sicc_pipe_tx_frame(impl_->handle, slot, h_info_bits, reinterpret_cast<float*>(h_tx_frame)),
+          "submit_tx_frame_async");
 }
 
-const Complex32* Pipeline::submit_tx_frame_device_async(int, const uint8_t*, float, uint64_t, bool)
+const Complex32* Pipeline::submit_tx_frame_device_async(int slot, const uint8_t* h_info_bits, float frequency_noise_var,
+                                                        uint64_t noise_seed, bool add_frequency_noise)
 {
-    throw std::runtime_error("the GB300 receive library has no TX chain (submit_tx_frame_device_async)");
+    const float* d = nullptr;
+    check(sicc_pipe_tx_frame_device(impl_->handle, slot, h_info_bits, frequency_noise_var, noise_seed,
+                                    add_frequency_noise ? 1 : 0, &d),
+          "submit_tx_frame_device_async");
+    return reinterpret_cast<const Complex32*>(d);
 }
 
-void Pipeline::synchronize_tx(int)
+void Pipeline::synchronize_tx(int slot)
 {
-    throw std::runtime_error("the GB300 receive library has no TX chain (synchronize_tx)");
+    check(sicc_pipe_tx_synchronize(impl_->handle, slot), "synchronize_tx");
 }
 
 SyncResult Pipeline::find_frame(int slot, const Complex32* h_samples, int sample_count)

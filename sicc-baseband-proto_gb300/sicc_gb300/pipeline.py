@@ -4,7 +4,9 @@ Mirrors the reference bridge class usrp_gpu_pipeline_bridge::Pipeline
 (source/cpp_cuda/uhd_cpp/src/gpu_ofdm_pipeline.hpp:65-93): constructor with a
 Config and a slot count, upload_static_tables, find_frame[_device],
 demod_frame_to_device_llr, demod_frame_device_to_device_llr,
-demod_frame_to_host_llr; plus the batched device extension.
+demod_frame_to_host_llr, and the transmit members submit_tx_frame_async,
+submit_tx_frame_device_async, synchronize_tx; plus the batched device
+extensions (receive and transmit).
 """
 from __future__ import annotations
 
@@ -32,6 +34,11 @@ class PipeTables(C.Structure):
                 ("preamble", C.c_void_p)]
 
 
+class PipeTxTables(C.Structure):
+    _fields_ = [("generator_kn", C.c_void_p), ("dvb_s2_accumulator", C.c_int), ("row_info_offsets", C.c_void_p),
+                ("row_info_cols", C.c_void_p), ("precomp_h", C.c_void_p), ("actual_h", C.c_void_p)]
+
+
 class PipeSync(C.Structure):
     _fields_ = [("start", C.c_int), ("metric", C.c_float), ("cfo_hz", C.c_float)]
 
@@ -56,6 +63,13 @@ _SIGS = {
     "sicc_pipe_demod_gather": (C.c_int, [C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_void_p]),
     "sicc_pipe_last_batch_ms": (C.c_int, [C.c_ulonglong, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "sicc_pipe_upload_tx_tables": (C.c_int, [C.c_ulonglong, C.POINTER(PipeTxTables)]),
+    "sicc_pipe_tx_frame_device": (C.c_int, [C.c_ulonglong, C.c_int, C.c_void_p, C.c_float, C.c_ulonglong, C.c_int,
+                                            C.POINTER(C.c_void_p)]),
+    "sicc_pipe_tx_frame": (C.c_int, [C.c_ulonglong, C.c_int, C.c_void_p, C.c_void_p]),
+    "sicc_pipe_tx_synchronize": (C.c_int, [C.c_ulonglong, C.c_int]),
+    "sicc_pipe_tx_batch": (C.c_int, [C.c_ulonglong, C.c_void_p, C.c_int, C.c_void_p, C.c_float, C.c_ulonglong,
+                                     C.c_void_p]),
 }
 
 
@@ -172,3 +186,52 @@ class RxPipeline:
         a, b = C.c_float(), C.c_float()
         _lib.check(_fn("sicc_pipe_last_batch_ms")(self.handle, C.byref(a), C.byref(b)), "sicc_pipe_last_batch_ms")
         return a.value, b.value
+
+    # ---- transmit (gpu_ofdm_pipeline.cu:854-1075) ----
+    def upload_tx_tables(self, generator_kn=None, accumulator=None, precomp_h=None, actual_h=None):
+        """generator_kn: [k][n] 0/1; or accumulator=(row_info_offsets [m+1], row_info_cols)."""
+        keep = {}
+        t = PipeTxTables()
+        if accumulator is not None:
+            keep["off"] = np.ascontiguousarray(accumulator[0], np.int32)
+            keep["cols"] = np.ascontiguousarray(accumulator[1], np.int32)
+            t.dvb_s2_accumulator = 1
+            t.row_info_offsets = keep["off"].ctypes.data
+            t.row_info_cols = keep["cols"].ctypes.data if keep["cols"].size else None
+        else:
+            keep["gen"] = np.ascontiguousarray(generator_kn, np.uint8)
+            t.generator_kn = keep["gen"].ctypes.data
+        for name, arr in (("precomp_h", precomp_h), ("actual_h", actual_h)):
+            if arr is not None:
+                keep[name] = np.ascontiguousarray(arr, np.complex64)
+                setattr(t, name, keep[name].ctypes.data)
+        _lib.check(_fn("sicc_pipe_upload_tx_tables")(self.handle, C.byref(t)), "upload_static_tables (TX)")
+
+    def tx_frame(self, slot: int, info_bits: np.ndarray) -> np.ndarray:
+        """submit_tx_frame_async + synchronize_tx: one frame of info bits -> complex64 frame."""
+        u = np.ascontiguousarray(info_bits, np.uint8)
+        out = np.zeros(self.frame_samples, np.complex64)
+        _lib.check(_fn("sicc_pipe_tx_frame")(self.handle, slot, u.ctypes.data, out.ctypes.data), "submit_tx_frame_async")
+        self.tx_synchronize(slot)
+        return out
+
+    def tx_frame_device(self, slot: int, info_bits: np.ndarray, noise_var: float = 0.0, seed: int = 0,
+                        add_noise: bool = False) -> int:
+        """submit_tx_frame_device_async: the device address of the slot's frame."""
+        u = np.ascontiguousarray(info_bits, np.uint8)
+        d = C.c_void_p()
+        _lib.check(_fn("sicc_pipe_tx_frame_device")(self.handle, slot, u.ctypes.data, noise_var, seed,
+                                                    1 if add_noise else 0, C.byref(d)), "submit_tx_frame_device_async")
+        return d.value
+
+    def tx_synchronize(self, slot: int):
+        _lib.check(_fn("sicc_pipe_tx_synchronize")(self.handle, slot), "synchronize_tx")
+
+    def tx_batch(self, d_info, frames: int, d_frames, noise_var: float = 0.0, seed: int = 0, stream=None):
+        st = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+        _lib.check(_fn("sicc_pipe_tx_batch")(self.handle, _lib.ptr(d_info), frames, _lib.ptr(d_frames), noise_var,
+                                             seed, st), "sicc_pipe_tx_batch")
+
+
+#: The bridge class name of the reference: one pipeline object serves both directions.
+Pipeline = RxPipeline

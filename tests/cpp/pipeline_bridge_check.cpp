@@ -2,7 +2,7 @@
 // way the reference link driver does (GpuRxSyncExtractor / GpuRxDemodChain,
 // uhd_ldpc_ofdm_link.cpp:6831-7182): construct, upload tables, find a frame in
 // a host buffer, demodulate it to host LLRs, and demodulate the same frame
-// from device memory.  Inputs and outputs are raw files in one directory,
+// from device memory; then transmit a frame (host and device paths).  Inputs and outputs are raw files in one directory,
 // written and checked by tests/test_gpu_ofdm.py.
 //
 // usage: pipeline_bridge_check <dir>
@@ -92,12 +92,26 @@ int main(int argc, char** argv)
         cudaFree(d_frame);
         write_bin(dir + "/llr_device.bin", llr_dev.data(), llr_dev.size());
 
+        // transmit: refused before a generator is uploaded (gpu_ofdm_pipeline.cu:930-932), then one
+        // frame through submit_tx_frame_async and one with frequency-domain noise through the device path
         bool tx_threw = false;
+        const auto info = read_bin<uint8_t>(dir + "/tx_info.bin");
+        std::vector<Complex32> txf(static_cast<size_t>(cfg.frame_samples()));
         try {
-            pipe.synchronize_tx(0);
+            pipe.submit_tx_frame_async(0, info.data(), txf.data());
         } catch (const std::runtime_error&) {
             tx_threw = true;
         }
+        t.generator_kn = read_bin<uint8_t>(dir + "/gen.bin");
+        pipe.upload_static_tables(t);
+        pipe.submit_tx_frame_async(0, info.data(), txf.data());
+        pipe.synchronize_tx(0);
+        write_bin(dir + "/tx_frame.bin", txf.data(), txf.size());
+        const Complex32* d_tx = pipe.submit_tx_frame_device_async(1, info.data(), 0.05f, 99, true);
+        pipe.synchronize_tx(1);
+        std::vector<Complex32> txn(txf.size());
+        cudaMemcpy(txn.data(), d_tx, txn.size() * sizeof(Complex32), cudaMemcpyDeviceToHost);
+        write_bin(dir + "/tx_frame_noise.bin", txn.data(), txn.size());
         bool bad_slot_threw = false;
         try {
             pipe.find_frame(7, frame.data(), static_cast<int>(frame.size()));

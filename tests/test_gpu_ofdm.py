@@ -230,6 +230,12 @@ def test_no_frame_in_noise(cuda):
     assert s == -1 and np.all(llr == 0)
 
 
+def tx_oracle_generator(code):
+    """[k][n] systematic generator [I | P] of a QC code."""
+    P = codes.gf2_parity_matrix(code)
+    return np.ascontiguousarray(np.concatenate([np.eye(code.k, dtype=np.uint8), P], axis=1), np.uint8)
+
+
 def test_cpp_pipeline_class_drop_in(cuda):
     """The C++ class of include/gpu_ofdm_pipeline.hpp, compiled and run as a caller would."""
     from sicc_gb300 import _lib
@@ -257,6 +263,10 @@ def test_cpp_pipeline_class_drop_in(cuda):
                               ("grid", t.pilot_grid, np.complex64), ("pre", t.preamble, np.complex64),
                               ("frame", d["iq"][i][: d["lengths"][i]], np.complex64)):
             np.ascontiguousarray(arr, dt).tofile(os.path.join(tmp, name + ".bin"))
+        gen = tx_oracle_generator(code)
+        info = np.random.default_rng(5).integers(0, 2, size=16 * code.k, dtype=np.uint8)
+        gen.tofile(os.path.join(tmp, "gen.bin"))
+        info.tofile(os.path.join(tmp, "tx_info.bin"))
         r = subprocess.run([exe, tmp], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
         vals = open(os.path.join(tmp, "sync.txt")).read().split()
@@ -267,3 +277,15 @@ def test_cpp_pipeline_class_drop_in(cuda):
         assert host.size == 16 * 128
         # the host path re-searches the frame (start 0) and the device path is told the CFO: same LLRs
         assert np.max(np.abs(host - dev)) <= 1e-3 * max(np.max(np.abs(host)), 1.0)
+        # the transmit members against the restated GPU transmitter (tolerance: fp32 inverse FFT)
+        import tx_oracle
+        coded = tx_oracle.encode_generator(info.reshape(16, code.k), gen).reshape(1, -1)
+        kw = dict(nfft=cfg.nfft, cp=cfg.cp, num_symbols=cfg.num_symbols, active_sc=cfg.active_sc,
+                  bps=cfg.bits_per_symbol, used_bins=t.used_bins, pilot_symbols=t.pilot_symbols,
+                  data_symbols=t.data_symbols, pilot_grid=t.pilot_grid, preamble=t.preamble,
+                  amplitude=0.20)  # the bridge Config's tx_amplitude default (PH:30), which the check keeps
+        for name, extra in (("tx_frame", {}), ("tx_frame_noise", dict(noise_var=0.05, noise_seed=99))):
+            got = np.fromfile(os.path.join(tmp, name + ".bin"), np.complex64)
+            ref = tx_oracle.tx_frames(coded, **kw, **extra)[0]
+            assert got.size == ref.size
+            assert np.max(np.abs(got - ref)) <= 2e-5 * np.max(np.abs(ref)), name
