@@ -414,6 +414,116 @@ def run_ofdm(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------ OFDM transmit workload
+def run_ofdm_tx(args, rank, world):
+    """Encode + modulate 256-frame batches of the 16-QAM OFDM workload (the GPU transmitter)."""
+    import torch
+    from sicc_gb300 import codes, ofdm
+    from sicc_gb300.pipeline import RxPipeline
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    t = ofdm.reference_tables(ofdm.OFDM_C3)
+    code = codes.ofdm_code()
+    frames = args.ofdm_frames
+    per_step = len(OFDM_SNRS)  # batches per step, as the receive workload
+    resident = 6                # 6 x 35.5 MB of output frames cycled (> L2)
+    blocks = t.coded_bits // code.n
+    G = np.ascontiguousarray(np.concatenate([np.eye(code.k, dtype=np.uint8), codes.gf2_parity_matrix(code)], 1))
+    pipe = RxPipeline(t, code.n, code.k, blocks, 1e-3, max_batch_frames=frames)
+    pipe.upload_tx_tables(generator_kn=G)
+    rng = np.random.default_rng(900 + rank)
+    info = [rng.integers(0, 2, size=(frames, blocks * code.k), dtype=np.uint8) for _ in range(resident)]
+    d_info = [torch.from_numpy(x).cuda() for x in info]
+    L = t.frame_len
+    d_out = [torch.empty((frames, L), dtype=torch.complex64, device="cuda") for _ in range(resident)]
+    stream = torch.cuda.current_stream()
+
+    def step(s):
+        for b in range(per_step):
+            i = (s * per_step + b) % resident
+            pipe.tx_batch(d_info[i], frames, d_out[i], stream=stream)
+
+    for s in range(args.warmup):
+        step(s)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for s in range(args.steps):
+        step(s)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    info_bits = per_step * frames * blocks * code.k
+    value = world * info_bits * args.steps / (elapsed_ms * 1e-3) / 1e6
+
+    # one batch alone: the roofline of the transmitter (encode + symbol kernels)
+    reps = 10
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for r in range(reps):
+        pipe.tx_batch(d_info[r % resident], frames, d_out[r % resident], stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batch_ms = e0.elapsed_time(e1) / reps
+    tx_bytes = frames * (blocks * code.k + 2 * blocks * code.n + 8 * L)  # info in, coded out + in, frame out
+
+    # end to end: pinned host info bits -> device -> frames -> pinned host
+    h_info = torch.empty((frames, blocks * code.k), dtype=torch.uint8, pin_memory=True)
+    h_info.numpy()[:] = info[0]
+    h_out = torch.empty((frames, L), dtype=torch.complex64, pin_memory=True)
+    d_in = torch.empty((frames, blocks * code.k), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        for b in range(per_step):
+            d_in.copy_(h_info, non_blocking=True)
+            pipe.tx_batch(d_in, frames, d_out[0], stream=stream)
+            h_out.copy_(d_out[0], non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:  # the restated transmitter on one host core
+        import tx_oracle
+        cfg = t.cfg
+        sample = 4
+        c0 = time.perf_counter()
+        cw = tx_oracle.encode_generator(info[1][:sample].reshape(-1, code.k), G).reshape(sample, -1)
+        tx_oracle.tx_frames(cw, nfft=cfg.nfft, cp=cfg.cp, num_symbols=cfg.num_symbols, active_sc=cfg.active_sc,
+                            bps=cfg.bits_per_symbol, used_bins=t.used_bins, pilot_symbols=t.pilot_symbols,
+                            data_symbols=t.data_symbols, pilot_grid=t.pilot_grid, preamble=t.preamble,
+                            amplitude=cfg.amplitude)
+        cs = time.perf_counter() - c0
+        cpu = {"value": round(sample * blocks * code.k / cs / 1e6, 4), "unit": "Mbit/s", "cores": 1, "kind": "port",
+               "sample": f"{sample} frames: generator encode + grid + inverse FFT + frame (oracle/tx_oracle.py, NumPy)"}
+
+    peak, peak_kind = peaks()
+    achieved = tx_bytes / (batch_ms * 1e-3) / 1e9
+    line = {"metric": "info-bit Mbps OFDM TX (encode+modulate+IFFT+frame), 16-QAM, (1024,512)",
+            "value": round(value, 3), "unit": "Mbit/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(elapsed_ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded information bits)",
+            "config": {"workload": "ofdm_tx_1024_512", "frames_per_batch": frames, "batches_per_step": per_step,
+                       "fft": 1024, "cp": 72, "active_sc": 600, "symbols": 14, "code": "QC (1024,512) Z=64",
+                       "codewords_per_frame": blocks, "l2": "6 resident output batches of 35.5 MB cycled (> L2)"},
+            "batch_ms": round(batch_ms, 4),
+            "gpu_launches": args.steps * per_step * 2, "clocks": clk,
+            "roofline": {"bound": "hbm", "kernel": "tx_encode + tx_symbol_kernel", "achieved": round(achieved, 2),
+                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": None,
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": tx_bytes},
+            "e2e": {"value": round(world * info_bits * args.steps / e2e_s / 1e6, 3), "unit": "Mbit/s",
+                    "h2d_bytes_per_step": per_step * frames * blocks * code.k,
+                    "d2h_bytes_per_step": per_step * frames * L * 8},
+            "cpu_baseline": cpu}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # --------------------------------------------------- mixed-code batched workload
 def run_mixed(args, rank, world):
     """100,000 codewords of 15 codes in one persistent launch, against one launch per request."""
@@ -744,7 +854,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=BATCH, help="frames per batch (profiling runs only)")
     ap.add_argument("--resident", type=int, default=RESIDENT_BATCHES, help="resident batches per Eb/N0")
-    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "ofdm_rx_1024_512", "mixed_100k", "serve_mixed"])
+    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "ofdm_rx_1024_512", "ofdm_tx_1024_512", "mixed_100k",
+                                                        "serve_mixed"])
     ap.add_argument("--serve-requests", type=int, default=1500)
     ap.add_argument("--serve-batch", type=int, default=16384, help="codewords per server launch")
     ap.add_argument("--serve-inflight", type=int, default=2, help="batches overlapping on the device")
@@ -759,6 +870,8 @@ def main():
         run_reference(args, rank, world)
     elif args.workload == "ofdm_rx_1024_512":
         run_ofdm(args, rank, world)
+    elif args.workload == "ofdm_tx_1024_512":
+        run_ofdm_tx(args, rank, world)
     elif args.workload == "mixed_100k":
         run_mixed(args, rank, world)
     elif args.workload == "serve_mixed":

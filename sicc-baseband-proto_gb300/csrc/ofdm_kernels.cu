@@ -721,8 +721,10 @@ __device__ __forceinline__ uint32_t spread4(uint32_t x)
 
 }  // namespace
 
-// c = u G over GF(2): one warp per codeword, the set information bits select
-// bit-packed generator rows, 4 words of the codeword per lane per pass.
+// c = u G over GF(2): one warp per codeword, 4 words of the codeword per lane
+// per pass.  With the byte tables each 8 information bits select one
+// precomputed XOR of their 8 generator rows; otherwise each set bit selects
+// its bit-packed row.
 __global__ void __launch_bounds__(kEncWarps * 32)
 tx_encode_generator_kernel(TxView v, const uint8_t* __restrict__ info, uint8_t* __restrict__ coded, int count)
 {
@@ -735,6 +737,20 @@ tx_encode_generator_kernel(TxView v, const uint8_t* __restrict__ info, uint8_t* 
             uint32_t acc[4] = {0u, 0u, 0u, 0u};
             for (int i0 = 0; i0 < k; i0 += 32) {
                 unsigned bits = __ballot_sync(0xffffffffu, i0 + lane < k && (u[i0 + lane] & 1u));
+                if (v.gen_tab) {  // one table entry per byte of information bits: independent loads
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int g = (i0 >> 3) + q;
+                        if (g * 8 >= k) break;
+                        const uint32_t* e = v.gen_tab + (static_cast<size_t>(g) * 256 + ((bits >> (8 * q)) & 255u)) * gw;
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) {
+                            const int w = w0 + r * 32 + lane;
+                            if (w < gw) acc[r] ^= __ldg(e + w);
+                        }
+                    }
+                    continue;
+                }
                 while (bits) {
                     const int b = __ffs(bits) - 1;
                     bits &= bits - 1;
@@ -821,16 +837,20 @@ tx_symbol_kernel(TxView v, const uint8_t* __restrict__ coded, float2* __restrict
     const unsigned long long fs = noise_seed + static_cast<unsigned long long>(f);
     const uint32_t seed = static_cast<uint32_t>(fs ^ (fs >> 32));
     const float sigma = sqrtf(__fmul_rn(fmaxf(noise_var, 0.0f), 0.5f));
+    uint8_t* sbits = reinterpret_cast<uint8_t*>(buf1);  // the symbol's coded bits (buf1 is free until the FFT)
+    if (didx >= 0 && pidx < 0) {
+        const int b0 = didx * v.active_sc * v.bits_per_symbol;
+        for (int i = threadIdx.x; i < v.active_sc * v.bits_per_symbol; i += blockDim.x)
+            sbits[i] = b0 + i < coded_bits ? bits[b0 + i] : 0;  // bits past the coded bits are filler zeros
+        __syncthreads();
+    }
     for (int sc = threadIdx.x; sc < v.active_sc; sc += blockDim.x) {
         const int re = sym * v.active_sc + sc;
         float2 value = make_float2(0.0f, 0.0f);
         if (pidx >= 0) {
             value = v.pilot_grid[static_cast<size_t>(pidx) * v.active_sc + sc];
         } else if (didx >= 0) {
-            const int b0 = (didx * v.active_sc + sc) * v.bits_per_symbol;
-            uint8_t q[6] = {0, 0, 0, 0, 0, 0};  // bits past the coded bits are filler zeros
-            for (int i = 0; i < v.bits_per_symbol; ++i) q[i] = b0 + i < coded_bits ? bits[b0 + i] : 0;
-            value = qam_from_bits(q, v.bits_per_symbol);
+            value = qam_from_bits(sbits + sc * v.bits_per_symbol, v.bits_per_symbol);
         }
         if (v.precomp_h) {
             const float2 h = v.precomp_h[re];
@@ -843,7 +863,7 @@ tx_symbol_kernel(TxView v, const uint8_t* __restrict__ coded, float2* __restrict
                                 __fadd_rn(value.y, __fmul_rn(sigma, normal_dev(seed ^ 0xa5a5a5a5u, static_cast<uint32_t>(re)))));
         buf0[v.used_bins[sc]] = make_float2(value.x, -value.y);  // conjugated for the inverse transform
     }
-    __syncthreads();
+    __syncthreads();  // the grid row is complete and the staged bits are read
     const float2* Y = fft_stockham(buf0, buf1, v.nfft, v.twiddle);
     const float scale = v.amplitude / static_cast<float>(v.nfft);
     const int sym_len = v.nfft + v.cp;

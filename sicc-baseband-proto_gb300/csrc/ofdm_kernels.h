@@ -80,6 +80,7 @@ struct TxView {
     const float2* twiddle;       // [nfft] exp(-2 pi i j / nfft)
     const uint32_t* gen_words;   // [code_k][gen_stride] bit-packed generator rows (bit j of word w: column 32w + j)
     int gen_stride;
+    const uint32_t* gen_tab;     // [ceil(code_k/8)][256][gen_stride]: XOR of the 8 rows 8g.. selected by a byte, or null
     const int* acc_offsets;      // accumulator encoder: [m + 1] row starts in acc_cols (null: generator encoder)
     const int* acc_cols;         // information columns of each parity row
 };

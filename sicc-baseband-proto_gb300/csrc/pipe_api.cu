@@ -79,7 +79,7 @@ struct Pipe {
     bool tx_tables = false;
     TxView txv{};
     Buf<int> pilot_of_sym, data_of_sym;
-    Buf<uint32_t> gen;
+    Buf<uint32_t> gen, gen_tab;
     Buf<int> acc_off, acc_cols;
     Buf<float2> precomp, actual;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
@@ -580,6 +580,8 @@ int sicc_pipe_upload_tx_tables(unsigned long long handle, const sicc_pipe_tx_tab
             if (nnz > 0) upload(p->acc_cols, t->row_info_cols, static_cast<size_t>(nnz));
             else p->acc_cols.alloc(1);
             p->gen.release();
+            p->gen_tab.release();
+            x.gen_tab = nullptr;
             x.acc_offsets = p->acc_off.p;
             x.acc_cols = p->acc_cols.p;
             x.gen_words = nullptr;
@@ -592,9 +594,28 @@ int sicc_pipe_upload_tx_tables(unsigned long long handle, const sicc_pipe_tx_tab
                 for (int j = 0; j < n; ++j)
                     if (t->generator_kn[static_cast<size_t>(r) * n + j] & 1u) words[static_cast<size_t>(r) * gw + j / 32] |= 1u << (j % 32);
             upload(p->gen, words.data(), words.size());
+            // byte tables: entry (g, e) = XOR of rows 8g + b for the set bits b of e (when they fit in 256 MB)
+            const int groups = (k + 7) / 8;
+            const size_t tab_words = static_cast<size_t>(groups) * 256 * gw;
+            if (tab_words * 4 <= (static_cast<size_t>(256) << 20)) {
+                std::vector<uint32_t> tab(tab_words, 0u);
+                for (int g = 0; g < groups; ++g)
+                    for (int e = 1; e < 256; ++e) {
+                        const int b = __builtin_ctz(static_cast<unsigned>(e));
+                        uint32_t* dst = &tab[(static_cast<size_t>(g) * 256 + e) * gw];
+                        const uint32_t* prev = &tab[(static_cast<size_t>(g) * 256 + (e & (e - 1))) * gw];
+                        const int row = 8 * g + b;
+                        for (int w = 0; w < gw; ++w)
+                            dst[w] = prev[w] ^ (row < k ? words[static_cast<size_t>(row) * gw + w] : 0u);
+                    }
+                upload(p->gen_tab, tab.data(), tab.size());
+            } else {
+                p->gen_tab.release();
+            }
             p->acc_off.release();
             p->acc_cols.release();
             x.gen_words = p->gen.p;
+            x.gen_tab = p->gen_tab.p;
             x.gen_stride = gw;
             x.acc_offsets = nullptr;
             x.acc_cols = nullptr;
