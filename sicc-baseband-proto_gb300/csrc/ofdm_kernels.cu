@@ -95,6 +95,231 @@ __device__ __forceinline__ float fine_metric(const float2* __restrict__ x, const
     return (cr * cr + ci * ci) / fmaxf(eng * pre_energy, 1e-18f);
 }
 
+// Shared-memory working set of a frame search by one CTA.
+struct SyncShared {
+    float2* win;      // [kSyncPass + pre_len] the pass's samples
+    float* metric;    // [kSyncPass] coarse metric
+    float4* chunk;    // [kSyncThreads] window sums at chunk starts: P.re, P.im, E1, E2
+    float* memo;      // [kSyncPass + 2 * kMaxRadius] fine metric around crossings
+    float* red;       // [4][kSyncThreads / 32] reductions
+    float* rmetric;   // [kMaxRefine] mode-1 refinement
+    int* s_key;       // [kSyncThreads / 32]
+    PassResult* s_res;
+};
+
+__device__ __forceinline__ SyncShared sync_shared(unsigned char* smem_raw, int pre_len, float* red, float* rmetric,
+                                                  int* s_key, PassResult* s_res)
+{
+    SyncShared sh;
+    sh.win = reinterpret_cast<float2*>(smem_raw);
+    sh.metric = reinterpret_cast<float*>(sh.win + kSyncPass + pre_len);
+    sh.chunk = reinterpret_cast<float4*>(sh.metric + kSyncPass);
+    sh.memo = reinterpret_cast<float*>(sh.chunk + kSyncThreads);
+    sh.red = red;
+    sh.rmetric = rmetric;
+    sh.s_key = s_key;
+    sh.s_res = s_res;
+    return sh;
+}
+
+// One pass of the frame search over candidates [4352 pass, 4352 (pass + 1)) of x
+// (avail samples, limit candidates), by the whole CTA.  Mode 0: *sh.s_res takes the
+// pass's earliest successful crossing (key stays INT_MAX when none); mode 1: the
+// pass maximum is folded into *sh.s_res.  Ends with a barrier.
+__device__ void sync_scan_pass(const float2* __restrict__ x, int avail, int limit, int pass,
+                               const float2* __restrict__ preamble, const SyncParams& p, const SyncShared& sh)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int L = p.half_len, pre = p.pre_len, R = p.radius;
+    const int base = pass * kSyncPass;
+    const int span = min(kSyncPass + pre, avail - base);
+    for (int i = tid; i < kSyncPass + pre; i += kSyncThreads) sh.win[i] = (i < span) ? x[base + i] : make_float2(0.f, 0.f);
+    __syncthreads();
+    // window sums at chunk starts, one warp per chunk
+    for (int t = warp; t < kSyncThreads; t += kSyncThreads / 32) {
+        const int d0 = t * kSyncChunk;
+        float pr = 0.f, pi = 0.f, e1 = 0.f, e2 = 0.f;
+        for (int i = lane; i < L; i += 32) {
+            const float2 a = sh.win[d0 + i], b = sh.win[d0 + i + L];
+            const float2 c = cmulconj(b, a);  // conj(a) * b
+            pr += c.x;
+            pi += c.y;
+            e1 += cnorm(a);
+            e2 += cnorm(b);
+        }
+        pr = warp_sum(pr);
+        pi = warp_sum(pi);
+        e1 = warp_sum(e1);
+        e2 = warp_sum(e2);
+        if (lane == 0) sh.chunk[t] = make_float4(pr, pi, e1, e2);
+    }
+    __syncthreads();
+    {
+        float4 w = sh.chunk[tid];
+        const int d0 = tid * kSyncChunk;
+        for (int c = 0; c < kSyncChunk; ++c) {
+            const int d = d0 + c;
+            const float den = fmaxf(w.z * w.w, 1e-18f);
+            sh.metric[d] = (base + d < limit) ? (w.x * w.x + w.y * w.y) / den : -1.0f;
+            const float2 x0 = sh.win[d], x1 = sh.win[d + L], x2 = sh.win[d + pre];
+            const float2 add = cmulconj(x2, x1), sub = cmulconj(x1, x0);
+            w.x += add.x - sub.x;
+            w.y += add.y - sub.y;
+            w.z += cnorm(x1) - cnorm(x0);
+            w.w += cnorm(x2) - cnorm(x1);
+        }
+    }
+    __syncthreads();
+    if (p.mode == 1) {
+        // maximum of the pass, first occurrence (strict >)
+        float bm = -1.0f;
+        int bd = 0x7fffffff;
+        for (int c = 0; c < kSyncChunk; ++c) {
+            const int d = tid * kSyncChunk + c;
+            const float m = sh.metric[d];
+            if (m > bm) { bm = m; bd = d; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const float om = __shfl_xor_sync(0xffffffffu, bm, o);
+            const int od = __shfl_xor_sync(0xffffffffu, bd, o);
+            if (om > bm || (om == bm && od < bd)) { bm = om; bd = od; }
+        }
+        if (lane == 0) { sh.red[warp] = bm; sh.red[8 + warp] = __int_as_float(bd); }
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 0; w < kSyncThreads / 32; ++w) {
+                const float m = sh.red[w];
+                const int d = __float_as_int(sh.red[8 + w]);
+                if (d == 0x7fffffff) continue;  // no valid candidate in that warp's chunks
+                if (m > sh.s_res->fine || (m == sh.s_res->fine && base + d < sh.s_res->key)) {
+                    sh.s_res->fine = m;
+                    sh.s_res->key = base + d;
+                }
+            }
+        }
+    } else {
+        // positions within +-R of a crossing of this pass: memo index i <-> sample x = base - R + i
+        const int mspan = kSyncPass + 2 * R;
+        {
+            const int seg = (mspan + kSyncThreads - 1) / kSyncThreads;
+            const int i0 = tid * seg, i1 = min(mspan, i0 + seg);
+            auto crossing = [&](int y) -> int {  // memo index y holds candidate d = y - R
+                const int d = y - R;
+                return (d >= 0 && d < kSyncPass && sh.metric[d] >= p.threshold) ? 1 : 0;
+            };
+            int cnt = 0;
+            if (i0 < i1)
+                for (int y = i0 - R; y <= i0 + R; ++y) cnt += crossing(y);
+            for (int i = i0; i < i1; ++i) {
+                const int xs = base - R + i;
+                sh.memo[i] = (cnt > 0 && xs >= 0 && xs <= avail - pre) ? -2.0f : -1.0f;
+                cnt += crossing(i + R + 1) - crossing(i - R);
+            }
+        }
+        __syncthreads();
+        for (int i = warp; i < mspan; i += kSyncThreads / 32) {
+            if (sh.memo[i] != -2.0f) continue;
+            const float m = fine_metric(x, sh.win, base, kSyncPass + pre, base - R + i, preamble, pre, p.pre_energy, lane);
+            if (lane == 0) sh.memo[i] = m;
+        }
+        __syncthreads();
+        // earliest crossing of the pass whose window maximum reaches the threshold
+        int first = 0x7fffffff, fstart = -1;
+        float fbm = 0.0f;
+        for (int c = 0; c < kSyncChunk; ++c) {
+            const int d = tid * kSyncChunk + c;
+            if (!(sh.metric[d] >= p.threshold)) continue;
+            const int cand = base + d;
+            const int lo = max(0, cand - R);
+            const int hi = min(avail - pre, cand + R);
+            float bm = 0.0f;
+            int bd = cand;
+            for (int dd = lo; dd <= hi; ++dd) {
+                const float m = sh.memo[dd - base + R];
+                if (m > bm) { bm = m; bd = dd; }
+            }
+            if (bm >= p.threshold) { first = d; fstart = bd; fbm = bm; break; }
+        }
+        const int wmin = __reduce_min_sync(0xffffffffu, static_cast<unsigned>(first));
+        if (lane == 0) sh.s_key[warp] = wmin;
+        __syncthreads();
+        int bmin = 0x7fffffff;
+        for (int w = 0; w < kSyncThreads / 32; ++w) bmin = min(bmin, sh.s_key[w]);
+        if (bmin != 0x7fffffff && first == bmin) {
+            sh.s_res->key = base + first;
+            sh.s_res->start = fstart;
+            sh.s_res->fine = fbm;
+            sh.s_res->coarse = sh.metric[first];
+                    }
+    }
+    __syncthreads();
+}
+
+// The record of a frame search from its resolved result `fin` (mode 1: refined
+// first), with the CFO of the start found; valid in thread 0.  All threads call it.
+__device__ SyncOut sync_finish(const float2* __restrict__ x, int avail, int limit, const PassResult fin,
+                               const float2* __restrict__ preamble, const SyncParams& p, const SyncShared& sh)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int L = p.half_len, pre = p.pre_len, R = p.radius;
+
+    SyncOut res{0, -1, 0.0f, 0.0f, 0.0f, -1};
+    if (p.mode == 0) {
+        if (fin.key != 0x7fffffff) {
+            res.coarse_start = fin.key;
+            res.coarse = fin.coarse >= 0.0f ? fin.coarse : 0.0f;
+            res.start = fin.start;
+            res.fine = fin.fine;
+            res.found = (p.frame_len > 0 && res.start + p.frame_len > avail) ? 2 : 1;
+        }
+    } else if (fin.key >= 0 && fin.fine >= p.threshold) {
+        const int cand = fin.key;
+        const int lo = max(0, cand - R);
+        const int hi = min(limit - 1, cand + R);
+        for (int dd = lo + warp; dd <= hi; dd += kSyncThreads / 32) {
+            const float m = fine_metric(x, sh.win, 0, 0, dd, preamble, pre, p.pre_energy, lane);
+            if (lane == 0) sh.rmetric[dd - lo] = m;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            float bm = 0.0f;
+            int bd = cand;
+            for (int dd = lo; dd <= hi; ++dd)
+                if (sh.rmetric[dd - lo] > bm) { bm = sh.rmetric[dd - lo]; bd = dd; }
+            sh.s_res->start = bd;
+            sh.s_res->fine = bm;
+        }
+        __syncthreads();
+        res.coarse_start = cand;
+        res.coarse = fin.fine;
+        res.fine = sh.s_res->fine;
+        if (sh.s_res->fine >= p.threshold) {
+            res.start = sh.s_res->start;
+            res.found = 1;
+        }
+    }
+
+    if (res.found == 1 || res.found == 2) {  // an incomplete frame also gets its CFO (for one-frame buffers)
+        const int s0 = res.start;
+        float ar = 0.f, ai = 0.f;
+        for (int i = tid; i < L; i += kSyncThreads) {
+            const float2 c = cmulconj(x[s0 + i + L], x[s0 + i]);  // conj(x[s0+i]) * x[s0+i+L]
+            ar += c.x;
+            ai += c.y;
+        }
+        ar = warp_sum(ar);
+        ai = warp_sum(ai);
+        if (lane == 0) { sh.red[16 + warp] = ar; sh.red[24 + warp] = ai; }
+        __syncthreads();
+        if (tid == 0) {
+            float sr = 0.f, si = 0.f;
+            for (int w = 0; w < kSyncThreads / 32; ++w) { sr += sh.red[16 + w]; si += sh.red[24 + w]; }
+            res.cfo_hz = atan2f(si, sr) * p.sample_rate / (2.0f * 3.14159265358979323846f * static_cast<float>(L));
+        }
+    }
+    return res;
+}
+
 // Frame search, one CTA per (pass, frame): pass q scans candidates
 // [4352 q, 4352 (q + 1)).  Within a pass every threshold crossing is refined
 // at once: the fine metric of each position within +-radius of any crossing is
@@ -114,25 +339,21 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const long lon
             SyncParams p, PassResult* __restrict__ pres, int* __restrict__ ticket, SyncOut* __restrict__ out)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2* win = reinterpret_cast<float2*>(smem_raw);                 // [kSyncPass + pre_len]
-    float* metric = reinterpret_cast<float*>(win + kSyncPass + p.pre_len);  // [kSyncPass]
-    float4* chunk = reinterpret_cast<float4*>(metric + kSyncPass);     // [kSyncThreads] P.re, P.im, E1, E2
-    float* memo = reinterpret_cast<float*>(chunk + kSyncThreads);       // [kSyncPass + 2 * kMaxRadius]
-    __shared__ float red[4][kSyncThreads / 32];
+    __shared__ float red[4 * (kSyncThreads / 32)];
     __shared__ float rmetric[kMaxRefine];
     __shared__ int s_key[kSyncThreads / 32];
     __shared__ PassResult s_res;
     __shared__ int s_flag;
+    const SyncShared sh = sync_shared(smem_raw, p.pre_len, red, rmetric, s_key, &s_res);
 
     // pass-major order: the first passes of all frames run first, so later
     // passes of a frame found early skip their scans
     const int pass = blockIdx.x / frames;
     const int f = blockIdx.x - pass * frames;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x;
     const float2* x = samples + (frame_off ? frame_off[f] : static_cast<long long>(f) * stride);
     const int avail = counts ? counts[f] : count;
-    const int L = p.half_len, pre = p.pre_len, R = p.radius;
-    int limit = avail - pre + 1;
+    int limit = avail - p.pre_len + 1;
     if (p.max_search > 0) limit = min(limit, p.max_search + 1);
     int* done = ticket + frames;
 
@@ -146,130 +367,9 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const long lon
     __syncthreads();
 
     const int base = pass * kSyncPass;
-    if (!s_flag && base < limit) {
-        const int span = min(kSyncPass + pre, avail - base);
-        for (int i = tid; i < kSyncPass + pre; i += kSyncThreads) win[i] = (i < span) ? x[base + i] : make_float2(0.f, 0.f);
-        __syncthreads();
-        // window sums at chunk starts, one warp per chunk
-        for (int t = warp; t < kSyncThreads; t += kSyncThreads / 32) {
-            const int d0 = t * kSyncChunk;
-            float pr = 0.f, pi = 0.f, e1 = 0.f, e2 = 0.f;
-            for (int i = lane; i < L; i += 32) {
-                const float2 a = win[d0 + i], b = win[d0 + i + L];
-                const float2 c = cmulconj(b, a);  // conj(a) * b
-                pr += c.x;
-                pi += c.y;
-                e1 += cnorm(a);
-                e2 += cnorm(b);
-            }
-            pr = warp_sum(pr);
-            pi = warp_sum(pi);
-            e1 = warp_sum(e1);
-            e2 = warp_sum(e2);
-            if (lane == 0) chunk[t] = make_float4(pr, pi, e1, e2);
-        }
-        __syncthreads();
-        {
-            float4 w = chunk[tid];
-            const int d0 = tid * kSyncChunk;
-            for (int c = 0; c < kSyncChunk; ++c) {
-                const int d = d0 + c;
-                const float den = fmaxf(w.z * w.w, 1e-18f);
-                metric[d] = (base + d < limit) ? (w.x * w.x + w.y * w.y) / den : -1.0f;
-                const float2 x0 = win[d], x1 = win[d + L], x2 = win[d + pre];
-                const float2 add = cmulconj(x2, x1), sub = cmulconj(x1, x0);
-                w.x += add.x - sub.x;
-                w.y += add.y - sub.y;
-                w.z += cnorm(x1) - cnorm(x0);
-                w.w += cnorm(x2) - cnorm(x1);
-            }
-        }
-        __syncthreads();
-        if (p.mode == 1) {
-            // maximum of the pass, first occurrence (strict >)
-            float bm = -1.0f;
-            int bd = 0x7fffffff;
-            for (int c = 0; c < kSyncChunk; ++c) {
-                const int d = tid * kSyncChunk + c;
-                const float m = metric[d];
-                if (m > bm) { bm = m; bd = d; }
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                const float om = __shfl_xor_sync(0xffffffffu, bm, o);
-                const int od = __shfl_xor_sync(0xffffffffu, bd, o);
-                if (om > bm || (om == bm && od < bd)) { bm = om; bd = od; }
-            }
-            if (lane == 0) { red[0][warp] = bm; red[1][warp] = __int_as_float(bd); }
-            __syncthreads();
-            if (tid == 0) {
-                for (int w = 0; w < kSyncThreads / 32; ++w) {
-                    const float m = red[0][w];
-                    const int d = __float_as_int(red[1][w]);
-                    if (d == 0x7fffffff) continue;  // no valid candidate in that warp's chunks
-                    if (m > s_res.fine || (m == s_res.fine && base + d < s_res.key)) {
-                        s_res.fine = m;
-                        s_res.key = base + d;
-                    }
-                }
-            }
-        } else {
-            // positions within +-R of a crossing of this pass: memo index i <-> sample x = base - R + i
-            const int mspan = kSyncPass + 2 * R;
-            {
-                const int seg = (mspan + kSyncThreads - 1) / kSyncThreads;
-                const int i0 = tid * seg, i1 = min(mspan, i0 + seg);
-                auto crossing = [&](int y) -> int {  // memo index y holds candidate d = y - R
-                    const int d = y - R;
-                    return (d >= 0 && d < kSyncPass && metric[d] >= p.threshold) ? 1 : 0;
-                };
-                int cnt = 0;
-                if (i0 < i1)
-                    for (int y = i0 - R; y <= i0 + R; ++y) cnt += crossing(y);
-                for (int i = i0; i < i1; ++i) {
-                    const int xs = base - R + i;
-                    memo[i] = (cnt > 0 && xs >= 0 && xs <= avail - pre) ? -2.0f : -1.0f;
-                    cnt += crossing(i + R + 1) - crossing(i - R);
-                }
-            }
-            __syncthreads();
-            for (int i = warp; i < mspan; i += kSyncThreads / 32) {
-                if (memo[i] != -2.0f) continue;
-                const float m = fine_metric(x, win, base, kSyncPass + pre, base - R + i, preamble, pre, p.pre_energy, lane);
-                if (lane == 0) memo[i] = m;
-            }
-            __syncthreads();
-            // earliest crossing of the pass whose window maximum reaches the threshold
-            int first = 0x7fffffff, fstart = -1;
-            float fbm = 0.0f;
-            for (int c = 0; c < kSyncChunk; ++c) {
-                const int d = tid * kSyncChunk + c;
-                if (!(metric[d] >= p.threshold)) continue;
-                const int cand = base + d;
-                const int lo = max(0, cand - R);
-                const int hi = min(avail - pre, cand + R);
-                float bm = 0.0f;
-                int bd = cand;
-                for (int dd = lo; dd <= hi; ++dd) {
-                    const float m = memo[dd - base + R];
-                    if (m > bm) { bm = m; bd = dd; }
-                }
-                if (bm >= p.threshold) { first = d; fstart = bd; fbm = bm; break; }
-            }
-            const int wmin = __reduce_min_sync(0xffffffffu, static_cast<unsigned>(first));
-            if (lane == 0) s_key[warp] = wmin;
-            __syncthreads();
-            int bmin = 0x7fffffff;
-            for (int w = 0; w < kSyncThreads / 32; ++w) bmin = min(bmin, s_key[w]);
-            if (bmin != 0x7fffffff && first == bmin) {
-                s_res.key = base + first;
-                s_res.start = fstart;
-                s_res.fine = fbm;
-                s_res.coarse = metric[first];
-                atomicMax(done + f, passes - pass);
-            }
-        }
-    }
+    if (!s_flag && base < limit) sync_scan_pass(x, avail, limit, pass, preamble, p, sh);
     __syncthreads();
+    if (tid == 0 && p.mode == 0 && s_res.key != 0x7fffffff) atomicMax(done + f, passes - pass);
 
     // publish this pass; the frame's last pass to finish resolves it
     if (tid == 0) {
@@ -303,63 +403,102 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const long lon
         s_res = best;
     }
     __syncthreads();
-    const PassResult fin = s_res;
-
-    SyncOut res{0, -1, 0.0f, 0.0f, 0.0f, -1};
-    if (p.mode == 0) {
-        if (fin.key != 0x7fffffff) {
-            res.coarse_start = fin.key;
-            res.coarse = fin.coarse >= 0.0f ? fin.coarse : 0.0f;
-            res.start = fin.start;
-            res.fine = fin.fine;
-            res.found = (p.frame_len > 0 && res.start + p.frame_len > avail) ? 2 : 1;
-        }
-    } else if (fin.key >= 0 && fin.fine >= p.threshold) {
-        const int cand = fin.key;
-        const int lo = max(0, cand - R);
-        const int hi = min(limit - 1, cand + R);
-        for (int dd = lo + warp; dd <= hi; dd += kSyncThreads / 32) {
-            const float m = fine_metric(x, win, 0, 0, dd, preamble, pre, p.pre_energy, lane);
-            if (lane == 0) rmetric[dd - lo] = m;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            float bm = 0.0f;
-            int bd = cand;
-            for (int dd = lo; dd <= hi; ++dd)
-                if (rmetric[dd - lo] > bm) { bm = rmetric[dd - lo]; bd = dd; }
-            s_res.start = bd;
-            s_res.fine = bm;
-        }
-        __syncthreads();
-        res.coarse_start = cand;
-        res.coarse = fin.fine;
-        res.fine = s_res.fine;
-        if (s_res.fine >= p.threshold) {
-            res.start = s_res.start;
-            res.found = 1;
-        }
-    }
-
-    if (res.found == 1 || res.found == 2) {  // an incomplete frame also gets its CFO (for one-frame buffers)
-        const int s0 = res.start;
-        float ar = 0.f, ai = 0.f;
-        for (int i = tid; i < L; i += kSyncThreads) {
-            const float2 c = cmulconj(x[s0 + i + L], x[s0 + i]);  // conj(x[s0+i]) * x[s0+i+L]
-            ar += c.x;
-            ai += c.y;
-        }
-        ar = warp_sum(ar);
-        ai = warp_sum(ai);
-        if (lane == 0) { red[2][warp] = ar; red[3][warp] = ai; }
-        __syncthreads();
-        if (tid == 0) {
-            float sr = 0.f, si = 0.f;
-            for (int w = 0; w < kSyncThreads / 32; ++w) { sr += red[2][w]; si += red[3][w]; }
-            res.cfo_hz = atan2f(si, sr) * p.sample_rate / (2.0f * 3.14159265358979323846f * static_cast<float>(L));
-        }
-    }
+    const SyncOut res = sync_finish(x, avail, limit, s_res, preamble, p, sh);
     if (tid == 0) out[f] = res;
+}
+
+// Frame extraction over one window (one CTA): the receive loop's sequence of
+// searches, each over [base, base + window) with the tracking or acquisition
+// window, the earliest crossing found by scanning passes in order (mode 0),
+// then the miss / late-peak / incomplete rules of extract_device; a found frame
+// is copied into the next free pool slot and the search continues after it.
+__global__ void __launch_bounds__(kSyncThreads)
+ingest_extract_kernel(const float2* __restrict__ window, int n, const float2* __restrict__ preamble, SyncParams p,
+                      IngestParams ip, const int* __restrict__ slots, float2* __restrict__ pool,
+                      IngestRecord* __restrict__ rec, IngestState* __restrict__ state)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float red[4 * (kSyncThreads / 32)];
+    __shared__ float rmetric[kMaxRefine];
+    __shared__ int s_key[kSyncThreads / 32];
+    __shared__ PassResult s_res;
+    __shared__ SyncOut s_out;
+    __shared__ IngestState s_st;
+    const SyncShared sh = sync_shared(smem_raw, p.pre_len, red, rmetric, s_key, &s_res);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        s_st = *state;
+        s_st.base = 0;
+        s_st.frames = 0;
+    }
+    __syncthreads();
+    while (s_st.frames < ip.max_frames) {
+        const int base = s_st.base;
+        const int available = n - base;
+        if (available < p.pre_len) break;
+        const int count = min(available, s_st.tracking ? ip.track_window : ip.acq_window);
+        const float2* x = window + base;
+        const int limit = count - p.pre_len + 1;
+        if (tid == 0) {
+            s_res.key = 0x7fffffff;
+            s_res.start = -1;
+            s_res.fine = -1.0f;
+            s_res.coarse = 0.0f;
+        }
+        __syncthreads();
+        for (int pass = 0; pass * kSyncPass < limit; ++pass) {  // the earliest success ends the search
+            sync_scan_pass(x, count, limit, pass, preamble, p, sh);
+            if (s_res.key != 0x7fffffff) break;
+        }
+        const SyncOut r = sync_finish(x, count, limit, s_res, preamble, p, sh);
+        if (tid == 0) s_out = r;
+        __syncthreads();
+        const SyncOut res = s_out;
+        const bool late = s_st.tracking && ip.late_threshold > 0.0f && res.start > ip.strict_window &&
+                          res.fine < ip.late_threshold;
+        int outcome = 0;  // 0 miss, 1 incomplete, 2 no pool slot, 3 found
+        if (res.found == 0 || res.fine < p.threshold || late) outcome = 0;
+        else if (res.start + ip.frame_len > available) outcome = 1;
+        else if (s_st.frames >= ip.free_slots) outcome = 2;
+        else outcome = 3;
+        if (outcome == 3) {  // copy the frame into its pool slot
+            float2* dst = pool + static_cast<size_t>(slots[s_st.frames]) * ip.frame_len;
+            const float2* src = x + res.start;
+            for (int i = tid; i < ip.frame_len; i += kSyncThreads) dst[i] = src[i];
+        }
+        __syncthreads();
+        if (tid == 0) {
+            if (outcome == 0) {
+                if (s_st.tracking) {
+                    ++s_st.tracking_miss;
+                    s_st.tracking = 0;
+                } else {
+                    ++s_st.miss;
+                }
+            } else if (outcome == 1) {
+                ++s_st.incomplete;
+            } else if (outcome == 2) {
+                s_st.base = base + res.start + ip.frame_len;
+                ++s_st.miss;
+                ++s_st.pool_exhausted;
+            } else {
+                IngestRecord& o = rec[s_st.frames];
+                o.slot = slots[s_st.frames];
+                o.start = base + res.start;
+                o.peak = res.fine;
+                o.cfo_hz = res.cfo_hz;
+                ++s_st.found;
+                s_st.skipped_samples += static_cast<unsigned long long>(res.start);
+                if (static_cast<unsigned long long>(res.start) > s_st.max_start) s_st.max_start = res.start;
+                s_st.tracking = 1;
+                s_st.base = base + res.start + ip.frame_len;
+                ++s_st.frames;
+            }
+        }
+        __syncthreads();
+        if (outcome != 3) break;
+    }
+    if (tid == 0) *state = s_st;
 }
 
 namespace {
@@ -903,6 +1042,22 @@ void launch_tx(const TxView& v, const uint8_t* info_bits, int frames, float2* fr
     const cudaError_t ferr = cudaFreeAsync(coded, st);
     check_cuda(err, "tx launch");
     check_cuda(ferr, "cudaFreeAsync(tx)");
+}
+
+void launch_ingest_extract(const float2* window, int n, const float2* preamble, const SyncParams& sp,
+                           const IngestParams& ip, const int* slots, float2* pool, IngestRecord* rec,
+                           IngestState* state, cudaStream_t st)
+{
+    const size_t smem = static_cast<size_t>(kSyncPass + sp.pre_len) * sizeof(float2) +
+                        static_cast<size_t>(kSyncPass) * sizeof(float) + kSyncThreads * sizeof(float4) +
+                        static_cast<size_t>(kSyncPass + 2 * kMaxRadius) * sizeof(float);
+    if (smem > 200 * 1024) throw InvalidArgument("preamble too long for the sync kernel");
+    if (sp.radius > kMaxRadius || sp.radius < 0) throw InvalidArgument("refinement radius must be 0..511");
+    check_cuda(cudaFuncSetAttribute(ingest_extract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)),
+               "cudaFuncSetAttribute(ingest)");
+    ingest_extract_kernel<<<1, kSyncThreads, smem, st>>>(window, n, preamble, sp, ip, slots, pool, rec, state);
+    check_cuda(cudaGetLastError(), "ingest_extract_kernel launch");
 }
 
 }  // namespace sicc

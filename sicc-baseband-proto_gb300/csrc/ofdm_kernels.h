@@ -64,6 +64,37 @@ void launch_demod(const DemodView& v, const float2* samples, long long stride, c
                   float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta = 0,
                   const long long* frame_off = nullptr, const long long* llr_off = nullptr);
 
+// Device side of the real-time ingest: the frame-extraction loop of the receive
+// path (GpuRxSyncExtractor::extract_device, uhd_ldpc_ofdm_link.cpp:6901-6979, as the
+// RX loop drives it, :8549-8567) over one window of samples.
+struct IngestState {
+    int tracking;  // in: sync state (1 tracking, 0 acquisition); out: state after the loop
+    int base;      // out: samples of the window used (start of the next search)
+    int frames;    // out: frames extracted
+    int pad;
+    unsigned long long found, miss, tracking_miss, incomplete, skipped_samples, max_start, pool_exhausted;
+};
+struct IngestRecord {
+    int slot;      // pool slot holding the frame
+    int start;     // first sample of the frame in the window
+    float peak;    // fine correlation metric
+    float cfo_hz;
+};
+struct IngestParams {
+    int frame_len;       // samples per frame
+    int acq_window;      // acquisition search: max(frame_len, max_buffered_frames * frame_len)
+    int track_window;    // tracking search: preamble + max(256, sync_tracking_window)
+    int strict_window;   // late peaks beyond max(256, 4 cp) need the late threshold
+    float late_threshold;// 0: off
+    int max_frames;
+    int free_slots;      // pool slots available (slot list)
+};
+// One CTA: extract frames one after another from window[0, n) into pool slots
+// (pool + slots[i] * frame_len), records to `rec`, state in/out.
+void launch_ingest_extract(const float2* window, int n, const float2* preamble, const SyncParams& sp,
+                           const IngestParams& ip, const int* slots, float2* pool, IngestRecord* rec,
+                           IngestState* state, cudaStream_t st);
+
 // Transmit tables resident on the device (the TX chain of gpu_ofdm_pipeline.cu:129-343, 922-1075).
 struct TxView {
     int nfft, cp, num_symbols, active_sc, bits_per_symbol, pre_len;

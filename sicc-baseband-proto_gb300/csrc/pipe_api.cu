@@ -4,11 +4,15 @@
 // a caller-managed ring of slots; every synchronous call waits for its slot's
 // stream before returning; returned device LLRs stay valid until the slot is
 // reused.
+#include "../../include/sicc_ingest.h"
 #include "../../include/sicc_pipe.h"
 #include "ofdm_kernels.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -709,6 +713,361 @@ int sicc_pipe_tx_batch(unsigned long long handle, const unsigned char* device_in
         cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
         launch_tx(p->txv, device_info_bits, frames, reinterpret_cast<float2*>(device_frames), frequency_noise_var,
                   noise_seed, st);
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+}  // extern "C"
+
+namespace sicc {
+namespace {
+
+// Real-time ingest: device IQ ring (mirrored tail of `mirror` samples, so any
+// window of up to `mirror` samples from any read position is contiguous), a
+// leased frame pool, and the extraction loop of the receive path.
+struct Ingest {
+    std::shared_ptr<Pipe> pipe;
+    sicc_ingest_config_t cfg{};
+    int frame_samples = 0;
+    long long cap = 0, mirror = 0;
+    Buf<float2> ring;  // [cap + mirror]
+    Buf<float2> pool;  // [pool_frames][frame_samples]
+    Buf<int> d_slots;
+    Buf<IngestRecord> d_rec;
+    Buf<IngestState> d_state;
+    IngestState* h_state = nullptr;  // pinned
+    IngestRecord* h_rec = nullptr;   // pinned
+    int* h_slots = nullptr;          // pinned
+    cudaStream_t copy_stream = nullptr, stream = nullptr;
+    cudaEvent_t pushed = nullptr;
+    long long read_pos = 0, size = 0, pos_index = 0;  // pos_index: stream index of ring[read_pos]
+    unsigned long long dropped = 0;
+    bool busy = false, tracking = false, closed = false;
+    std::deque<int> free_slots;
+    std::vector<char> leased;
+    IngestState acc{};
+    std::mutex mu, step_mu;
+    std::condition_variable cv;
+    ~Ingest()
+    {
+        if (stream) cudaStreamSynchronize(stream);
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
+        if (h_state) cudaFreeHost(h_state);
+        if (h_rec) cudaFreeHost(h_rec);
+        if (h_slots) cudaFreeHost(h_slots);
+        if (pushed) cudaEventDestroy(pushed);
+        if (stream) cudaStreamDestroy(stream);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
+    }
+    void consume(long long c)  // under mu
+    {
+        c = std::min(c, size);
+        read_pos = (read_pos + c) % cap;
+        size -= c;
+        pos_index += c;
+    }
+};
+
+std::map<unsigned long long, std::shared_ptr<Ingest>> g_ingests;
+unsigned long long g_next_ingest = 0x9100;
+
+std::shared_ptr<Ingest> get_ingest(unsigned long long h)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_ingests.find(h);
+    if (it == g_ingests.end()) throw InvalidArgument("invalid ingest handle");
+    return it->second;
+}
+
+}  // namespace
+}  // namespace sicc
+
+extern "C" {
+
+int sicc_ingest_create(unsigned long long pipe_handle, const sicc_ingest_config_t* config, unsigned long long* out_handle)
+{
+    return guarded([&] {
+        if (!config || !out_handle) throw InvalidArgument("null argument");
+        *out_handle = 0;
+        auto p = get(pipe_handle);
+        std::lock_guard<std::mutex> plock(p->mu);
+        require_tables(*p);
+        const sicc_ingest_config_t& c = *config;
+        if (c.buffered_max <= 0 || c.buffered_min < 0) throw InvalidArgument("buffered_max must be positive");
+        if (c.max_buffered_frames < 0 || c.sync_tracking_window < 0) throw InvalidArgument("invalid search windows");
+        auto g = std::make_shared<Ingest>();
+        g->pipe = p;
+        g->cfg = c;
+        g->cfg.pool_frames = std::max(c.pool_frames, 4);
+        g->frame_samples = p->frame_samples;
+        g->mirror = std::max<long long>(std::max(c.buffered_min, c.buffered_max), p->cfg.preamble_len);
+        g->cap = std::max<long long>(std::max<long long>(c.ring_samples, 4096), g->mirror);
+        check_cuda(cudaSetDevice(p->device), "cudaSetDevice");
+        g->ring.alloc(static_cast<size_t>(g->cap + g->mirror));
+        check_cuda(cudaMemset(g->ring.p, 0, static_cast<size_t>(g->cap + g->mirror) * sizeof(float2)), "zero ring");
+        g->pool.alloc(static_cast<size_t>(g->cfg.pool_frames) * g->frame_samples);
+        g->d_slots.alloc(static_cast<size_t>(g->cfg.pool_frames));
+        g->d_rec.alloc(static_cast<size_t>(g->cfg.pool_frames));
+        g->d_state.alloc(1);
+        check_cuda(cudaMallocHost(&g->h_state, sizeof(IngestState)), "cudaMallocHost(ingest)");
+        check_cuda(cudaMallocHost(&g->h_rec, sizeof(IngestRecord) * g->cfg.pool_frames), "cudaMallocHost(ingest)");
+        check_cuda(cudaMallocHost(&g->h_slots, sizeof(int) * g->cfg.pool_frames), "cudaMallocHost(ingest)");
+        check_cuda(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate(ingest)");
+        check_cuda(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking), "cudaStreamCreate(ingest)");
+        check_cuda(cudaEventCreateWithFlags(&g->pushed, cudaEventDisableTiming), "cudaEventCreate(ingest)");
+        g->leased.assign(static_cast<size_t>(g->cfg.pool_frames), 0);
+        for (int i = 0; i < g->cfg.pool_frames; ++i) g->free_slots.push_back(i);
+        std::lock_guard<std::mutex> lock(g_mu);
+        *out_handle = ++g_next_ingest;
+        g_ingests[*out_handle] = g;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_ingest_destroy(unsigned long long handle)
+{
+    return guarded([&] {
+        std::shared_ptr<Ingest> g;
+        {
+            std::lock_guard<std::mutex> lock(g_mu);
+            auto it = g_ingests.find(handle);
+            if (it == g_ingests.end()) throw InvalidArgument("invalid ingest handle");
+            g = it->second;
+            g_ingests.erase(it);
+        }
+        {
+            std::lock_guard<std::mutex> lock(g->mu);
+            g->closed = true;
+        }
+        g->cv.notify_all();
+        std::lock_guard<std::mutex> step(g->step_mu);  // a running step finishes first
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_ingest_push(unsigned long long handle, const float* host_iq, long long count)
+{
+    return guarded([&] {
+        auto g = get_ingest(handle);
+        if (count < 0) throw InvalidArgument("count must be >= 0");
+        if (!host_iq || count == 0) return CUDA_OSD_STATUS_OK;
+        const float2* src = reinterpret_cast<const float2*>(host_iq);
+        {
+            std::lock_guard<std::mutex> lock(g->mu);
+            if (g->closed) return CUDA_OSD_STATUS_OK;
+            check_cuda(cudaSetDevice(g->pipe->device), "cudaSetDevice");
+            if (count > g->cap) {  // only the newest cap samples can be kept
+                const long long skip = count - g->cap;
+                src += skip;
+                count = g->cap;
+                g->dropped += static_cast<unsigned long long>(skip);
+            }
+            if (g->size + count > g->cap) {
+                if (g->busy) {  // the oldest samples are being searched: the new ones that do not fit are lost
+                    const long long room = g->cap - g->size;
+                    g->dropped += static_cast<unsigned long long>(count - room);
+                    count = room;
+                } else {  // drop the oldest, as GpuOnlineIqBuffer::push
+                    const long long drop = g->size + count - g->cap;
+                    g->consume(drop);
+                    g->dropped += static_cast<unsigned long long>(drop);
+                }
+            }
+            long long write_pos = (g->read_pos + g->size) % g->cap;
+            long long remaining = count;
+            const float2* s2 = src;
+            while (remaining > 0) {
+                const long long n = std::min(remaining, g->cap - write_pos);
+                check_cuda(cudaMemcpyAsync(g->ring.p + write_pos, s2, static_cast<size_t>(n) * sizeof(float2),
+                                           cudaMemcpyHostToDevice, g->copy_stream),
+                           "copy RX samples to the device ring");
+                if (write_pos < g->mirror) {  // the mirrored tail repeats the ring's first samples
+                    const long long m = std::min(n, g->mirror - write_pos);
+                    check_cuda(cudaMemcpyAsync(g->ring.p + g->cap + write_pos, s2, static_cast<size_t>(m) * sizeof(float2),
+                                               cudaMemcpyHostToDevice, g->copy_stream),
+                               "copy RX samples to the ring tail");
+                }
+                s2 += n;
+                remaining -= n;
+                write_pos = (write_pos + n) % g->cap;
+            }
+            check_cuda(cudaEventRecord(g->pushed, g->copy_stream), "cudaEventRecord(ingest push)");
+            g->size += count;
+        }
+        g->cv.notify_one();
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_ingest_step(unsigned long long handle, int max_frames, int timeout_ms, sicc_ingest_frame_t* out_frames,
+                     int* out_count)
+{
+    return guarded([&] {
+        auto g = get_ingest(handle);
+        if (!out_count || (max_frames > 0 && !out_frames)) throw InvalidArgument("null argument");
+        *out_count = 0;
+        std::lock_guard<std::mutex> step(g->step_mu);
+        Pipe& p = *g->pipe;
+        const int F = g->frame_samples;
+        long long window = 0, n = 0, w_index = 0;
+        bool latest = false;
+        int nslots = 0;
+        IngestState st{};
+        {
+            std::unique_lock<std::mutex> lock(g->mu);
+            latest = g->size > g->cap * 3 / 4;
+            if (latest) {  // pop_latest_device (L:7754-7766): keep the newest buffered_max, restart acquisition
+                if (g->size > g->cfg.buffered_max) {
+                    const long long drop = g->size - g->cfg.buffered_max;
+                    g->consume(drop);
+                    g->dropped += static_cast<unsigned long long>(drop);
+                }
+                g->tracking = false;
+                n = g->size;
+            } else {  // peek_batch_device (L:7721-7739)
+                g->cv.wait_for(lock, std::chrono::milliseconds(std::max(timeout_ms, 0)),
+                               [&] { return g->closed || g->size >= g->cfg.buffered_min; });
+                n = std::min<long long>(g->size, std::max(g->cfg.buffered_min, g->cfg.buffered_max));
+            }
+            if (n == 0) return CUDA_OSD_STATUS_OK;
+            window = g->read_pos;
+            w_index = g->pos_index;
+            g->busy = true;
+            nslots = std::min(static_cast<int>(g->free_slots.size()), std::max(max_frames, 0));
+            for (int i = 0; i < nslots; ++i) g->h_slots[i] = g->free_slots[static_cast<size_t>(i)];
+            st.tracking = g->tracking ? 1 : 0;
+        }
+        *g->h_state = st;
+        IngestParams ip{};
+        ip.frame_len = F;
+        ip.acq_window = std::max(F, g->cfg.max_buffered_frames * F);
+        ip.track_window = p.cfg.preamble_len + std::max(256, g->cfg.sync_tracking_window);
+        ip.strict_window = std::max(256, 4 * p.cfg.cp);
+        ip.late_threshold = g->cfg.sync_late_peak_threshold;
+        ip.max_frames = std::max(max_frames, 0);
+        ip.free_slots = nslots;
+        try {
+            check_cuda(cudaSetDevice(p.device), "cudaSetDevice");
+            check_cuda(cudaStreamWaitEvent(g->stream, g->pushed, 0), "cudaStreamWaitEvent(ingest)");
+            if (nslots > 0)
+                check_cuda(cudaMemcpyAsync(g->d_slots.p, g->h_slots, sizeof(int) * nslots, cudaMemcpyHostToDevice, g->stream),
+                           "copy ingest slots");
+            check_cuda(cudaMemcpyAsync(g->d_state.p, g->h_state, sizeof(IngestState), cudaMemcpyHostToDevice, g->stream),
+                       "copy ingest state");
+            launch_ingest_extract(g->ring.p + window, static_cast<int>(n), p.preamble.p, p.sync_params(0), ip,
+                                  g->d_slots.p, g->pool.p, g->d_rec.p, g->d_state.p, g->stream);
+            check_cuda(cudaMemcpyAsync(g->h_state, g->d_state.p, sizeof(IngestState), cudaMemcpyDeviceToHost, g->stream),
+                       "copy ingest state back");
+            check_cuda(cudaStreamSynchronize(g->stream), "synchronize ingest step");
+        } catch (...) {
+            std::lock_guard<std::mutex> lock(g->mu);
+            g->busy = false;
+            throw;
+        }
+        const IngestState& r = *g->h_state;
+        if (r.frames > 0) {
+            check_cuda(cudaMemcpy(g->h_rec, g->d_rec.p, sizeof(IngestRecord) * r.frames, cudaMemcpyDeviceToHost),
+                       "copy ingest records");
+        }
+        std::lock_guard<std::mutex> lock(g->mu);
+        g->busy = false;
+        for (int i = 0; i < r.frames; ++i) {
+            const IngestRecord& rec = g->h_rec[i];
+            g->leased[static_cast<size_t>(rec.slot)] = 1;
+            g->free_slots.pop_front();  // the slots were taken in list order
+            sicc_ingest_frame_t& o = out_frames[i];
+            o.slot = rec.slot;
+            o.peak = rec.peak;
+            o.cfo_hz = rec.cfo_hz;
+            o.pad = 0;
+            o.position = w_index + rec.start;
+        }
+        *out_count = r.frames;
+        g->acc.found += r.found;
+        g->acc.miss += r.miss;
+        g->acc.tracking_miss += r.tracking_miss;
+        g->acc.incomplete += r.incomplete;
+        g->acc.skipped_samples += r.skipped_samples;
+        g->acc.max_start = std::max(g->acc.max_start, r.max_start);
+        g->acc.pool_exhausted += r.pool_exhausted;
+        g->tracking = r.tracking != 0;
+        if (latest) {
+            g->consume(n);  // the latest window was taken out of the ring
+        } else if (r.base > 0) {
+            g->consume(r.base);
+        } else if (n > F) {  // nothing found: keep one frame's worth, search again from acquisition
+            g->consume(n - F);
+            g->tracking = false;
+        }
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_ingest_frame_ptr(unsigned long long handle, int slot, const float** out_device_frame)
+{
+    return guarded([&] {
+        auto g = get_ingest(handle);
+        if (!out_device_frame) throw InvalidArgument("null argument");
+        if (slot < 0 || slot >= g->cfg.pool_frames) throw InvalidArgument("invalid pool slot");
+        *out_device_frame = reinterpret_cast<const float*>(g->pool.p + static_cast<size_t>(slot) * g->frame_samples);
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_ingest_pool(unsigned long long handle, const float** out_device_pool, int* out_frame_samples)
+{
+    return guarded([&] {
+        auto g = get_ingest(handle);
+        if (!out_device_pool || !out_frame_samples) throw InvalidArgument("null argument");
+        *out_device_pool = reinterpret_cast<const float*>(g->pool.p);
+        *out_frame_samples = g->frame_samples;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_ingest_release(unsigned long long handle, int slot)
+{
+    return guarded([&] {
+        auto g = get_ingest(handle);
+        std::lock_guard<std::mutex> lock(g->mu);
+        if (slot < 0 || slot >= g->cfg.pool_frames || !g->leased[static_cast<size_t>(slot)])
+            throw InvalidArgument("pool slot is not leased");
+        g->leased[static_cast<size_t>(slot)] = 0;
+        g->free_slots.push_back(slot);
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_ingest_stats(unsigned long long handle, sicc_ingest_stats_t* out)
+{
+    return guarded([&] {
+        auto g = get_ingest(handle);
+        if (!out) throw InvalidArgument("null argument");
+        std::lock_guard<std::mutex> lock(g->mu);
+        out->found = g->acc.found;
+        out->miss = g->acc.miss;
+        out->tracking_miss = g->acc.tracking_miss;
+        out->incomplete = g->acc.incomplete;
+        out->skipped_samples = g->acc.skipped_samples;
+        out->max_start = g->acc.max_start;
+        out->dropped_samples = g->dropped;
+        out->pool_exhausted = g->acc.pool_exhausted;
+        out->buffered = g->size;
+        out->tracking = g->tracking ? 1 : 0;
+        out->free_slots = static_cast<int>(g->free_slots.size());
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_ingest_close(unsigned long long handle)
+{
+    return guarded([&] {
+        auto g = get_ingest(handle);
+        {
+            std::lock_guard<std::mutex> lock(g->mu);
+            g->closed = true;
+        }
+        g->cv.notify_all();
         return CUDA_OSD_STATUS_OK;
     });
 }

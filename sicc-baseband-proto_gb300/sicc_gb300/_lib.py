@@ -137,9 +137,9 @@ def check(status: int, where: str) -> None:
 
 
 def ptr(x) -> int | None:
-    """Address of a numpy array or torch tensor (None passes through)."""
-    if x is None:
-        return None
+    """Address of a numpy array or torch tensor (None and raw addresses pass through)."""
+    if x is None or isinstance(x, int):
+        return x
     if hasattr(x, "data_ptr"):
         return x.data_ptr()
     return x.ctypes.data
