@@ -524,6 +524,82 @@ def run_ofdm_tx(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------ real-time ingest workload
+def run_ingest(args, rank, world):
+    """A continuous C3-PHY stream through the device ring: push 16,384-sample blocks, step after each."""
+    import torch
+    from sicc_gb300 import codes, ofdm
+    from sicc_gb300.ingest import Ingest
+    from sicc_gb300.pipeline import RxPipeline
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    t = ofdm.reference_tables(ofdm.OFDM_C3)
+    code = codes.ofdm_code()
+    blocks = t.coded_bits // code.n
+    fl = t.frame_len
+    frames = 96
+    G = np.ascontiguousarray(np.concatenate([np.eye(code.k, dtype=np.uint8), codes.gf2_parity_matrix(code)], 1))
+    pipe = RxPipeline(t, code.n, code.k, blocks, 1e-3, max_batch_frames=frames)
+    pipe.upload_tx_tables(generator_kn=G)
+    rng = np.random.default_rng(700 + rank)
+    info = torch.from_numpy(rng.integers(0, 2, size=(frames, blocks * code.k), dtype=np.uint8)).cuda()
+    d_fr = torch.empty((frames, fl), dtype=torch.complex64, device="cuda")
+    pipe.tx_batch(info, frames, d_fr, stream=torch.cuda.current_stream())
+    tx = d_fr.cpu().numpy()
+    # back-to-back frames with gaps inside the tracking window, AWGN and a 0.05-subcarrier offset
+    gaps = rng.integers(0, 200, size=frames)
+    x = np.concatenate([np.concatenate([tx[f], np.zeros(gaps[f], np.complex64)]) for f in range(frames)])
+    n = np.arange(x.size)
+    x = (x * np.exp(2j * np.pi * 0.05 / t.cfg.nfft * n)).astype(np.complex64)
+    x += (1e-3 * (rng.standard_normal(x.size) + 1j * rng.standard_normal(x.size))).astype(np.complex64)
+    host = torch.empty(x.size, dtype=torch.complex64, pin_memory=True)
+    host.numpy()[:] = x
+    block = 16384
+    reps = max(args.steps, 1)
+
+    def run_once():
+        ing = Ingest(pipe, ring_samples=1 << 20, pool_frames=64)
+        found = 0
+        for at in range(0, x.size, block):
+            ing.push(host[at: at + block])
+            for slot, _, _, _ in ing.step(timeout_ms=0):
+                ing.release(slot)
+                found += 1
+        st = ing.stats()
+        ing.close()
+        return found, st
+
+    for _ in range(args.warmup):
+        run_once()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        found, st = run_once()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    value = world * reps * x.size / wall / 1e6
+    line = {"metric": "Msample/s real-time ingest (device ring push + frame extraction), OFDM 16-QAM PHY",
+            "value": round(value, 3), "unit": "Msample/s", "n_gpus": world, "steps": reps, "warmup": args.warmup,
+            "ms_per_step": round(wall / reps * 1e3, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (GPU-transmitted frames, AWGN, CFO)",
+            "config": {"workload": "ofdm_ingest_1024_512", "frames": frames, "samples": int(x.size),
+                       "push_block": block, "ring_samples": 1 << 20, "pool_frames": 64,
+                       "real_time_msps": t.cfg.sample_rate / 1e6},
+            "frames_found": found, "stats": {k: int(v) for k, v in st.items()},
+            "x_real_time": round(value / (t.cfg.sample_rate / 1e6), 2),
+            "gpu_launches": int(reps * np.ceil(x.size / block)), "clocks": clk, "roofline": None,
+            "e2e": {"value": round(value, 3), "unit": "Msample/s", "h2d_bytes_per_step": int(x.size * 8),
+                    "d2h_bytes_per_step": int(found * 16)},
+            "cpu_baseline": None}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # --------------------------------------------------- mixed-code batched workload
 def run_mixed(args, rank, world):
     """100,000 codewords of 15 codes in one persistent launch, against one launch per request."""
@@ -854,8 +930,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=BATCH, help="frames per batch (profiling runs only)")
     ap.add_argument("--resident", type=int, default=RESIDENT_BATCHES, help="resident batches per Eb/N0")
-    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "ofdm_rx_1024_512", "ofdm_tx_1024_512", "mixed_100k",
-                                                        "serve_mixed"])
+    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "ofdm_rx_1024_512", "ofdm_tx_1024_512", "ofdm_ingest_1024_512",
+                                                        "mixed_100k", "serve_mixed"])
     ap.add_argument("--serve-requests", type=int, default=1500)
     ap.add_argument("--serve-batch", type=int, default=16384, help="codewords per server launch")
     ap.add_argument("--serve-inflight", type=int, default=2, help="batches overlapping on the device")
@@ -872,6 +948,8 @@ def main():
         run_ofdm(args, rank, world)
     elif args.workload == "ofdm_tx_1024_512":
         run_ofdm_tx(args, rank, world)
+    elif args.workload == "ofdm_ingest_1024_512":
+        run_ingest(args, rank, world)
     elif args.workload == "mixed_100k":
         run_mixed(args, rank, world)
     elif args.workload == "serve_mixed":

@@ -135,8 +135,10 @@ __device__ void sync_scan_pass(const float2* __restrict__ x, int avail, int limi
     const int span = min(kSyncPass + pre, avail - base);
     for (int i = tid; i < kSyncPass + pre; i += kSyncThreads) sh.win[i] = (i < span) ? x[base + i] : make_float2(0.f, 0.f);
     __syncthreads();
+    // chunks holding candidates below the limit (the rest only hold -1)
+    const int nchunks = min(kSyncThreads, (limit - base + kSyncChunk - 1) / kSyncChunk);
     // window sums at chunk starts, one warp per chunk
-    for (int t = warp; t < kSyncThreads; t += kSyncThreads / 32) {
+    for (int t = warp; t < nchunks; t += kSyncThreads / 32) {
         const int d0 = t * kSyncChunk;
         float pr = 0.f, pi = 0.f, e1 = 0.f, e2 = 0.f;
         for (int i = lane; i < L; i += 32) {
@@ -154,7 +156,9 @@ __device__ void sync_scan_pass(const float2* __restrict__ x, int avail, int limi
         if (lane == 0) sh.chunk[t] = make_float4(pr, pi, e1, e2);
     }
     __syncthreads();
-    {
+    if (tid >= nchunks) {
+        for (int c = 0; c < kSyncChunk; ++c) sh.metric[tid * kSyncChunk + c] = -1.0f;
+    } else {
         float4 w = sh.chunk[tid];
         const int d0 = tid * kSyncChunk;
         for (int c = 0; c < kSyncChunk; ++c) {

@@ -733,10 +733,10 @@ struct Ingest {
     Buf<float2> ring;  // [cap + mirror]
     Buf<float2> pool;  // [pool_frames][frame_samples]
     Buf<int> d_slots;
-    Buf<IngestRecord> d_rec;
-    Buf<IngestState> d_state;
-    IngestState* h_state = nullptr;  // pinned
-    IngestRecord* h_rec = nullptr;   // pinned
+    Buf<unsigned char> d_out;        // IngestState, then [pool_frames] IngestRecord: one readback
+    unsigned char* h_out = nullptr;  // pinned copy of d_out
+    IngestState* h_state = nullptr;  // in h_out
+    IngestRecord* h_rec = nullptr;   // in h_out
     int* h_slots = nullptr;          // pinned
     cudaStream_t copy_stream = nullptr, stream = nullptr;
     cudaEvent_t pushed = nullptr;
@@ -752,8 +752,7 @@ struct Ingest {
     {
         if (stream) cudaStreamSynchronize(stream);
         if (copy_stream) cudaStreamSynchronize(copy_stream);
-        if (h_state) cudaFreeHost(h_state);
-        if (h_rec) cudaFreeHost(h_rec);
+        if (h_out) cudaFreeHost(h_out);
         if (h_slots) cudaFreeHost(h_slots);
         if (pushed) cudaEventDestroy(pushed);
         if (stream) cudaStreamDestroy(stream);
@@ -807,10 +806,11 @@ int sicc_ingest_create(unsigned long long pipe_handle, const sicc_ingest_config_
         check_cuda(cudaMemset(g->ring.p, 0, static_cast<size_t>(g->cap + g->mirror) * sizeof(float2)), "zero ring");
         g->pool.alloc(static_cast<size_t>(g->cfg.pool_frames) * g->frame_samples);
         g->d_slots.alloc(static_cast<size_t>(g->cfg.pool_frames));
-        g->d_rec.alloc(static_cast<size_t>(g->cfg.pool_frames));
-        g->d_state.alloc(1);
-        check_cuda(cudaMallocHost(&g->h_state, sizeof(IngestState)), "cudaMallocHost(ingest)");
-        check_cuda(cudaMallocHost(&g->h_rec, sizeof(IngestRecord) * g->cfg.pool_frames), "cudaMallocHost(ingest)");
+        const size_t out_bytes = sizeof(IngestState) + sizeof(IngestRecord) * g->cfg.pool_frames;
+        g->d_out.alloc(out_bytes);
+        check_cuda(cudaMallocHost(&g->h_out, out_bytes), "cudaMallocHost(ingest)");
+        g->h_state = reinterpret_cast<IngestState*>(g->h_out);
+        g->h_rec = reinterpret_cast<IngestRecord*>(g->h_out + sizeof(IngestState));
         check_cuda(cudaMallocHost(&g->h_slots, sizeof(int) * g->cfg.pool_frames), "cudaMallocHost(ingest)");
         check_cuda(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate(ingest)");
         check_cuda(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking), "cudaStreamCreate(ingest)");
@@ -952,12 +952,15 @@ int sicc_ingest_step(unsigned long long handle, int max_frames, int timeout_ms, 
             if (nslots > 0)
                 check_cuda(cudaMemcpyAsync(g->d_slots.p, g->h_slots, sizeof(int) * nslots, cudaMemcpyHostToDevice, g->stream),
                            "copy ingest slots");
-            check_cuda(cudaMemcpyAsync(g->d_state.p, g->h_state, sizeof(IngestState), cudaMemcpyHostToDevice, g->stream),
+            IngestState* d_state = reinterpret_cast<IngestState*>(g->d_out.p);
+            IngestRecord* d_rec = reinterpret_cast<IngestRecord*>(g->d_out.p + sizeof(IngestState));
+            check_cuda(cudaMemcpyAsync(d_state, g->h_state, sizeof(IngestState), cudaMemcpyHostToDevice, g->stream),
                        "copy ingest state");
             launch_ingest_extract(g->ring.p + window, static_cast<int>(n), p.preamble.p, p.sync_params(0), ip,
-                                  g->d_slots.p, g->pool.p, g->d_rec.p, g->d_state.p, g->stream);
-            check_cuda(cudaMemcpyAsync(g->h_state, g->d_state.p, sizeof(IngestState), cudaMemcpyDeviceToHost, g->stream),
-                       "copy ingest state back");
+                                  g->d_slots.p, g->pool.p, d_rec, d_state, g->stream);
+            check_cuda(cudaMemcpyAsync(g->h_out, g->d_out.p, sizeof(IngestState) + sizeof(IngestRecord) * nslots,
+                                       cudaMemcpyDeviceToHost, g->stream),
+                       "copy ingest state and records back");
             check_cuda(cudaStreamSynchronize(g->stream), "synchronize ingest step");
         } catch (...) {
             std::lock_guard<std::mutex> lock(g->mu);
@@ -965,10 +968,6 @@ int sicc_ingest_step(unsigned long long handle, int max_frames, int timeout_ms, 
             throw;
         }
         const IngestState& r = *g->h_state;
-        if (r.frames > 0) {
-            check_cuda(cudaMemcpy(g->h_rec, g->d_rec.p, sizeof(IngestRecord) * r.frames, cudaMemcpyDeviceToHost),
-                       "copy ingest records");
-        }
         std::lock_guard<std::mutex> lock(g->mu);
         g->busy = false;
         for (int i = 0; i < r.frames; ++i) {
