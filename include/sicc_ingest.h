@@ -57,7 +57,9 @@ SICC_API int sicc_ingest_create(unsigned long long pipe_handle, const sicc_inges
 SICC_API int sicc_ingest_destroy(unsigned long long handle);
 /* GpuOnlineIqBuffer::push (L:7593-7630): copy host samples into the ring
  * (asynchronously; pinned memory overlaps), dropping the oldest samples when
- * it is full.  Thread-safe against sicc_ingest_step. */
+ * it is full.  Thread-safe against sicc_ingest_step; while a step searches
+ * the oldest samples in place, a push that does not fit drops its own newest
+ * samples instead (the reference searches a copy of the window). */
 SICC_API int sicc_ingest_push(unsigned long long handle, const float* host_iq, long long count);
 /* One step of the RX loop's device branch (L:8480-8567); frames found go to
  * out_frames[max_frames] (*out_count of them), each holding a pool slot until
