@@ -629,6 +629,11 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             const int c0 = cut_of(j0), c1 = cut_of(j1), c2 = cut_of(j2);
             const float r0 = j0 != INT_MAX ? s.rel[j0] : 0.0f, r1 = j1 != INT_MAX ? s.rel[j1] : 0.0f,
                         r2 = j2 != INT_MAX ? s.rel[j2] : 0.0f;
+            {  // the flipped positions' own sum (in position order) bounds the metric from below
+                const float lb = __fadd_rn(__fadd_rn(r0, r1), r2);
+                const unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(&s_best);
+                if (cur != ~0ull && lb > __uint_as_float(static_cast<unsigned>(cur >> 32))) continue;
+            }
             int fi = 0;  // flips added so far
             int ncut = c0;
             float nrel = r0;
