@@ -385,8 +385,7 @@ static void launch_layered_t(const LayeredView& cv, const BpParams& p, const BpI
 {
     int slot_floats = 0;
     const size_t smem = layered_smem_bytes(cv, slots, track_best, &slot_floats);
-    check_cuda(cudaFuncSetAttribute(bp_layered_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(smem)),
+    check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(bp_layered_kernel<D>), smem),
                "cudaFuncSetAttribute(bp_layered)");
     if (ctas <= 0) {
         int per_sm = 0;
@@ -440,8 +439,7 @@ void launch_bp_flooding(const FloodView& cv, const BpParams& p, const BpIO& io, 
     while (warps > 1 && flooding_smem_bytes(cv, warps, &slot_floats) > 160 * 1024) --warps;
     const size_t smem = flooding_smem_bytes(cv, warps, &slot_floats);
     if (smem > 227 * 1024) throw InvalidArgument("code too large for the shared-memory flooding kernel");
-    check_cuda(cudaFuncSetAttribute(bp_flooding_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(smem)),
+    check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(bp_flooding_kernel), smem),
                "cudaFuncSetAttribute(bp_flooding)");
     const int per_sm = std::max(1, static_cast<int>((227 * 1024) / std::max<size_t>(smem, 1)));
     int ctas = std::min(per_sm, 8) * device_sm_count();

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 
@@ -28,6 +29,21 @@ int device_sm_count()
     check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
     if (dev >= 0 && dev < 64) cache[dev] = sms;
     return sms;
+}
+
+cudaError_t grant_dynamic_smem(const void* kernel, size_t bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> granted;
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return err;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& g = granted[{kernel, dev}];
+    if (bytes <= g) return cudaSuccess;
+    err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+    if (err == cudaSuccess) g = bytes;
+    return err;
 }
 
 bool systematic_parity(int n, int m, const int* row_ptr, const int* col_ind, std::vector<uint64_t>& out,

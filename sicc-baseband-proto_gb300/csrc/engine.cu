@@ -63,7 +63,8 @@ struct MixedIO {
     int* work2;
     int* work1;
     const int* bounds;           // [2] end of the 4-warp units, end of the 2-warp units
-    float* best;                 // [warps][4][n_max] best-syndrome posteriors (global scratch)
+    float* best;                 // [warps][best_slots][n_max] best-syndrome posteriors (global scratch)
+    int best_slots;              // codewords a warp holds at once (32 / group of the narrowest code, >= 1)
     int n_max;
     float* osd_llr;              // compact rows of the codewords handed to OSD
     int* osd_index;              // [items] codeword of each row
@@ -301,7 +302,7 @@ __device__ void wide_phase(const MixedIO& io, float* smem_f, int warp_floats, in
     const int bar = (W == 4 ? 1 : 3) + g;
     float* app = smem_f + static_cast<size_t>(g * W) * warp_floats;
     const int gwarp0 = blockIdx.x * (blockDim.x >> 5) + g * W;
-    float* best = io.best + static_cast<size_t>(gwarp0) * 4 * io.n_max;
+    float* best = io.best + static_cast<size_t>(gwarp0) * io.best_slots * io.n_max;
     for (;;) {
         if (gl == 0) s_unit[g] = atomicAdd(counter, 1);
         group_sync(bar, G);
@@ -340,7 +341,7 @@ __device__ __forceinline__ void narrow_unit(const MixedIO& io, const CodeDesc& d
     float* r1 = app + n_pad;
     float* r2 = r1 + mp;
     unsigned* meta = reinterpret_cast<unsigned*>(r2 + mp);
-    float* best = io.best + (static_cast<size_t>(gwarp) * 4 + sub) * io.n_max;
+    float* best = io.best + (static_cast<size_t>(gwarp) * io.best_slots + sub) * io.n_max;
     int iter = 0, best_w = 0;
     if (active) {
         const float* src = io.llr + io.llr_off[cw];
@@ -464,7 +465,7 @@ struct Engine {
     int* d_osd_index = nullptr;
     float* d_osd_llr = nullptr;
     float* d_best = nullptr;
-    size_t best_warps = 0;
+    size_t best_floats = 0;
     bool dirty = true;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaStream_t side[kOsdHClasses - 1] = {};  // large-code OSD classes beside the first
@@ -580,8 +581,7 @@ void launch_mixed(Engine& e, const MixedIO& io, cudaStream_t st)
     if (static_cast<size_t>(warps) * wf * sizeof(float) > 200 * 1024) warps = 4;
     const size_t smem = static_cast<size_t>(warps) * wf * sizeof(float);
     if (smem > 227 * 1024) throw InvalidArgument("a registered code is too large for the mixed kernel");
-    check_cuda(cudaFuncSetAttribute(bp_mixed_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(smem)),
+    check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(bp_mixed_kernel<D>), smem),
                "cudaFuncSetAttribute(bp_mixed)");
     int ctas = e.ctas;
     if (ctas <= 0) {
@@ -592,14 +592,19 @@ void launch_mixed(Engine& e, const MixedIO& io, cudaStream_t st)
             per_sm = 1;
         ctas = per_sm * device_sm_count();
     }
-    const size_t need = static_cast<size_t>(ctas) * warps;
-    if (need > e.best_warps) {
+    // a warp holds one codeword of a wide code, or 32 / group codewords of a narrow one
+    int slots = 1;
+    for (const auto& c : e.codes)
+        if (c.desc.warps == 1) slots = std::max(slots, 32 / c.desc.group);
+    const size_t need = static_cast<size_t>(ctas) * warps * slots * static_cast<size_t>(e.n_max);
+    if (need > e.best_floats) {
         if (e.d_best) cudaFree(e.d_best);
-        check_cuda(cudaMalloc(&e.d_best, need * 4 * static_cast<size_t>(e.n_max) * sizeof(float)), "cudaMalloc(best)");
-        e.best_warps = need;
+        check_cuda(cudaMalloc(&e.d_best, need * sizeof(float)), "cudaMalloc(best)");
+        e.best_floats = need;
     }
     MixedIO m = io;
     m.best = e.d_best;
+    m.best_slots = slots;
     bp_mixed_kernel<D><<<ctas, warps * 32, smem, st>>>(m, wf);
     check_cuda(cudaGetLastError(), "bp_mixed_kernel launch");
 }

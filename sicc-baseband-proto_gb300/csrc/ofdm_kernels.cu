@@ -97,7 +97,8 @@ __device__ __forceinline__ float fine_metric(const float2* __restrict__ x, const
 
 // Shared-memory working set of a frame search by one CTA.
 struct SyncShared {
-    float2* win;      // [kSyncPass + pre_len] the pass's samples
+    float2* win;      // [kSyncPass + pre_len] the pass's samples (rounded up to an even count: the
+                      // float4 chunk sums after the metric stay 16-byte aligned)
     float* metric;    // [kSyncPass] coarse metric
     float4* chunk;    // [kSyncThreads] window sums at chunk starts: P.re, P.im, E1, E2
     float* memo;      // [kSyncPass + 2 * kMaxRadius] fine metric around crossings
@@ -112,7 +113,7 @@ __device__ __forceinline__ SyncShared sync_shared(unsigned char* smem_raw, int p
 {
     SyncShared sh;
     sh.win = reinterpret_cast<float2*>(smem_raw);
-    sh.metric = reinterpret_cast<float*>(sh.win + kSyncPass + pre_len);
+    sh.metric = reinterpret_cast<float*>(sh.win + ((kSyncPass + pre_len + 1) & ~1));
     sh.chunk = reinterpret_cast<float4*>(sh.metric + kSyncPass);
     sh.memo = reinterpret_cast<float*>(sh.chunk + kSyncThreads);
     sh.red = red;
@@ -536,7 +537,7 @@ void launch_sync(const float2* samples, long long stride, const int* counts, int
                  const long long* frame_off)
 {
     if (frames <= 0) return;
-    const size_t smem = static_cast<size_t>(kSyncPass + p.pre_len) * sizeof(float2) +
+    const size_t smem = static_cast<size_t>((kSyncPass + p.pre_len + 1) & ~1) * sizeof(float2) +
                         static_cast<size_t>(kSyncPass) * sizeof(float) + kSyncThreads * sizeof(float4) +
                         static_cast<size_t>(kSyncPass + 2 * kMaxRadius) * sizeof(float);
     if (smem > 200 * 1024) throw InvalidArgument("preamble too long for the sync kernel");
@@ -558,7 +559,7 @@ void launch_sync(const float2* samples, long long stride, const int* counts, int
     int* ticket = reinterpret_cast<int*>(static_cast<unsigned char*>(scratch) + res_bytes);
     cudaError_t err = cudaMemsetAsync(ticket, 0, ticket_bytes, st);
     if (err == cudaSuccess)
-        err = cudaFuncSetAttribute(sync_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        err = grant_dynamic_smem(reinterpret_cast<const void*>(sync_kernel), smem);
     if (err == cudaSuccess) {
         sync_kernel<<<static_cast<unsigned>(passes * frames), kSyncThreads, smem, st>>>(
             samples, stride, frame_off, counts, count, frames, static_cast<int>(passes), preamble, p, pres, ticket, out);
@@ -790,8 +791,7 @@ void launch_demod(const DemodView& v, const float2* samples, long long stride, c
     }
     const size_t smem = (2 * static_cast<size_t>(v.nfft) + kMaxPilotsPerCta * static_cast<size_t>(v.active_sc)) *
                         sizeof(float2);
-    check_cuda(cudaFuncSetAttribute(demod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
-               "cudaFuncSetAttribute(demod)");
+    check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(demod_kernel), smem), "cudaFuncSetAttribute(demod)");
     const dim3 grid(frames, (v.num_data + spc - 1) / spc);
     demod_kernel<<<grid, kDemodThreads, smem, st>>>(v, samples, stride, sync, llr, llr_stride, spc, frame_off,
                                                     llr_off);
@@ -1037,7 +1037,7 @@ void launch_tx(const TxView& v, const uint8_t* info_bits, int frames, float2* fr
         tx_encode_generator_kernel<<<ctas, kEncWarps * 32, 0, st>>>(v, info_bits, cb, codewords);
     cudaError_t err = cudaGetLastError();
     if (err == cudaSuccess)
-        err = cudaFuncSetAttribute(tx_symbol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        err = grant_dynamic_smem(reinterpret_cast<const void*>(tx_symbol_kernel), smem);
     if (err == cudaSuccess) {
         tx_symbol_kernel<<<dim3(v.num_symbols + 1, frames), kTxThreads, smem, st>>>(v, cb, frames_out, noise_var,
                                                                                     noise_seed);
@@ -1052,13 +1052,12 @@ void launch_ingest_extract(const float2* window, int n, const float2* preamble, 
                            const IngestParams& ip, const int* slots, float2* pool, IngestRecord* rec,
                            IngestState* state, cudaStream_t st)
 {
-    const size_t smem = static_cast<size_t>(kSyncPass + sp.pre_len) * sizeof(float2) +
+    const size_t smem = static_cast<size_t>((kSyncPass + sp.pre_len + 1) & ~1) * sizeof(float2) +
                         static_cast<size_t>(kSyncPass) * sizeof(float) + kSyncThreads * sizeof(float4) +
                         static_cast<size_t>(kSyncPass + 2 * kMaxRadius) * sizeof(float);
     if (smem > 200 * 1024) throw InvalidArgument("preamble too long for the sync kernel");
     if (sp.radius > kMaxRadius || sp.radius < 0) throw InvalidArgument("refinement radius must be 0..511");
-    check_cuda(cudaFuncSetAttribute(ingest_extract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(smem)),
+    check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(ingest_extract_kernel), smem),
                "cudaFuncSetAttribute(ingest)");
     ingest_extract_kernel<<<1, kSyncThreads, smem, st>>>(window, n, preamble, sp, ip, slots, pool, rec, state);
     check_cuda(cudaGetLastError(), "ingest_extract_kernel launch");

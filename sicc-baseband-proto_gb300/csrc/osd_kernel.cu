@@ -174,7 +174,8 @@ osd_kernel(OsdView ov0, OsdIO io)
                     col[o >> 6] = 1ull << (o & 63);
                 } else {
 #pragma unroll
-                    for (int x = 0; x < KW; ++x) col[x] = ov.pcols[static_cast<size_t>(o - k) * ov.kw + x];
+                    for (int x = 0; x < KW; ++x)  // the code's own words (kw <= KW)
+                        col[x] = x < ov.kw ? ov.pcols[static_cast<size_t>(o - k) * ov.kw + x] : 0ull;
                 }
             }
             // 32 x 32 bit transposes (butterfly over lane ^ j): lane j's bits a*32.. of its
@@ -267,12 +268,14 @@ osd_kernel(OsdView ov0, OsdIO io)
         // Pivots come in sorted-position order, so |llr| does not increase with the pivot
         // index t: t's rank is the count of later runs plus its place in its run of equal
         // |llr| (the run found by binary search).
+        // |llr| compared as bit patterns, the order the sort used (a permutation whatever the values)
+        auto relbits = [&](int t) -> unsigned { return __float_as_uint(s.rel_sorted[s.mrb_pos[t]]); };
         for (int t = lane; t < k; t += 32) {
-            const float bt = s.rel_sorted[s.mrb_pos[t]];
+            const unsigned bt = relbits(t);
             int lo = 0, hi = t;  // first index with |llr| <= bt
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
-                if (s.rel_sorted[s.mrb_pos[mid]] > bt) lo = mid + 1;
+                if (relbits(mid) > bt) lo = mid + 1;
                 else hi = mid;
             }
             const int a = lo;
@@ -280,7 +283,7 @@ osd_kernel(OsdView ov0, OsdIO io)
             hi = k;  // first index with |llr| < bt
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
-                if (s.rel_sorted[s.mrb_pos[mid]] < bt) hi = mid;
+                if (relbits(mid) < bt) hi = mid;
                 else lo = mid + 1;
             }
             const int r = (k - lo) + (t - a);

@@ -149,7 +149,6 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
     carve(lay, smem_raw, &s);
     __shared__ int s_rp[2][kRound];
     __shared__ int s_np[2], s_used[2], s_jstop[2];
-    __shared__ int s_nd;
     __shared__ unsigned long long s_best;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int TS = lay.ts;
@@ -249,7 +248,6 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
             const int e0 = hv.col_ptr[c];
             colinfo[j] = (e0 << 8) | (hv.col_ptr[c + 1] - e0);
         }
-        if (tid == 0) s_nd = 0;
         __syncthreads();
 
         // ---- 3. Gauss-Jordan scan of H's columns in increasing reliability ----
@@ -518,7 +516,6 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                 j -= pused;
             }
         }
-        if (tid == 0) s_nd = nd;
         if (t < m) {  // H rank deficient: leave the BP decision in place
             __syncthreads();
             continue;
@@ -530,14 +527,16 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
         // so the pool entry i is taken from the mirror image of i within its run of equal |llr|
         // (the runs found by binary search: |llr| is non-decreasing along that order).
         {
-            const int nd = s_nd, total = nd + jstop, want = hv.pool;
+            const int total = nd + jstop, want = hv.pool;  // nd and jstop: the same in every thread
             auto mrb_at = [&](int c) -> int { return c < nd ? s.mrb[c] : jstop - 1 - (c - nd); };
+            // |llr| compared as bit patterns, the order the sort used (a permutation whatever the values)
+            auto relbits = [&](int c) -> unsigned { return __float_as_uint(s.rel[mrb_at(c)]); };
             for (int i = tid; i < want; i += kThreads) {
-                const float ri = s.rel[mrb_at(i)];
+                const unsigned ri = relbits(i);
                 int lo = 0, hi = i;  // first index with |llr| >= ri
                 while (lo < hi) {
                     const int mid = (lo + hi) >> 1;
-                    if (s.rel[mrb_at(mid)] < ri) lo = mid + 1;
+                    if (relbits(mid) < ri) lo = mid + 1;
                     else hi = mid;
                 }
                 const int a = lo;
@@ -545,7 +544,7 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
                 hi = total;  // first index with |llr| > ri
                 while (lo < hi) {
                     const int mid = (lo + hi) >> 1;
-                    if (s.rel[mrb_at(mid)] > ri) hi = mid;
+                    if (relbits(mid) > ri) hi = mid;
                     else lo = mid + 1;
                 }
                 s.pool_j[i] = static_cast<int16_t>(mrb_at(a + lo - 1 - i));
@@ -752,8 +751,8 @@ void launch_osd_h_class(const OsdHBounds& bd, int mlo, int mhi, const OsdIO& io,
     l.nnzmax = bd.nnzmax;
     if (bd.nnzmax <= 0 || carve(l, nullptr, nullptr) > (smem <= per_sm_bytes ? per_sm_bytes : 227 * 1024)) l.nnzmax = 0;
     smem = carve(l, nullptr, nullptr);
-    check_cuda(cudaFuncSetAttribute(osd_h_kernel<kThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(smem)),
+    // the two 256-thread classes share this kernel with different sizes: the limit only grows
+    check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(osd_h_kernel<kThreads>), smem),
                "cudaFuncSetAttribute(osd_h)");
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, osd_h_kernel<kThreads>, kThreads, smem) != cudaSuccess ||

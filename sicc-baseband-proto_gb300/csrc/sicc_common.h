@@ -29,6 +29,11 @@ const char* last_error();
 // Number of streaming multiprocessors on the current device (cached per device).
 int device_sm_count();
 
+// Raises a kernel's dynamic shared-memory limit on the current device to at
+// least `bytes`; never lowers it, so launches of the same kernel with other
+// sizes that are still queued on other streams keep their grant.
+cudaError_t grant_dynamic_smem(const void* kernel, size_t bytes);
+
 // ---------------------------------------------------------------------------
 // Device views shared by the kernels and their launchers.
 // ---------------------------------------------------------------------------
