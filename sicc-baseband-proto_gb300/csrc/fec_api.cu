@@ -248,6 +248,7 @@ struct StreamDecoder : Decoder {
         std::vector<unsigned> blocks;
         int count = 0;
         bool in_flight = false;
+        bool held = false;  // retired: its results wait in the ready queue, read in place
         cudaEvent_t done = nullptr;
         cudaEvent_t start = nullptr;
         ~Batch()
@@ -256,11 +257,19 @@ struct StreamDecoder : Decoder {
             if (start) cudaEventDestroy(start);
         }
     };
-    std::vector<std::unique_ptr<Batch>> batches;  // ring
+    // Ring of batches: two can decode while the caller fills the next one and still holds
+    // the results of the one before.
+    static constexpr int kRing = 4;
+    std::vector<std::unique_ptr<Batch>> batches;
     int filling = 0;
+    bool claimed = true;  // batches[filling] is free for new codewords
     std::deque<int> flight;  // batch ids in launch order
-    // Results of retired batches, handed out by poll in ranges.
+    // Results of retired batches, handed out by poll in ranges: read in place from the
+    // batch's pinned host buffers (batch >= 0), or from copies when the ring needed the
+    // batch again before the caller polled it (batch < 0).
     struct ReadySeg {
+        int batch = -1;
+        size_t count = 0;
         std::vector<uint8_t> info, used;
         std::vector<unsigned long long> ts, ids;
         std::vector<unsigned> blocks;
@@ -308,7 +317,7 @@ struct StreamDecoder : Decoder {
         scratch.alloc(max_batch, n, k);
         check_cuda(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate(copy)");
         check_cuda(cudaEventCreateWithFlags(&copied, cudaEventDisableTiming), "cudaEventCreate(copy)");
-        for (int i = 0; i < 3; ++i) {
+        for (int i = 0; i < kRing; ++i) {
             auto b = std::make_unique<Batch>();
             b->llr.alloc(static_cast<size_t>(max_batch) * n);
             b->info.alloc(static_cast<size_t>(max_batch) * k);
@@ -329,6 +338,7 @@ struct StreamDecoder : Decoder {
 
     void launch_filling()
     {
+        if (!claimed) return;
         Batch& b = *batches[filling];
         if (b.count == 0) return;
         check_cuda(cudaEventRecord(copied, copy_stream), "cudaEventRecord(copy)");
@@ -347,9 +357,45 @@ struct StreamDecoder : Decoder {
         b.in_flight = true;
         flight.push_back(filling);
         stats.decoded_batches += 1;
-        // next filling batch: wait for it if it is still in flight
+        // the next batch to fill; claimed by the next submit (by then the caller has usually
+        // polled its previous results)
         filling = (filling + 1) % static_cast<int>(batches.size());
+        claimed = !(batches[filling]->in_flight || batches[filling]->held);
+    }
+
+    // Frees batches[filling] for new codewords: waits for it if it is still decoding, copies
+    // its results out if the caller has not polled them yet.
+    void claim()
+    {
+        if (claimed) return;
         if (batches[filling]->in_flight) collect_until(filling);
+        if (batches[filling]->held) spill(filling);
+        claimed = true;
+    }
+
+    void release(Batch& b)
+    {
+        b.count = 0;
+        b.held = false;
+        b.ts.clear();  // capacity kept
+        b.ids.clear();
+        b.blocks.clear();
+    }
+
+    // Copies the unpolled results of held batch `id` into its ready segment and frees the batch.
+    void spill(int id)
+    {
+        Batch& b = *batches[id];
+        for (auto& sg : ready) {
+            if (sg.batch != id) continue;
+            sg.info.assign(b.h_info.p, b.h_info.p + static_cast<size_t>(b.count) * k);
+            sg.used.assign(b.h_used_osd.p, b.h_used_osd.p + b.count);
+            sg.ts = b.ts;
+            sg.ids = b.ids;
+            sg.blocks = b.blocks;
+            sg.batch = -1;
+        }
+        release(b);
     }
 
     // Moves the front in-flight batch to the ready queue.
@@ -361,11 +407,8 @@ struct StreamDecoder : Decoder {
         cudaEventElapsedTime(&ms, b.start, b.done);
         stats.total_decode_ms += ms;
         ReadySeg sg;
-        sg.info.assign(b.h_info.p, b.h_info.p + static_cast<size_t>(b.count) * k);
-        sg.used.assign(b.h_used_osd.p, b.h_used_osd.p + b.count);
-        sg.ts.swap(b.ts);
-        sg.ids.swap(b.ids);
-        sg.blocks.swap(b.blocks);
+        sg.batch = id;
+        sg.count = static_cast<size_t>(b.count);
         for (int i = 0; i < b.count; ++i) {
             stats.osd_fallback_codewords += b.h_used_osd.p[i] ? 1 : 0;
             stats.bp_success_codewords += b.h_success.p[i] ? 1 : 0;
@@ -374,14 +417,8 @@ struct StreamDecoder : Decoder {
         stats.decoded_codewords += static_cast<unsigned long long>(b.count);
         stats.average_batch_size = static_cast<double>(stats.decoded_codewords) /
                                    static_cast<double>(std::max<unsigned long long>(stats.decoded_batches, 1));
-        b.count = 0;
         b.in_flight = false;
-        b.ts.clear();
-        b.ids.clear();
-        b.blocks.clear();
-        b.ts.reserve(max_batch);
-        b.ids.reserve(max_batch);
-        b.blocks.reserve(max_batch);
+        b.held = true;
         flight.pop_front();
     }
 
@@ -411,10 +448,14 @@ struct StreamDecoder : Decoder {
         }
     }
 
-    unsigned long long pending() const { return static_cast<unsigned long long>(batches[filling]->count); }
+    unsigned long long pending() const
+    {
+        return claimed ? static_cast<unsigned long long>(batches[filling]->count) : 0ull;
+    }
 
     void maybe_launch()
     {
+        if (!claimed) return;
         Batch& b = *batches[filling];
         if (b.count <= 0) return;
         const uint64_t age = now_us() - (b.ts.empty() ? now_us() : b.ts.front());
@@ -435,6 +476,7 @@ struct StreamDecoder : Decoder {
         }
         last_arrival_us = now;
         while (done < count) {
+            claim();
             Batch& b = *batches[filling];
             const int take = std::min(count - done, max_batch - b.count);
             const size_t bytes = static_cast<size_t>(take) * n * sizeof(float);
@@ -442,10 +484,14 @@ struct StreamDecoder : Decoder {
                                        llrs + static_cast<size_t>(done) * n, bytes,
                                        device_ptr ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, copy_stream),
                        "copy submitted LLRs");
-            for (int i = 0; i < take; ++i) {
-                b.ts.push_back(ts ? ts[done + i] : now);
-                b.ids.push_back(ids ? ids[done + i] : 0);
-                b.blocks.push_back(blocks ? blocks[done + i] : static_cast<unsigned>(done + i));
+            if (ts) b.ts.insert(b.ts.end(), ts + done, ts + done + take);
+            else b.ts.insert(b.ts.end(), static_cast<size_t>(take), now);
+            if (ids) b.ids.insert(b.ids.end(), ids + done, ids + done + take);
+            else b.ids.insert(b.ids.end(), static_cast<size_t>(take), 0ull);
+            if (blocks) {
+                b.blocks.insert(b.blocks.end(), blocks + done, blocks + done + take);
+            } else {
+                for (int i = 0; i < take; ++i) b.blocks.push_back(static_cast<unsigned>(done + i));
             }
             b.count += take;
             done += take;
@@ -476,16 +522,24 @@ struct StreamDecoder : Decoder {
         int out = 0;
         while (out < max_cw && !ready.empty()) {
             ReadySeg& sg = ready.front();
-            const size_t take = std::min<size_t>(sg.ts.size() - sg.pos, static_cast<size_t>(max_cw - out));
-            if (out_info)
-                std::memcpy(out_info + static_cast<size_t>(out) * k, sg.info.data() + sg.pos * k, take * k);
-            if (out_ts) std::copy(sg.ts.begin() + sg.pos, sg.ts.begin() + sg.pos + take, out_ts + out);
-            if (out_ids) std::copy(sg.ids.begin() + sg.pos, sg.ids.begin() + sg.pos + take, out_ids + out);
-            if (out_blocks) std::copy(sg.blocks.begin() + sg.pos, sg.blocks.begin() + sg.pos + take, out_blocks + out);
-            if (out_used) std::copy(sg.used.begin() + sg.pos, sg.used.begin() + sg.pos + take, out_used + out);
+            Batch* b = sg.batch >= 0 ? batches[sg.batch].get() : nullptr;
+            const uint8_t* info = b ? b->h_info.p : sg.info.data();
+            const uint8_t* used = b ? b->h_used_osd.p : sg.used.data();
+            const unsigned long long* ts = b ? b->ts.data() : sg.ts.data();
+            const unsigned long long* ids = b ? b->ids.data() : sg.ids.data();
+            const unsigned* blocks = b ? b->blocks.data() : sg.blocks.data();
+            const size_t take = std::min<size_t>(sg.count - sg.pos, static_cast<size_t>(max_cw - out));
+            if (out_info) std::memcpy(out_info + static_cast<size_t>(out) * k, info + sg.pos * k, take * k);
+            if (out_ts) std::memcpy(out_ts + out, ts + sg.pos, take * sizeof(*ts));
+            if (out_ids) std::memcpy(out_ids + out, ids + sg.pos, take * sizeof(*ids));
+            if (out_blocks) std::memcpy(out_blocks + out, blocks + sg.pos, take * sizeof(*blocks));
+            if (out_used) std::memcpy(out_used + out, used + sg.pos, take);
             sg.pos += take;
             out += static_cast<int>(take);
-            if (sg.pos == sg.ts.size()) ready.pop_front();
+            if (sg.pos == sg.count) {
+                if (b) release(*b);
+                ready.pop_front();
+            }
         }
         if (ready.empty() && flight.empty() && pending() == 0) draining = false;
         stats.current_pending_codewords = pending();
