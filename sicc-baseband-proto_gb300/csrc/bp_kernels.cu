@@ -405,12 +405,15 @@ void launch_bp_layered(const LayeredView& cv, const BpParams& p, const BpIO& io,
 {
     if (io.count <= 0) return;
     const bool track_best = p.route_failures_to_osd && io.osd_llr != nullptr;
+    if (layered_needs_wide(cv, track_best)) {
+        launch_bp_layered_wide(cv, p, io, st);
+        return;
+    }
     const int step = std::max(1, 32 / cv.group);
     int slots = shape.slots_per_cta > 0 ? shape.slots_per_cta : layered_default_slots(cv, track_best);
     slots = std::max(step, slots - slots % step);
     if (slots * cv.group > kBpThreads) slots = kBpThreads / cv.group;
-    if (layered_smem_bytes(cv, slots, track_best, nullptr) > 227 * 1024)
-        throw InvalidArgument("code too large for the shared-memory layered kernel");
+    while (slots > step && layered_smem_bytes(cv, slots, track_best, nullptr) > 227 * 1024) slots -= step;
     check_cuda(cudaMemsetAsync(io.work_counter, 0, sizeof(int), st), "reset work counter");
     // the row loops are unrolled to D slots: the closest D above the code's row degree
     if (cv.maxdeg <= 6) launch_layered_t<6>(cv, p, io, slots, shape.ctas, track_best, st);
@@ -433,12 +436,15 @@ size_t flooding_smem_bytes(const FloodView& cv, int warps, int* slot_floats_out)
 void launch_bp_flooding(const FloodView& cv, const BpParams& p, const BpIO& io, cudaStream_t st)
 {
     if (io.count <= 0) return;
+    if (flooding_needs_wide(cv)) {
+        launch_bp_flooding_wide(cv, p, io, st);
+        return;
+    }
     const bool track_best = p.route_failures_to_osd && io.osd_llr != nullptr;
     int warps = kBpThreads / 32;
     int slot_floats = 0;
     while (warps > 1 && flooding_smem_bytes(cv, warps, &slot_floats) > 160 * 1024) --warps;
     const size_t smem = flooding_smem_bytes(cv, warps, &slot_floats);
-    if (smem > 227 * 1024) throw InvalidArgument("code too large for the shared-memory flooding kernel");
     check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(bp_flooding_kernel), smem),
                "cudaFuncSetAttribute(bp_flooding)");
     const int per_sm = std::max(1, static_cast<int>((227 * 1024) / std::max<size_t>(smem, 1)));

@@ -20,6 +20,15 @@ void launch_bp_layered(const LayeredView& cv, const BpParams& p, const BpIO& io,
 void launch_bp_flooding(const FloodView& cv, const BpParams& p, const BpIO& io, cudaStream_t st);
 size_t layered_smem_bytes(const LayeredView& cv, int slots, bool track_best, int* slot_floats_out);
 int layered_default_slots(const LayeredView& cv, bool track_best);
+size_t flooding_smem_bytes(const FloodView& cv, int warps, int* slot_floats_out);
+
+// Long codes whose state does not fit one CTA's shared memory (bp_wide.cu): one CTA per
+// codeword, state in an L2-sized global scratch block.  launch_bp_layered /
+// launch_bp_flooding hand such codes to these.
+bool layered_needs_wide(const LayeredView& cv, bool track_best);
+bool flooding_needs_wide(const FloodView& cv);
+void launch_bp_layered_wide(const LayeredView& cv, const BpParams& p, const BpIO& io, cudaStream_t st);
+void launch_bp_flooding_wide(const FloodView& cv, const BpParams& p, const BpIO& io, cudaStream_t st);
 
 // OSD over a device work list; `warps_per_cta`/`ctas` <= 0 take defaults.
 void launch_osd(const OsdView& ov, const OsdIO& io, int max_items, cudaStream_t st, int warps_per_cta = 0,

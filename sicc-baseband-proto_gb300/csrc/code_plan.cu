@@ -31,6 +31,26 @@ int device_sm_count()
     return sms;
 }
 
+cudaMemPool_t scratch_pool(int device)
+{
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    std::lock_guard<std::mutex> lock(mu);
+    if (device < 0 || device >= 64) throw InvalidArgument("device ordinal out of range");
+    if (!pools[device]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        cudaMemPool_t pool = nullptr;
+        check_cuda(cudaMemPoolCreate(&pool, &props), "cudaMemPoolCreate(scratch)");
+        uint64_t keep = UINT64_MAX;  // freed blocks stay in the pool for the next launch
+        check_cuda(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
+        pools[device] = pool;
+    }
+    return pools[device];
+}
+
 cudaError_t grant_dynamic_smem(const void* kernel, size_t bytes)
 {
     static std::mutex mu;

@@ -29,7 +29,6 @@
 #include <cfloat>
 
 #include <cstdint>
-#include <mutex>
 
 namespace sicc {
 
@@ -506,32 +505,6 @@ ingest_extract_kernel(const float2* __restrict__ window, int n, const float2* __
     if (tid == 0) *state = s_st;
 }
 
-namespace {
-
-// Stream-ordered pool for kernel scratch (sync pass results and tickets, TX coded bits), one per
-// device; freed blocks stay in the pool for the next launch.
-cudaMemPool_t sync_pool(int device)
-{
-    static std::mutex mu;
-    static cudaMemPool_t pools[64] = {};
-    std::lock_guard<std::mutex> lock(mu);
-    if (device < 0 || device >= 64) throw InvalidArgument("device ordinal out of range");
-    if (!pools[device]) {
-        cudaMemPoolProps props{};
-        props.allocType = cudaMemAllocationTypePinned;
-        props.location.type = cudaMemLocationTypeDevice;
-        props.location.id = device;
-        cudaMemPool_t pool = nullptr;
-        check_cuda(cudaMemPoolCreate(&pool, &props), "cudaMemPoolCreate(sync)");
-        uint64_t keep = UINT64_MAX;
-        check_cuda(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
-        pools[device] = pool;
-    }
-    return pools[device];
-}
-
-}  // namespace
-
 void launch_sync(const float2* samples, long long stride, const int* counts, int count, int frames,
                  const float2* preamble, const SyncParams& p, SyncOut* out, cudaStream_t st,
                  const long long* frame_off)
@@ -553,7 +526,7 @@ void launch_sync(const float2* samples, long long stride, const int* counts, int
     const size_t res_bytes = static_cast<size_t>(frames) * passes * sizeof(PassResult);
     const size_t ticket_bytes = static_cast<size_t>(2) * frames * sizeof(int);
     void* scratch = nullptr;
-    check_cuda(cudaMallocFromPoolAsync(&scratch, res_bytes + ticket_bytes, sync_pool(device), st),
+    check_cuda(cudaMallocFromPoolAsync(&scratch, res_bytes + ticket_bytes, scratch_pool(device), st),
                "cudaMallocFromPoolAsync(sync)");
     PassResult* pres = static_cast<PassResult*>(scratch);
     int* ticket = reinterpret_cast<int*>(static_cast<unsigned char*>(scratch) + res_bytes);
@@ -1027,7 +1000,7 @@ void launch_tx(const TxView& v, const uint8_t* info_bits, int frames, float2* fr
     int device = 0;
     check_cuda(cudaGetDevice(&device), "cudaGetDevice");
     void* coded = nullptr;
-    check_cuda(cudaMallocFromPoolAsync(&coded, static_cast<size_t>(codewords) * v.code_n, sync_pool(device), st),
+    check_cuda(cudaMallocFromPoolAsync(&coded, static_cast<size_t>(codewords) * v.code_n, scratch_pool(device), st),
                "cudaMallocFromPoolAsync(tx)");
     uint8_t* cb = static_cast<uint8_t*>(coded);
     const int ctas = std::max(1, std::min((codewords + kEncWarps - 1) / kEncWarps, 8 * device_sm_count()));

@@ -29,6 +29,10 @@ const char* last_error();
 // Number of streaming multiprocessors on the current device (cached per device).
 int device_sm_count();
 
+// Stream-ordered pool of kernel scratch on `device` (cudaMallocFromPoolAsync /
+// cudaFreeAsync around a launch); blocks are kept for later launches.
+cudaMemPool_t scratch_pool(int device);
+
 // Raises a kernel's dynamic shared-memory limit on the current device to at
 // least `bytes`; never lowers it, so launches of the same kernel with other
 // sizes that are still queued on other streams keep their grant.

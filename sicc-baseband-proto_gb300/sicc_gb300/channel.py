@@ -37,7 +37,7 @@ def awgn_llrs(code: QcCode, frames: int, ebn0_db, seed: int, all_zero: bool = Fa
         info = np.zeros((frames, code.k), dtype=np.uint8)
     else:
         info = rng.integers(0, 2, size=(frames, code.k), dtype=np.uint8)
-    cw = encode(parity_matrix(code), info)
+    cw = code.encode_bits(info) if hasattr(code, "encode_bits") else encode(parity_matrix(code), info)
     ebn0 = np.broadcast_to(np.asarray(ebn0_db, dtype=np.float64), (frames,))
     sigma2 = 1.0 / (2.0 * code.rate * 10.0 ** (ebn0 / 10.0))
     sigma = np.sqrt(sigma2)[:, None]

@@ -131,6 +131,115 @@ def mixed_codes() -> list[QcCode]:
     return out
 
 
+# Long irregular repeat-accumulate codes -----------------------------------
+
+@dataclass(frozen=True)
+class IraCode:
+    """An irregular repeat-accumulate LDPC code with the structure of the DVB-S2 codes.
+
+    The information bits come in groups of 360.  Group g has a list of d_g
+    base addresses x; bit j of the group (j < 360) joins the parity
+    accumulators (x + j q) mod m for every x, q = m / 360 (the construction of
+    ETSI EN 302 307 5.3.2).  The parity part is the accumulator chain:
+    p_0 = s_0, p_r = p_{r-1} + s_r, so row r of H holds its information bits
+    and parity columns k + r - 1 (r > 0) and k + r.  The base addresses are
+    drawn from a NumPy PCG64 generator seeded with ``seed``, balanced over the
+    q residues so every row gets the same number of information bits (up to
+    one).  The degree profile is the standard's for the named frame and rate
+    (information column degrees per group), the address tables are synthetic.
+    """
+
+    n: int
+    m: int
+    k: int
+    q: int
+    seed: int
+    degrees: tuple  # information column degree of each 360-column group
+    row_ptr: np.ndarray = field(repr=False)  # [m+1] int32
+    col_ind: np.ndarray = field(repr=False)  # [E] int32
+    label: str = ""
+
+    @property
+    def edges(self) -> int:
+        return int(self.row_ptr[-1])
+
+    @property
+    def rate(self) -> float:
+        return self.k / self.n
+
+    def name(self) -> str:
+        return f"ira({self.n},{self.k})s{self.seed}"
+
+    def encode_bits(self, info: np.ndarray) -> np.ndarray:
+        """Systematic-front codewords [B][n] of info [B][k] (uint8) through the accumulator."""
+        info = np.asarray(info, np.uint8) & 1
+        b = info.shape[0]
+        rows = np.repeat(np.arange(self.m), np.diff(self.row_ptr))
+        info_edges = self.col_ind < self.k
+        cols = self.col_ind[info_edges]
+        starts = np.searchsorted(rows[info_edges], np.arange(self.m))
+        s = np.add.reduceat(info[:, cols].astype(np.int64), starts, axis=1) & 1
+        empty = np.diff(np.append(starts, cols.size)) == 0
+        s[:, empty] = 0
+        parity = np.bitwise_xor.accumulate(s.astype(np.uint8), axis=1)
+        return np.concatenate([info, parity], axis=1).astype(np.uint8).reshape(b, self.n)
+
+
+#: Information-column degree profiles of DVB-S2 frames: (n, k, [(groups, degree), ...]).
+DVBS2_PROFILES = {
+    "N64800_R1/2": (64800, 32400, [(36, 8), (54, 3)]),
+    "N16200_R1/4": (16200, 3240, [(4, 12), (5, 3)]),
+    "N16200_R1/2": (16200, 7200, [(5, 8), (15, 3)]),
+    "N16200_R5/6": (16200, 13320, [(1, 13), (36, 3)]),
+}
+#: Seed of the synthetic address tables of the long-code workload.
+IRA_CODE_SEED = 20260300
+
+
+def ira_code(n: int, k: int, profile, seed: int, label: str = "") -> IraCode:
+    """Build an IRA code of length n, dimension k, information-group degrees ``profile``."""
+    m = n - k
+    if k % 360 or m % 360:
+        raise ValueError("k and n - k must be multiples of 360")
+    q = m // 360
+    degrees = tuple(d for cnt, d in profile for _ in range(cnt))
+    if len(degrees) != k // 360:
+        raise ValueError("profile must cover k / 360 groups")
+    rng = np.random.default_rng(seed)
+    total = sum(degrees)
+    residues = np.resize(rng.permutation(q), total)  # each residue (total / q) times, up to one
+    rng.shuffle(residues)
+    pairs_r, pairs_c = [], []
+    at = 0
+    j = np.arange(360)
+    for g, d in enumerate(degrees):
+        seen = set()
+        for t in range(d):
+            while True:
+                x = int(residues[at + t]) + q * int(rng.integers(0, 360))
+                if x not in seen:
+                    break
+            seen.add(x)
+            pairs_r.append((x + j * q) % m)
+            pairs_c.append(g * 360 + j)
+        at += d
+    r = np.concatenate(pairs_r + [np.arange(m), np.arange(1, m)])
+    c = np.concatenate(pairs_c + [k + np.arange(m), k + np.arange(m - 1)])
+    order = np.lexsort((c, r))
+    r, c = r[order], c[order]
+    row_ptr = np.zeros(m + 1, np.int32)
+    np.add.at(row_ptr, r + 1, 1)
+    row_ptr = np.cumsum(row_ptr).astype(np.int32)
+    return IraCode(n=n, m=m, k=k, q=q, seed=seed, degrees=degrees, row_ptr=row_ptr,
+                   col_ind=c.astype(np.int32), label=label)
+
+
+def dvbs2_code(name: str, seed: int = IRA_CODE_SEED) -> IraCode:
+    """Synthetic code with the DVB-S2 frame size, rate and degree profile ``name`` (see DVBS2_PROFILES)."""
+    n, k, profile = DVBS2_PROFILES[name]
+    return ira_code(n, k, profile, seed, label=name)
+
+
 # alist I/O (format read by the reference: uhd_ldpc_ofdm_link.cpp:2722-2770,
 # matrix_loader.cpp:13-87) ---------------------------------------------------
 
