@@ -733,6 +733,104 @@ def run_mixed(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------ long-code workload
+DVBS2_PROFILE, DVBS2_EBN0, DVBS2_ITERS, DVBS2_FRAMES = "N64800_R1/2", 2.0, 30, 1216
+
+
+def run_dvbs2(args, rank, world):
+    """Colored-layered BP of a DVB-S2-sized (64800,32400) IRA code through the CSR BP decoder."""
+    import torch
+    from sicc_gb300 import channel, codes, fec
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    code = codes.dvbs2_code(DVBS2_PROFILE)
+    frames = args.dvbs2_frames
+    resident = 2  # 2 x 315 MB of LLRs cycled (> L2) at 1216 frames
+    data = [channel.awgn_llrs(code, frames, DVBS2_EBN0, seed=3000 + 10 * rank + i) for i in range(resident)]
+    d_llr = [torch.from_numpy(x[2]).cuda() for x in data]
+    d_bits = torch.empty((frames, code.n), dtype=torch.uint8, device="cuda")
+    d_ok = torch.empty(frames, dtype=torch.uint8, device="cuda")
+    d_it = torch.empty(frames, dtype=torch.uint8, device="cuda")
+    dec = fec.CsrBpDecoder(code.n, code.m, code.row_ptr, code.col_ind, max_batch=frames, max_iter=DVBS2_ITERS,
+                           normalization=ALPHA, schedule=fec.COLORED_LAYERED)
+    stream = torch.cuda.current_stream()
+
+    def step(s):
+        dec.decode_device_batch(d_llr[s % resident], d_bits, d_ok, None, d_it, stream=stream)
+
+    for s in range(args.warmup):
+        step(s)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for s in range(args.steps):
+        step(s)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    value = world * frames * code.k * args.steps / (elapsed_ms * 1e-3) / 1e6
+    step(0)
+    torch.cuda.synchronize()
+    ok = d_ok.cpu().numpy().astype(bool)
+    bits = d_bits.cpu().numpy()
+    fer = float(np.mean(~ok | np.any(bits[:, : code.k] != data[0][0], axis=1)))
+    iters = float(d_it.cpu().numpy().mean())
+
+    # end to end: the host entry point (cuda_osd_decode_bp_csr_batch) with pinned host LLRs
+    e2e = None
+    if not args.no_e2e:
+        h_llr = torch.empty((frames, code.n), dtype=torch.float32, pin_memory=True)
+        h_llr.numpy()[:] = data[0][2]
+        dec.decode(h_llr.numpy())
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            dec.decode(h_llr.numpy())
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": round(world * frames * code.k * args.steps / e2e_s / 1e6, 3), "unit": "Mbit/s",
+               "h2d_bytes_per_step": frames * code.n * 4, "d2h_bytes_per_step": frames * (code.n + 1),
+               "api": "cuda_osd_decode_bp_csr_batch (pinned host LLRs in, host code bits out)"}
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:  # the restated layered decoder on one host core
+        from oracle import Oracle, build_oracle
+        build_oracle()
+        oc = Oracle().code(code.n, code.m, code.row_ptr, code.col_ind)
+        order, _, _ = oc.color_order()
+        sample = 8
+        c0 = time.perf_counter()
+        for x in data[1][2][:sample]:
+            oc.layered(x, DVBS2_ITERS, ALPHA, row_order=order)
+        cs = time.perf_counter() - c0
+        cpu = {"value": round(sample * code.k / cs / 1e6, 4), "unit": "Mbit/s", "cores": 1, "kind": "port",
+               "sample": f"{sample} codewords, colored-layered min-sum (oracle/sicc_oracle.c), one core"}
+
+    peak, peak_kind = peaks()
+    algo = frames * (4 * code.n + code.n + 2)  # LLRs in; code bits, success, iterations out
+    achieved = algo / (elapsed_ms / args.steps * 1e-3) / 1e9
+    line = {"metric": "info-bit Mbps BP, long IRA code (DVB-S2 size), colored-layered min-sum",
+            "value": round(value, 3), "unit": "Mbit/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(elapsed_ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded BPSK/AWGN LLRs, seeded IRA address tables)",
+            "config": {"workload": "dvbs2_64800_r12", "code": f"IRA (64800,32400), DVB-S2 {DVBS2_PROFILE} degree profile",
+                       "ebn0_db": DVBS2_EBN0, "max_iter": DVBS2_ITERS, "alpha": ALPHA, "schedule": "colored layered",
+                       "frames_per_step": frames, "l2": f"2 resident batches of {frames * code.n * 4 / 1e6:.0f} MB cycled"},
+            "fer": fer, "mean_iterations": round(iters, 3), "gpu_launches": args.steps,
+            "clocks": clk,
+            "roofline": {"bound": "hbm", "kernel": "bp_layered_wide_kernel<8>", "achieved": round(achieved, 2),
+                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": None,
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": algo,
+                         "note": "decoder state is L2-resident per CTA; the kernel is latency-bound, HBM fraction "
+                                 "shown per contract"},
+            "e2e": e2e, "cpu_baseline": cpu}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------------ serving loop
 SERVE_LOADS = (0.1, 0.3, 0.5, 0.7, 0.8, 0.9, 1.0, 1.2)
 
@@ -942,12 +1040,13 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH, help="frames per batch (profiling runs only)")
     ap.add_argument("--resident", type=int, default=RESIDENT_BATCHES, help="resident batches per Eb/N0")
     ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "ofdm_rx_1024_512", "ofdm_tx_1024_512", "ofdm_ingest_1024_512",
-                                                        "mixed_100k", "serve_mixed"])
+                                                        "mixed_100k", "serve_mixed", "dvbs2_64800_r12"])
     ap.add_argument("--serve-requests", type=int, default=1500)
     ap.add_argument("--serve-batch", type=int, default=16384, help="codewords per server launch")
     ap.add_argument("--serve-inflight", type=int, default=2, help="batches overlapping on the device")
     ap.add_argument("--mixed-codewords", type=int, default=100_000)
     ap.add_argument("--ofdm-frames", type=int, default=OFDM_FRAMES)
+    ap.add_argument("--dvbs2-frames", type=int, default=DVBS2_FRAMES, help="codewords per long-code step")
     args = ap.parse_args()
     globals()["BATCH"] = args.batch
     globals()["RESIDENT_BATCHES"] = args.resident
@@ -965,6 +1064,8 @@ def main():
         run_mixed(args, rank, world)
     elif args.workload == "serve_mixed":
         run_serve(args, rank, world)
+    elif args.workload == "dvbs2_64800_r12":
+        run_dvbs2(args, rank, world)
     else:
         run_ours(args, rank, world)
 

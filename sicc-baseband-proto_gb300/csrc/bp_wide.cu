@@ -105,6 +105,102 @@ __device__ __forceinline__ int wide_next(const BpIO& io, int* s_next)
     return *s_next;
 }
 
+// Rows a thread updates together in a layer: their loads are all issued before the
+// first store (the rows of a layer touch disjoint variables), so the latencies overlap.
+// Two for row degrees up to 16; one above, where the registers would spill.
+template <int D>
+constexpr int row_batch() { return D <= 16 ? 2 : 1; }
+
+// Layered update of rows rs0, rs0 + kWideThreads, ... (kRowBatch of them, those below
+// `rows`) of layer L, whose messages start at row `first` of the layer-ordered message
+// arrays: the shared-memory layered kernel's per-row arithmetic (bp_kernels.cu).
+template <int D, int kRowBatch = row_batch<D>()>
+__device__ __forceinline__ void wide_rows(const LayeredView& cv, const BpParams& p, int L, int rs0, int rows,
+                                          int first, float* app, float* r1, float* r2, unsigned* meta)
+{
+    int v[kRowBatch][D];
+    float o1[kRowBatch], o2[kRowBatch], x[kRowBatch][D];
+    unsigned om[kRowBatch];
+#pragma unroll
+    for (int b = 0; b < kRowBatch; ++b) {
+        const int rs = rs0 + b * kWideThreads;
+        const bool live = rs < rows;
+        const int* vp = cv.vars + (L * cv.maxdeg) * cv.width + rs;
+#pragma unroll
+        for (int j = 0; j < D; ++j) v[b][j] = (live && j < cv.maxdeg) ? __ldg(vp + j * cv.width) : -1;
+        const int ridx = first + rs;
+        o1[b] = live ? r1[ridx] : 0.0f;
+        o2[b] = live ? r2[ridx] : 0.0f;
+        om[b] = live ? meta[ridx] : 0u;
+    }
+#pragma unroll
+    for (int b = 0; b < kRowBatch; ++b)
+#pragma unroll
+        for (int j = 0; j < D; ++j) x[b][j] = v[b][j] >= 0 ? app[v[b][j]] : 0.0f;
+#pragma unroll
+    for (int b = 0; b < kRowBatch; ++b) {
+        if (v[b][0] < 0) continue;  // past the layer
+        float q[D];
+        float m1 = FLT_MAX, m2 = FLT_MAX;
+        int idx = 0;
+        unsigned neg = 0;
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+            q[j] = 0.0f;
+            if (v[b][j] >= 0) {
+                const float qj = __fsub_rn(x[b][j], rebuild(o1[b], o2[b], om[b], j));
+                q[j] = qj;
+                neg |= (qj < 0.0f) ? (1u << j) : 0u;
+                const float a = fabsf(qj);
+                idx = (a < m1) ? j : idx;
+                m2 = fminf(m2, fmaxf(m1, a));
+                m1 = fminf(m1, a);
+            }
+        }
+        const unsigned tot = static_cast<unsigned>(__popc(neg)) & 1u;
+        const float n1 = nms_mag(p.alpha, p.beta, m1);
+        const float n2 = nms_mag(p.alpha, p.beta, m2);
+        const unsigned nm = ((neg ^ (0u - tot)) & 0x07FFFFFFu) | (static_cast<unsigned>(idx) << 27);
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+            if (v[b][j] >= 0) {
+                const unsigned sg = (nm >> j) & 1u;
+                const float mag = (j == idx) ? n2 : n1;
+                app[v[b][j]] = __fadd_rn(q[j], sg ? -mag : mag);
+            }
+        }
+        const int ridx = first + rs0 + b * kWideThreads;
+        r1[ridx] = n1;
+        r2[ridx] = n2;
+        meta[ridx] = nm;
+    }
+}
+
+// Unsatisfied checks among the same rows under hard(app).
+template <int D, int kRowBatch = row_batch<D>()>
+__device__ __forceinline__ int wide_parity(const LayeredView& cv, int L, int rs0, int rows, const float* app)
+{
+    int v[kRowBatch][D];
+#pragma unroll
+    for (int b = 0; b < kRowBatch; ++b) {
+        const int rs = rs0 + b * kWideThreads;
+        const bool live = rs < rows;
+        const int* vp = cv.vars + (L * cv.maxdeg) * cv.width + rs;
+#pragma unroll
+        for (int j = 0; j < D; ++j) v[b][j] = (live && j < cv.maxdeg) ? __ldg(vp + j * cv.width) : -1;
+    }
+    int cnt = 0;
+#pragma unroll
+    for (int b = 0; b < kRowBatch; ++b) {
+        unsigned par = 0;
+#pragma unroll
+        for (int j = 0; j < D; ++j)
+            if (v[b][j] >= 0) par ^= (app[v[b][j]] < 0.0f) ? 1u : 0u;
+        cnt += static_cast<int>(par);
+    }
+    return cnt;
+}
+
 }  // namespace
 
 template <int D>
@@ -117,7 +213,7 @@ bp_layered_wide_kernel(LayeredView cv, BpParams p, BpIO io, float* scratch, long
     __shared__ int s_next, s_slot;
     const int tid = threadIdx.x;
     const int n = cv.n, n_pad = (n + 3) & ~3;
-    const int mp = cv.num_layers * cv.width;
+    const int mp = cv.m;  // messages of the rows in layer order, packed
     float* g = scratch + static_cast<size_t>(blockIdx.x) * static_cast<size_t>(slice);
     float* app = app_smem ? s_app : g;
     float* best = app_smem ? g : g + n_pad;
@@ -128,23 +224,9 @@ bp_layered_wide_kernel(LayeredView cv, BpParams p, BpIO io, float* scratch, long
     auto syndrome = [&]() -> int {
         int cnt = 0;
         for (int L = 0; L < cv.num_layers; ++L) {
-            for (int rs = tid; rs < cv.width; rs += kWideThreads) {
-                const int* vp = cv.vars + (L * cv.maxdeg) * cv.width + rs;
-                unsigned par = 0;
-#pragma unroll
-                for (int j0 = 0; j0 < D; j0 += 8) {
-                    int v[8];
-#pragma unroll
-                    for (int x = 0; x < 8; ++x) {
-                        const int j = j0 + x;
-                        v[x] = (j < D && j < cv.maxdeg) ? __ldg(vp + j * cv.width) : -1;
-                    }
-#pragma unroll
-                    for (int x = 0; x < 8; ++x)
-                        if (v[x] >= 0) par ^= (app[v[x]] < 0.0f) ? 1u : 0u;
-                }
-                cnt += static_cast<int>(par);
-            }
+            const int first = __ldg(cv.layer_start + L), rows = __ldg(cv.layer_start + L + 1) - first;
+            for (int rs0 = tid; rs0 < rows; rs0 += row_batch<D>() * kWideThreads)
+                cnt += wide_parity<D>(cv, L, rs0, rows, app);
         }
         return cta_sum(cnt, s_red);
     };
@@ -166,48 +248,9 @@ bp_layered_wide_kernel(LayeredView cv, BpParams p, BpIO io, float* scratch, long
         int iter = 0, w = 0;
         for (;;) {
             for (int L = 0; L < cv.num_layers; ++L) {
-                for (int rs = tid; rs < cv.width; rs += kWideThreads) {
-                    const int ridx = L * cv.width + rs;
-                    const int* vp = cv.vars + (L * cv.maxdeg) * cv.width + rs;
-                    int v[D];
-#pragma unroll
-                    for (int j = 0; j < D; ++j) v[j] = (j < cv.maxdeg) ? __ldg(vp + j * cv.width) : -1;
-                    if (v[0] < 0) continue;  // a padding slot of this layer
-                    const float o1 = r1[ridx], o2 = r2[ridx];
-                    const unsigned om = meta[ridx];
-                    float q[D];
-                    float m1 = FLT_MAX, m2 = FLT_MAX;
-                    int idx = 0;
-                    unsigned neg = 0;
-#pragma unroll
-                    for (int j = 0; j < D; ++j) {
-                        q[j] = 0.0f;
-                        if (v[j] >= 0) {
-                            const float qj = __fsub_rn(app[v[j]], rebuild(o1, o2, om, j));
-                            q[j] = qj;
-                            neg |= (qj < 0.0f) ? (1u << j) : 0u;
-                            const float a = fabsf(qj);
-                            idx = (a < m1) ? j : idx;
-                            m2 = fminf(m2, fmaxf(m1, a));
-                            m1 = fminf(m1, a);
-                        }
-                    }
-                    const unsigned tot = static_cast<unsigned>(__popc(neg)) & 1u;
-                    const float n1 = nms_mag(p.alpha, p.beta, m1);
-                    const float n2 = nms_mag(p.alpha, p.beta, m2);
-                    const unsigned nm = ((neg ^ (0u - tot)) & 0x07FFFFFFu) | (static_cast<unsigned>(idx) << 27);
-#pragma unroll
-                    for (int j = 0; j < D; ++j) {
-                        if (v[j] >= 0) {
-                            const unsigned s = (nm >> j) & 1u;
-                            const float mag = (j == idx) ? n2 : n1;
-                            app[v[j]] = __fadd_rn(q[j], s ? -mag : mag);
-                        }
-                    }
-                    r1[ridx] = n1;
-                    r2[ridx] = n2;
-                    meta[ridx] = nm;
-                }
+                const int first = __ldg(cv.layer_start + L), rows = __ldg(cv.layer_start + L + 1) - first;
+                for (int rs0 = tid; rs0 < rows; rs0 += row_batch<D>() * kWideThreads)
+                    wide_rows<D>(cv, p, L, rs0, rows, first, app, r1, r2, meta);
                 __syncthreads();
             }
             w = syndrome();
@@ -375,7 +418,7 @@ template <int D>
 void launch_layered_wide_t(const LayeredView& cv, const BpParams& p, const BpIO& io, bool track_best, cudaStream_t st)
 {
     const long long n_pad = (cv.n + 3) & ~3;
-    const long long mp = static_cast<long long>(cv.num_layers) * cv.width;
+    const long long mp = cv.m;
     const size_t app_bytes = static_cast<size_t>(n_pad) * sizeof(float);
     const bool app_smem = app_bytes <= 200 * 1024;
     long long slice = (app_smem ? 0 : n_pad) + (track_best ? n_pad : 0) + 3 * mp;

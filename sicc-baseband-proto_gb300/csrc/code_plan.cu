@@ -251,6 +251,10 @@ void DeviceCode::build_layered()
     lv_.group = group;
     lv_.rows_per_lane = rows_per_lane;
     lv_.vars = device_upload(vars, owned_);
+    std::vector<int> starts(static_cast<size_t>(L) + 1, 0);
+    for (int l = 0; l < L; ++l) starts[l + 1] = starts[l] + sizes[l];
+    lv_.m = m_;
+    lv_.layer_start = device_upload(starts, owned_);
 }
 
 void DeviceCode::build_flood()

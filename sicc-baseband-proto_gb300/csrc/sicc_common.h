@@ -55,6 +55,8 @@ struct LayeredView {
     int group;          // lanes per codeword: power of two, <= 32
     int rows_per_lane;  // width / group
     const int* vars;    // [num_layers][maxdeg][width]
+    int m;              // rows of the code
+    const int* layer_start;  // [num_layers + 1] first row of each layer in layer order (rows packed)
 };
 
 // Flooding schedule: rows in CSR order plus the column view used for the
