@@ -220,6 +220,182 @@ bp_layered_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int sl
     }
 }
 
+// Layered kernel for codes whose group lane owns at most NL rows in all
+// (num_layers x rows_per_lane <= NL, the (128,64) code: 4): the lane's row
+// tables (variable indices) stay in registers for the whole launch and its
+// rows' compressed messages in registers for the codeword, so the row updates
+// and the syndrome go to shared memory only for the posteriors.  Rows, order
+// and arithmetic are those of bp_layered_kernel.
+template <int D, int NL>
+__global__ void __launch_bounds__(kBpThreads, 3)
+bp_layered_reg_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int slot_floats, int track_best)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int G = cv.group;
+    const int lane = threadIdx.x & 31;
+    const int gl = lane & (G - 1);
+    const int sub = lane / G;
+    const int slot = threadIdx.x / G;
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
+    const int leader = sub * G;
+
+    const int n = cv.n;
+    const int n_pad = (n + 3) & ~3;
+    const int rpl = cv.rows_per_lane;
+    const int nrows = cv.num_layers * rpl;
+    float* app = reinterpret_cast<float*>(smem) + static_cast<size_t>(slot) * slot_floats;
+    float* best = app + n_pad;  // only when track_best
+
+    // row t of this lane: layer t / rpl, slot gl + (t mod rpl) G
+    int vr[NL][D];
+#pragma unroll
+    for (int t = 0; t < NL; ++t) {
+        const int L = t / rpl, rs = gl + (t - L * rpl) * G;
+#pragma unroll
+        for (int j = 0; j < D; ++j)
+            vr[t][j] = (t < nrows && j < cv.maxdeg) ? __ldg(cv.vars + (L * cv.maxdeg + j) * cv.width + rs) : -1;
+    }
+    float m1r[NL], m2r[NL];
+    unsigned mr[NL];
+
+    auto syndrome = [&]() -> int {
+        int cnt = 0;
+#pragma unroll
+        for (int t = 0; t < NL; ++t) {
+            unsigned par = 0;
+#pragma unroll
+            for (int j = 0; j < D; ++j)
+                if (vr[t][j] >= 0) par ^= (app[vr[t][j]] < 0.0f) ? 1u : 0u;
+            cnt += static_cast<int>(par);
+        }
+        return static_cast<int>(__reduce_add_sync(gmask, static_cast<unsigned>(cnt)));
+    };
+
+    const int total_groups = gridDim.x * slots_per_cta;
+    int c = blockIdx.x * slots_per_cta + slot;
+    bool active = c < io.count;
+    int iter = 0, best_w = 0;
+
+    auto init = [&](int cw) {
+        const float* src = io.llr + static_cast<size_t>(cw) * n;
+        if ((n & 3) == 0) {
+            const float4* s4 = reinterpret_cast<const float4*>(src);
+            for (int i = gl; i < (n >> 2); i += G) {
+                const float4 v = __ldcs(s4 + i);
+                reinterpret_cast<float4*>(app)[i] = v;
+                if (track_best) reinterpret_cast<float4*>(best)[i] = v;
+            }
+        } else {
+            for (int i = gl; i < n; i += G) {
+                const float v = __ldcs(src + i);
+                app[i] = v;
+                if (track_best) best[i] = v;
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < NL; ++t) {
+            m1r[t] = 0.0f;
+            m2r[t] = 0.0f;
+            mr[t] = 0u;
+        }
+        __syncwarp(gmask);
+        best_w = syndrome();
+        iter = 0;
+    };
+
+    if (active) init(c);
+
+    while (__any_sync(0xffffffffu, active)) {
+        if (active) {
+            // ---- one layered iteration ----
+#pragma unroll
+            for (int t = 0; t < NL; ++t) {
+                if (vr[t][0] >= 0) {
+                    float q[D];
+                    float m1 = FLT_MAX, m2 = FLT_MAX;
+                    int idx = 0;
+                    unsigned neg = 0;
+#pragma unroll
+                    for (int j = 0; j < D; ++j) {
+                        q[j] = 0.0f;
+                        if (vr[t][j] >= 0) {
+                            const float qj = __fsub_rn(app[vr[t][j]], rebuild(m1r[t], m2r[t], mr[t], j));
+                            q[j] = qj;
+                            neg |= (qj < 0.0f) ? (1u << j) : 0u;
+                            const float a = fabsf(qj);
+                            idx = (a < m1) ? j : idx;
+                            m2 = fminf(m2, fmaxf(m1, a));
+                            m1 = fminf(m1, a);
+                        }
+                    }
+                    const unsigned tot = static_cast<unsigned>(__popc(neg)) & 1u;
+                    const float n1 = nms_mag(p.alpha, p.beta, m1);
+                    const float n2 = nms_mag(p.alpha, p.beta, m2);
+                    const unsigned nm = ((neg ^ (0u - tot)) & 0x07FFFFFFu) | (static_cast<unsigned>(idx) << 27);
+#pragma unroll
+                    for (int j = 0; j < D; ++j) {
+                        if (vr[t][j] >= 0) {
+                            const unsigned sg = (nm >> j) & 1u;
+                            const float mag = (j == idx) ? n2 : n1;
+                            app[vr[t][j]] = __fadd_rn(q[j], sg ? -mag : mag);
+                        }
+                    }
+                    m1r[t] = n1;
+                    m2r[t] = n2;
+                    mr[t] = nm;
+                }
+                if ((t + 1) % rpl == 0) __syncwarp(gmask);  // end of a layer
+            }
+            const int w = syndrome();
+            ++iter;
+            if (track_best && (w < best_w || (w == 0 && best_w == 0))) {
+                for (int i = gl; i < n; i += G) best[i] = app[i];
+                __syncwarp(gmask);
+            }
+            if (w < best_w) best_w = w;
+            if (w == 0 || iter >= p.max_iter) {
+                // ---- finalize (bp_layered_kernel's) ----
+                bool accept = (w == 0);
+                if (accept && p.min_abs_accept > 0.0f) {
+                    unsigned mn = 0x7f800000u;
+                    for (int i = gl; i < n; i += G) mn = min(mn, __float_as_uint(fabsf(app[i])));
+                    mn = __reduce_min_sync(gmask, mn);
+                    accept = __uint_as_float(mn) >= p.min_abs_accept;
+                }
+                const bool route = !accept && p.route_failures_to_osd && io.osd_llr != nullptr;
+                if (gl == 0) {
+                    if (io.success) io.success[c] = accept ? 1 : 0;
+                    if (io.iterations) io.iterations[c] = static_cast<uint8_t>(iter);
+                    if (io.used_osd) io.used_osd[c] = 0;
+                }
+                if (io.out_bits) {
+                    uint8_t* dst = io.out_bits + static_cast<size_t>(c) * io.out_stride;
+                    for (int i = gl; i < io.out_len; i += G) dst[i] = app[i] < 0.0f ? 1 : 0;
+                }
+                if (io.app_out) {
+                    float* dst = io.app_out + static_cast<size_t>(c) * n;
+                    for (int i = gl; i < n; i += G) dst[i] = app[i];
+                }
+                if (route) {
+                    int s = 0;
+                    if (gl == 0) s = atomicAdd(io.osd_count, 1);
+                    s = __shfl_sync(gmask, s, leader);
+                    const float* b = track_best ? best : app;
+                    float* dst = io.osd_llr + static_cast<size_t>(s) * n;
+                    for (int i = gl; i < n; i += G) dst[i] = b[i];
+                    if (gl == 0) io.osd_index[s] = c;
+                }
+                int nxt = 0;
+                if (gl == 0) nxt = total_groups + atomicAdd(io.work_counter, 1);
+                c = __shfl_sync(gmask, nxt, leader);
+                active = c < io.count;
+                __syncwarp(gmask);
+                if (active) init(c);
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kBpThreads)
 bp_flooding_kernel(FloodView cv, BpParams p, BpIO io, int slot_floats, int track_best)
 {
@@ -379,10 +555,42 @@ int layered_default_slots(const LayeredView& cv, bool track_best)
     return slots;
 }
 
+// Register-resident variant: codes whose lane owns at most kRegRows rows (num_layers x
+// rows_per_lane), row degree <= 8.
+constexpr int kRegRows = 4;
+
+template <int D>
+static void launch_layered_reg_t(const LayeredView& cv, const BpParams& p, const BpIO& io, int slots, int ctas,
+                                 bool track_best, cudaStream_t st)
+{
+    const int n_pad = (cv.n + 3) & ~3;
+    int slot_floats = ((track_best ? 2 : 1) * n_pad + 3) & ~3;
+    if (cv.group < 32) slot_floats += ((cv.group - slot_floats % 32) + 32) % 32;  // groups G banks apart
+    const size_t smem = static_cast<size_t>(slots) * slot_floats * sizeof(float);
+    const auto kernel = bp_layered_reg_kernel<D, kRegRows>;
+    check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(kernel), smem), "cudaFuncSetAttribute(bp_layered_reg)");
+    if (ctas <= 0) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, slots * cv.group, smem) != cudaSuccess ||
+            per_sm <= 0)
+            per_sm = 1;
+        ctas = per_sm * device_sm_count();
+        ctas = std::max(1, std::min(ctas, (io.count + slots - 1) / slots));
+    }
+    kernel<<<ctas, slots * cv.group, smem, st>>>(cv, p, io, slots, slot_floats, track_best ? 1 : 0);
+    check_cuda(cudaGetLastError(), "bp_layered_reg_kernel launch");
+}
+
 template <int D>
 static void launch_layered_t(const LayeredView& cv, const BpParams& p, const BpIO& io, int slots, int ctas,
                              bool track_best, cudaStream_t st)
 {
+    if constexpr (D <= 8) {
+        if (cv.num_layers * cv.rows_per_lane <= kRegRows) {
+            launch_layered_reg_t<D>(cv, p, io, slots, ctas, track_best, st);
+            return;
+        }
+    }
     int slot_floats = 0;
     const size_t smem = layered_smem_bytes(cv, slots, track_best, &slot_floats);
     check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(bp_layered_kernel<D>), smem),
