@@ -1043,7 +1043,7 @@ def main():
                                                         "mixed_100k", "serve_mixed", "dvbs2_64800_r12"])
     ap.add_argument("--serve-requests", type=int, default=1500)
     ap.add_argument("--serve-batch", type=int, default=16384, help="codewords per server launch")
-    ap.add_argument("--serve-inflight", type=int, default=2, help="batches overlapping on the device")
+    ap.add_argument("--serve-inflight", type=int, default=4, help="batches overlapping on the device")
     ap.add_argument("--mixed-codewords", type=int, default=100_000)
     ap.add_argument("--ofdm-frames", type=int, default=OFDM_FRAMES)
     ap.add_argument("--dvbs2-frames", type=int, default=DVBS2_FRAMES, help="codewords per long-code step")
