@@ -73,8 +73,9 @@ struct PassResult {
 };
 
 // Full-preamble correlation metric of candidate dd, one warp: lane-strided
-// products summed per lane, then a butterfly sum.  Samples come from the
-// shared window when it covers them (win[i] = x[wbase + i]).
+// products accumulated per lane with fused multiply-adds, then a butterfly
+// sum.  Samples come from the shared window when it covers them
+// (win[i] = x[wbase + i]).
 __device__ __forceinline__ float fine_metric(const float2* __restrict__ x, const float2* win, int wbase, int wlen, int dd,
                                              const float2* __restrict__ preamble, int pre, float pre_energy, int lane)
 {
@@ -83,10 +84,9 @@ __device__ __forceinline__ float fine_metric(const float2* __restrict__ x, const
     for (int i = lane; i < pre; i += 32) {
         const float2 y = local ? win[dd - wbase + i] : x[dd + i];
         const float2 q = preamble[i];
-        const float2 c = cmulconj(y, q);
-        cr += c.x;
-        ci += c.y;
-        eng += cnorm(y);
+        cr = fmaf(y.x, q.x, fmaf(y.y, q.y, cr));    // Re(y conj(q))
+        ci = fmaf(y.y, q.x, fmaf(-y.x, q.y, ci));   // Im(y conj(q))
+        eng = fmaf(y.x, y.x, fmaf(y.y, y.y, eng));  // |y|^2
     }
     cr = warp_sum(cr);
     ci = warp_sum(ci);
