@@ -210,7 +210,8 @@ def test_stream_decoder_device_submit_and_async_window(cuda, oracle):
 
 
 def test_stream_decoder_host_submits_past_the_ring_and_odd_polls(cuda, oracle):
-    """Five full batches submitted before any poll (the ring holds three), then polled 7 at a time."""
+    """Five full batches submitted before any poll (the ring holds four: the oldest results are
+    copied out of their batch when it is needed again), then polled 7 at a time."""
     from sicc_gb300 import fec
     code = codes.short_code()
     oc = oracle.code(code.n, code.m, code.row_ptr, code.col_ind)
