@@ -69,6 +69,40 @@ def _cpu_worker(args):
     return time.perf_counter() - t0, info, used
 
 
+def _cpu_mixed_worker(args):
+    """One code's sample of the mixed workload through the restated layered BP + OSD (host core)."""
+    n, m, row_ptr, col_ind, llr, iters, order = args
+    from oracle import Oracle
+    oc = Oracle().code(n, m, row_ptr, col_ind)
+    table = oc.systematic_parity()
+    t0 = time.perf_counter()
+    oc.bp_osd_batch(llr, schedule=3, max_iter=iters, alpha=ALPHA, osd_order=order, osd_max_flip=OSD_FLIP,
+                    osd_max_tests=OSD_TESTS, table=table)
+    return time.perf_counter() - t0
+
+
+def _cpu_ofdm_worker(args):
+    """Frames of the OFDM workload through the restated CPU receive chain: sync, demod, layered decode."""
+    iq, noise_var, iters = args
+    from oracle import Oracle
+    from sicc_gb300 import codes, ofdm
+    o = Oracle()
+    t = ofdm.reference_tables(ofdm.OFDM_C3)
+    code = codes.ofdm_code()
+    ph = o.phy(t)
+    oc = o.code(code.n, code.m, code.row_ptr, code.col_ind)
+    blocks = t.coded_bits // code.n
+    t0 = time.perf_counter()
+    for x in iq:
+        r = o.sync_earliest(ph, x)
+        if r[0] != 1:
+            continue
+        llr = o.demod_frame(ph, x[r[1]: r[1] + t.frame_len], r[4], noise_var)
+        for b in range(blocks):
+            oc.layered(llr[b * code.n: (b + 1) * code.n], iters, ALPHA)
+    return time.perf_counter() - t0
+
+
 def cpu_decode(pool, workers, llr):
     chunks = np.array_split(llr, workers)
     t0 = time.perf_counter()
@@ -332,6 +366,11 @@ def run_ofdm(args, rank, world):
     from sicc_gb300.pipeline import RxPipeline, SYNC_RECORD
 
     dev = int(os.environ.get("LOCAL_RANK", 0))
+    # CPU baseline pool: spawned before the first GPU call of this process
+    pool = workers = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        workers = os.cpu_count() or 1
+        pool = mp.get_context("spawn").Pool(workers)
     torch.cuda.set_device(dev)
     t = ofdm.reference_tables(ofdm.OFDM_C3)
     code = codes.ofdm_code()
@@ -410,6 +449,25 @@ def run_ofdm(args, rank, world):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
 
+    cpu = None
+    if pool is not None:  # 64 frames per SNR point through the restated CPU receiver, all host cores
+        sample = min(64, frames)
+        tasks = []
+        for snr in OFDM_SNRS:
+            b = batches[snr][1]  # 256 frames per batch by default
+            nv = float(np.float32(np.mean(b.noise_var)))
+            for part in np.array_split(np.arange(sample), max(1, workers // len(OFDM_SNRS))):
+                if len(part):
+                    tasks.append((b.iq[part], nv, OFDM_ITERS))
+        c0 = time.perf_counter()
+        pool.map(_cpu_ofdm_worker, tasks)
+        cs = time.perf_counter() - c0
+        pool.close()
+        cpu = {"value": round(len(OFDM_SNRS) * sample * blocks * code.k / cs / 1e6, 4), "unit": "Mbit/s",
+               "cores": workers, "kind": "port",
+               "sample": f"{sample} frames at each SNR: the restated CPU receiver (sync, demod, 30 layered decodes "
+                         "of 25 iterations per frame; oracle/sicc_oracle.c)"}
+
     peak, peak_kind = peaks()
     demod_bytes = frames * (8 * t.cfg.num_symbols * t.cfg.nfft + 4 * blocks * code.n)
     maxdeg = int(np.max(np.diff(code.row_ptr)))
@@ -433,7 +491,7 @@ def run_ofdm(args, rank, world):
             "e2e": {"value": round(world * info_bits * args.steps / e2e_s / 1e6, 3), "unit": "Mbit/s",
                     "h2d_bytes_per_step": len(OFDM_SNRS) * frames * L * 8,
                     "d2h_bytes_per_step": len(OFDM_SNRS) * frames * blocks * code.n},
-            "cpu_baseline": None}
+            "cpu_baseline": cpu}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -631,6 +689,11 @@ def run_mixed(args, rank, world):
     from sicc_gb300 import engine, fec
 
     dev = int(os.environ.get("LOCAL_RANK", 0))
+    # CPU baseline pool: spawned before the first GPU call of this process
+    pool = workers = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        workers = os.cpu_count() or 1
+        pool = mp.get_context("spawn").Pool(workers)
     torch.cuda.set_device(dev)
     w = engine.mixed_workload(total=args.mixed_codewords, seed=4242 + rank)
     stream = torch.cuda.current_stream()
@@ -716,6 +779,50 @@ def run_mixed(args, rank, world):
     plain_pass()
     plain_s = time.perf_counter() - t0
     plain_mbps = w.info_bits / plain_s / 1e6
+
+    # end to end: pinned host LLRs in, host information bits out, every step on the decode stream
+    e2e = None
+    if not args.no_e2e:
+        h_llr = torch.empty(w.llr.shape, dtype=torch.float32, pin_memory=True)
+        h_llr.numpy()[:] = w.llr
+        h_info = torch.empty(w.info_bits, dtype=torch.uint8, pin_memory=True)
+
+        def e2e_step():
+            d_llr.copy_(h_llr, non_blocking=True)
+            batched()
+            h_info.copy_(d_info, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": round(world * w.info_bits * args.steps / e2e_s / 1e6, 3), "unit": "Mbit/s",
+               "h2d_bytes_per_step": int(w.llr.nbytes), "d2h_bytes_per_step": int(w.info_bits),
+               "api": "sicc_engine_decode_device between pinned-host copies on the same stream"}
+
+    cpu = None
+    if pool is not None:  # every code's first requests, up to 256 codewords per code, on all host cores
+        tasks, bits = [], 0
+        for ci, c in enumerate(w.codes):
+            rows = [i for i in range(w.count) if w.code_of[i] == ci][:256]
+            if not rows:
+                continue
+            llr = np.stack([w.llr[w.llr_off[i]: w.llr_off[i] + c.n] for i in rows])
+            for part in np.array_split(llr, max(1, min(len(rows), workers // len(w.codes) + 1))):
+                if len(part):
+                    tasks.append((c.n, c.m, c.row_ptr, c.col_ind, part, engine.iteration_cap(c.n),
+                                  engine.osd_order_for(c)))
+            bits += len(rows) * c.k
+        c0 = time.perf_counter()
+        pool.map(_cpu_mixed_worker, tasks)
+        cs = time.perf_counter() - c0
+        cpu = {"value": round(bits / cs / 1e6, 4), "unit": "Mbit/s", "cores": workers, "kind": "port",
+               "sample": f"up to 256 codewords of each of the 15 codes ({bits} information bits): the restated "
+                         "row-sequential layered min-sum + generator OSD (oracle/sicc_oracle.c)"}
+        pool.close()
     peak, peak_kind = peaks()
     line = {"metric": "info-bit Mbps mixed-code BP(+OSD), 100k codewords, 15 codes", "value": round(value, 3),
             "unit": "Mbit/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -741,7 +848,7 @@ def run_mixed(args, rank, world):
                          "frac": round((w.llr.nbytes + w.info_bits) / (bp_ms * 1e-3) / 1e9 / peak, 5),
                          "traffic": None, "peak_source": peak_kind,
                          "note": "issue-bound; HBM fraction shown per contract"},
-            "e2e": None, "cpu_baseline": None}
+            "e2e": e2e, "cpu_baseline": cpu}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
