@@ -25,6 +25,11 @@ namespace {
 
 constexpr int kOsdWarps = 8;
 
+// Small shapes also keep the reduced rows in flip-pool order, so a candidate reads its
+// flipped rows without the rank lookup (the larger shapes would lose occupancy to it).
+template <int NW, int KR>
+constexpr bool kFlipRows = NW * KR <= 4;
+
 template <int NW, int KR>
 struct OsdSmem {
     float rel_sorted[NW * 64];
@@ -33,6 +38,7 @@ struct OsdSmem {
     int16_t flip[KR * 32];    // weakness rank -> pivot index
     uint32_t hard_orig[NW * 2];
     unsigned long long rows[KR * 32][NW];  // reduced rows by pivot index
+    unsigned long long frows[kFlipRows<NW, KR> ? KR * 32 : 1][NW];  // the same rows by flip-pool rank
     int16_t mrb_pos[KR * 32];
 };
 
@@ -287,7 +293,12 @@ osd_kernel(OsdView ov0, OsdIO io)
                 else lo = mid + 1;
             }
             const int r = (k - lo) + (t - a);
-            if (r < ov.pool) s.flip[r] = static_cast<int16_t>(t);
+            if (r < ov.pool) {
+                s.flip[r] = static_cast<int16_t>(t);
+                if (kFlipRows<NW, KR>)
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) s.frows[kFlipRows<NW, KR> ? r : 0][w] = s.rows[t][w];
+            }
         }
         __syncwarp();
         // ---- 6. all candidates in parallel ----
@@ -310,9 +321,14 @@ osd_kernel(OsdView ov0, OsdIO io)
                     for (int f = 0; f < 3; ++f) {
                         const uint32_t fi = (cmb >> (10 * f)) & 0x3FFu;
                         if (fi != 0x3FFu) {
-                            const int t = s.flip[fi];
+                            if (kFlipRows<NW, KR>) {
 #pragma unroll
-                            for (int w = 0; w < NW; ++w) d[w] ^= s.rows[t][w];
+                                for (int w = 0; w < NW; ++w) d[w] ^= s.frows[kFlipRows<NW, KR> ? fi : 0][w];
+                            } else {
+                                const int t = s.flip[fi];
+#pragma unroll
+                                for (int w = 0; w < NW; ++w) d[w] ^= s.rows[t][w];
+                            }
                         }
                     }
                 }
