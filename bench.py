@@ -864,7 +864,7 @@ def run_dvbs2(args, rank, world):
 
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
-    code = codes.dvbs2_code(DVBS2_PROFILE)
+    code = codes.dvbs2_code(args.dvbs2_profile)
     frames = args.dvbs2_frames
     resident = 2  # 2 x 315 MB of LLRs cycled (> L2) at 1216 frames
     data = [channel.awgn_llrs(code, frames, DVBS2_EBN0, seed=3000 + 10 * rank + i) for i in range(resident)]
@@ -936,7 +936,10 @@ def run_dvbs2(args, rank, world):
             "value": round(value, 3), "unit": "Mbit/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(elapsed_ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded BPSK/AWGN LLRs, seeded IRA address tables)",
-            "config": {"workload": "dvbs2_64800_r12", "code": f"IRA (64800,32400), DVB-S2 {DVBS2_PROFILE} degree profile",
+            "config": {"workload": "dvbs2_64800_r12" if args.dvbs2_profile == DVBS2_PROFILE else
+                       "dvbs2_" + args.dvbs2_profile.lower().replace("/", ""),
+                       "code": f"IRA ({code.n},{code.k}), DVB-S2 {args.dvbs2_profile} "
+                                                                  "degree profile",
                        "ebn0_db": DVBS2_EBN0, "max_iter": DVBS2_ITERS, "alpha": ALPHA, "schedule": "colored layered",
                        "frames_per_step": frames, "l2": f"2 resident batches of {frames * code.n * 4 / 1e6:.0f} MB cycled"},
             "fer": fer, "mean_iterations": round(iters, 3), "gpu_launches": args.steps,
@@ -1167,6 +1170,9 @@ def main():
     ap.add_argument("--mixed-codewords", type=int, default=100_000)
     ap.add_argument("--ofdm-frames", type=int, default=OFDM_FRAMES)
     ap.add_argument("--dvbs2-frames", type=int, default=DVBS2_FRAMES, help="codewords per long-code step")
+    ap.add_argument("--dvbs2-profile", default=DVBS2_PROFILE, choices=["N64800_R1/2", "N16200_R1/4", "N16200_R1/2",
+                                                                       "N16200_R5/6"],
+                    help="frame size and degree profile of the long-code workload")
     args = ap.parse_args()
     globals()["BATCH"] = args.batch
     globals()["RESIDENT_BATCHES"] = args.resident
