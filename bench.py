@@ -4,7 +4,9 @@ Workload (default, ``bp_osd_128_64``): the QC (128,64) code, BPSK over AWGN,
 65,536 frames per batch at Eb/N0 = 2 dB and 3 dB, layered normalized min-sum
 (alpha 0.75, at most 20 iterations, early stop) with order-2 OSD (1 + 64 +
 2016 tests) on every frame whose syndrome fails.  One step decodes one batch
-at each Eb/N0 (131,072 codewords, 8.39 Mbit of information).  Inputs are
+at each Eb/N0 (131,072 codewords, 8.39 Mbit of information), each Eb/N0 point
+on its own decoder and CUDA stream (two receive chains: one chain's BP runs
+beside the other's OSD).  Inputs are
 seeded synthetic LLRs; several distinct batches are kept resident on the GPU
 (larger than L2 together) and cycled between steps.
 
@@ -194,22 +196,38 @@ def run_ours(args, rank, world):
 
     stream = torch.cuda.current_stream()
     d_llr = {e: [torch.from_numpy(x[2]).cuda() for x in inputs[e]] for e in EBN0}
-    d_info = torch.zeros((BATCH, code.k), dtype=torch.uint8, device="cuda")
-    d_used = torch.zeros(BATCH, dtype=torch.uint8, device="cuda")
-    d_ok = torch.zeros(BATCH, dtype=torch.uint8, device="cuda")
-    d_it = torch.zeros(BATCH, dtype=torch.uint8, device="cuda")
-    dec = fec.StreamBpOsdDecoder(code, max_batch=BATCH, max_iter=ITERS, normalization=ALPHA, offset=0.0,
-                                 damping=0.0, min_abs_llr_accept=0.0, osd_order=OSD_ORDER, osd_max_flip=OSD_FLIP,
-                                 osd_max_tests=OSD_TESTS)
+    # one decoder and stream per Eb/N0 point (two receive chains): one chain's BP overlaps the
+    # other's OSD
+    chain = {}
+    for e in EBN0:
+        chain[e] = dict(
+            dec=fec.StreamBpOsdDecoder(code, max_batch=BATCH, max_iter=ITERS, normalization=ALPHA, offset=0.0,
+                                       damping=0.0, min_abs_llr_accept=0.0, osd_order=OSD_ORDER,
+                                       osd_max_flip=OSD_FLIP, osd_max_tests=OSD_TESTS),
+            stream=torch.cuda.Stream(),
+            out=[torch.zeros((BATCH, code.k), dtype=torch.uint8, device="cuda")] +
+                [torch.zeros(BATCH, dtype=torch.uint8, device="cuda") for _ in range(3)])  # info, ok, used, iters
 
     def step(s):
         for e in EBN0:
-            dec.decode_device_batch(d_llr[e][s % RESIDENT_BATCHES], d_info, d_ok, d_used, d_it, stream=stream)
+            c = chain[e]
+            c["dec"].decode_device_batch(d_llr[e][s % RESIDENT_BATCHES], *c["out"], stream=c["stream"])
+
+    def fork(ev):
+        for e in EBN0:
+            chain[e]["stream"].wait_event(ev)
+
+    def join():
+        for e in EBN0:
+            ev = torch.cuda.Event()
+            ev.record(chain[e]["stream"])
+            stream.wait_event(ev)
 
     for s in range(args.warmup):
         step(s)
     torch.cuda.synchronize()
-    dec.set_timing(True)
+    for e in EBN0:
+        chain[e]["dec"].set_timing(True)
     clocks = ClockSampler(dev)
     if world > 1:
         dist.barrier()
@@ -218,14 +236,19 @@ def run_ours(args, rank, world):
     time.sleep(0.3)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
+    fork(ev0)
     for s in range(args.steps):
         step(s)
+    join()
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
     elapsed_ms = ev0.elapsed_time(ev1)
-    calls, bp_ms, osd_ms, osd_cw = dec.kernel_ms()
-    dec.set_timing(False)
+    calls = bp_ms = osd_ms = osd_cw = 0
+    for e in EBN0:
+        k_calls, k_bp, k_osd, k_cw = chain[e]["dec"].kernel_ms()
+        chain[e]["dec"].set_timing(False)
+        calls, bp_ms, osd_ms, osd_cw = calls + k_calls, bp_ms + k_bp, osd_ms + k_osd, osd_cw + k_cw
     if world > 1:
         dist.barrier()
         t = torch.tensor([elapsed_ms], device="cuda")
@@ -237,7 +260,8 @@ def run_ours(args, rank, world):
     edge_updates = 0
     for e in EBN0:
         info_true = inputs[e][0][0]
-        dec.decode_device_batch(d_llr[e][0], d_info, d_ok, d_used, d_it, stream=stream)
+        d_info, d_ok, d_used, d_it = chain[e]["out"]
+        chain[e]["dec"].decode_device_batch(d_llr[e][0], d_info, d_ok, d_used, d_it, stream=stream)
         torch.cuda.synchronize()
         got = d_info.cpu().numpy()
         fer[f"{e:g}dB"] = float(np.mean(np.any(got != info_true, axis=1)))
@@ -252,9 +276,11 @@ def run_ours(args, rank, world):
     # ---- end to end through the reference-facing C ABI with host buffers ----
     e2e = None
     if not args.no_e2e:
-        dec_api = fec.StreamBpOsdDecoder(code, max_batch=BATCH, min_batch=BATCH, max_iter=ITERS, normalization=ALPHA,
-                                         offset=0.0, damping=0.0, min_abs_llr_accept=0.0, osd_order=OSD_ORDER,
-                                         osd_max_flip=OSD_FLIP, osd_max_tests=OSD_TESTS)
+        # one reference-API decoder per receive chain (Eb/N0 point), as the device-timed step
+        dec_api = {e: fec.StreamBpOsdDecoder(code, max_batch=BATCH, min_batch=BATCH, max_iter=ITERS,
+                                             normalization=ALPHA, offset=0.0, damping=0.0, min_abs_llr_accept=0.0,
+                                             osd_order=OSD_ORDER, osd_max_flip=OSD_FLIP, osd_max_tests=OSD_TESTS)
+                   for e in EBN0}
         pinned = {}
         for e in EBN0:
             pinned[e] = []
@@ -268,25 +294,26 @@ def run_ours(args, rank, world):
         # so uploads and host-side result copies overlap the decode; the last step is flushed and
         # drained before the clock stops.  Every step's LLRs cross host->device and its information
         # bits device->host inside the timed region.
-        total = len(EBN0) * BATCH
-        bufs = dec_api.poll_buffers(total)
+        bufs = dec_api[EBN0[0]].poll_buffers(BATCH)
         blocks = np.arange(BATCH, dtype=np.uint32)
 
         def e2e_submit(s):
             for i, e in enumerate(EBN0):
-                dec_api.submit(pinned[e][s % 2], np.full(BATCH, 2 * s + i, np.uint64), blocks)
+                dec_api[e].submit(pinned[e][s % 2], np.full(BATCH, 2 * s + i, np.uint64), blocks)
 
         def e2e_collect():
-            got = 0
-            while got < total:
-                got += len(dec_api.poll(total - got, bufs)[0])
+            for e in EBN0:
+                got = 0
+                while got < BATCH:
+                    got += len(dec_api[e].poll(BATCH - got, bufs)[0])
 
         def e2e_run(steps):
             for s in range(steps):
                 e2e_submit(s)
                 if s > 0:
                     e2e_collect()
-            dec_api.flush()
+            for e in EBN0:
+                dec_api[e].flush()
             e2e_collect()
 
         e2e_run(min(args.warmup, 2))
@@ -298,8 +325,9 @@ def run_ours(args, rank, world):
         e2e = {"value": round(world * bits_per_step * args.steps / e2e_s / 1e6, 3), "unit": "Mbit/s",
                "h2d_bytes_per_step": len(EBN0) * BATCH * code.n * 4,
                "d2h_bytes_per_step": len(EBN0) * BATCH * (code.k + 1),
-               "api": "cuda_osd_submit_codewords + cuda_osd_poll_ready, streaming (a step's submits overlap the "
-                      "previous step's decode; flush + drain at the end), pinned host LLRs"}
+               "api": "cuda_osd_submit_codewords + cuda_osd_poll_ready, one stream decoder per Eb/N0 chain, "
+                      "streaming (a step's submits overlap the previous step's decode; flush + drain at the end), "
+                      "pinned host LLRs"}
 
     # ---- roofline of the dominant kernel (layered BP) ----
     peak, peak_kind = peaks()
@@ -341,6 +369,7 @@ def run_ours(args, rank, world):
                 "ms_per_step": round(elapsed_ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded BPSK/AWGN LLRs)",
                 "config": {"workload": WORKLOAD, "code": "QC (128,64) 4x8 base Z=16", "frames_per_batch": BATCH,
+                           "chains": "one decoder and CUDA stream per Eb/N0 point",
                            "ebn0_db": list(EBN0), "bp": f"layered NMS alpha {ALPHA}, <= {ITERS} iterations",
                            "osd": f"order {OSD_ORDER}, {1 + OSD_FLIP + OSD_FLIP * (OSD_FLIP - 1) // 2} tests",
                            "l2": f"{2 * RESIDENT_BATCHES} resident batches of 33.5 MB cycled (> L2)",
