@@ -606,18 +606,22 @@ def run_ofdm_tx(args, rank, world):
     batch_ms = e0.elapsed_time(e1) / reps
     tx_bytes = frames * (blocks * code.k + 2 * blocks * code.n + 8 * L)  # info in, coded out + in, frame out
 
-    # end to end: pinned host info bits -> device -> frames -> pinned host
-    h_info = torch.empty((frames, blocks * code.k), dtype=torch.uint8, pin_memory=True)
-    h_info.numpy()[:] = info[0]
-    h_out = torch.empty((frames, L), dtype=torch.complex64, pin_memory=True)
-    d_in = torch.empty((frames, blocks * code.k), dtype=torch.uint8, device="cuda")
+    # end to end: pinned host info bits -> device -> frames -> pinned host, the step's batches on
+    # their own CUDA streams so one batch's copies overlap another's kernels
+    lanes = [dict(stream=torch.cuda.Stream(),
+                  h_info=torch.empty((frames, blocks * code.k), dtype=torch.uint8, pin_memory=True),
+                  d_in=torch.empty((frames, blocks * code.k), dtype=torch.uint8, device="cuda"),
+                  h_out=torch.empty((frames, L), dtype=torch.complex64, pin_memory=True)) for _ in range(per_step)]
+    for ln in lanes:
+        ln["h_info"].numpy()[:] = info[0]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for s in range(args.steps):
-        for b in range(per_step):
-            d_in.copy_(h_info, non_blocking=True)
-            pipe.tx_batch(d_in, frames, d_out[0], stream=stream)
-            h_out.copy_(d_out[0], non_blocking=True)
+        for b, ln in enumerate(lanes):
+            with torch.cuda.stream(ln["stream"]):
+                ln["d_in"].copy_(ln["h_info"], non_blocking=True)
+                pipe.tx_batch(ln["d_in"], frames, d_out[b], stream=ln["stream"])
+                ln["h_out"].copy_(d_out[b], non_blocking=True)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
 
