@@ -262,6 +262,36 @@ def test_device_batch_entry_matches_stream_api(cuda, oracle):
         assert np.array_equal(info[i], exp) and bool(used[i]) == osd, i
 
 
+def test_two_chains_on_their_own_streams_match_one_stream(cuda):
+    """Two decoders decoding at once on two CUDA streams (the bench's receive chains) give the
+    bits of the same batches decoded one after another on one stream."""
+    from sicc_gb300 import fec
+    torch = cuda
+    code = codes.short_code()
+    llrs = [channel.awgn_llrs(code, 8192, e, seed=300 + i)[2] for i, e in enumerate((2.0, 3.0))]
+    decs = [fec.StreamBpOsdDecoder(code, max_batch=8192, max_iter=20, normalization=0.75, offset=0.0, damping=0.0,
+                                   min_abs_llr_accept=0.0) for _ in llrs]
+
+    def buffers():
+        return [torch.zeros((8192, code.k), dtype=torch.uint8, device="cuda")] + \
+               [torch.zeros(8192, dtype=torch.uint8, device="cuda") for _ in range(3)]
+
+    d_llr = [_dev(torch, x) for x in llrs]
+    one = [buffers() for _ in llrs]
+    for i, dec in enumerate(decs):
+        dec.decode_device_batch(d_llr[i], *one[i], stream=torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    two = [buffers() for _ in llrs]
+    streams = [torch.cuda.Stream() for _ in llrs]
+    for _ in range(3):  # repeated, so the chains overlap in different phases
+        for i, dec in enumerate(decs):
+            dec.decode_device_batch(d_llr[i], *two[i], stream=streams[i])
+    torch.cuda.synchronize()
+    for a, b in zip(one, two):
+        for x, y in zip(a, b):
+            assert torch.equal(x, y)
+
+
 def test_default_ccsds_code_and_osd_only_decoder(cuda, oracle):
     from sicc_gb300 import fec
     g = dict(np.load(os.path.join(GOLDEN, "fec_short_code.npz")))
