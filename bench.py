@@ -115,6 +115,21 @@ def cpu_decode(pool, workers, llr):
     return wall, info, used
 
 
+def max_over_ranks(value, device):
+    """The largest of every rank's `value` (all ranks get it): a step's time is the slowest rank's."""
+    import torch
+    import torch.distributed as dist
+    dist.barrier()
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank, world, steps, elapsed_ms):
+    """Whole-job throughput: the units every rank processed over the slowest rank's time."""
+    return world * units_per_rank * steps / (elapsed_ms * 1e-3)
+
+
 def make_inputs(batch, n_batches, seed0):
     from sicc_gb300 import channel, codes
     code = codes.short_code()
@@ -250,10 +265,7 @@ def run_ours(args, rank, world):
         chain[e]["dec"].set_timing(False)
         calls, bp_ms, osd_ms, osd_cw = calls + k_calls, bp_ms + k_bp, osd_ms + k_osd, osd_cw + k_cw
     if world > 1:
-        dist.barrier()
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+        elapsed_ms = max_over_ranks(elapsed_ms, "cuda")
 
     # frame error rate and iterations on one resident batch per Eb/N0
     fer, mean_iter, osd_frac = {}, {}, {}
