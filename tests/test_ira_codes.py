@@ -69,3 +69,20 @@ def test_seeded_and_reproducible():
     assert np.array_equal(a.col_ind, b.col_ind)
     other = codes.dvbs2_code("N16200_R1/2", seed=codes.IRA_CODE_SEED + 1)
     assert not np.array_equal(a.col_ind, other.col_ind)
+
+
+def test_oracle_decodes_a_long_code(oracle):
+    """The oracle the long-code GPU tests compare against: a noiseless frame in one pass, a noisy
+    one to the transmitted word, both schedules the GPU tests use."""
+    c = codes.dvbs2_code("N16200_R1/2")
+    oc = oracle.code(c.n, c.m, c.row_ptr, c.col_ind)
+    order, _, ncolors = oc.color_order()
+    assert 1 < ncolors <= 64
+    info, cw, llr = channel.awgn_llrs(c, 1, 30.0, seed=11)
+    ok, bits, _, _, it, _ = oc.layered(llr[0], 25, 0.75, row_order=order)
+    assert ok and it == 1 and np.array_equal(bits, cw[0])
+    info, cw, llr = channel.awgn_llrs(c, 1, 2.5, seed=12)
+    ok, bits, _, _, it, _ = oc.layered(llr[0], 25, 0.75, row_order=order)
+    assert ok and np.array_equal(bits, cw[0])
+    ok, bits, _, _, it, _ = oc.flooding(llr[0], 40, 0.8, 0.15, 0.0)
+    assert ok and np.array_equal(bits, cw[0])
