@@ -46,6 +46,16 @@ OSD_ORDER, OSD_FLIP, OSD_TESTS = 2, 64, 4096
 WORKLOAD = "bp_osd_128_64"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC = os.path.join(ROOT, "profiles", "bp_layered_128_64_traffic.json")
+KERNEL_TRAFFIC = os.path.join(ROOT, "profiles", "kernel_traffic.json")
+
+
+def traffic_for(kernel, units):
+    """DRAM bytes of `kernel` for `units` (frames or codewords) from its ncu capture, or None."""
+    try:
+        with open(KERNEL_TRAFFIC) as f:
+            return int(round(json.load(f)[kernel]["bytes_per_unit"] * units))
+    except Exception:
+        return None
 
 
 def peaks():
@@ -550,7 +560,8 @@ def run_ofdm(args, rank, world):
             "fer": fer, "kernel_ms_per_step": {k: round(v, 4) for k, v in kern.items()}, "dominant_kernel": top,
             "gpu_launches": args.steps * len(OFDM_SNRS) * 3, "clocks": clk,
             "roofline": {"bound": "hbm", "kernel": "demod_kernel", "achieved": round(achieved, 2), "peak": peak,
-                         "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": None, "peak_source": peak_kind,
+                         "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": traffic_for("demod_kernel", frames),
+                         "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": demod_bytes},
             "e2e": {"value": round(world * info_bits * args.steps / e2e_s / 1e6, 3), "unit": "Mbit/s",
                     "h2d_bytes_per_step": len(OFDM_SNRS) * frames * L * 8,
@@ -664,7 +675,8 @@ def run_ofdm_tx(args, rank, world):
             "batch_ms": round(batch_ms, 4),
             "gpu_launches": args.steps * per_step * 2, "clocks": clk,
             "roofline": {"bound": "hbm", "kernel": "tx_encode + tx_symbol_kernel", "achieved": round(achieved, 2),
-                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": None,
+                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5),
+                         "traffic": traffic_for("tx_encode + tx_symbol_kernel", frames),
                          "peak_source": peak_kind, "algorithmic_bytes_per_launch": tx_bytes},
             "e2e": {"value": round(world * info_bits * args.steps / e2e_s / 1e6, 3), "unit": "Mbit/s",
                     "h2d_bytes_per_step": per_step * frames * blocks * code.k,
@@ -914,7 +926,7 @@ def run_mixed(args, rank, world):
                          "achieved": round((w.llr.nbytes + w.info_bits) / (bp_ms * 1e-3) / 1e9, 2), "peak": peak,
                          "unit": "GB/s",
                          "frac": round((w.llr.nbytes + w.info_bits) / (bp_ms * 1e-3) / 1e9 / peak, 5),
-                         "traffic": None, "peak_source": peak_kind,
+                         "traffic": traffic_for("bp_mixed_kernel<16>", w.count), "peak_source": peak_kind,
                          "note": "issue-bound; HBM fraction shown per contract"},
             "e2e": e2e, "cpu_baseline": cpu}
     if rank == 0:
