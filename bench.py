@@ -68,16 +68,21 @@ def peaks():
 
 
 # ---------------------------------------------------------------- CPU baseline
+_CPU_CODE = {}
+
+
 def _cpu_worker(args):
     llr, iters, alpha = args
-    from oracle import Oracle
-    from sicc_gb300 import codes
-    o = Oracle()
-    c = codes.short_code()
-    oc = o.code(c.n, c.m, c.row_ptr, c.col_ind)
+    if "oc" not in _CPU_CODE:  # code tables built once per worker process
+        from oracle import Oracle
+        from sicc_gb300 import codes
+        c = codes.short_code()
+        oc = Oracle().code(c.n, c.m, c.row_ptr, c.col_ind)
+        _CPU_CODE.update(oc=oc, table=oc.systematic_parity())
+    oc, table = _CPU_CODE["oc"], _CPU_CODE["table"]
     t0 = time.perf_counter()
     info, used = oc.bp_osd_batch(llr, schedule=0, max_iter=iters, alpha=alpha, osd_order=OSD_ORDER,
-                                 osd_max_flip=OSD_FLIP, osd_max_tests=OSD_TESTS)
+                                 osd_max_flip=OSD_FLIP, osd_max_tests=OSD_TESTS, table=table)
     return time.perf_counter() - t0, info, used
 
 
@@ -115,8 +120,28 @@ def _cpu_ofdm_worker(args):
     return time.perf_counter() - t0
 
 
+def fer_parity_point(sent, ref_info, gpu_info, gpu_flood_info):
+    """Error rates of the reference decoder and the GPU decoders on identical frames."""
+    from sicc_gb300 import errstats
+    ref = errstats.rate_summary(ref_info, sent)
+    lay = errstats.rate_summary(gpu_info, sent)
+    pair = errstats.mcnemar(errstats.frame_errors(gpu_info, sent) > 0, errstats.frame_errors(ref_info, sent) > 0)
+    lo, hi = ref["fer_ci95"]
+    return {"frames": ref["frames"],
+            "reference": {"fer": ref["fer"], "fer_ci95": [round(lo, 6), round(hi, 6)], "ber": ref["ber"],
+                          "ber_ci95": [round(x, 7) for x in ref["ber_ci95"]]},
+            "gpu_layered": {"fer": lay["fer"], "ber": lay["ber"],
+                            "fer_vs_reference_ci": "inside" if lo <= lay["fer"] <= hi else
+                            ("below" if lay["fer"] < lo else "above"),
+                            "ber_vs_reference_ci": "inside" if errstats.inside(lay["ber"], ref["ber_ci95"]) else
+                            ("below" if lay["ber"] < ref["ber_ci95"][0] else "above"),
+                            "frames_only_gpu_fails": pair["only_a"], "frames_only_reference_fails": pair["only_b"],
+                            "mcnemar_p": round(pair["p_value"], 6)},
+            "gpu_flooding_bit_exact": bool(np.array_equal(gpu_flood_info, ref_info))}
+
+
 def cpu_decode(pool, workers, llr):
-    chunks = np.array_split(llr, workers)
+    chunks = np.array_split(llr, 4 * workers)
     t0 = time.perf_counter()
     res = pool.map(_cpu_worker, [(c, ITERS, ALPHA) for c in chunks])
     wall = time.perf_counter() - t0
@@ -279,6 +304,7 @@ def run_ours(args, rank, world):
 
     # frame error rate and iterations on one resident batch per Eb/N0
     fer, mean_iter, osd_frac = {}, {}, {}
+    gpu_info = {}
     edge_updates = 0
     for e in EBN0:
         info_true = inputs[e][0][0]
@@ -286,11 +312,42 @@ def run_ours(args, rank, world):
         chain[e]["dec"].decode_device_batch(d_llr[e][0], d_info, d_ok, d_used, d_it, stream=stream)
         torch.cuda.synchronize()
         got = d_info.cpu().numpy()
+        gpu_info[e] = got
         fer[f"{e:g}dB"] = float(np.mean(np.any(got != info_true, axis=1)))
         it = d_it.cpu().numpy().astype(np.int64)
         mean_iter[f"{e:g}dB"] = float(it.mean())
         osd_frac[f"{e:g}dB"] = float(d_used.cpu().numpy().mean())
         edge_updates += int(it.sum()) * code.edges
+
+    # the reference's schedule on the GPU: flooding min-sum + OSD on the best-syndrome posterior
+    # (the reference decoder's arithmetic, bit for bit): its throughput and its bits on batch 0
+    flood = {e: fec.StreamBpOsdDecoder(code, max_batch=BATCH, max_iter=ITERS, normalization=ALPHA, offset=0.0,
+                                       damping=0.0, min_abs_llr_accept=0.0, schedule=0, osd_order=OSD_ORDER,
+                                       osd_max_flip=OSD_FLIP, osd_max_tests=OSD_TESTS) for e in EBN0}
+
+    def flood_step(s):
+        for e in EBN0:
+            flood[e].decode_device_batch(d_llr[e][s % RESIDENT_BATCHES], *chain[e]["out"], stream=chain[e]["stream"])
+
+    for s in range(min(args.warmup, 3)):
+        flood_step(s)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    fork(ev0)
+    for s in range(args.steps):
+        flood_step(s)
+    join()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    flood_ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        flood_ms = max_over_ranks(flood_ms, "cuda")
+    flood_info = {}
+    for e in EBN0:
+        d_info = chain[e]["out"][0]
+        flood[e].decode_device_batch(d_llr[e][0], d_info, stream=stream)
+        torch.cuda.synchronize()
+        flood_info[e] = d_info.cpu().numpy()
 
     bits_per_step = len(EBN0) * BATCH * code.k
     value = world * bits_per_step * args.steps / (elapsed_ms * 1e-3) / 1e6
@@ -372,18 +429,26 @@ def run_ours(args, rank, world):
                 "note": "BP is issue-bound (messages and row tables in registers, posteriors in shared memory); "
                         "HBM fraction shown per contract"}
 
-    cpu = None
+    # ---- CPU baseline: the reference decoder on the same frames, and the error-rate parity ----
+    cpu = fer_parity = None
     if pool is not None:
-        sample = {e: inputs[e][1][2][: args.cpu_sample] for e in EBN0}
         wall = 0.0
+        fer_parity = {}
         for e in EBN0:
-            w, _, _ = cpu_decode(pool, workers, sample[e])
+            info_true = inputs[e][0][0]
+            w, ref_info, _ = cpu_decode(pool, workers, inputs[e][0][2])
             wall += w
+            fer_parity[f"{e:g}dB"] = fer_parity_point(info_true, ref_info, gpu_info[e], flood_info[e])
         pool.close()
-        cpu = {"value": round(len(EBN0) * args.cpu_sample * code.k / wall / 1e6, 4), "unit": "Mbit/s",
+        fer_parity["reference_schedule_on_gpu"] = {
+            "value": round(world * bits_per_step * args.steps / (flood_ms * 1e-3) / 1e6, 3), "unit": "Mbit/s",
+            "what": "flooding min-sum + OSD on the best-syndrome posterior (bit-exact with the reference decoder), "
+                    "same chains and batches as the headline step"}
+        cpu = {"value": round(len(EBN0) * BATCH * code.k / wall / 1e6, 4), "unit": "Mbit/s",
                "cores": workers, "kind": "port",
-               "sample": f"{args.cpu_sample} frames at each of 2 and 3 dB (flooding min-sum alpha 0.75, 20 "
-                         f"iterations, order-2 OSD on failures), {workers} worker processes"}
+               "sample": f"the first resident batch at each of 2 and 3 dB ({BATCH} frames each, the frames of "
+                         f"fer_parity): the reference decoder (flooding min-sum alpha 0.75, 20 iterations, "
+                         f"order-2 OSD on the best-syndrome posterior), {workers} worker processes"}
 
     if rank == 0:
         line = {"metric": "info-bit Mbps BP+OSD (128,64), Eb/N0 2 and 3 dB", "value": round(value, 3),
@@ -396,7 +461,7 @@ def run_ours(args, rank, world):
                            "osd": f"order {OSD_ORDER}, {1 + OSD_FLIP + OSD_FLIP * (OSD_FLIP - 1) // 2} tests",
                            "l2": f"{2 * RESIDENT_BATCHES} resident batches of 33.5 MB cycled (> L2)",
                            "parallelism": f"replicas x{world}"},
-                "fer": fer, "mean_iterations": mean_iter, "osd_fraction": osd_frac,
+                "fer": fer, "fer_parity": fer_parity, "mean_iterations": mean_iter, "osd_fraction": osd_frac,
                 "gpu_launches": args.steps * len(EBN0) * 2, "clocks": clk, "roofline": roofline,
                 "e2e": e2e, "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
@@ -1202,22 +1267,25 @@ def run_reference(args, rank, world):
         return
     workers = os.cpu_count() or 1
     pool = mp.get_context("spawn").Pool(workers)
-    code, inputs = make_inputs(args.cpu_sample, 1, seed0=1000)
-    for _ in range(min(args.warmup, 1)):
-        cpu_decode(pool, workers, inputs[EBN0[0]][0][2][: workers * 8])
+    # the same frames as the GPU arm's first resident batch (rank 0's seeds), first cpu_sample of each
+    code, inputs = make_inputs(BATCH, 1, seed0=1000)
+    sample = {e: (inputs[e][0][0][: args.cpu_sample], inputs[e][0][2][: args.cpu_sample]) for e in EBN0}
+    for _ in range(max(1, min(args.warmup, 1))):  # also builds each worker's code tables
+        cpu_decode(pool, workers, sample[EBN0[0]][1][: workers * 32])
     wall = 0.0
     fer = {}
     for s in range(args.steps):
         for e in EBN0:
-            w, info, _ = cpu_decode(pool, workers, inputs[e][0][2])
+            w, info, _ = cpu_decode(pool, workers, sample[e][1])
             wall += w
             if s == 0:
-                fer[f"{e:g}dB"] = float(np.mean(np.any(info != inputs[e][0][0], axis=1)))
+                fer[f"{e:g}dB"] = float(np.mean(np.any(info != sample[e][0], axis=1)))
     pool.close()
     bits = args.steps * len(EBN0) * args.cpu_sample * code.k
     value = bits / wall / 1e6
-    sample = (f"{args.cpu_sample} frames at each of 2 and 3 dB per step: the reference's flooding min-sum "
-              f"(alpha 0.75, 20 iterations) + order-2 OSD on failures, {workers} worker processes")
+    sample = (f"the first {args.cpu_sample} frames of the GPU arm's first batch at each of 2 and 3 dB, every step: "
+              f"the reference decoder (flooding min-sum alpha 0.75, 20 iterations, order-2 OSD on the "
+              f"best-syndrome posterior), {workers} worker processes")
     line = {"impl": "reference", "metric": "info-bit Mbps BP+OSD (128,64), Eb/N0 2 and 3 dB",
             "value": round(value, 4), "unit": "Mbit/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(wall * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
@@ -1229,6 +1297,17 @@ def run_reference(args, rank, world):
                              "sample": sample},
             "e2e": {"value": round(value, 4), "unit": "Mbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def spawn_ranks(n, argv):
+    """Runs bench.py with `argv` as `n` ranks on this node (127.0.0.1 rendezvous); returns the exit code."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + list(argv)
+    return subprocess.call(cmd)
 
 
 def main():
@@ -1256,8 +1335,13 @@ def main():
     args = ap.parse_args()
     globals()["BATCH"] = args.batch
     globals()["RESIDENT_BATCHES"] = args.resident
+    if args.gpus > 1 and "RANK" not in os.environ:
+        # one process per GPU: run this command again under torch.distributed.run with N ranks
+        sys.exit(spawn_ranks(args.gpus, sys.argv[1:]))
     rank = int(os.environ.get("RANK", 0))
-    world = int(os.environ.get("WORLD_SIZE", args.gpus if "RANK" in os.environ else 1))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if world != args.gpus:
+        sys.exit(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}")
     if args.impl == "reference":
         run_reference(args, rank, world)
     elif args.workload == "ofdm_rx_1024_512":

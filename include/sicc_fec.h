@@ -202,9 +202,10 @@ SICC_API int sicc_fec_get_kernel_ms(unsigned long long handle, int* out_calls, f
 
 /* Device-resident BP->OSD decode that allocates nothing.  It has no
  * counterpart in the reference.  It is for callers that cannot allocate
- * device memory when they decode: a receiver whose memory is fixed once it
- * starts, or code recorded into a CUDA graph, where cudaMalloc is not
- * permitted during stream capture.  The BP->OSD hand-off scratch lives in one
+ * device memory when they decode: a receiver whose device memory is fixed once
+ * it starts (reserved up front, the rest owned by the application), or a
+ * receive loop with a sample deadline, where a cudaMalloc may wait on work
+ * already queued on the GPU.  The BP->OSD hand-off scratch lives in one
  * static device array of the library (about 8.4 MB on every GPU that loads
  * it, held until the process exits); batches hold at most
  * SICC_FEC_STATIC_MAX_CODEWORDS codewords of n <= 256, independent of the
@@ -213,7 +214,11 @@ SICC_API int sicc_fec_get_kernel_ms(unsigned long long handle, int* out_calls, f
  * there (set-up), so make that first call before any stream capture.  Every
  * call shares the one array: calls whose work overlaps on the GPU (other
  * streams, other handles, other threads) race and must be serialised by the
- * caller.  Outputs match sicc_fec_decode_device bit for bit. */
+ * caller.  Outputs match sicc_fec_decode_device bit for bit.  These calls are
+ * not counted by sicc_fec_set_timing / sicc_fec_get_kernel_ms (timing records
+ * would need host allocations).  The array's address is cached per device for
+ * the life of the process: a cudaDeviceReset while the library is loaded is
+ * not supported. */
 #define SICC_FEC_STATIC_MAX_CODEWORDS 8192
 SICC_API int sicc_fec_decode_device_static(unsigned long long handle, const float* device_llrs, int codewords,
                                            unsigned char* device_info_bits, unsigned char* device_success,

@@ -27,6 +27,13 @@ _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
 
 
+def ref_root() -> str:
+    """Root of the reference tree as the oracle recipe resolves it (REF_ROOT, else its default)."""
+    out = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "print-ref-root"], check=True,
+                         capture_output=True, text=True)
+    return out.stdout.strip()
+
+
 def build_oracle(ref: bool = False) -> None:
     """Compile liboracle.so (and, when asked and the reference exists, _ref)."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
@@ -405,3 +412,73 @@ class RefPhy:
         if n < 0:
             raise RuntimeError(self.r.L.ref_last_error().decode())
         return out
+
+
+# ---- batch decoding on a process pool (the CPU reference run on every host core) ----
+def _bp_osd_chunk(args):
+    """One worker's share of a batch: BP (+ OSD) through the oracle, with its wall time."""
+    import time
+    n, m, row_ptr, col_ind, table, llr, kw = args
+    oc = Oracle().code(n, m, row_ptr, col_ind)
+    t0 = time.perf_counter()
+    info, used = oc.bp_osd_batch(llr, table=table, **kw)
+    return time.perf_counter() - t0, info, used
+
+
+def bp_osd_parallel(pool, code, llrs, chunks: int | None = None, **kw):
+    """Decodes `llrs` [F][n] with ``OracleCode.bp_osd_batch(**kw)`` split over a process pool.
+
+    `code` needs n, m, row_ptr and col_ind.  The pool must come from a ``spawn``
+    context (a forked child of a process that has touched CUDA can hang).
+    Returns (wall seconds, info [F][k], used_osd [F]).
+    """
+    import time
+    workers = getattr(pool, "_processes", None) or os.cpu_count() or 1
+    parts = np.array_split(np.ascontiguousarray(llrs, np.float32), chunks or 4 * workers)
+    table = kw.pop("table", None)
+    if table is None:
+        table = Oracle().code(code.n, code.m, code.row_ptr, code.col_ind).systematic_parity()
+    t0 = time.perf_counter()
+    res = pool.map(_bp_osd_chunk, [(code.n, code.m, np.asarray(code.row_ptr), np.asarray(code.col_ind), table, p, kw)
+                                   for p in parts if len(p)])
+    wall = time.perf_counter() - t0
+    return wall, np.concatenate([r[1] for r in res]), np.concatenate([r[2] for r in res])
+
+
+def _ofdm_chain_chunk(args):
+    """The restated CPU receiver on a few frames: earliest-crossing sync, demod with the
+    known noise variance, then layered BP of every codeword of the frame."""
+    cfg, n, m, row_ptr, col_ind, iq, noise_var, max_iter, alpha = args
+    from sicc_gb300 import ofdm  # the package is on the parent's sys.path, passed to spawned workers
+    o = Oracle()
+    t = ofdm.reference_tables(cfg)
+    ph = o.phy(t)
+    oc = o.code(n, m, row_ptr, col_ind)
+    k = oc.k
+    blocks = t.coded_bits // n
+    found = np.zeros(len(iq), np.int32)
+    start = np.full(len(iq), -1, np.int64)
+    cfo = np.zeros(len(iq), np.float64)
+    info = np.zeros((len(iq), blocks * k), np.uint8)
+    for f, x in enumerate(iq):
+        r = o.sync_earliest(ph, x)
+        found[f] = r[0]
+        if r[0] != 1:
+            continue
+        start[f], cfo[f] = r[1], r[4]
+        llr = o.demod_frame(ph, x[r[1]: r[1] + t.frame_len], r[4], noise_var)
+        dec, _ = oc.bp_osd_batch(llr[: blocks * n], schedule=3, max_iter=max_iter, alpha=alpha, osd_order=-1)
+        info[f] = dec.reshape(-1)
+    return found, start, cfo, info
+
+
+def ofdm_chain_parallel(pool, cfg, code, iq, noise_var, max_iter, alpha, chunks: int | None = None):
+    """Runs ``_ofdm_chain_chunk`` over frames `iq` [F][samples] on a spawn-context pool.
+
+    Returns (found [F], start [F], cfo_hz [F], info [F][blocks*k]).
+    """
+    workers = getattr(pool, "_processes", None) or os.cpu_count() or 1
+    idx = [p for p in np.array_split(np.arange(len(iq)), chunks or 2 * workers) if len(p)]
+    res = pool.map(_ofdm_chain_chunk, [(cfg, code.n, code.m, np.asarray(code.row_ptr), np.asarray(code.col_ind),
+                                        iq[p], noise_var, max_iter, alpha) for p in idx])
+    return tuple(np.concatenate([r[i] for r in res]) for i in range(4))

@@ -674,7 +674,12 @@ int or_bp_osd_batch(const or_code* c, const uint64_t* parity_table, int parity_w
         int it = 0, bw = 0, ok;
         const float* post = app;
         if (schedule == 0) {
-            ok = or_nms_flooding_ref(c, x, max_iter, (double)alpha, bits, app, &it);
+            /* cpu_bp_osd_decode.m as the reference runs it (MB:55-62): flooding min-sum
+             * (with no damping and no offset the same operations as L:3013-3094), and on
+             * a failed syndrome OSD on bestAppLlr, the posterior of the lowest syndrome
+             * weight seen (MB:116-119, 160-171). */
+            ok = or_nms_flooding_f32(c, x, max_iter, alpha, 0.0f, 0.0f, bits, app, best, &it, &bw);
+            post = best;
         } else {
             ok = or_nms_layered_f32(c, NULL, x, max_iter, alpha, 0.0f, bits, app, best, &it, &bw);
             post = best;

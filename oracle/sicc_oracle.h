@@ -92,11 +92,14 @@ int or_osd(int n, int k, const uint64_t* parity_table, int parity_words, const f
            int max_flip_positions, int max_tests, uint8_t* out_code, float* out_metric,
            int* out_best_test);
 
-/* Batch decode for the CPU baseline: `schedule` 0 = the reference flooding
- * decoder (L:3013-3094), 3 = row-sequential layered; frames whose syndrome
- * is not zero go to OSD when osd_order >= 0 (flooding: its final posterior,
- * layered: the best-syndrome posterior).  Writes the first k decoded bits of
- * each codeword and whether OSD ran.  Returns the number of OSD frames. */
+/* Batch BP -> OSD decode: `schedule` 0 = the reference's BP + OSD decoder
+ * (cpu_bp_osd_decode.m, MB:55-62: flooding min-sum, which without damping or
+ * offset performs the operations of L:3013-3094), 3 = row-sequential layered.
+ * Frames whose syndrome is not zero go to OSD when osd_order >= 0, on the
+ * posterior of the lowest syndrome weight seen (MB's bestAppLlr, MB:160-171;
+ * the channel LLRs when no iteration improved on them) for both schedules.
+ * Writes the first k decoded bits of each codeword and whether OSD ran.
+ * Returns the number of OSD frames. */
 int or_bp_osd_batch(const or_code* c, const uint64_t* parity_table, int parity_words, const float* llrs, int count,
                     int schedule, int max_iter, float alpha, int osd_order, int osd_max_flip, int osd_max_tests,
                     uint8_t* out_info, uint8_t* out_used_osd);

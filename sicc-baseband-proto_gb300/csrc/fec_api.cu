@@ -247,6 +247,7 @@ struct StreamDecoder : Decoder {
         std::vector<unsigned long long> ts, ids;
         std::vector<unsigned> blocks;
         int count = 0;
+        uint64_t first_arrival_us = 0;  // decoder clock when the batch took its first codeword
         bool in_flight = false;
         bool held = false;  // retired: its results wait in the ready queue, read in place
         cudaEvent_t done = nullptr;
@@ -458,7 +459,10 @@ struct StreamDecoder : Decoder {
         if (!claimed) return;
         Batch& b = *batches[filling];
         if (b.count <= 0) return;
-        const uint64_t age = now_us() - (b.ts.empty() ? now_us() : b.ts.front());
+        // the latency budget runs from the batch's first arrival at this decoder (not from the
+        // caller's timestamps, which may count on another clock)
+        const uint64_t now = now_us();
+        const uint64_t age = now > b.first_arrival_us ? now - b.first_arrival_us : 0;
         if (b.count >= std::max(1, cfg.min_batch_size) || b.count >= max_batch ||
             age >= std::max<unsigned long long>(cfg.max_latency_us, 1))
             launch_filling();
@@ -479,6 +483,7 @@ struct StreamDecoder : Decoder {
             claim();
             Batch& b = *batches[filling];
             const int take = std::min(count - done, max_batch - b.count);
+            if (b.count == 0) b.first_arrival_us = now;
             const size_t bytes = static_cast<size_t>(take) * n * sizeof(float);
             check_cuda(cudaMemcpyAsync(b.llr.p + static_cast<size_t>(b.count) * n,
                                        llrs + static_cast<size_t>(done) * n, bytes,

@@ -1,9 +1,10 @@
 // BP -> OSD decoding without any device allocation.
 //
 // Some callers cannot allocate device memory when they decode: a receiver
-// whose device memory is fixed once it starts (its budget reserved up front),
-// or code that records its work into a CUDA graph, where cudaMalloc is not
-// permitted while a stream is being captured.  For them this entry point
+// whose device memory is fixed once it starts (its budget reserved up front,
+// the rest owned by other parts of the application), or a receive loop with a
+// sample deadline, where a cudaMalloc may wait on work already queued on the
+// GPU and has no bound on its time.  For them this entry point
 // keeps the BP -> OSD hand-off scratch (failed-codeword posteriors, their
 // index list, two counters) in one file-scope device array of fixed size,
 // so a call allocates nothing and its batch size is not bound by the
@@ -37,7 +38,9 @@ std::mutex g_addr_mu;
 unsigned char* g_addr[64] = {nullptr};
 
 // Set-up: resolves the array's device address on the current device the
-// first time that device is used, and caches it.
+// first time that device is used, and caches it for the life of the process
+// (a cudaDeviceReset while the library is loaded is not supported: the cached
+// address would outlive the context it belongs to).
 unsigned char* static_scratch_address()
 {
     int dev = 0;

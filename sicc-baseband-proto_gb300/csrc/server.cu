@@ -685,7 +685,11 @@ int sicc_server_replay(unsigned long long handle, const sicc_request_t* requests
     return guarded([&]() -> int {
         auto s = get(handle);
         if (!requests || !arrival_us || !out_completions || count <= 0) throw InvalidArgument("bad arguments");
+        // Both threads below touch index, orphans, out_completions and t_last under idx_mu.
         std::map<unsigned long long, int> index;  // request id -> position
+        // A request can complete before sicc_server_submit has returned its id to the submitting
+        // thread; such completions wait here until the submitter records the id, then finish.
+        std::map<unsigned long long, sicc_completion_t> orphans;
         std::vector<double> late(count, 0.0);      // submit time minus scheduled arrival
         std::mutex idx_mu;
         std::atomic<int> done_count{0};
@@ -693,6 +697,14 @@ int sicc_server_replay(unsigned long long handle, const sicc_request_t* requests
         std::string error;
         const auto t0 = Clock::now();
         Clock::time_point t_last = t0;
+        auto finish = [&](int pos, const sicc_completion_t& c) {  // caller holds idx_mu
+            out_completions[pos] = c;
+            out_completions[pos].latency_us += late[pos];
+            out_completions[pos].queue_us += late[pos];
+            out_completions[pos].launch_us += late[pos];
+            t_last = Clock::now();
+            done_count.fetch_add(1);
+        };
         std::thread collector([&] {
             std::vector<sicc_completion_t> buf(256);
             while (done_count.load() < count && !failed.load()) {
@@ -702,20 +714,11 @@ int sicc_server_replay(unsigned long long handle, const sicc_request_t* requests
                     failed.store(true);
                     break;
                 }
+                std::lock_guard<std::mutex> lock(idx_mu);
                 for (int i = 0; i < got; ++i) {
-                    int pos = -1;
-                    for (int spin = 0; pos < 0 && spin < 1000000; ++spin) {  // the submitter records the id first
-                        std::lock_guard<std::mutex> lock(idx_mu);
-                        auto it = index.find(buf[i].request_id);
-                        if (it != index.end()) pos = it->second;
-                    }
-                    if (pos < 0) continue;
-                    out_completions[pos] = buf[i];
-                    out_completions[pos].latency_us += late[pos];
-                    out_completions[pos].queue_us += late[pos];
-                    out_completions[pos].launch_us += late[pos];
-                    t_last = Clock::now();
-                    done_count.fetch_add(1);
+                    auto it = index.find(buf[i].request_id);
+                    if (it != index.end()) finish(it->second, buf[i]);
+                    else orphans.emplace(buf[i].request_id, buf[i]);
                 }
             }
         });
@@ -737,6 +740,11 @@ int sicc_server_replay(unsigned long long handle, const sicc_request_t* requests
             late[i] = us_between(due, Clock::now());
             std::lock_guard<std::mutex> lock(idx_mu);
             index[id] = i;
+            auto early = orphans.find(id);
+            if (early != orphans.end()) {
+                finish(i, early->second);
+                orphans.erase(early);
+            }
         }
         collector.join();
         if (failed.load()) throw std::runtime_error("replay failed: " + error);

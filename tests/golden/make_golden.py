@@ -18,7 +18,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, os.path.join(ROOT, "sicc-baseband-proto_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-from oracle import Reference  # noqa: E402
+from oracle import Reference, ref_root  # noqa: E402
 from sicc_gb300 import channel, codes, ofdm  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
@@ -50,7 +50,7 @@ def fec_fixture(ref: Reference) -> dict:
 
 
 def ccsds_csr():
-    path = "/root/reference/data/code_matrices/Code_Matrices_Lib/LDPC/CCSDS_ldpc_n128_k64.alist"
+    path = os.path.join(ref_root(), "data", "code_matrices", "Code_Matrices_Lib", "LDPC", "CCSDS_ldpc_n128_k64.alist")
     return codes.read_alist(path)
 
 

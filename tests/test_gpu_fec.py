@@ -241,6 +241,38 @@ def test_stream_decoder_host_submits_past_the_ring_and_odd_polls(cuda, oracle):
     assert st["decoded_codewords"] == 320 and st["decoded_batches"] == 5
 
 
+def test_partial_batch_dispatches_after_latency_budget(cuda, oracle):
+    """A batch smaller than min_batch_size is held until its oldest codeword is max_latency_us old,
+    then launched by the next poll with no flush (the latency budget of API:17-32)."""
+    import time
+    from sicc_gb300 import fec
+    code = codes.short_code()
+    oc = oracle.code(code.n, code.m, code.row_ptr, code.col_ind)
+    table = oc.systematic_parity()
+    _, _, llr = channel.awgn_llrs(code, 10, 2.0, seed=91)
+    budget_us = 200_000
+    dec = fec.StreamBpOsdDecoder(code, max_batch=256, min_batch=64, latency_us=budget_us, max_iter=20,
+                                 normalization=0.75, offset=0.0, damping=0.0, min_abs_llr_accept=0.0)
+    t0 = time.monotonic()
+    dec.submit(llr, np.arange(10, dtype=np.uint64), np.zeros(10, np.uint32))
+    bufs = dec.poll_buffers(16)
+    early, *_ = dec.poll(16, bufs)
+    if time.monotonic() - t0 < 0.9 * budget_us * 1e-6:  # (a descheduled test process could pass the budget)
+        assert len(early) == 0 and dec.stats()["decoded_batches"] == 0
+    time.sleep(1.25 * budget_us * 1e-6)
+    got = {}
+    deadline = time.monotonic() + 10.0
+    while len(got) < 10 and time.monotonic() < deadline:
+        info, _, ids, _, _ = dec.poll(16, bufs)
+        for r in range(len(info)):
+            got[int(ids[r])] = info[r].copy()
+    assert len(got) == 10, "the held batch was not launched after its latency budget"
+    assert dec.stats()["decoded_batches"] == 1
+    for i in range(10):
+        exp, _ = _oracle_bp_osd(oracle, oc, table, code, llr[i])
+        assert np.array_equal(got[i], exp)
+
+
 def test_device_batch_entry_matches_stream_api(cuda, oracle):
     from sicc_gb300 import fec
     torch = cuda

@@ -14,7 +14,9 @@ import pytest
 
 from sicc_gb300 import channel, codes
 
-REF_LDPC = "/root/reference/data/code_matrices/Code_Matrices_Lib/LDPC"
+from oracle import ref_root
+
+REF_LDPC = os.path.join(ref_root(), "data", "code_matrices", "Code_Matrices_Lib", "LDPC")
 # (profile, reference alist file, edges, {column degree: columns})
 SHAPES = [
     ("N64800_R1/2", "DVB_S2_N64800_R12.alist", 226799, {1: 1, 2: 32399, 3: 19440, 8: 12960}),

@@ -51,3 +51,21 @@ def test_ranks_decode_distinct_replicas():
     a = channel.awgn_llrs(code, 16, 2.0, seed=1000 * 1 + 200)[2]
     b = channel.awgn_llrs(code, 16, 2.0, seed=1000 * 2 + 200)[2]
     assert a.shape == b.shape and not (a == b).all()
+
+
+def test_bench_gpus_n_spawns_n_ranks():
+    """`bench.py --gpus 2` without a launcher starts two ranks itself (torch.distributed.run on
+    127.0.0.1) and rank 0 alone prints the line, labelled with both ranks.  The reference arm needs
+    no GPU, so this runs the spawn path on CPU."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--gpus", "2",
+                          "--steps", "1", "--warmup", "1", "--cpu-sample", "64"],
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, out.stdout
+    line = json.loads(lines[0])
+    assert line["n_gpus"] == 2 and line["impl"] == "reference"

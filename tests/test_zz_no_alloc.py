@@ -1,10 +1,10 @@
 """The allocation-free BP->OSD entry point checked against the allocating one.
 
 Some callers cannot allocate device memory when they decode: a receiver whose
-device memory is fixed once it starts, or code recorded into a CUDA graph,
-where cudaMalloc is not permitted during stream capture.  They call
-sicc_fec_decode_device_static, which keeps the BP->OSD hand-off scratch in a
-static device array of the library instead of per-decoder memory.  On the same
+device memory is fixed once it starts, or a receive loop with a sample
+deadline, where a cudaMalloc may wait on work already queued on the GPU.  They
+call sicc_fec_decode_device_static, which keeps the BP->OSD hand-off scratch in
+a static device array of the library instead of per-decoder memory.  On the same
 inputs its outputs must equal those of sicc_fec_decode_device bit for bit, on
 every call: the array keeps the previous call's contents, so a second call in
 a row checks that what must start at zero is cleared.
