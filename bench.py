@@ -464,9 +464,9 @@ def run_ours(args, rank, world):
                 "fer": fer, "fer_parity": fer_parity, "mean_iterations": mean_iter, "osd_fraction": osd_frac,
                 "gpu_launches": args.steps * len(EBN0) * 2, "clocks": clk, "roofline": roofline,
                 "e2e": e2e, "cpu_baseline": cpu}
-        print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+    return line if rank == 0 else None
 
 
 # ------------------------------------------------------- OFDM receive workload
@@ -632,8 +632,7 @@ def run_ofdm(args, rank, world):
                     "h2d_bytes_per_step": len(OFDM_SNRS) * frames * L * 8,
                     "d2h_bytes_per_step": len(OFDM_SNRS) * frames * blocks * code.n},
             "cpu_baseline": cpu}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line if rank == 0 else None
 
 
 # ------------------------------------------------------ OFDM transmit workload
@@ -747,8 +746,7 @@ def run_ofdm_tx(args, rank, world):
                     "h2d_bytes_per_step": per_step * frames * blocks * code.k,
                     "d2h_bytes_per_step": per_step * frames * L * 8},
             "cpu_baseline": cpu}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line if rank == 0 else None
 
 
 # ------------------------------------------------------ real-time ingest workload
@@ -823,8 +821,7 @@ def run_ingest(args, rank, world):
             "e2e": {"value": round(value, 3), "unit": "Msample/s", "h2d_bytes_per_step": int(x.size * 8),
                     "d2h_bytes_per_step": int(found * 16)},
             "cpu_baseline": None}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line if rank == 0 else None
 
 
 # --------------------------------------------------- mixed-code batched workload
@@ -994,8 +991,7 @@ def run_mixed(args, rank, world):
                          "traffic": traffic_for("bp_mixed_kernel<16>", w.count), "peak_source": peak_kind,
                          "note": "issue-bound; HBM fraction shown per contract"},
             "e2e": e2e, "cpu_baseline": cpu}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line if rank == 0 else None
 
 
 # ------------------------------------------------------------ long-code workload
@@ -1095,8 +1091,7 @@ def run_dvbs2(args, rank, world):
                          "note": "decoder state is L2-resident per CTA; the kernel is latency-bound, HBM fraction "
                                  "shown per contract"},
             "e2e": e2e, "cpu_baseline": cpu}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line if rank == 0 else None
 
 
 # ------------------------------------------------------------------ serving loop
@@ -1205,7 +1200,7 @@ def run_serve(args, rank, world):
     fe = [int(np.any(q[2] != tr, axis=1).sum()) for q, tr in zip(reqs, truth)]
     cw_total = sum(q[2].shape[0] for q in reqs)
     sweep = []
-    for load in SERVE_LOADS:
+    for load in (args.serve_loads or SERVE_LOADS):
         rate = load * n_req / peak_s  # requests per second
         gaps = rng.exponential(1.0 / rate, n_req)
         arr = np.cumsum(gaps) * 1e6
@@ -1235,7 +1230,7 @@ def run_serve(args, rank, world):
     clk = clocks.stop()
     st = srv.stats()
     srv.close()
-    p80 = next(x for x in sweep if x["load"] == 0.8)
+    p80 = next((x for x in sweep if x["load"] == 0.8), sweep[-1])
     launches = int(st1.batches - st0.batches) * 3 + args.steps * iq_reqs * 2
     line = {"metric": "served info-bit Mbps (Poisson mixed-code + OFDM IQ requests), p50/p99/p99.9 latency",
             "value": round(peak_mbps, 3), "unit": "Mbit/s", "n_gpus": world, "steps": args.steps,
@@ -1257,8 +1252,93 @@ def run_serve(args, rank, world):
             "e2e": {"value": round(peak_mbps, 3), "unit": "Mbit/s", "h2d_bytes_per_step": in_bytes,
                     "d2h_bytes_per_step": out_bytes},
             "cpu_baseline": None}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line if rank == 0 else None
+
+
+# ------------------------------------- per-frame Pipeline class (reference benchmark configuration)
+FRAME_BENCH_SRC = os.path.join(ROOT, "tests", "cpp", "ofdm_frame_bench.cpp")
+
+
+def _frame_bench_line(impl, res, wall_s, frames, clk, extra):
+    """JSON line of the per-frame Pipeline workload from the driver's output."""
+    mbps = res["rx_fps"] * res["info_bits_per_frame"] / 1e6
+    line = {"metric": "frames/s through Pipeline::demod_frame_to_host_llr (host frame -> sync + demod -> host LLRs), "
+                      "reference GPU pipeline benchmark configuration",
+            "value": round(res["rx_fps"], 2), "unit": "frames/s", "n_gpus": 1, "steps": frames, "warmup": 64,
+            "ms_per_step": round(1e3 / res["rx_fps"], 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (noiseless QPSK OFDM loop-back frames)",
+            "config": {"workload": "ofdm_frame_pipeline", "fft": 1024, "cp": 72, "symbols": 96, "pilot_period": 4,
+                       "active_sc": 768, "modulation": "QPSK", "pre_half_len": 256,
+                       "frame_samples": res["frame_samples"], "coded_bits_per_frame": res["coded_bits_per_frame"],
+                       "code": "repetition (128,64)", "slots": 3,
+                       "source": "gpu_ofdm_pipeline_bench.cpp:21-38 defaults"},
+            "rx_info_mbps": round(mbps, 2), "tx_fps": round(res["tx_fps"], 2),
+            "roundtrip_fps": round(res["roundtrip_fps"], 2),
+            "hard_check": {"bits": res["checked_bits"], "errors": res["hard_errors"]},
+            "clocks": clk, "e2e": {"value": round(res["rx_fps"], 2), "unit": "frames/s",
+                                   "h2d_bytes_per_step": res["frame_samples"] * 8,
+                                   "d2h_bytes_per_step": res["coded_bits_per_frame"] * 4}}
+    if impl == "reference":
+        line["impl"] = "reference"
+    line.update(extra)
+    return line
+
+
+def _run_frame_bench(exe, frames):
+    out = subprocess.run([exe, "--frames", str(frames), "--warmup", "64"], capture_output=True, text=True,
+                         timeout=900)
+    if out.returncode != 0:
+        raise RuntimeError(f"{os.path.basename(exe)} exited {out.returncode}: {out.stderr[-500:]}")
+    return json.loads([ln for ln in out.stdout.splitlines() if ln.startswith("{")][-1])
+
+
+def run_frame_pipeline(args, rank, world):
+    """The per-frame Pipeline class path, timed by one driver (tests/cpp/ofdm_frame_bench.cpp) built
+    against this library; the reference arm builds the same driver against the reference's pipeline."""
+    if rank != 0:
+        return None
+    from sicc_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        raise RuntimeError(f"{_lib.LIB_PATH} is missing: run __graft_entry__.build() first")
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    os.makedirs(os.path.join(ROOT, "_build"), exist_ok=True)
+    exe = os.path.join(ROOT, "_build", "ofdm_frame_bench_gb300")
+    subprocess.run(["g++", "-O3", "-std=c++17", "-I" + os.path.join(ROOT, "include"), FRAME_BENCH_SRC, "-o", exe,
+                    "-L" + libdir, "-lsicc_gb300", "-Wl,-rpath," + libdir], check=True)
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    t0 = time.perf_counter()
+    res = _run_frame_bench(exe, args.frame_bench_frames)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    return _frame_bench_line("ours", res, wall, args.frame_bench_frames, clk,
+                             {"gpu_launches": args.frame_bench_frames * 2,  # the timed receive loop
+                              "kernels_per_rx_frame": ["sync_kernel", "demod_kernel"],
+                              "cpu_baseline": None, "roofline": None})
+
+
+def run_frame_pipeline_reference(args, rank, world):
+    """Reference arm of the per-frame workload: the same driver linked with the reference's own CUDA
+    pipeline (gpu_ofdm_pipeline.cu, staged under oracle/_ref/src), plus the reference's unmodified
+    benchmark program for comparison."""
+    if rank != 0:
+        return None
+    stage = os.path.join(ROOT, "oracle", "_ref", "src", "pipeline", "gpu_ofdm_pipeline.cu")
+    if not os.path.exists(stage):
+        return {"impl": "reference", "unavailable": "the reference's GPU pipeline sources were not staged "
+                                                    "(make -C oracle stage where the reference tree is present)"}
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ofdm-bench"], check=True)
+    exe = os.path.join(ROOT, "oracle", "_ref", "ofdm_frame_bench_ref")
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    res = _run_frame_bench(exe, args.frame_bench_frames)
+    clk = clocks.stop()
+    own = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "gpu_ofdm_pipeline_bench_ref"), "--frames",
+                          str(args.frame_bench_frames)], capture_output=True, text=True, timeout=900)
+    own_lines = [ln for ln in own.stdout.splitlines() if ln.startswith("[GPU-BENCH]")]
+    return _frame_bench_line("reference", res, 0.0, args.frame_bench_frames, clk,
+                             {"gpu_launches": 0, "cpu_baseline": None, "roofline": None,
+                              "reference_own_benchmark": {"rc": own.returncode, "output": own_lines}})
 
 
 # ------------------------------------------------------------- reference arm
@@ -1296,7 +1376,37 @@ def run_reference(args, rank, world):
             "cpu_baseline": {"value": round(value, 4), "unit": "Mbit/s", "cores": workers, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 4), "unit": "Mbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_targets(args):
+    """Short runs of the two systems targets, reported beside the headline (1 GPU, same process).
+
+    * Mixed-code batching (100,000 codewords of 15 codes): one persistent batched launch against the
+      plain form, one synchronous decode call per request; target: batched >= 50x plain.
+    * Serving: every request offered at once gives the peak, then one Poisson pass at 80% of it;
+      target: p99 request latency < 1 ms at 80% load.
+    """
+    import copy
+    sub = copy.copy(args)
+    sub.steps, sub.warmup, sub.no_e2e, sub.no_cpu_baseline = 5, 3, True, True
+    mixed = run_mixed(sub, 0, 1)
+    sub = copy.copy(args)
+    sub.steps, sub.warmup, sub.no_e2e, sub.no_cpu_baseline = 3, 1, True, True
+    sub.serve_loads = (0.8,)
+    serve = run_serve(sub, 0, 1)
+    plain = mixed["plain_one_code_per_launch"]
+    p80 = serve["load_sweep"][0]
+    return {"mixed_batched_vs_plain": {"batched_mbps": mixed["value"], "plain_mbps": plain["value"],
+                                       "ratio": plain["speedup_of_batched"], "target_ratio": 50,
+                                       "kernel_ms": mixed["kernel_ms"], "fer": mixed["fer"],
+                                       "workload": "mixed_100k (5 timed steps)"},
+            "serving_p99_at_80pct": {"peak_mbps": serve["value"], "offered_mbps": p80["offered_mbps"],
+                                     "achieved_mbps": p80["achieved_mbps"], "p50_ms": p80["p50_ms"],
+                                     "p99_ms": p80["p99_ms"], "p99_9_ms": p80["p99_9_ms"],
+                                     "p99_ms_bp_only": p80["p99_ms_bp_only"], "p99_ms_bp_osd": p80["p99_ms_bp_osd"],
+                                     "target_p99_ms": 1.0,
+                                     "workload": f"serve_mixed, {serve['config']['requests']} requests"}}
 
 
 def spawn_ranks(n, argv):
@@ -1319,11 +1429,15 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-targets", action="store_true", help="default workload: skip the short C4/C5 target runs")
     ap.add_argument("--batch", type=int, default=BATCH, help="frames per batch (profiling runs only)")
     ap.add_argument("--resident", type=int, default=RESIDENT_BATCHES, help="resident batches per Eb/N0")
     ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "ofdm_rx_1024_512", "ofdm_tx_1024_512", "ofdm_ingest_1024_512",
-                                                        "mixed_100k", "serve_mixed", "dvbs2_64800_r12"])
+                                                        "mixed_100k", "serve_mixed", "dvbs2_64800_r12",
+                                                        "ofdm_frame_pipeline"])
+    ap.add_argument("--frame-bench-frames", type=int, default=4000, help="frames per stage of ofdm_frame_pipeline")
     ap.add_argument("--serve-requests", type=int, default=1500)
+    ap.add_argument("--serve-loads", type=float, nargs="*", default=None, help="offered loads (fractions of peak)")
     ap.add_argument("--serve-batch", type=int, default=16384, help="codewords per server launch")
     ap.add_argument("--serve-inflight", type=int, default=4, help="batches overlapping on the device")
     ap.add_argument("--mixed-codewords", type=int, default=100_000)
@@ -1342,22 +1456,30 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", 1))
     if world != args.gpus:
         sys.exit(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}")
-    if args.impl == "reference":
-        run_reference(args, rank, world)
+    if args.impl == "reference" and args.workload == "ofdm_frame_pipeline":
+        line = run_frame_pipeline_reference(args, rank, world)
+    elif args.impl == "reference":
+        line = run_reference(args, rank, world)
+    elif args.workload == "ofdm_frame_pipeline":
+        line = run_frame_pipeline(args, rank, world)
     elif args.workload == "ofdm_rx_1024_512":
-        run_ofdm(args, rank, world)
+        line = run_ofdm(args, rank, world)
     elif args.workload == "ofdm_tx_1024_512":
-        run_ofdm_tx(args, rank, world)
+        line = run_ofdm_tx(args, rank, world)
     elif args.workload == "ofdm_ingest_1024_512":
-        run_ingest(args, rank, world)
+        line = run_ingest(args, rank, world)
     elif args.workload == "mixed_100k":
-        run_mixed(args, rank, world)
+        line = run_mixed(args, rank, world)
     elif args.workload == "serve_mixed":
-        run_serve(args, rank, world)
+        line = run_serve(args, rank, world)
     elif args.workload == "dvbs2_64800_r12":
-        run_dvbs2(args, rank, world)
+        line = run_dvbs2(args, rank, world)
     else:
-        run_ours(args, rank, world)
+        line = run_ours(args, rank, world)
+        if line is not None and world == 1 and not args.no_targets:
+            line["targets"] = run_targets(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

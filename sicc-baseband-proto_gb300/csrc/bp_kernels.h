@@ -9,8 +9,10 @@ constexpr int kBpThreads = 256;
 
 // Launch shape of the persistent layered kernel; zero fields take defaults.
 struct BpLaunch {
-    int slots_per_cta = 0;  // codewords resident per CTA (multiple of 32/group)
-    int ctas = 0;           // grid size (persistent CTAs)
+    int slots_per_cta = 0;    // codewords resident per CTA (multiple of 32/group)
+    int ctas = 0;             // grid size (persistent CTAs)
+    int osd_share_rounds = 0; // warp OSD: candidate rounds between best-metric exchanges (0 = 2)
+    int osd_ctas = 0;         // warp OSD grid size (0 = occupancy x SMs)
 };
 
 // All launchers are asynchronous on `st`; io.work_counter must point at one

@@ -181,11 +181,14 @@ std::vector<uint32_t> osd_combos(int pool, int order, int max_tests)
 }
 
 DeviceCode::DeviceCode(int n, int m, const int* row_ptr, const int* col_ind, int schedule,
-                       const uint64_t* parity, int parity_words, bool need_osd, const OsdSettings& osd)
-    : n_(n), m_(m), schedule_(schedule)
+                       const uint64_t* parity, int parity_words, bool need_osd, const OsdSettings& osd,
+                       int layered_group)
+    : n_(n), m_(m), schedule_(schedule), layered_group_(layered_group)
 {
     if (n <= 0 || m <= 0 || m >= n) throw InvalidArgument("code dimensions must satisfy 0 < m < n");
     if (schedule < 0 || schedule > 3) throw InvalidArgument("schedule must be 0..3");
+    if (layered_group < 0 || layered_group > 32 || (layered_group & (layered_group - 1)) != 0)
+        throw InvalidArgument("lanes per codeword must be 0 (default) or a power of two <= 32");
     edges_ = row_ptr[m];
     if (edges_ <= 0) throw InvalidArgument("parity-check matrix has no edges");
     row_ptr_.assign(row_ptr, row_ptr + m + 1);
@@ -232,6 +235,7 @@ void DeviceCode::build_layered()
     if (maxdeg > 27) throw InvalidArgument("layered schedule supports row degree <= 27");
     int group = 1;
     while (group < maxw && group < 32) group <<= 1;
+    if (layered_group_ > 0) group = std::min(layered_group_, group);  // never wider than the default
     const int rows_per_lane = (maxw + group - 1) / group;
     const int width = rows_per_lane * group;
     const int L = static_cast<int>(sizes.size());

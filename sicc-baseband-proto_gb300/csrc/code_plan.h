@@ -24,8 +24,13 @@ struct OsdSettings {
 // between decoders on the same device.
 class DeviceCode {
 public:
+    // layered_group: lanes that update one codeword's rows of a layer together (a power of
+    // two <= 32; each lane then owns ceil(widest layer / group) rows of every layer).  0 = the
+    // smallest power of two covering the widest layer.  Rows of one layer share no variable,
+    // so every group size gives the same arithmetic.
     DeviceCode(int n, int m, const int* row_ptr, const int* col_ind, int schedule,
-               const uint64_t* parity, int parity_words, bool need_osd, const OsdSettings& osd);
+               const uint64_t* parity, int parity_words, bool need_osd, const OsdSettings& osd,
+               int layered_group = 0);
     ~DeviceCode();
     DeviceCode(const DeviceCode&) = delete;
     DeviceCode& operator=(const DeviceCode&) = delete;
@@ -46,6 +51,7 @@ public:
     const std::vector<int>& row_order() const { return row_order_; }
     const std::vector<uint64_t>& parity_table() const { return parity_; }
     int parity_words() const { return parity_words_; }
+    int layered_group_request() const { return layered_group_; }
 
     void set_osd(const OsdSettings& s);
     // Tables of the large-code OSD kernel (elimination on H): any full-rank
@@ -57,6 +63,7 @@ private:
     void build_flood();
 
     int n_ = 0, m_ = 0, k_ = 0, edges_ = 0, schedule_ = kFlatLayered;
+    int layered_group_ = 0;
     std::vector<int> row_ptr_, col_ind_;
     std::vector<int> row_order_;
     std::vector<uint64_t> parity_;

@@ -188,7 +188,8 @@ void run_bp_osd(const DeviceCode& code, const BpParams& bp, const BpLaunch& shap
         oio.out_info = d_bits;
         oio.info_stride = out_stride;
         oio.used_osd = d_used_osd;
-        launch_osd(code.osd_view(), oio, count, st);
+        oio.share_rounds = shape.osd_share_rounds;
+        launch_osd(code.osd_view(), oio, count, st, 0, shape.osd_ctas);
     }
     if (rec) {
         check_cuda(cudaEventRecord(rec->ev[2], st), "cudaEventRecord");
@@ -729,7 +730,8 @@ int decode_with_caller_scratch(unsigned long long handle, const float* d_llr, in
         oio.out_info = d_info;
         oio.info_stride = d->k;
         oio.used_osd = d_used_osd;
-        launch_osd(d->code->osd_view(), oio, count, st);
+        oio.share_rounds = d->shape.osd_share_rounds;
+        launch_osd(d->code->osd_view(), oio, count, st, 0, d->shape.osd_ctas);
     }
     return CUDA_OSD_STATUS_OK;
 }
@@ -907,7 +909,8 @@ int cuda_osd_decode_osd_batch(unsigned long long handle, const float* llrs, int 
             io.out_info = d->info.p;
             io.info_stride = d->k;
             io.out_metric = d->dist.p;
-            launch_osd(d->code->osd_view(), io, cnt, d->stream);
+            io.share_rounds = d->shape.osd_share_rounds;
+            launch_osd(d->code->osd_view(), io, cnt, d->stream, 0, d->shape.osd_ctas);
             check_cuda(cudaMemcpyAsync(out_info_bits + static_cast<size_t>(off) * d->k, d->info.p,
                                        static_cast<size_t>(cnt) * d->k, cudaMemcpyDeviceToHost, d->stream),
                        "copy info bits");
@@ -1165,7 +1168,9 @@ int sicc_osd_decode_device(unsigned long long handle, const float* device_llrs, 
         io.info_stride = d->k;
         io.out_code = device_code_bits;
         io.out_metric = device_distances;
-        launch_osd(d->code->osd_view(), io, codewords, static_cast<cudaStream_t>(cuda_stream));
+        io.share_rounds = d->shape.osd_share_rounds;
+        launch_osd(d->code->osd_view(), io, codewords, static_cast<cudaStream_t>(cuda_stream), 0,
+                   d->shape.osd_ctas);
         return CUDA_OSD_STATUS_OK;
     });
 }

@@ -15,6 +15,10 @@
 //      (metric bits, test index) keys.
 // Candidates are evaluated by all 32 lanes in parallel; each candidate's
 // difference vector is the base difference XOR at most three reduced rows.
+// A lane stops summing a candidate once its partial metric exceeds the best
+// metric it knows; the warp exchanges its best every `share_rounds` rounds of
+// 32 candidates (a launch parameter, chosen by the autotuner).  Pruning only
+// drops candidates that cannot win, so the winner is the same for any value.
 #include "bp_kernels.h"
 
 #include <algorithm>
@@ -309,6 +313,7 @@ osd_kernel(OsdView ov0, OsdIO io)
         unsigned long long best_key = ~0ull;
         float thr = INFINITY;
         const int rounds = (ov.num_tests + 31) / 32;
+        const int share = io.share_rounds > 0 ? io.share_rounds : 2;
         for (int rd = 0; rd < rounds; ++rd) {
             const int q = rd * 32 + lane;
             if (q < ov.num_tests) {
@@ -354,7 +359,7 @@ osd_kernel(OsdView ov0, OsdIO io)
                     }
                 }
             }
-            if (rd & 1) {  // share the best metric so far across the warp
+            if (rd % share == share - 1) {  // share the best metric so far across the warp
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
                     const unsigned long long other = shfl_xor_u64(best_key, o);

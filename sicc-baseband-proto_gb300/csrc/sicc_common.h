@@ -142,6 +142,10 @@ struct OsdIO {
     const long long* llr_off;
     const long long* info_off;
     const long long* row_off;
+    // warp OSD: rounds of 32 candidates (one per lane) between exchanges of the
+    // warp's best metric, which tightens every lane's pruning bound (0 = 2);
+    // the winner does not depend on it
+    int share_rounds;
 };
 
 }  // namespace sicc
