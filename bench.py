@@ -258,6 +258,17 @@ def run_ours(args, rank, world):
             out=[torch.zeros((BATCH, code.k), dtype=torch.uint8, device="cuda")] +
                 [torch.zeros(BATCH, dtype=torch.uint8, device="cuda") for _ in range(3)])  # info, ok, used, iters
 
+    # launch shapes picked by the autotuner on each chain's first batch (cached for the
+    # reference-API decoders of the end-to-end leg, which decode the same code with the same settings)
+    shapes = {}
+    for e in EBN0:
+        if args.no_tune:
+            shapes[f"{e:g}dB"] = chain[e]["dec"].shape()
+        else:
+            res = chain[e]["dec"].autotune(d_llr[e][0], reps=3)
+            shapes[f"{e:g}dB"] = dict(res.best, tuned_ms=round(res.best_ms, 4), default_ms=round(res.default_ms, 4),
+                                      trials=len(res.trials))
+
     def step(s):
         for e in EBN0:
             c = chain[e]
@@ -460,7 +471,7 @@ def run_ours(args, rank, world):
                            "ebn0_db": list(EBN0), "bp": f"layered NMS alpha {ALPHA}, <= {ITERS} iterations",
                            "osd": f"order {OSD_ORDER}, {1 + OSD_FLIP + OSD_FLIP * (OSD_FLIP - 1) // 2} tests",
                            "l2": f"{2 * RESIDENT_BATCHES} resident batches of 33.5 MB cycled (> L2)",
-                           "parallelism": f"replicas x{world}"},
+                           "parallelism": f"replicas x{world}", "launch_shapes": shapes},
                 "fer": fer, "fer_parity": fer_parity, "mean_iterations": mean_iter, "osd_fraction": osd_frac,
                 "gpu_launches": args.steps * len(EBN0) * 2, "clocks": clk, "roofline": roofline,
                 "e2e": e2e, "cpu_baseline": cpu}
@@ -851,6 +862,12 @@ def run_mixed(args, rank, world):
     for c in w.codes:  # OSD order 2 for n <= 256, order 1 for the longer codes
         eng.add_code(c, engine.iteration_cap(c.n), ALPHA, 0.0, engine.osd_order_for(c), OSD_FLIP, OSD_TESTS)
 
+    tuned = None
+    if not args.no_tune:  # warps per codeword of each code and warps per CTA, on this batch
+        base_ms, tuned_ms = eng.autotune(w.count, d_code, d_llr, d_llr_off, d_info, d_info_off, reps=2)
+        tuned = {"bp_default_ms": round(base_ms, 4), "bp_tuned_ms": round(tuned_ms, 4)}
+    code_warps = {c.name(): eng.code_warps(i) for i, c in enumerate(w.codes)}
+
     def batched():
         eng.decode_device(w.count, d_code, d_llr, d_llr_off, d_info, d_info_off, d_ok, d_used, d_it, stream=stream)
 
@@ -974,7 +991,8 @@ def run_mixed(args, rank, world):
                        "lengths": [128, 256, 512, 1024, 2048], "rates": ["1/2", "11/16", "3/4"],
                        "bp": "layered NMS alpha 0.75, 20/25/30 iterations by length",
                        "osd": "on failing codewords: order 2 (n <= 256), order 1 (n >= 512)",
-                       "l2": f"{w.llr.nbytes / 1e6:.0f} MB of LLRs per step (> L2)"},
+                       "l2": f"{w.llr.nbytes / 1e6:.0f} MB of LLRs per step (> L2)",
+                       "warps_per_codeword": code_warps, "autotune": tuned},
             "fer_by_length": fer_by_n, "fer": float(fe.mean()),
             "kernel_ms": {"prepare": round(prep_ms, 4), "bp_mixed": round(bp_ms, 4), "osd": round(osd_ms, 4)},
             "plain_one_code_per_launch": {"value": round(plain_mbps, 3), "unit": "Mbit/s",
@@ -1430,6 +1448,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-targets", action="store_true", help="default workload: skip the short C4/C5 target runs")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no autotuner)")
     ap.add_argument("--batch", type=int, default=BATCH, help="frames per batch (profiling runs only)")
     ap.add_argument("--resident", type=int, default=RESIDENT_BATCHES, help="resident batches per Eb/N0")
     ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "ofdm_rx_1024_512", "ofdm_tx_1024_512", "ofdm_ingest_1024_512",

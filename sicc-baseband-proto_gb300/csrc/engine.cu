@@ -20,6 +20,8 @@
 #include "bp_kernels.h"
 #include "code_plan.h"
 #include "engine_internal.h"
+#include "tune_internal.h"
+#include "../../include/sicc_tune.h"
 
 #include <algorithm>
 #include <cfloat>
@@ -439,7 +441,42 @@ struct EngineCode {
     bool osd = false;    // OSD by the warp kernel (n <= 256, k <= 128)
     bool osd_h = false;  // OSD by the large-code kernel
     long long cost = 0;
+    uint64_t fingerprint = 0;  // key of the code's tuned warps per codeword
 };
+
+// Warps that decode one codeword of a code with layers of `width` rows: 4 (128 lanes)
+// for layers of >= 128 rows, 2 (64 lanes) for 64-row layers, else one warp.
+int default_code_warps(int width)
+{
+    if (width >= 128 && width % 128 == 0) return 4;
+    if (width >= 64 && width % 64 == 0) return 2;
+    return 1;
+}
+
+bool code_warps_allowed(int width, int warps)
+{
+    return warps == 1 || ((warps == 2 || warps == 4) && width >= 32 * warps && width % (32 * warps) == 0);
+}
+
+// Lanes and rows per lane of a code decoded by `warps` warps per codeword, and the
+// shared-memory floats of one codeword slot.
+void set_code_warps(EngineCode& ec, int warps)
+{
+    const LayeredView& lv = ec.code->layered_view();
+    CodeDesc& d = ec.desc;
+    if (!code_warps_allowed(lv.width, warps)) throw InvalidArgument("warps per codeword must be 1, 2 or 4 and divide the layer width in 32-lane units");
+    d.warps = warps;
+    d.group = lv.group;
+    d.rows_per_lane = lv.rows_per_lane;
+    if (warps > 1) {
+        d.group = 32 * warps;
+        d.rows_per_lane = lv.width / d.group;
+    }
+    const int n_pad = (d.n + 3) & ~3;
+    int sf = (n_pad + 3 * d.num_layers * d.width + 3) & ~3;
+    if (d.group < 32) sf += ((d.group - sf % 32) + 32) % 32;  // groups of a warp G banks apart
+    d.slot_floats = sf;
+}
 
 struct Engine {
     sicc_engine_config_t cfg{};
@@ -700,22 +737,26 @@ int sicc_engine_add_code(unsigned long long handle, const sicc_engine_code_t* co
         d.maxdeg = lv.maxdeg;
         d.group = lv.group;
         d.rows_per_lane = lv.rows_per_lane;
-        d.warps = 1;
-        if (lv.width >= 128 && lv.width % 128 == 0) d.warps = 4;      // layers of >= 128 rows: 128 lanes
-        else if (lv.width >= 64 && lv.width % 64 == 0) d.warps = 2;   // 64-row layers: 64 lanes
-        if (d.warps > 1) {
-            d.group = 32 * d.warps;
-            d.rows_per_lane = lv.width / d.group;
-        }
         d.max_iter = code->max_iterations;
         d.alpha = code->normalization;
         d.beta = code->offset;
         d.route_osd = want_osd ? 1 : 0;
         d.vars = lv.vars;
-        const int n_pad = (d.n + 3) & ~3;
-        int sf = (n_pad + 3 * d.num_layers * d.width + 3) & ~3;
-        if (d.group < 32) sf += ((d.group - sf % 32) + 32) % 32;  // groups of a warp G banks apart
-        d.slot_floats = sf;
+        Fingerprint fp;
+        fp.add(code->n);
+        fp.add(code->m);
+        fp.add(code->row_ptr, static_cast<size_t>(code->m) + 1);
+        fp.add(code->col_ind, static_cast<size_t>(code->row_ptr[code->m]));
+        fp.add(code->max_iterations);
+        fp.add_float(code->normalization);
+        fp.add_float(code->offset);
+        ec.fingerprint = fp.h;
+        int warps = default_code_warps(lv.width);
+        std::vector<int> cached;
+        if (tune_cache_get(tune_key("engine-code", fp.h), cached) && cached.size() == 1 &&
+            code_warps_allowed(lv.width, cached[0]))
+            warps = cached[0];  // tuned earlier for this code on this device
+        set_code_warps(ec, warps);
         ec.osd = warp_osd;
         ec.osd_h = want_osd && !warp_osd;
         ec.cost = static_cast<long long>(ec.code->edges()) * d.max_iter;
@@ -729,6 +770,31 @@ int sicc_engine_add_code(unsigned long long handle, const sicc_engine_code_t* co
         e->codes.push_back(std::move(ec));
         e->dirty = true;
         *out_code_id = static_cast<int>(e->codes.size()) - 1;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_engine_set_code_warps(unsigned long long handle, int code_id, int warps)
+{
+    return guarded([&] {
+        auto e = get(handle);
+        std::lock_guard<std::mutex> lock(e->mu);
+        if (code_id < 0 || code_id >= static_cast<int>(e->codes.size())) throw InvalidArgument("invalid code id");
+        check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+        set_code_warps(e->codes[code_id], warps);
+        e->dirty = true;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_engine_get_code_warps(unsigned long long handle, int code_id, int* out_warps)
+{
+    return guarded([&] {
+        auto e = get(handle);
+        std::lock_guard<std::mutex> lock(e->mu);
+        if (code_id < 0 || code_id >= static_cast<int>(e->codes.size()) || !out_warps)
+            throw InvalidArgument("invalid code id or null argument");
+        *out_warps = e->codes[code_id].desc.warps;
         return CUDA_OSD_STATUS_OK;
     });
 }
@@ -905,6 +971,112 @@ int sicc_engine_last_ms(unsigned long long handle, float* out_prepare_ms, float*
         if (out_prepare_ms) *out_prepare_ms = a;
         if (out_bp_ms) *out_bp_ms = b;
         if (out_osd_ms) *out_osd_ms = c;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+// Coordinate search on the caller's batch: codes in decreasing BP cost, each tried at every
+// allowed warps per codeword (kept when the mixed BP kernel gets at least 1% faster), then the
+// engine's warps per CTA.  Trials decode with every codeword's protection at BP only, so OSD
+// time stays out of the comparison; each trial is one warm-up and `reps` timed decodes.
+int sicc_engine_autotune(unsigned long long handle, int codewords, const unsigned char* device_code_ids,
+                         const float* device_llr, const long long* device_llr_offsets, unsigned char* device_info,
+                         const long long* device_info_offsets, int reps, float* out_default_ms, float* out_tuned_ms)
+{
+    return guarded([&] {
+        auto e = get(handle);
+        if (!device_code_ids || !device_llr || !device_llr_offsets || !device_info || !device_info_offsets)
+            throw InvalidArgument("null device pointer");
+        if (codewords <= 0 || codewords > e->cfg.max_codewords) throw InvalidArgument("codewords out of range");
+        if (reps < 1 || reps > 50) throw InvalidArgument("reps must be in 1..50");
+        check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+        struct Bytes {  // per-codeword scratch of the trials, freed on every exit
+            uint8_t* p = nullptr;
+            ~Bytes() { if (p) cudaFree(p); }
+        } protect, ok, used, iters;
+        for (Bytes* b : {&protect, &ok, &used, &iters})
+            check_cuda(cudaMalloc(&b->p, static_cast<size_t>(codewords)), "cudaMalloc(autotune)");
+        check_cuda(cudaMemset(protect.p, 0, codewords), "clear protection");
+        cudaStream_t st = nullptr;
+        check_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate(tune)");
+        struct StreamGuard {
+            cudaStream_t s;
+            ~StreamGuard() { cudaStreamDestroy(s); }
+        } guard{st};
+
+        auto time_bp = [&]() -> float {
+            std::vector<float> ms;
+            for (int r = 0; r <= reps; ++r) {
+                if (engine_decode(handle, codewords, device_code_ids, protect.p, device_llr, device_llr_offsets,
+                                  device_info, device_info_offsets, ok.p, used.p, iters.p, st, nullptr) !=
+                    CUDA_OSD_STATUS_OK)
+                    throw std::runtime_error(std::string("autotune decode: ") + last_error());
+                std::lock_guard<std::mutex> lock(e->mu);
+                check_cuda(cudaEventSynchronize(e->ev[2]), "cudaEventSynchronize");
+                float t = 0.0f;
+                check_cuda(cudaEventElapsedTime(&t, e->ev[1], e->ev[2]), "cudaEventElapsedTime");
+                if (r > 0) ms.push_back(t);
+            }
+            return median_of(ms);
+        };
+        auto set_warps = [&](int c, int w) {
+            std::lock_guard<std::mutex> lock(e->mu);
+            set_code_warps(e->codes[c], w);
+            e->dirty = true;
+        };
+
+        const float default_ms = time_bp();
+        float best = default_ms;
+        std::vector<int> order;
+        {
+            std::lock_guard<std::mutex> lock(e->mu);
+            for (int c = 0; c < static_cast<int>(e->codes.size()); ++c) order.push_back(c);
+            std::sort(order.begin(), order.end(),
+                      [&](int a, int b) { return e->codes[a].cost > e->codes[b].cost; });
+        }
+        for (int c : order) {
+            int width = 0, keep = 0;
+            {
+                std::lock_guard<std::mutex> lock(e->mu);
+                width = e->codes[c].code->layered_view().width;
+                keep = e->codes[c].desc.warps;
+            }
+            for (int w : {1, 2, 4}) {
+                if (w == keep || !code_warps_allowed(width, w)) continue;
+                set_warps(c, w);
+                const float t = time_bp();
+                if (t < 0.99f * best) {
+                    best = t;
+                    keep = w;
+                } else {
+                    set_warps(c, keep);
+                }
+            }
+        }
+        int wpc_keep = 0;
+        {
+            std::lock_guard<std::mutex> lock(e->mu);
+            wpc_keep = e->warps_per_cta;
+        }
+        for (int wpc : {4, 8}) {
+            if (wpc == (wpc_keep == 0 ? 8 : wpc_keep)) continue;
+            {
+                std::lock_guard<std::mutex> lock(e->mu);
+                e->warps_per_cta = wpc;
+            }
+            const float t = time_bp();
+            if (t < 0.99f * best) {
+                best = t;
+                wpc_keep = wpc;
+            }
+        }
+        {
+            std::lock_guard<std::mutex> lock(e->mu);
+            e->warps_per_cta = wpc_keep;
+            for (const auto& c : e->codes) tune_cache_put(tune_key("engine-code", c.fingerprint), {c.desc.warps});
+        }
+        if (out_default_ms) *out_default_ms = default_ms;
+        if (out_tuned_ms) *out_tuned_ms = best;
         return CUDA_OSD_STATUS_OK;
     });
 }

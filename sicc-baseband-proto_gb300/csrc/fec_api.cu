@@ -3,6 +3,8 @@
 #include "../../include/sicc_fec.h"
 #include "bp_kernels.h"
 #include "code_plan.h"
+#include "tune_internal.h"
+#include "../../include/sicc_tune.h"
 
 #include <algorithm>
 #include <chrono>
@@ -590,6 +592,8 @@ struct CsrDecoder : Decoder {
         k = n - m;
         max_batch = std::max(1, c.max_batch_size);
         init_common();
+        h_row_ptr.assign(rp, rp + m + 1);
+        h_col_ind.assign(ci, ci + rp[m]);
         code = std::make_unique<DeviceCode>(n, m, rp, ci, c.schedule, nullptr, 0, false, osd);
         bp.alpha = c.normalization;
         bp.beta = c.offset;
@@ -602,6 +606,107 @@ struct CsrDecoder : Decoder {
         success.alloc(max_batch);
     }
 };
+
+// ---- launch shapes (include/sicc_tune.h) ----
+
+uint64_t decoder_fingerprint(const Decoder& d)
+{
+    Fingerprint f;
+    f.add(static_cast<int>(d.kind));
+    f.add(d.n);
+    f.add(d.m);
+    f.add(d.h_row_ptr.data(), d.h_row_ptr.size());
+    f.add(d.h_col_ind.data(), d.h_col_ind.size());
+    f.add(d.code->schedule());
+    f.add(d.bp.max_iter);
+    f.add_float(d.bp.alpha);
+    f.add_float(d.bp.beta);
+    if (d.kind == Decoder::kStream) {
+        f.add(d.osd_enabled ? 1 : 0);
+        f.add(d.osd.order);
+        f.add(d.osd.max_flip_positions);
+        f.add(d.osd.max_tests);
+    }
+    return f.h;
+}
+
+// Lanes per codeword the layered tables get by default: the smallest power of two
+// covering the widest layer, at most 32.
+int default_layered_group(const Decoder& d)
+{
+    std::vector<int> order, sizes;
+    if (d.code->schedule() == kColoredLayered)
+        greedy_coloring(d.n, d.m, d.h_row_ptr.data(), d.h_col_ind.data(), order, sizes);
+    else
+        consecutive_layers(d.n, d.m, d.h_row_ptr.data(), d.h_col_ind.data(), sizes);
+    int maxw = 1;
+    for (int x : sizes) maxw = std::max(maxw, x);
+    int g = 1;
+    while (g < maxw && g < 32) g <<= 1;
+    return g;
+}
+
+sicc_fec_shape_t current_shape(const Decoder& d)
+{
+    sicc_fec_shape_t s{};
+    s.lanes_per_codeword = d.code->layered_group_request();
+    s.slots_per_cta = d.shape.slots_per_cta;
+    s.ctas = d.shape.ctas;
+    s.osd_share_rounds = d.shape.osd_share_rounds;
+    s.osd_ctas = d.shape.osd_ctas;
+    return s;
+}
+
+// Rebuilds the decoder's code tables with `group` lanes per codeword (same schedule,
+// parity table and OSD settings).  The caller holds d.mu and has drained d.stream.
+void rebuild_code(Decoder& d, int group)
+{
+    if (group == d.code->layered_group_request()) return;
+    const auto parity = d.code->parity_table();
+    const bool need_osd = d.kind == Decoder::kStream;
+    auto fresh = std::make_unique<DeviceCode>(d.n, d.m, d.h_row_ptr.data(), d.h_col_ind.data(), d.code->schedule(),
+                                              parity.empty() ? nullptr : parity.data(), d.code->parity_words(),
+                                              need_osd, d.osd, group);
+    d.code = std::move(fresh);
+}
+
+void check_shape(const Decoder& d, const sicc_fec_shape_t& s)
+{
+    const int g = s.lanes_per_codeword;
+    if (g < 0 || g > 32 || (g & (g - 1)) != 0)
+        throw InvalidArgument("lanes_per_codeword must be 0 or a power of two <= 32");
+    if (s.slots_per_cta < 0 || s.ctas < 0 || s.osd_ctas < 0 || s.osd_share_rounds < 0 || s.osd_share_rounds > 64)
+        throw InvalidArgument("launch shape fields must be >= 0 (osd_share_rounds <= 64)");
+    if (s.slots_per_cta > 0 && d.code->layered()) {
+        const int eff = g > 0 ? std::min(g, default_layered_group(d)) : default_layered_group(d);
+        if (s.slots_per_cta % std::max(1, 32 / eff) != 0 || s.slots_per_cta * eff > kBpThreads)
+            throw InvalidArgument("slots_per_cta must be a multiple of 32 / lanes and slots x lanes <= 256");
+    }
+}
+
+// The caller holds d.mu and has drained d.stream.
+void apply_shape(Decoder& d, const sicc_fec_shape_t& s)
+{
+    check_shape(d, s);
+    if (d.code->layered()) rebuild_code(d, s.lanes_per_codeword);
+    d.shape.slots_per_cta = s.slots_per_cta;
+    d.shape.ctas = s.ctas;
+    d.shape.osd_share_rounds = s.osd_share_rounds;
+    d.shape.osd_ctas = s.osd_ctas;
+}
+
+// Decoders start from the shape tuned for their code on this device, if any.
+void apply_cached_shape(Decoder& d)
+{
+    std::vector<int> v;
+    if (!tune_cache_get(tune_key("fec", decoder_fingerprint(d)), v) || v.size() != 5) return;
+    const sicc_fec_shape_t s{v[0], v[1], v[2], v[3], v[4]};
+    try {
+        apply_shape(d, s);
+    } catch (const InvalidArgument&) {
+        // a stale or hand-edited entry: keep the defaults
+    }
+}
 
 std::mutex g_registry_mu;
 std::map<unsigned long long, std::shared_ptr<Decoder>> g_registry;
@@ -757,6 +862,7 @@ int cuda_osd_create_stream_decoder(const cuda_osd_stream_config_t* config, unsig
         auto d = std::make_shared<StreamDecoder>();
         d->kind = Decoder::kStream;
         d->setup(*config, rp, ci, nullptr, 0);
+        apply_cached_shape(*d);
         *out_handle = register_decoder(d);
         return CUDA_OSD_STATUS_OK;
     });
@@ -776,6 +882,7 @@ int cuda_osd_create_stream_decoder_with_matrices(const cuda_osd_stream_config_t*
         auto d = std::make_shared<StreamDecoder>();
         d->kind = Decoder::kStream;
         d->setup(*config, rp, ci, reinterpret_cast<const uint64_t*>(systematic_parity), parity_words_per_row);
+        apply_cached_shape(*d);
         *out_handle = register_decoder(d);
         return CUDA_OSD_STATUS_OK;
     });
@@ -825,6 +932,7 @@ int cuda_osd_create_bp_csr_decoder(const cuda_osd_bp_csr_config_t* config, const
         auto d = std::make_shared<CsrDecoder>();
         d->kind = Decoder::kCsr;
         d->setup(*config, row_ptr, col_ind);
+        apply_cached_shape(*d);
         *out_handle = register_decoder(d);
         return CUDA_OSD_STATUS_OK;
     });
@@ -1034,6 +1142,7 @@ int sicc_fec_set_schedule(unsigned long long handle, int schedule)
         auto fresh = std::make_unique<DeviceCode>(d->n, d->m, d->h_row_ptr.data(), d->h_col_ind.data(), schedule,
                                                   parity.data(), d->code->parity_words(), true, d->osd);
         d->code = std::move(fresh);
+        apply_cached_shape(*d);
         return CUDA_OSD_STATUS_OK;
     });
 }
@@ -1051,6 +1160,7 @@ int sicc_fec_set_osd_params(unsigned long long handle, int order, int max_flip_p
         d->osd.max_flip_positions = max_flip_positions;
         d->osd.max_tests = max_tests;
         d->code->set_osd(d->osd);
+        if (d->kind == Decoder::kStream) apply_cached_shape(*d);
         return CUDA_OSD_STATUS_OK;
     });
 }
@@ -1073,6 +1183,146 @@ int sicc_fec_set_launch_shape(unsigned long long handle, int slots_per_cta, int 
         require(slots_per_cta >= 0 && ctas >= 0, "launch shape must be >= 0");
         d->shape.slots_per_cta = slots_per_cta;
         d->shape.ctas = ctas;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_fec_get_shape(unsigned long long handle, sicc_fec_shape_t* out_shape)
+{
+    return guarded([&] {
+        auto d = lookup_any(handle);
+        std::lock_guard<std::mutex> lock(d->mu);
+        require(out_shape != nullptr, "null argument");
+        *out_shape = current_shape(*d);
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_fec_set_shape(unsigned long long handle, const sicc_fec_shape_t* shape)
+{
+    return guarded([&] {
+        auto d = lookup_any(handle);
+        std::lock_guard<std::mutex> lock(d->mu);
+        require(shape != nullptr, "null argument");
+        require(d->kind != Decoder::kOsd, "OSD-only decoders have no BP shape");
+        check_cuda(cudaSetDevice(d->device), "cudaSetDevice");
+        check_cuda(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize");
+        apply_shape(*d, *shape);
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+// Coordinate search: for each lanes-per-codeword candidate (the default group, half and a
+// quarter of it), the slots per CTA with the default grid, then the grid with the best slots;
+// then the OSD exchange interval and grid with the best BP shape.  Each trial is one warm-up
+// decode and `reps` timed decodes of the caller's batch (median).
+int sicc_fec_autotune(unsigned long long handle, const float* device_llrs, int codewords, int reps,
+                      sicc_fec_shape_t* out_best, sicc_tune_trial_t* out_trials, int max_trials, int* out_trial_count)
+{
+    return guarded([&] {
+        auto d = lookup_any(handle);
+        std::lock_guard<std::mutex> lock(d->mu);
+        require(d->kind != Decoder::kOsd, "OSD-only decoders have no BP shape to tune");
+        require(device_llrs != nullptr && codewords > 0 && codewords <= d->max_batch,
+                "codewords must be in 1..max_batch_size");
+        require(reps >= 1 && reps <= 50, "reps must be in 1..50");
+        check_cuda(cudaSetDevice(d->device), "cudaSetDevice");
+        check_cuda(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize");
+        const bool stream_kind = d->kind == Decoder::kStream;
+        const bool with_osd = stream_kind && d->osd_enabled;
+        const int out_len = stream_kind ? d->k : d->n;
+        DevBuf<uint8_t> bits, ok, used, iters;
+        bits.alloc(static_cast<size_t>(codewords) * out_len);
+        ok.alloc(codewords);
+        used.alloc(codewords);
+        iters.alloc(codewords);
+        std::vector<sicc_tune_trial_t> trials;
+
+        auto time_shape = [&](const sicc_fec_shape_t& sh) -> float {
+            apply_shape(*d, sh);
+            std::vector<float> ms;
+            for (int r = 0; r <= reps; ++r) {
+                check_cuda(cudaEventRecord(d->ev0, d->stream), "cudaEventRecord");
+                run_bp_osd(*d->code, d->bp, d->shape, with_osd, device_llrs, codewords, bits.p, out_len, out_len,
+                           ok.p, with_osd ? used.p : nullptr, iters.p, nullptr, d->scratch, d->stream, nullptr);
+                check_cuda(cudaEventRecord(d->ev1, d->stream), "cudaEventRecord");
+                check_cuda(cudaEventSynchronize(d->ev1), "cudaEventSynchronize");
+                float t = 0.0f;
+                check_cuda(cudaEventElapsedTime(&t, d->ev0, d->ev1), "cudaEventElapsedTime");
+                if (r > 0) ms.push_back(t);  // the first decode is the warm-up
+            }
+            const float med = median_of(ms);
+            trials.push_back(sicc_tune_trial_t{sh, med});
+            return med;
+        };
+
+        sicc_fec_shape_t best{};
+        float best_ms = time_shape(best);  // the library defaults
+        auto consider = [&](const sicc_fec_shape_t& sh) {
+            const float t = time_shape(sh);
+            if (t < best_ms) {
+                best_ms = t;
+                best = sh;
+            }
+        };
+        const int sms = device_sm_count();
+        if (d->code->layered()) {
+            const LayeredView& lv = d->code->layered_view();
+            const bool wide = layered_needs_wide(lv, with_osd);
+            if (!wide) {
+                const int g0 = default_layered_group(*d);
+                for (int g = g0; g >= std::max(1, g0 / 4); g >>= 1) {
+                    sicc_fec_shape_t base{};
+                    base.lanes_per_codeword = g == g0 ? 0 : g;
+                    const int step = std::max(1, 32 / g);
+                    sicc_fec_shape_t g_best = base;
+                    float g_ms = g == g0 ? best_ms : time_shape(base);
+                    if (g != g0 && g_ms < best_ms) {
+                        best_ms = g_ms;
+                        best = base;
+                    }
+                    for (int slots = step; slots * g <= kBpThreads; slots *= 2) {
+                        sicc_fec_shape_t sh = base;
+                        sh.slots_per_cta = slots;
+                        const float t = time_shape(sh);
+                        if (t < g_ms) {
+                            g_ms = t;
+                            g_best = sh;
+                        }
+                        if (t < best_ms) {
+                            best_ms = t;
+                            best = sh;
+                        }
+                    }
+                    for (int per_sm : {1, 2, 4}) {
+                        sicc_fec_shape_t sh = g_best;
+                        sh.ctas = per_sm * sms;
+                        consider(sh);
+                    }
+                }
+            }
+        }
+        if (with_osd && d->code->has_osd()) {
+            const sicc_fec_shape_t bp_best = best;
+            for (int share : {1, 4, 8}) {
+                sicc_fec_shape_t sh = bp_best;
+                sh.osd_share_rounds = share;
+                consider(sh);
+            }
+            const sicc_fec_shape_t osd_best = best;
+            for (int per_sm : {1, 2}) {
+                sicc_fec_shape_t sh = osd_best;
+                sh.osd_ctas = per_sm * sms;
+                consider(sh);
+            }
+        }
+        apply_shape(*d, best);
+        tune_cache_put(tune_key("fec", decoder_fingerprint(*d)),
+                       {best.lanes_per_codeword, best.slots_per_cta, best.ctas, best.osd_share_rounds, best.osd_ctas});
+        if (out_best) *out_best = best;
+        if (out_trials)
+            for (int i = 0; i < std::min(max_trials, static_cast<int>(trials.size())); ++i) out_trials[i] = trials[i];
+        if (out_trial_count) *out_trial_count = static_cast<int>(trials.size());
         return CUDA_OSD_STATUS_OK;
     });
 }

@@ -72,6 +72,21 @@ class Engine:
             _lib.check(_fn("sicc_engine_destroy")(self.handle), "sicc_engine_destroy")
             self.handle = 0
 
+    # -- launch shapes (include/sicc_tune.h) --
+    def code_warps(self, code_id: int) -> int:
+        from . import tune
+        return tune.code_warps(self.handle, code_id)
+
+    def set_code_warps(self, code_id: int, warps: int) -> None:
+        from . import tune
+        tune.set_code_warps(self.handle, code_id, warps)
+
+    def autotune(self, codewords, d_code, d_llr, d_llr_off, d_info, d_info_off, reps: int = 3):
+        """Tunes warps per codeword of each code and warps per CTA on this batch (outputs are
+        overwritten); returns (default BP ms, tuned BP ms)."""
+        from . import tune
+        return tune.engine_autotune(self.handle, codewords, d_code, d_llr, d_llr_off, d_info, d_info_off, reps)
+
     def __del__(self):
         try:
             self.close()

@@ -44,7 +44,25 @@ def systematic_parity_table(n: int, k: int, p_matrix: np.ndarray) -> np.ndarray:
     return np.packbits(padded, axis=1, bitorder="little").view(np.uint64).reshape(k, words).copy()
 
 
-class StreamBpOsdDecoder:
+class _Shaped:
+    """Launch shape and autotuner of a stream or CSR decoder (include/sicc_tune.h)."""
+
+    def shape(self) -> dict:
+        from . import tune
+        return tune.get_shape(self.handle)
+
+    def set_shape(self, **fields) -> None:
+        from . import tune
+        tune.set_shape(self.handle, **fields)
+
+    def autotune(self, d_llr, codewords: int | None = None, reps: int = 5):
+        """Times candidate shapes on device LLRs, applies the fastest and caches it per code and
+        device; returns a tune.TuneResult (the best shape and every trial)."""
+        from . import tune
+        return tune.autotune(self.handle, d_llr, codewords, reps)
+
+
+class StreamBpOsdDecoder(_Shaped):
     """Stream BP -> OSD decoder (the reference's CudaBpOsdDecoder)."""
 
     def __init__(self, code: QcCode | None = None, *, max_batch: int = 4096, min_batch: int = 30,
@@ -213,7 +231,7 @@ class StreamBpOsdDecoder:
             _lib.ptr(d_iter), _stream_ptr(stream)), "sicc_fec_decode_device")
 
 
-class CsrBpDecoder:
+class CsrBpDecoder(_Shaped):
     """Generic CSR BP decoder (the reference's CudaBpDecoder)."""
 
     def __init__(self, n: int, m: int, row_ptr, col_ind, *, max_batch: int = 4096, max_iter: int = 20,
