@@ -539,9 +539,7 @@ size_t layered_smem_bytes(const LayeredView& cv, int slots, bool track_best, int
     const int n_pad = (cv.n + 3) & ~3;
     const int mp = cv.num_layers * cv.width;
     int slot_floats = ((track_best ? 2 : 1) * n_pad + 3 * mp + 3) & ~3;
-    // Groups that share a warp sit G banks apart (slot stride = G mod 32 words), so
-    // their simultaneous gathers of the same table column never collide.
-    if (cv.group < 32) slot_floats += ((cv.group - slot_floats % 32) + 32) % 32;
+    slot_floats = pad_slot_stride(slot_floats, cv.group);
     if (slot_floats_out) *slot_floats_out = slot_floats;
     const int table = (cv.num_layers * cv.maxdeg * cv.width + 3) & ~3;
     return (static_cast<size_t>(table) + static_cast<size_t>(slots) * slot_floats) * sizeof(float);
@@ -565,7 +563,7 @@ static void launch_layered_reg_t(const LayeredView& cv, const BpParams& p, const
 {
     const int n_pad = (cv.n + 3) & ~3;
     int slot_floats = ((track_best ? 2 : 1) * n_pad + 3) & ~3;
-    if (cv.group < 32) slot_floats += ((cv.group - slot_floats % 32) + 32) % 32;  // groups G banks apart
+    slot_floats = pad_slot_stride(slot_floats, cv.group);
     const size_t smem = static_cast<size_t>(slots) * slot_floats * sizeof(float);
     const auto kernel = bp_layered_reg_kernel<D, kRegRows>;
     check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(kernel), smem), "cudaFuncSetAttribute(bp_layered_reg)");

@@ -8,6 +8,17 @@ namespace sicc {
 constexpr int kBpThreads = 256;
 
 // Launch shape of the persistent layered kernel; zero fields take defaults.
+// Slot stride (floats) of codewords that share a warp, G lanes each: groups sit
+// max(G, 4) banks apart, so their simultaneous gathers of the same table column
+// do not collide, and every slot stays 16-byte aligned for the float4 copies of
+// the posteriors (`floats` is a multiple of 4 on entry).
+inline int pad_slot_stride(int floats, int group)
+{
+    if (group >= 32) return floats;
+    const int bank = group < 4 ? 4 : group;
+    return floats + ((bank - floats % 32) + 32) % 32;
+}
+
 struct BpLaunch {
     int slots_per_cta = 0;    // codewords resident per CTA (multiple of 32/group)
     int ctas = 0;             // grid size (persistent CTAs)

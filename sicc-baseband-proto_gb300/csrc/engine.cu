@@ -474,7 +474,7 @@ void set_code_warps(EngineCode& ec, int warps)
     }
     const int n_pad = (d.n + 3) & ~3;
     int sf = (n_pad + 3 * d.num_layers * d.width + 3) & ~3;
-    if (d.group < 32) sf += ((d.group - sf % 32) + 32) % 32;  // groups of a warp G banks apart
+    sf = pad_slot_stride(sf, d.group);
     d.slot_floats = sf;
 }
 
