@@ -565,7 +565,8 @@ def run_ofdm(args, rank, world):
     value = world * info_bits * args.steps / (elapsed_ms * 1e-3) / 1e6
 
     # kernel split of one step (chains one after another), FER per SNR point
-    fer, sync_ms, demod_ms, bp_ms = {}, 0.0, 0.0, 0.0
+    fer, cer, sync_ms, demod_ms, bp_ms = {}, {}, 0.0, 0.0, 0.0
+    good_cw = 0  # correctly decoded codewords of the first batch at every SNR
     for snr in OFDM_SNRS:
         b = batches[snr][0]
         c = chain[snr]
@@ -581,6 +582,9 @@ def run_ofdm(args, rank, world):
         bp_ms += e0.elapsed_time(e1)
         info = c["bits"].cpu().numpy()[:, : code.k].reshape(frames, -1)
         fer[f"{snr:g}dB"] = float(np.mean(np.any(info != b.info, axis=1)))
+        cw_ok = ~np.any(info.reshape(frames, blocks, code.k) != b.info.reshape(frames, blocks, code.k), axis=2)
+        cer[f"{snr:g}dB"] = float(1.0 - cw_ok.mean())
+        good_cw += int(cw_ok.sum())
 
     # end to end: pinned host IQ -> device, search + demod + decode, decoded bits -> host
     h_iq = {snr: torch.empty((frames, L), dtype=torch.complex64, pin_memory=True) for snr in OFDM_SNRS}
@@ -633,7 +637,12 @@ def run_ofdm(args, rank, world):
                        "fft": 1024, "cp": 72, "active_sc": 600, "symbols": 14, "code": "QC (1024,512) Z=64",
                        "bp_iterations": OFDM_ITERS, "codewords_per_frame": blocks,
                        "l2": "6 resident batches of 34 MB cycled (> L2)"},
-            "fer": fer, "kernel_ms_per_step": {k: round(v, 4) for k, v in kern.items()}, "dominant_kernel": top,
+            "fer": fer, "codeword_error_rate": cer,
+            "goodput": {"value": round(value * good_cw / (len(OFDM_SNRS) * frames * blocks), 3), "unit": "Mbit/s",
+                        "what": "information bits of correctly decoded codewords per second (the value times the "
+                                "correct fraction of the first batch at each SNR); frames the receiver does not "
+                                "find count as lost, as in the reference receiver"},
+            "kernel_ms_per_step": {k: round(v, 4) for k, v in kern.items()}, "dominant_kernel": top,
             "gpu_launches": args.steps * len(OFDM_SNRS) * 3, "clocks": clk,
             "roofline": {"bound": "hbm", "kernel": "demod_kernel", "achieved": round(achieved, 2), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": traffic_for("demod_kernel", frames),
