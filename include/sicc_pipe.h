@@ -146,6 +146,12 @@ SICC_API int sicc_pipe_tx_batch(unsigned long long handle, const unsigned char* 
 
 /* Kernel durations (ms) of the last sicc_pipe_demod_batch / _gather call: sync, demod. */
 SICC_API int sicc_pipe_last_batch_ms(unsigned long long handle, float* out_sync_ms, float* out_demod_ms);
+/* (No counterpart in the reference.)  The demodulator stages each symbol's samples in
+ * shared memory with bulk asynchronous copies and waits on them with an iteration limit;
+ * this reports how many waits on the current device hit that limit since the library
+ * loaded (each one is counted and the symbol is read from global memory instead).
+ * Expected to stay 0. */
+SICC_API int sicc_pipe_wait_timeouts(unsigned int* out_count);
 
 #ifdef __cplusplus
 }

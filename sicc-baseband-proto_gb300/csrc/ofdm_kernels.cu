@@ -600,17 +600,92 @@ __device__ float2* fft_stockham(float2* a, float2* b, int nfft, const float2* __
     return a;
 }
 
-// Loads symbol `sym` of a frame (CP stripped, CFO derotated) into buf.
-__device__ void load_symbol(const DemodView& v, const float2* __restrict__ x, float cfo_norm, int sym, float2* buf)
+// ---- bulk-async staging of a symbol's samples (cp.async.bulk + mbarrier) ----
+
+__device__ unsigned int g_demod_wait_timeouts = 0;  // waits that hit their iteration limit (never expected)
+constexpr int kMaxWaitSpins = 1 << 22;
+
+__device__ __forceinline__ unsigned smem_addr(const void* p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity)
+{
+    unsigned ok = 0;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the barrier's phase `parity` with an iteration limit; on the limit the
+// timeout is counted, one more bounded wait lets an in-flight copy land, and false
+// is returned (the caller skips the symbol's data).
+__device__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity)
+{
+    for (int i = 0; i < kMaxWaitSpins; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    if (threadIdx.x == 0) atomicAdd(&g_demod_wait_timeouts, 1u);
+    for (int i = 0; i < kMaxWaitSpins; ++i)
+        if (mbar_try_wait(bar, parity)) break;
+    return false;
+}
+
+// Where symbol `sym` of the frame at x lies, and how its samples are staged: the
+// 16-byte-aligned middle [s, s + len) by one bulk copy into stage[0 .. len), the
+// samples before s and from s + len on (at most one each: the rows are 8-byte
+// complex samples) by plain loads when they are used.
+struct SymbolStage {
+    const float2* src;  // first sample of the symbol (CP stripped)
+    int s, len;
+};
+
+__device__ __forceinline__ SymbolStage symbol_stage(const DemodView& v, const float2* x, int sym)
+{
+    SymbolStage g;
+    g.src = x + v.pre_len + sym * (v.nfft + v.cp) + v.cp;
+    g.s = (reinterpret_cast<uintptr_t>(g.src) & 15u) ? 1 : 0;
+    g.len = v.nfft - 2 * g.s;  // nfft is even: len * 8 bytes is a multiple of 16
+    return g;
+}
+
+// Thread 0: arms `bar` for the symbol's bytes and starts its bulk copy into `stage`.
+__device__ __forceinline__ void stage_symbol(const SymbolStage& g, float2* stage, uint64_t* bar)
+{
+    const unsigned bytes = static_cast<unsigned>(g.len) * 8u;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier reads of `stage` come first
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(stage)),
+                 "l"(g.src + g.s), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// CFO derotation and CP strip: work[i] = sample i of the symbol times
+// exp(-j 2 pi cfo n / fs), n its index from the frame start; the samples come from
+// the staged copy, the edge samples (and every sample if the copy did not land)
+// from global memory.
+__device__ __forceinline__ void derotate_symbol(const DemodView& v, const SymbolStage& g, const float2* stage,
+                                                float2* work, float cfo_norm, int sym, bool staged)
 {
     const int off = v.pre_len + sym * (v.nfft + v.cp) + v.cp;
     for (int i = threadIdx.x; i < v.nfft; i += blockDim.x) {
-        const int n = off + i;  // sample index from the frame start
-        const float2 s = x[n];
+        const float2 smp = (!staged || i < g.s || i >= g.s + g.len) ? g.src[i] : stage[i - g.s];
         float sn, cs;
         // exp(-j 2 pi cfo n / fs) with cfo_norm = cfo / fs
-        sincospif(-2.0f * cfo_norm * static_cast<float>(n), &sn, &cs);
-        buf[i] = cmul(s, make_float2(cs, sn));
+        sincospif(-2.0f * cfo_norm * static_cast<float>(off + i), &sn, &cs);
+        work[i] = cmul(smp, make_float2(cs, sn));
     }
     __syncthreads();
 }
@@ -629,10 +704,11 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
              const long long* __restrict__ llr_off)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2* buf0 = reinterpret_cast<float2*>(smem_raw);
-    float2* buf1 = buf0 + v.nfft;
-    float2* hp = buf1 + v.nfft;  // [kMaxPilotsPerCta][active_sc]
-    __shared__ int s_pilot_of[kMaxPilotsPerCta];
+    float2* work = reinterpret_cast<float2*>(smem_raw);  // derotated symbol, FFT buffer
+    // stage(b) = work + (1 + b) * nfft: staged raw symbols (two buffers), FFT buffer after use
+    auto stage = [&](int b) { return work + static_cast<size_t>(1 + b) * v.nfft; };
+    float2* hp = work + 3 * v.nfft;                      // [kMaxPilotsPerCta][active_sc]
+    __shared__ __align__(8) uint64_t s_bar[2];
 
     const int f = blockIdx.x;
     const int ds0 = blockIdx.y * symbols_per_cta;
@@ -661,29 +737,49 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
         pmin = min(pmin, min(v.interp_p0[d], v.interp_p1[d]));
         pmax = max(pmax, max(v.interp_p0[d], v.interp_p1[d]));
     }
-    const int npil = v.use_pilot_est ? (pmax - pmin + 1) : 0;
-    for (int q = 0; q < npil && q < kMaxPilotsPerCta; ++q) {
-        const int p = pmin + q;
-        load_symbol(v, x, cfo_norm, v.pilot_symbols[p], buf0);
-        const float2* Y = fft_stockham(buf0, buf1, v.nfft, v.twiddle);
-        for (int sc = threadIdx.x; sc < v.active_sc; sc += blockDim.x) {
-            const float2 y = Y[v.used_bins[sc]];
-            const float2 pil = v.pilot_grid[static_cast<size_t>(p) * v.active_sc + sc];
-            const float den = fmaxf(cnorm(pil), 1e-9f);
-            const float2 t = cmulconj(y, pil);
-            hp[q * v.active_sc + sc] = make_float2(__fdiv_rn(t.x, den), __fdiv_rn(t.y, den));
-        }
-        if (threadIdx.x == 0) s_pilot_of[q] = p;
-        __syncthreads();
+    const int npil = v.use_pilot_est ? min(pmax - pmin + 1, kMaxPilotsPerCta) : 0;
+    const int nsym = npil + (ds1 - ds0);
+    // the CTA's symbols in processing order: its pilots, then its data symbols
+    auto sym_at = [&](int i) { return i < npil ? v.pilot_symbols[pmin + i] : v.data_symbols[ds0 + i - npil]; };
+
+    // Symbol i+1's samples are copied into stage[(i+1)&1] by the bulk-copy engine while
+    // symbol i is transformed; each buffer's barrier completes once per copy.
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    __syncthreads();
+    if (threadIdx.x == 0) stage_symbol(symbol_stage(v, x, sym_at(0)), stage(0), &s_bar[0]);
+    unsigned phase = 0u;  // bit b: parity of buffer b's next completion
 
     const int bps = v.bits_per_symbol;
     const int abits = bps >> 1;
     const int levels = 1 << abits;
     float* out = llr + (llr_off ? llr_off[f] : static_cast<long long>(f) * llr_stride);
-    for (int d = ds0; d < ds1; ++d) {
-        load_symbol(v, x, cfo_norm, v.data_symbols[d], buf0);
-        const float2* Y = fft_stockham(buf0, buf1, v.nfft, v.twiddle);
+    for (int i = 0; i < nsym; ++i) {
+        const int b = i & 1;
+        const int sym = sym_at(i);
+        if (threadIdx.x == 0 && i + 1 < nsym)
+            stage_symbol(symbol_stage(v, x, sym_at(i + 1)), stage(b ^ 1), &s_bar[b ^ 1]);
+        const SymbolStage g = symbol_stage(v, x, sym);
+        const bool staged = mbar_wait_bounded(b ? &s_bar[1] : &s_bar[0], (phase >> b) & 1u);
+        phase ^= 1u << b;
+        derotate_symbol(v, g, stage(b), work, cfo_norm, sym, staged);
+        const float2* Y = fft_stockham(work, stage(b), v.nfft, v.twiddle);
+        if (i < npil) {  // LS estimate at the pilot symbol
+            const int p = pmin + i;
+            for (int sc = threadIdx.x; sc < v.active_sc; sc += blockDim.x) {
+                const float2 y = Y[v.used_bins[sc]];
+                const float2 pil = v.pilot_grid[static_cast<size_t>(p) * v.active_sc + sc];
+                const float den = fmaxf(cnorm(pil), 1e-9f);
+                const float2 t = cmulconj(y, pil);
+                hp[i * v.active_sc + sc] = make_float2(__fdiv_rn(t.x, den), __fdiv_rn(t.y, den));
+            }
+            __syncthreads();
+            continue;
+        }
+        const int d = ds0 + i - npil;
         const int q0 = v.interp_p0[d] - pmin, q1 = v.interp_p1[d] - pmin;
         const float al = v.interp_alpha[d];
         const float w0 = __fsub_rn(1.0f, al);
@@ -712,27 +808,27 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
             float mi_all = FLT_MAX, mq_all = FLT_MAX;
             float mi0[3], mi1[3], mq0[3], mq1[3];
 #pragma unroll
-            for (int b = 0; b < 3; ++b) { mi0[b] = mi1[b] = mq0[b] = mq1[b] = INFINITY; }
-            for (int g = 0; g < levels; ++g) {
-                const float lv = v.axis_levels[g];
+            for (int bb = 0; bb < 3; ++bb) { mi0[bb] = mi1[bb] = mq0[bb] = mq1[bb] = INFINITY; }
+            for (int gq = 0; gq < levels; ++gq) {
+                const float lv = v.axis_levels[gq];
                 const float di = sq_dist(ex, lv), dq = sq_dist(ey, lv);
                 mi_all = fminf(mi_all, di);
                 mq_all = fminf(mq_all, dq);
 #pragma unroll
-                for (int b = 0; b < 3; ++b) {
-                    if (b < abits) {
-                        const int bit = (g >> (abits - 1 - b)) & 1;
-                        if (bit) { mi1[b] = fminf(mi1[b], di); mq1[b] = fminf(mq1[b], dq); }
-                        else { mi0[b] = fminf(mi0[b], di); mq0[b] = fminf(mq0[b], dq); }
+                for (int bb = 0; bb < 3; ++bb) {
+                    if (bb < abits) {
+                        const int bit = (gq >> (abits - 1 - bb)) & 1;
+                        if (bit) { mi1[bb] = fminf(mi1[bb], di); mq1[bb] = fminf(mq1[bb], dq); }
+                        else { mi0[bb] = fminf(mi0[bb], di); mq0[bb] = fminf(mq0[bb], dq); }
                     }
                 }
             }
             float vals[6];
 #pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                if (b < abits) {
-                    vals[b] = __fdiv_rn(__fsub_rn(__fadd_rn(mi1[b], mq_all), __fadd_rn(mi0[b], mq_all)), sig);
-                    vals[abits + b] = __fdiv_rn(__fsub_rn(__fadd_rn(mi_all, mq1[b]), __fadd_rn(mi_all, mq0[b])), sig);
+            for (int bb = 0; bb < 3; ++bb) {
+                if (bb < abits) {
+                    vals[bb] = __fdiv_rn(__fsub_rn(__fadd_rn(mi1[bb], mq_all), __fadd_rn(mi0[bb], mq_all)), sig);
+                    vals[abits + bb] = __fdiv_rn(__fsub_rn(__fadd_rn(mi_all, mq1[bb]), __fadd_rn(mi_all, mq0[bb])), sig);
                 }
             }
             if (bps == 4) {
@@ -740,11 +836,18 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
             } else if (bps == 2) {
                 *reinterpret_cast<float2*>(o) = make_float2(vals[0], vals[1]);
             } else {
-                for (int b = 0; b < bps; ++b) o[b] = vals[b];
+                for (int bb = 0; bb < bps; ++bb) o[bb] = vals[bb];
             }
         }
         __syncthreads();
     }
+}
+
+unsigned demod_wait_timeouts()
+{
+    unsigned v = 0;
+    check_cuda(cudaMemcpyFromSymbol(&v, g_demod_wait_timeouts, sizeof v), "read the demodulator's wait counter");
+    return v;
 }
 
 void launch_demod(const DemodView& v, const float2* samples, long long stride, const SyncOut* sync, int frames,
@@ -762,8 +865,9 @@ void launch_demod(const DemodView& v, const float2* samples, long long stride, c
         const int groups = (v.num_data + 3) / 4;
         spc = (v.num_data + groups - 1) / groups;
     }
-    const size_t smem = (2 * static_cast<size_t>(v.nfft) + kMaxPilotsPerCta * static_cast<size_t>(v.active_sc)) *
+    const size_t smem = (3 * static_cast<size_t>(v.nfft) + kMaxPilotsPerCta * static_cast<size_t>(v.active_sc)) *
                         sizeof(float2);
+    if (smem > 227 * 1024) throw InvalidArgument("nfft and active_sc exceed the demodulator's shared memory");
     check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(demod_kernel), smem), "cudaFuncSetAttribute(demod)");
     const dim3 grid(frames, (v.num_data + spc - 1) / spc);
     demod_kernel<<<grid, kDemodThreads, smem, st>>>(v, samples, stride, sync, llr, llr_stride, spc, frame_off,

@@ -63,6 +63,10 @@ struct DemodView {
 void launch_demod(const DemodView& v, const float2* samples, long long stride, const SyncOut* sync, int frames,
                   float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta = 0,
                   const long long* frame_off = nullptr, const long long* llr_off = nullptr);
+// Waits of the demodulator on its staged-sample copies that hit their iteration limit
+// since the library loaded on the current device (each one is counted and the symbol is
+// read from global memory instead; never expected).
+unsigned demod_wait_timeouts();
 
 // Device side of the real-time ingest: the frame-extraction loop of the receive
 // path (GpuRxSyncExtractor::extract_device, uhd_ldpc_ofdm_link.cpp:6901-6979, as the

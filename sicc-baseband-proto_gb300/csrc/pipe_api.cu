@@ -1071,6 +1071,15 @@ int sicc_ingest_close(unsigned long long handle)
     });
 }
 
+int sicc_pipe_wait_timeouts(unsigned int* out_count)
+{
+    return guarded([&] {
+        if (!out_count) throw InvalidArgument("null argument");
+        *out_count = demod_wait_timeouts();
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
 int sicc_pipe_last_batch_ms(unsigned long long handle, float* out_sync_ms, float* out_demod_ms)
 {
     return guarded([&] {

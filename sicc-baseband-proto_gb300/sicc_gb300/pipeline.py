@@ -73,6 +73,14 @@ _SIGS = {
 }
 
 
+def wait_timeouts() -> int:
+    """Demodulator waits on staged-sample copies that hit their iteration limit (expected 0)."""
+    out = C.c_uint(0)
+    _lib.check(_lib.bind("sicc_pipe_wait_timeouts", C.c_int, [C.POINTER(C.c_uint)])(C.byref(out)),
+               "sicc_pipe_wait_timeouts")
+    return out.value
+
+
 def _fn(name):
     res, args = _SIGS[name]
     return _lib.bind(name, res, args)

@@ -178,5 +178,7 @@ def test_c3_ofdm_chain_fer_parity(cuda, oracle, pool, snr):
           f"CER GPU {g_cer[0]:.4f} reference {r_cer[0]:.4f} {np.round(r_cer[1:], 4).tolist()}; "
           f"FER GPU {g_fer[0]:.4f} reference {r_fer[0]:.4f} {np.round(r_fer[1:], 4).tolist()}")
     assert agree >= 0.99
+    from sicc_gb300.pipeline import wait_timeouts
+    assert wait_timeouts() == 0  # every staged-sample copy of the demodulator landed in time
     assert errstats.inside(g_cer[0], r_cer[1:]) and errstats.inside(r_cer[0], g_cer[1:])
     assert errstats.inside(g_fer[0], r_fer[1:]) and errstats.inside(r_fer[0], g_fer[1:])
