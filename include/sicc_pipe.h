@@ -152,6 +152,12 @@ SICC_API int sicc_pipe_last_batch_ms(unsigned long long handle, float* out_sync_
  * loaded (each one is counted and the symbol is read from global memory instead).
  * Expected to stay 0. */
 SICC_API int sicc_pipe_wait_timeouts(unsigned int* out_count);
+/* (No counterpart in the reference.)  Data symbols each demodulator CTA takes
+ * (1..data symbols per frame; the default is about four).  Fewer per CTA gives more
+ * CTAs; each CTA also transforms the pilot symbols its data symbols interpolate from
+ * (at most four), so more per CTA repeats fewer pilot transforms.  Results do not
+ * depend on it.  Call after upload_static_tables. */
+SICC_API int sicc_pipe_set_demod_shape(unsigned long long handle, int symbols_per_cta);
 
 #ifdef __cplusplus
 }

@@ -550,10 +550,22 @@ void launch_sync(const float2* samples, long long stride, const int* counts, int
 namespace {
 
 constexpr int kDemodThreads = 256;
-constexpr int kMaxPilotsPerCta = 4;
+
+// Twiddle entries the FFT of nfft points reads (indices below 3 nfft / 4), rounded to an
+// even count so the buffers after them stay 16-byte aligned.
+__host__ __device__ constexpr int demod_twiddles(int nfft) { return ((3 * nfft / 4) + 1) & ~1; }
 
 // Stockham autosort FFT of `nfft` points held in buf[0] (natural order in and
 // out); returns the buffer that holds the result.
+// `tw` in shared memory (kSharedTw) or read through the read-only cache.
+template <bool kSharedTw = false>
+__device__ __forceinline__ float2 twiddle_at(const float2* __restrict__ tw, int i)
+{
+    if constexpr (kSharedTw) return tw[i];
+    else return __ldg(tw + i);
+}
+
+template <bool kSharedTw = false>
 __device__ float2* fft_stockham(float2* a, float2* b, int nfft, const float2* __restrict__ tw)
 {
     int ns = 1;
@@ -564,9 +576,9 @@ __device__ float2* fft_stockham(float2* a, float2* b, int nfft, const float2* __
             const int step = nfft / (4 * ns);
             float2 a0 = a[j], a1 = a[j + q], a2 = a[j + 2 * q], a3 = a[j + 3 * q];
             if (ns > 1) {
-                a1 = cmul(a1, __ldg(tw + k * step));
-                a2 = cmul(a2, __ldg(tw + 2 * k * step));
-                a3 = cmul(a3, __ldg(tw + 3 * k * step));
+                a1 = cmul(a1, twiddle_at<kSharedTw>(tw, k * step));
+                a2 = cmul(a2, twiddle_at<kSharedTw>(tw, 2 * k * step));
+                a3 = cmul(a3, twiddle_at<kSharedTw>(tw, 3 * k * step));
             }
             const float2 b0 = make_float2(a0.x + a2.x, a0.y + a2.y);
             const float2 b1 = make_float2(a0.x - a2.x, a0.y - a2.y);
@@ -589,7 +601,7 @@ __device__ float2* fft_stockham(float2* a, float2* b, int nfft, const float2* __
         for (int j = threadIdx.x; j < h; j += blockDim.x) {
             const int k = j & (ns - 1);
             const float2 a0 = a[j];
-            const float2 a1 = cmul(a[j + h], __ldg(tw + k * (nfft / (2 * ns))));
+            const float2 a1 = cmul(a[j + h], twiddle_at<kSharedTw>(tw, k * (nfft / (2 * ns))));
             const int o = (j / ns) * ns * 2 + k;
             b[o] = make_float2(a0.x + a1.x, a0.y + a1.y);
             b[o + ns] = make_float2(a0.x - a1.x, a0.y - a1.y);
@@ -707,7 +719,8 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
     float2* work = reinterpret_cast<float2*>(smem_raw);  // derotated symbol, FFT buffer
     // stage(b) = work + (1 + b) * nfft: staged raw symbols (two buffers), FFT buffer after use
     auto stage = [&](int b) { return work + static_cast<size_t>(1 + b) * v.nfft; };
-    float2* hp = work + 3 * v.nfft;                      // [kMaxPilotsPerCta][active_sc]
+    float2* tw = work + 3 * v.nfft;                       // twiddles 0 .. 3 nfft / 4 (all the FFT reads)
+    float2* hp = tw + demod_twiddles(v.nfft);             // [max_pilots_per_cta][active_sc]
     __shared__ __align__(8) uint64_t s_bar[2];
 
     const int f = blockIdx.x;
@@ -737,7 +750,7 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
         pmin = min(pmin, min(v.interp_p0[d], v.interp_p1[d]));
         pmax = max(pmax, max(v.interp_p0[d], v.interp_p1[d]));
     }
-    const int npil = v.use_pilot_est ? min(pmax - pmin + 1, kMaxPilotsPerCta) : 0;
+    const int npil = v.use_pilot_est ? min(pmax - pmin + 1, v.max_pilots_per_cta) : 0;
     const int nsym = npil + (ds1 - ds0);
     // the CTA's symbols in processing order: its pilots, then its data symbols
     auto sym_at = [&](int i) { return i < npil ? v.pilot_symbols[pmin + i] : v.data_symbols[ds0 + i - npil]; };
@@ -749,6 +762,11 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
         mbar_init(&s_bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    for (int i = threadIdx.x; i < demod_twiddles(v.nfft); i += blockDim.x) tw[i] = __ldg(v.twiddle + i);
+    // the constellation's axis levels (at most 8: 64-QAM) in registers
+    float lvl[8];
+#pragma unroll
+    for (int g = 0; g < 8; ++g) lvl[g] = (v.bits_per_symbol >= 2 && g < (1 << (v.bits_per_symbol >> 1))) ? __ldg(v.axis_levels + g) : 0.0f;
     __syncthreads();
     if (threadIdx.x == 0) stage_symbol(symbol_stage(v, x, sym_at(0)), stage(0), &s_bar[0]);
     unsigned phase = 0u;  // bit b: parity of buffer b's next completion
@@ -766,7 +784,7 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
         const bool staged = mbar_wait_bounded(b ? &s_bar[1] : &s_bar[0], (phase >> b) & 1u);
         phase ^= 1u << b;
         derotate_symbol(v, g, stage(b), work, cfo_norm, sym, staged);
-        const float2* Y = fft_stockham(work, stage(b), v.nfft, v.twiddle);
+        const float2* Y = fft_stockham<true>(work, stage(b), v.nfft, tw);
         if (i < npil) {  // LS estimate at the pilot symbol
             const int p = pmin + i;
             for (int sc = threadIdx.x; sc < v.active_sc; sc += blockDim.x) {
@@ -794,14 +812,16 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
             }
             const float h2 = fmaxf(cnorm(h), 1e-9f);
             const float2 t = cmulconj(y, h);
-            const float den = __fadd_rn(h2, v.noise_var);
-            const float ex = __fdiv_rn(t.x, den), ey = __fdiv_rn(t.y, den);
-            const float sig = fmaxf(__fdiv_rn(v.noise_var, h2), 1e-8f);
+            // eq = y conj(h) / (|h|^2 + N0) and LLR = (d1 - d0) / sigma^2 as products with the two
+            // reciprocals (as the reference's GPU equaliser scales by 1 / (|h|^2 + N0))
+            const float inv_den = __frcp_rn(__fadd_rn(h2, v.noise_var));
+            const float ex = __fmul_rn(t.x, inv_den), ey = __fmul_rn(t.y, inv_den);
+            const float inv_sig = __frcp_rn(fmaxf(__fdiv_rn(v.noise_var, h2), 1e-8f));
             float* o = out + (static_cast<long long>(d) * v.active_sc + sc) * bps;
             if (bps == 1) {
                 const float dy = __fmul_rn(ey, ey);
                 const float d0 = __fadd_rn(sq_dist(ex, 1.0f), dy), d1 = __fadd_rn(sq_dist(ex, -1.0f), dy);
-                o[0] = __fdiv_rn(__fsub_rn(d1, d0), sig);
+                o[0] = __fmul_rn(__fsub_rn(d1, d0), inv_sig);
                 continue;
             }
             // per-axis squared distances and minima
@@ -809,8 +829,10 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
             float mi0[3], mi1[3], mq0[3], mq1[3];
 #pragma unroll
             for (int bb = 0; bb < 3; ++bb) { mi0[bb] = mi1[bb] = mq0[bb] = mq1[bb] = INFINITY; }
-            for (int gq = 0; gq < levels; ++gq) {
-                const float lv = v.axis_levels[gq];
+#pragma unroll
+            for (int gq = 0; gq < 8; ++gq) {
+                if (gq >= levels) break;
+                const float lv = lvl[gq];
                 const float di = sq_dist(ex, lv), dq = sq_dist(ey, lv);
                 mi_all = fminf(mi_all, di);
                 mq_all = fminf(mq_all, dq);
@@ -827,8 +849,9 @@ demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, 
 #pragma unroll
             for (int bb = 0; bb < 3; ++bb) {
                 if (bb < abits) {
-                    vals[bb] = __fdiv_rn(__fsub_rn(__fadd_rn(mi1[bb], mq_all), __fadd_rn(mi0[bb], mq_all)), sig);
-                    vals[abits + bb] = __fdiv_rn(__fsub_rn(__fadd_rn(mi_all, mq1[bb]), __fadd_rn(mi_all, mq0[bb])), sig);
+                    vals[bb] = __fmul_rn(__fsub_rn(__fadd_rn(mi1[bb], mq_all), __fadd_rn(mi0[bb], mq_all)), inv_sig);
+                    vals[abits + bb] =
+                        __fmul_rn(__fsub_rn(__fadd_rn(mi_all, mq1[bb]), __fadd_rn(mi_all, mq0[bb])), inv_sig);
                 }
             }
             if (bps == 4) {
@@ -860,12 +883,13 @@ void launch_demod(const DemodView& v, const float2* samples, long long stride, c
         throw InvalidArgument("bits_per_symbol must be 1, 2, 4 or 6");
     if (v.kept_bits <= 0 || v.kept_bits > v.num_data * v.active_sc * v.bits_per_symbol || v.kept_bits % v.bits_per_symbol)
         throw InvalidArgument("kept LLRs must be a positive multiple of bits_per_symbol within the frame");
-    int spc = symbols_per_cta;
-    if (spc <= 0) {
-        const int groups = (v.num_data + 3) / 4;
-        spc = (v.num_data + groups - 1) / groups;
-    }
-    const size_t smem = (3 * static_cast<size_t>(v.nfft) + kMaxPilotsPerCta * static_cast<size_t>(v.active_sc)) *
+    // the owner of the view sized max_pilots_per_cta for exactly this grouping of data symbols
+    const int spc = symbols_per_cta;
+    if (spc <= 0 || spc > v.num_data) throw InvalidArgument("symbols_per_cta must be in 1..num_data");
+    if (v.max_pilots_per_cta < 0 || v.max_pilots_per_cta > kDemodMaxPilots)
+        throw InvalidArgument("a demodulator CTA can hold at most 4 pilot symbols");
+    const size_t smem = (3 * static_cast<size_t>(v.nfft) + demod_twiddles(v.nfft) +
+                         static_cast<size_t>(v.max_pilots_per_cta) * v.active_sc) *
                         sizeof(float2);
     if (smem > 227 * 1024) throw InvalidArgument("nfft and active_sc exceed the demodulator's shared memory");
     check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(demod_kernel), smem), "cudaFuncSetAttribute(demod)");

@@ -53,7 +53,10 @@ struct DemodView {
     const float2* pilot_grid;  // [num_pilots][active_sc]
     const float2* twiddle;     // [nfft]: exp(-2 pi i j / nfft)
     const float* axis_levels;  // [2^(bps/2)] constellation amplitude by Gray axis index (bps >= 2)
+    int max_pilots_per_cta;    // pilot symbols one CTA's data symbols refer to, at most kDemodMaxPilots
 };
+
+constexpr int kDemodMaxPilots = 4;
 
 // Fused demodulator: CFO derotation + CP strip + FFT + LS pilot estimate +
 // interpolation + MMSE equalisation + max-log LLR.  Frame f's samples start at
@@ -61,7 +64,7 @@ struct DemodView {
 // `cfo_override` is used); LLRs go to llr + f*llr_stride.  With frame_off / llr_off (device offsets in
 // complex samples / floats) frame f is read from samples + frame_off[f] and written to llr + llr_off[f].
 void launch_demod(const DemodView& v, const float2* samples, long long stride, const SyncOut* sync, int frames,
-                  float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta = 0,
+                  float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta,
                   const long long* frame_off = nullptr, const long long* llr_off = nullptr);
 // Waits of the demodulator on its staged-sample copies that hit their iteration limit
 // since the library loaded on the current device (each one is counted and the symbol is

@@ -71,6 +71,7 @@ struct Pipe {
     int max_rx = 0;
     int batch_frames = 256;
     int symbols_per_cta = 0;  // data symbols per demod CTA; their pilots span at most 4
+    std::vector<int> h_p0, h_p1;  // interpolation pilots of each data symbol (host copies)
     bool tables = false;
     float pre_energy = 0.0f;
     DemodView view{};
@@ -170,6 +171,24 @@ sicc_pipe_sync_t to_public(const SyncOut& s)
 }
 
 // Search `count` samples already in device memory (slot stream); returns the result.
+// The most pilot symbols one demodulator CTA needs when it takes `spc` data symbols
+// (0 without pilot channel estimation).
+int pilot_span(const Pipe& p, int spc)
+{
+    if (!p.cfg.use_pilot_channel_est) return 0;
+    const int nd = static_cast<int>(p.h_p0.size());
+    int worst = 0;
+    for (int d0 = 0; d0 < nd; d0 += std::max(spc, 1)) {
+        int lo = 1 << 30, hi = -1;
+        for (int d = d0; d < std::min(nd, d0 + spc); ++d) {
+            lo = std::min(lo, std::min(p.h_p0[d], p.h_p1[d]));
+            hi = std::max(hi, std::max(p.h_p0[d], p.h_p1[d]));
+        }
+        worst = std::max(worst, hi - lo + 1);
+    }
+    return worst;
+}
+
 SyncOut run_sync(Pipe& p, Slot& s, const float2* d_iq, int count)
 {
     if (count < p.cfg.preamble_len) throw InvalidArgument("RX sample_count is shorter than the preamble");
@@ -280,21 +299,12 @@ int sicc_pipe_upload_static_tables(unsigned long long handle, const sicc_pipe_ta
                 throw InvalidArgument("interpolation pilot indices out of range");
         }
         // data symbols per CTA: about four, fewer when their interpolation pilots would span more than four
+        p->h_p0.assign(t->interp_p0, t->interp_p0 + t->data_count);
+        p->h_p1.assign(t->interp_p1, t->interp_p1 + t->data_count);
         {
             const int groups = (t->data_count + 3) / 4;
             int spc = (t->data_count + groups - 1) / groups;
-            for (; spc > 1; --spc) {
-                bool ok = true;
-                for (int d0 = 0; d0 < t->data_count && ok; d0 += spc) {
-                    int lo = 1 << 30, hi = -1;
-                    for (int d = d0; d < std::min(t->data_count, d0 + spc); ++d) {
-                        lo = std::min(lo, std::min(t->interp_p0[d], t->interp_p1[d]));
-                        hi = std::max(hi, std::max(t->interp_p0[d], t->interp_p1[d]));
-                    }
-                    ok = !c.use_pilot_channel_est || hi - lo + 1 <= 4;
-                }
-                if (ok) break;
-            }
+            while (spc > 1 && pilot_span(*p, spc) > kDemodMaxPilots) --spc;
             p->symbols_per_cta = spc;
         }
         upload(p->used_bins, bins.data(), bins.size());
@@ -369,6 +379,7 @@ int sicc_pipe_upload_static_tables(unsigned long long handle, const sicc_pipe_ta
         v.pilot_grid = p->pilot_grid.p;
         v.twiddle = p->twiddle.p;
         v.axis_levels = p->axis.p;
+        v.max_pilots_per_cta = pilot_span(*p, p->symbols_per_cta);
         // per-symbol pilot / data indices for the transmitter's resource grid
         std::vector<int> pos(c.num_symbols, -1), dos(c.num_symbols, -1);
         for (int q = 0; q < t->pilot_count; ++q) pos[t->pilot_symbols[q]] = q;
@@ -1067,6 +1078,24 @@ int sicc_ingest_close(unsigned long long handle)
             g->closed = true;
         }
         g->cv.notify_all();
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_pipe_set_demod_shape(unsigned long long handle, int symbols_per_cta)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        require_tables(*p);
+        const int nd = static_cast<int>(p->h_p0.size());
+        if (symbols_per_cta < 1 || symbols_per_cta > nd)
+            throw InvalidArgument("symbols_per_cta must be in 1..data symbols per frame");
+        if (pilot_span(*p, symbols_per_cta) > kDemodMaxPilots)
+            throw InvalidArgument("the data symbols of one CTA would need more than " + std::to_string(kDemodMaxPilots) +
+                                  " pilot symbols");
+        p->symbols_per_cta = symbols_per_cta;
+        p->view.max_pilots_per_cta = pilot_span(*p, symbols_per_cta);
         return CUDA_OSD_STATUS_OK;
     });
 }

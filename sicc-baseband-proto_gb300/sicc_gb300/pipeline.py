@@ -190,6 +190,11 @@ class RxPipeline:
         _lib.check(_fn("sicc_pipe_demod_gather")(self.handle, p(d_iq), p(d_frame_off), sample_count, frames, p(d_llr),
                                                  p(d_llr_off), p(d_sync), st), "sicc_pipe_demod_gather")
 
+    def set_demod_shape(self, symbols_per_cta: int):
+        """Data symbols per demodulator CTA (results do not depend on it)."""
+        fn = _lib.bind("sicc_pipe_set_demod_shape", C.c_int, [_lib.u64, C.c_int])
+        _lib.check(fn(self.handle, symbols_per_cta), "sicc_pipe_set_demod_shape")
+
     def last_batch_ms(self):
         a, b = C.c_float(), C.c_float()
         _lib.check(_fn("sicc_pipe_last_batch_ms")(self.handle, C.byref(a), C.byref(b)), "sicc_pipe_last_batch_ms")

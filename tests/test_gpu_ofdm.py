@@ -220,6 +220,36 @@ def test_ofdm_rx_workload_frames(cuda, oracle):
     assert found >= 6 and agree >= found - 1
 
 
+def test_demod_shapes_give_identical_llrs(cuda):
+    """Data symbols per demodulator CTA changes the grid and the pilot transforms each CTA
+    repeats, never the LLRs; every staged-sample wait lands in time."""
+    torch = cuda
+    from sicc_gb300.pipeline import SYNC_RECORD, wait_timeouts
+    t = ofdm.reference_tables(ofdm.OFDM_C3)
+    code = codes.ofdm_code()
+    gen = ofdm.FrameGenerator(t, code, seed=31)
+    b = gen.batch(12, snr_db=14.0, cfo_subcarriers=0.1, max_offset=200, rayleigh_taps=6)
+    p = _pipe(t, float(np.mean(b.noise_var)), blocks=30, code=code, max_batch_frames=12)
+    d_iq = torch.from_numpy(b.iq).cuda()
+    L = b.iq.shape[1]
+
+    def run():
+        d_llr = torch.full((12, p.coded_bits), 7.0, dtype=torch.float32, device="cuda")
+        d_sync = torch.zeros(12 * SYNC_RECORD.itemsize, dtype=torch.uint8, device="cuda")
+        p.demod_batch(d_iq, L, L, 12, d_llr, d_sync, torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        return d_llr.cpu().numpy()
+
+    ref = run()
+    for spc in (1, 2, 3, 5, 7, 13):
+        p.set_demod_shape(spc)
+        assert np.array_equal(run().view(np.uint32), ref.view(np.uint32)), spc
+    from sicc_gb300 import _lib
+    with pytest.raises(_lib.SiccError):
+        p.set_demod_shape(14)
+    assert wait_timeouts() == 0
+
+
 def test_no_frame_in_noise(cuda):
     t = ofdm.reference_tables(ofdm.OFDM_SMALL)
     p = _pipe(t, 1.0, max_rx_search_samples=4000)
