@@ -58,6 +58,30 @@ def traffic_for(kernel, units):
         return None
 
 
+KERNEL_ISSUE = os.path.join(ROOT, "profiles", "kernel_issue.json")
+
+
+def issue_roofline(kernel, units, launch_ms, launches, sm_mhz):
+    """Issue-bound roofline of `kernel`: warp instructions per unit (one ncu capture, see
+    KERNEL_ISSUE) x units processed / kernel time, against SMs x 4 schedulers x 1 warp
+    instruction per cycle at the sampled SM clock.  None when the kernel has no capture."""
+    try:
+        with open(KERNEL_ISSUE) as f:
+            rec = json.load(f)[kernel]
+    except Exception:
+        return None
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = sm_mhz or 2070.0
+    peak = sms * 4 * mhz * 1e6 / 1e9  # G warp instructions / s
+    achieved = rec["warp_inst_per_unit"] * units / (launch_ms * launches * 1e-3) / 1e9
+    return {"bound": "issue", "kernel": kernel, "unit": "G warp instructions/s", "achieved": round(achieved, 2),
+            "peak": round(peak, 2), "frac": round(achieved / peak, 4),
+            "warp_inst_per_unit": rec["warp_inst_per_unit"], "per": rec["unit"], "units": int(units),
+            "avg_launch_ms": round(launch_ms, 4), "peak_source": f"{sms} SMs x 4 schedulers at {mhz:.0f} MHz",
+            "capture": rec.get("capture")}
+
+
 def peaks():
     try:
         with open(PEAKS) as f:
@@ -310,6 +334,9 @@ def run_ours(args, rank, world):
         k_calls, k_bp, k_osd, k_cw = chain[e]["dec"].kernel_ms()
         chain[e]["dec"].set_timing(False)
         calls, bp_ms, osd_ms, osd_cw = calls + k_calls, bp_ms + k_bp, osd_ms + k_osd, osd_cw + k_cw
+    # edge updates of the timed launches: the batches cycle, so count each resident batch's
+    # iterations (decoded again below for the error rates) by how often it ran
+    timed_edges = 0
     if world > 1:
         elapsed_ms = max_over_ranks(elapsed_ms, "cuda")
 
@@ -329,6 +356,12 @@ def run_ours(args, rank, world):
         mean_iter[f"{e:g}dB"] = float(it.mean())
         osd_frac[f"{e:g}dB"] = float(d_used.cpu().numpy().mean())
         edge_updates += int(it.sum()) * code.edges
+        for r in range(RESIDENT_BATCHES):  # every resident batch's iterations, weighted by its timed runs
+            runs = sum(1 for s_ in range(args.steps) if s_ % RESIDENT_BATCHES == r)
+            if runs:
+                chain[e]["dec"].decode_device_batch(d_llr[e][r], d_info, d_ok, d_used, d_it, stream=stream)
+                torch.cuda.synchronize()
+                timed_edges += runs * int(d_it.cpu().numpy().astype(np.int64).sum()) * code.edges
 
     # the reference's schedule on the GPU: flooding min-sum + OSD on the best-syndrome posterior
     # (the reference decoder's arithmetic, bit for bit): its throughput and its bits on batch 0
@@ -438,7 +471,11 @@ def run_ours(args, rank, world):
                 "avg_launch_ms": round(avg_bp_ms, 4), "osd_avg_launch_ms": round(osd_ms / max(calls, 1), 4),
                 "edge_updates_per_s": round(edge_updates / len(EBN0) / (avg_bp_ms * 1e-3), 1),
                 "note": "BP is issue-bound (messages and row tables in registers, posteriors in shared memory); "
-                        "HBM fraction shown per contract"}
+                        "HBM fraction shown per contract; roofline_issue has the issue-bound form"}
+    # issue-bound rooflines of the step's two kernels (OSD is the larger share of it)
+    roofline_issue = {
+        "osd": issue_roofline("osd_kernel<2,2>", osd_cw, osd_ms / max(calls, 1), calls, clk.get("sm_mhz")),
+        "bp": issue_roofline(_bp_kernel_name(code), timed_edges, avg_bp_ms, calls, clk.get("sm_mhz"))}
 
     # ---- CPU baseline: the reference decoder on the same frames, and the error-rate parity ----
     cpu = fer_parity = None
@@ -474,6 +511,7 @@ def run_ours(args, rank, world):
                            "parallelism": f"replicas x{world}", "launch_shapes": shapes},
                 "fer": fer, "fer_parity": fer_parity, "mean_iterations": mean_iter, "osd_fraction": osd_frac,
                 "gpu_launches": args.steps * len(EBN0) * 2, "clocks": clk, "roofline": roofline,
+                "roofline_issue": roofline_issue,
                 "e2e": e2e, "cpu_baseline": cpu}
     if world > 1:
         dist.destroy_process_group()
@@ -530,6 +568,18 @@ def run_ofdm(args, rank, world):
         c = chain[snr]
         pipes[snr].demod_batch(iq, L, L, frames, c["llr"], c["sync"], st)
         c["dec"].decode_device_batch(c["llr"], c["bits"], c["ok"], None, None, stream=st)
+
+    # BP launch shapes tuned on each chain's own demodulated LLRs (the first batch)
+    shapes = {}
+    for snr in OFDM_SNRS:
+        c = chain[snr]
+        pipes[snr].demod_batch(d_iq[snr][0], L, L, frames, c["llr"], c["sync"], stream)
+        torch.cuda.synchronize()
+        if args.no_tune:
+            shapes[f"{snr:g}dB"] = c["dec"].shape()
+        else:
+            res = c["dec"].autotune(c["llr"], reps=2)
+            shapes[f"{snr:g}dB"] = dict(res.best, tuned_ms=round(res.best_ms, 4), default_ms=round(res.default_ms, 4))
 
     def step(s):
         for snr in OFDM_SNRS:
@@ -636,7 +686,7 @@ def run_ofdm(args, rank, world):
                        "chains": "one pipeline, decoder and CUDA stream per SNR point",
                        "fft": 1024, "cp": 72, "active_sc": 600, "symbols": 14, "code": "QC (1024,512) Z=64",
                        "bp_iterations": OFDM_ITERS, "codewords_per_frame": blocks,
-                       "l2": "6 resident batches of 34 MB cycled (> L2)"},
+                       "l2": "6 resident batches of 34 MB cycled (> L2)", "launch_shapes": shapes},
             "fer": fer, "codeword_error_rate": cer,
             "goodput": {"value": round(value * good_cw / (len(OFDM_SNRS) * frames * blocks), 3), "unit": "Mbit/s",
                         "what": "information bits of correctly decoded codewords per second (the value times the "
