@@ -1,8 +1,8 @@
 """Generates the golden fixtures under tests/golden/ from the reference's own CPU
-receive path (oracle/_ref/libref.so, compiled from the reference sources by
-oracle/Makefile).  Run here, where the reference tree exists:
+receive and transmit path (oracle/_ref/libref.so, compiled from the reference
+sources by oracle/Makefile).  Run where the reference tree exists:
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [fec] [ofdm] [tx]
 
 The fixtures let the CPU and GPU tests check parity on machines without the
 reference tree.  Inputs are seeded synthetic data (no dataset is involved).
@@ -82,12 +82,38 @@ def ofdm_fixture(ref: Reference) -> dict:
                 sync=np.array([[s[0], s[1], s[2], s[3], s[4]] for s in sync]), decoded=np.stack(dec))
 
 
-def main():
+def tx_fixture(ref: Reference) -> dict:
+    """Frames of the reference's own CPU transmitter (build_tx_frame_from_info,
+    uhd_ldpc_ofdm_link.cpp:4589-4630: encode, map, pilots, inverse FFT, CP, preamble, peak
+    normalisation) for the small PHY and the (128,64) code, whose 16 codewords fill the frame."""
+    t = ofdm.reference_tables(ofdm.OFDM_SMALL)
+    rp = ref.phy(t)
+    code = codes.short_code()
+    rc = ref.code(code.n, code.m, code.row_ptr, code.col_ind)
+    blocks = t.coded_bits // code.n
+    rng = np.random.default_rng(404)
+    info = rng.integers(0, 2, size=(4, blocks * code.k), dtype=np.uint8)
+    info[0] = 0  # the all-zero frame: pilots and preamble only carry structure
+    frames = np.stack([rp.build_tx_frame(rc, info[i]) for i in range(info.shape[0])])
+    used = np.zeros(t.active_sc, np.int32)
+    pil = np.zeros(len(t.pilot_symbols), np.int32)
+    dat = np.zeros(len(t.data_symbols), np.int32)
+    const = np.zeros(1 << t.bits_per_symbol, np.complex64)
+    ref.L.ref_phy_tables(rp.h, used, pil, dat, const.view(np.float32))
+    return dict(info=info, frames=frames, used_indices=used, pilot_symbols=pil, data_symbols=dat,
+                constellation=const)
+
+
+def main(which=("fec", "ofdm", "tx")):
     ref = Reference()
-    np.savez_compressed(os.path.join(OUT, "fec_short_code.npz"), **fec_fixture(ref))
-    np.savez_compressed(os.path.join(OUT, "ofdm_small.npz"), **ofdm_fixture(ref))
+    if "fec" in which:
+        np.savez_compressed(os.path.join(OUT, "fec_short_code.npz"), **fec_fixture(ref))
+    if "ofdm" in which:
+        np.savez_compressed(os.path.join(OUT, "ofdm_small.npz"), **ofdm_fixture(ref))
+    if "tx" in which:
+        np.savez_compressed(os.path.join(OUT, "tx_reference_small.npz"), **tx_fixture(ref))
     print("wrote fixtures to", OUT)
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]) or ("fec", "ofdm", "tx"))

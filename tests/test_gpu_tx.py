@@ -1,4 +1,5 @@
-"""The GB300 transmit chain against the restated GPU transmitter, and TX -> RX.
+"""The GB300 transmit chain against the reference's CPU transmitter, the restated
+GPU transmitter, and TX -> RX.
 
 The oracle (oracle/tx_oracle.py) restates gpu_ofdm_pipeline.cu:129-343 and
 922-1075.  The coded bits must be identical (a wrong bit moves a QAM point by
@@ -39,6 +40,27 @@ def _close(got, ref, what):
     assert got.shape == ref.shape
     err = np.max(np.abs(got - ref))
     assert err <= 2e-5 * np.max(np.abs(ref)), (what, err)
+
+
+def test_tx_frames_match_the_reference_cpu_transmitter(cuda):
+    """Pinned to the reference itself: frames of its CPU transmitter (build_tx_frame_from_info,
+    uhd_ldpc_ofdm_link.cpp:4589-4630, tests/golden/tx_reference_small.npz) equal the GPU frames up
+    to the frame's scale (the reference normalises each frame to peak amplitude, the GPU
+    transmitter scales by the amplitude as gpu_ofdm_pipeline.cu:316-342 does), within 2e-5 of the
+    peak (single-precision inverse FFT on the GPU, double precision in the reference)."""
+    from test_tx_oracle import reference_tx_fixture, scaled_like_reference
+    torch = cuda
+    d = reference_tx_fixture()
+    code = codes.short_code()
+    p, t, blocks = _pipe(ofdm.OFDM_SMALL, code)
+    p.upload_tx_tables(generator_kn=_gen(code))
+    F = d["info"].shape[0]
+    d_fr = torch.zeros((F, t.frame_len), dtype=torch.complex64, device="cuda")
+    p.tx_batch(torch.from_numpy(d["info"]).cuda(), F, d_fr, stream=torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    got = scaled_like_reference(d_fr.cpu().numpy(), t.cfg.amplitude)
+    err = np.max(np.abs(got - d["frames"].astype(np.complex128)))
+    assert err <= 2e-5 * t.cfg.amplitude, err
 
 
 def test_tx_frames_match_the_restated_transmitter(cuda):

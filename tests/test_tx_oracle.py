@@ -4,8 +4,13 @@ Pins: the generator encoder yields codewords of the code (H c = 0) equal to the
 systematic encoder; the accumulator encoder equals its sequential definition
 (gpu_ofdm_pipeline.cu:169-214); the QAM map equals the reference constellation
 (uhd_ldpc_ofdm_link.cpp:2362-2414 as restated in sicc_gb300.ofdm); the noise
-deviates are standard normal; a frame demodulated back by FFT returns its bits.
+deviates are standard normal; a frame demodulated back by FFT returns its bits;
+and frames equal, up to the frame's scale, those of the reference's own CPU
+transmitter (tests/golden/tx_reference_small.npz, made by build_tx_frame_from_info,
+uhd_ldpc_ofdm_link.cpp:4589-4630).
 """
+import os
+
 import numpy as np
 
 import tx_oracle
@@ -80,3 +85,36 @@ def test_frame_returns_its_bits_through_an_fft():
         bits.append(((idx[:, None] >> (cfg.bits_per_symbol - 1 - np.arange(cfg.bits_per_symbol))) & 1).reshape(-1))
     assert np.array_equal(np.concatenate(bits), coded[0])
     assert np.allclose(fr[:pre], t.preamble * cfg.amplitude, atol=1e-6)
+
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def reference_tx_fixture():
+    return dict(np.load(os.path.join(GOLDEN, "tx_reference_small.npz")))
+
+
+def scaled_like_reference(frames, amplitude):
+    """The reference CPU transmitter normalises each frame to peak `amplitude`; the GPU
+    transmitter (gpu_ofdm_pipeline.cu:316-342) scales the preamble by the amplitude and the
+    unnormalised inverse FFT by amplitude / nfft.  The two differ by one factor per frame."""
+    f = np.asarray(frames, np.complex128)
+    return f * (amplitude / np.max(np.abs(f), axis=-1, keepdims=True))
+
+
+def test_restated_transmitter_matches_the_reference_cpu_transmitter():
+    d = reference_tx_fixture()
+    t = ofdm.reference_tables(ofdm.OFDM_SMALL)
+    assert np.array_equal(d["used_indices"], t.used_indices)
+    assert np.array_equal(d["pilot_symbols"], t.pilot_symbols) and np.array_equal(d["data_symbols"], t.data_symbols)
+    assert np.array_equal(d["constellation"], t.constellation)
+    c = codes.short_code()
+    coded = tx_oracle.encode_generator(d["info"].reshape(-1, c.k), _generator(c)).reshape(d["info"].shape[0], -1)
+    cfg = t.cfg
+    got = tx_oracle.tx_frames(coded, nfft=cfg.nfft, cp=cfg.cp, num_symbols=cfg.num_symbols, active_sc=cfg.active_sc,
+                              bps=cfg.bits_per_symbol, used_bins=t.used_bins, pilot_symbols=t.pilot_symbols,
+                              data_symbols=t.data_symbols, pilot_grid=t.pilot_grid, preamble=t.preamble,
+                              amplitude=cfg.amplitude)
+    ref = d["frames"].astype(np.complex128)
+    err = np.max(np.abs(scaled_like_reference(got, cfg.amplitude) - ref))
+    assert err <= 2e-6 * cfg.amplitude, err
