@@ -1,0 +1,760 @@
+// Device-resident request loop (include/sicc_devloop.h).
+//
+// The loop is a CUDA graph: a conditional while-node whose body is recorded
+// once (stream capture into the node's body graph) and then repeated on the
+// device until its condition kernel clears the condition.  Body of one
+// iteration, in stream order:
+//   admit_kernel     one thread: reads the request ring's tail (host-written,
+//                    pinned, acquire load at system scope), takes requests in
+//                    order while they fit the iteration's codeword and LLR
+//                    budgets and the completion ring has room, records them in
+//                    the admission table, publishes the ring head; waits a
+//                    bounded ~100 us for a request when the ring is empty;
+//   layout_kernel    one CTA per admitted request (grid-strided): copies its
+//                    LLRs from pinned host memory into the batch and writes the
+//                    per-codeword tables (code, protection, offsets);
+//   engine decode    the mixed-code engine's prepare, BP and OSD launches, sized
+//                    for the largest batch, reading the batch size on the device;
+//   complete_kernel  one CTA per admitted request: copies its information bits
+//                    to the request's pinned host buffer, counts its BP
+//                    failures and OSD codewords, writes its completion record;
+//   publish_kernel   one thread: makes the iteration's host writes visible,
+//                    advances the completion tail and sets the loop condition
+//                    (host stop flag, idle timeout, iteration cap).
+// The host side only fills the request ring and drains the completion ring.
+#include "../../include/sicc_devloop.h"
+#include "engine_internal.h"
+#include "sicc_common.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+namespace sicc {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct alignas(16) ReqEntry {  // host -> device, one per request
+    unsigned long long id, tag;
+    const float* in;            // [count][n] LLRs, device-addressable pinned host memory
+    unsigned char* out;         // [count][k] information bits, the same kind of memory
+    int code_id, count, protection, n, k, pad;
+};
+
+struct alignas(16) CmpEntry {  // device -> host, one per request
+    unsigned long long id, tag;
+    unsigned long long t_start_ns, t_done_ns;  // device clock: its iteration's decode start, publication
+    int codewords, failed, osd, status;
+};
+
+struct alignas(128) HostSide {  // written by the host, read by the device (pinned)
+    unsigned long long req_tail;   // requests published
+    unsigned long long cmp_head;   // completions consumed
+    int stop;
+};
+
+struct alignas(128) DevSide {  // written by the device, read by the host (pinned)
+    unsigned long long req_head;   // requests admitted
+    unsigned long long cmp_tail;   // completions published
+    unsigned long long iterations, codewords;
+    int ended;                     // 1: stop flag, 2: idle timeout, 3: iteration cap
+};
+
+struct LoopState {  // device memory
+    unsigned long long head, cmp_tail, iterations, codewords;
+    unsigned long long last_active_ns, t_start_ns;
+    int nreq, count;
+};
+
+struct Admitted {
+    ReqEntry e;
+    long long llr_off, info_off;
+    int first_cw;
+};
+
+constexpr int kAdmitPolls = 50;            // ~2 us naps: an empty ring is watched ~100 us per iteration
+constexpr unsigned long long kIterationCap = 1ull << 31;
+
+__device__ __forceinline__ unsigned long long globaltimer_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned long long load_acquire_sys(const unsigned long long* p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ int load_acquire_sys(const int* p)
+{
+    int v;
+    asm volatile("ld.acquire.sys.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void store_release_sys(unsigned long long* p, unsigned long long v)
+{
+    asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__global__ void admit_kernel(const ReqEntry* __restrict__ ring, unsigned mask, const HostSide* hs, DevSide* ds,
+                             LoopState* st, Admitted* adm, int max_req, int max_cw, long long max_floats,
+                             unsigned cmp_capacity)
+{
+    if (threadIdx.x != 0) return;
+    unsigned long long head = st->head;
+    unsigned long long tail = load_acquire_sys(&hs->req_tail);
+    for (int i = 0; i < kAdmitPolls && tail == head; ++i) {
+        __nanosleep(2000);
+        tail = load_acquire_sys(&hs->req_tail);
+    }
+    const unsigned long long consumed = load_acquire_sys(&hs->cmp_head);
+    const unsigned long long room = cmp_capacity - (st->cmp_tail - consumed);
+    int nreq = 0, cw = 0;
+    long long floats = 0, info = 0;
+    while (head < tail && nreq < max_req && static_cast<unsigned long long>(nreq) < room) {
+        const ReqEntry e = ring[head & mask];
+        const long long f = static_cast<long long>(e.count) * e.n;
+        if (cw + e.count > max_cw || floats + f > max_floats) break;  // in order: the next iteration takes it
+        Admitted& a = adm[nreq];
+        a.e = e;
+        a.first_cw = cw;
+        a.llr_off = floats;
+        a.info_off = info;
+        cw += e.count;
+        floats += f;
+        info += static_cast<long long>(e.count) * e.k;
+        ++nreq;
+        ++head;
+    }
+    st->head = head;
+    st->nreq = nreq;
+    st->count = cw;
+    const unsigned long long now = globaltimer_ns();
+    if (nreq > 0 || st->last_active_ns == 0) st->last_active_ns = now;
+    st->t_start_ns = now;
+    __threadfence_system();
+    store_release_sys(&ds->req_head, head);
+}
+
+__global__ void layout_kernel(const LoopState* st, const Admitted* __restrict__ adm, float* __restrict__ llr,
+                              uint8_t* __restrict__ code_of, uint8_t* __restrict__ protect,
+                              long long* __restrict__ llr_off, long long* __restrict__ info_off)
+{
+    const int nreq = st->nreq;
+    for (int r = blockIdx.x; r < nreq; r += gridDim.x) {
+        const Admitted a = adm[r];
+        const long long total = static_cast<long long>(a.e.count) * a.e.n;
+        const float* src = a.e.in;
+        float* dst = llr + a.llr_off;
+        if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0 && (total & 3) == 0) {
+            const float4* s4 = reinterpret_cast<const float4*>(src);
+            float4* d4 = reinterpret_cast<float4*>(dst);
+            for (long long i = threadIdx.x; i < (total >> 2); i += blockDim.x) d4[i] = s4[i];
+        } else {
+            for (long long i = threadIdx.x; i < total; i += blockDim.x) dst[i] = src[i];
+        }
+        for (int c = threadIdx.x; c < a.e.count; c += blockDim.x) {
+            const int w = a.first_cw + c;
+            code_of[w] = static_cast<uint8_t>(a.e.code_id);
+            protect[w] = static_cast<uint8_t>(a.e.protection);
+            llr_off[w] = a.llr_off + static_cast<long long>(c) * a.e.n;
+            info_off[w] = a.info_off + static_cast<long long>(c) * a.e.k;
+        }
+    }
+}
+
+__global__ void complete_kernel(const LoopState* st, const Admitted* __restrict__ adm,
+                                const uint8_t* __restrict__ info, const uint8_t* __restrict__ success,
+                                const uint8_t* __restrict__ used_osd, CmpEntry* ring, unsigned mask)
+{
+    __shared__ int s_failed, s_osd;
+    const int nreq = st->nreq;
+    for (int r = blockIdx.x; r < nreq; r += gridDim.x) {
+        const Admitted a = adm[r];
+        if (threadIdx.x == 0) {
+            s_failed = 0;
+            s_osd = 0;
+        }
+        __syncthreads();
+        const long long bytes = static_cast<long long>(a.e.count) * a.e.k;
+        const uint8_t* src = info + a.info_off;
+        for (long long i = threadIdx.x; i < bytes; i += blockDim.x) a.e.out[i] = src[i];
+        int failed = 0, osd = 0;
+        for (int c = threadIdx.x; c < a.e.count; c += blockDim.x) {
+            const int w = a.first_cw + c;
+            const int u = used_osd[w], ok = success[w];
+            osd += u;
+            failed += (!u && !ok) ? 1 : 0;
+        }
+        if (failed) atomicAdd(&s_failed, failed);
+        if (osd) atomicAdd(&s_osd, osd);
+        __threadfence_system();  // the information bits reach host memory before the record
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            CmpEntry c{};
+            c.id = a.e.id;
+            c.tag = a.e.tag;
+            c.t_start_ns = st->t_start_ns;
+            c.t_done_ns = globaltimer_ns();
+            c.codewords = a.e.count;
+            c.failed = s_failed;
+            c.osd = s_osd;
+            c.status = 0;
+            ring[(st->cmp_tail + r) & mask] = c;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void publish_kernel(LoopState* st, const HostSide* hs, DevSide* ds, cudaGraphConditionalHandle cond,
+                               unsigned long long idle_ns)
+{
+    __threadfence_system();  // every record of this iteration is out before the tail moves
+    st->cmp_tail += static_cast<unsigned long long>(st->nreq);
+    st->iterations += 1;
+    st->codewords += static_cast<unsigned long long>(st->count);
+    ds->iterations = st->iterations;
+    ds->codewords = st->codewords;
+    store_release_sys(&ds->cmp_tail, st->cmp_tail);
+    int reason = 0;
+    if (load_acquire_sys(&hs->stop)) reason = 1;
+    else if (st->nreq == 0 && globaltimer_ns() - st->last_active_ns > idle_ns) reason = 2;
+    else if (st->iterations >= kIterationCap) reason = 3;
+    if (reason) {
+        ds->ended = reason;
+        __threadfence_system();
+    }
+    cudaGraphSetConditional(cond, reason ? 0u : 1u);
+}
+
+__global__ void clock_kernel(unsigned long long* out) { *out = globaltimer_ns(); }
+
+template <class T>
+struct Pinned {
+    T* h = nullptr;  // host address
+    T* d = nullptr;  // device address of the same memory
+    void alloc(size_t count)
+    {
+        check_cuda(cudaHostAlloc(reinterpret_cast<void**>(&h), count * sizeof(T), cudaHostAllocMapped),
+                   "cudaHostAlloc(loop)");
+        std::memset(static_cast<void*>(h), 0, count * sizeof(T));
+        check_cuda(cudaHostGetDevicePointer(reinterpret_cast<void**>(&d), h, 0), "cudaHostGetDevicePointer");
+    }
+    ~Pinned()
+    {
+        if (h) cudaFreeHost(h);
+    }
+};
+
+template <class T>
+struct Dev {
+    T* p = nullptr;
+    void alloc(size_t count)
+    {
+        check_cuda(cudaMalloc(reinterpret_cast<void**>(&p), std::max<size_t>(count, 1) * sizeof(T)),
+                   "cudaMalloc(loop)");
+        check_cuda(cudaMemset(p, 0, std::max<size_t>(count, 1) * sizeof(T)), "cudaMemset(loop)");
+    }
+    ~Dev()
+    {
+        if (p) cudaFree(p);
+    }
+};
+
+struct CodeDims {
+    int n, k;
+};
+
+struct Pending {
+    Clock::time_point t_submit;
+};
+
+struct Loop {
+    sicc_devloop_config_t cfg{};
+    int device = 0;
+    unsigned long long engine = 0;
+    std::vector<CodeDims> codes;
+    int max_req = 0;
+    unsigned mask = 0;
+    // rings and control blocks (pinned, mapped)
+    Pinned<ReqEntry> ring;
+    Pinned<CmpEntry> cring;
+    Pinned<HostSide> hs;
+    Pinned<DevSide> ds;
+    Pinned<unsigned long long> clock;
+    // device state
+    Dev<LoopState> st;
+    Dev<Admitted> adm;
+    Dev<float> llr;
+    Dev<uint8_t> info, code_of, protect, success, used, iters;
+    Dev<long long> llr_off, info_off;
+    int info_cap = 0;
+    // the graph
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool recorded = false, launched = false;
+    // host bookkeeping
+    unsigned long long next_id = 1, req_tail = 0, cmp_head = 0;
+    std::map<unsigned long long, Pending> pending;
+    long long clock_offset_ns = 0;  // device globaltimer - host steady clock (ns)
+    Clock::time_point clock_base;
+    sicc_devloop_stats_t stats{};
+    std::mutex mu;      // submit side
+    std::mutex poll_mu; // poll side
+
+    ~Loop()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (stream) cudaStreamDestroy(stream);
+        if (engine) sicc_engine_destroy(engine);
+    }
+
+    bool graph_done() const
+    {
+        if (!launched) return true;
+        const cudaError_t q = cudaStreamQuery(stream);
+        if (q == cudaErrorNotReady) return false;
+        check_cuda(q, "loop stream");
+        return true;
+    }
+
+    void record()
+    {
+        int n_max = 0, k_max = 0;
+        if (engine_bounds(engine, &n_max, &k_max) != CUDA_OSD_STATUS_OK) throw std::runtime_error(last_error());
+        if (engine_prepare_capture(engine, cfg.max_batch_codewords) != CUDA_OSD_STATUS_OK)
+            throw std::runtime_error(last_error());
+        info_cap = cfg.max_batch_codewords * k_max;
+        info.alloc(static_cast<size_t>(info_cap));
+        check_cuda(cudaGraphCreate(&graph, 0), "cudaGraphCreate");
+        cudaGraphConditionalHandle cond;
+        check_cuda(cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault),
+                   "cudaGraphConditionalHandleCreate");
+        cudaGraphNodeParams p{};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = cond;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t node;
+        check_cuda(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &p), "cudaGraphAddNode(while)");
+        cudaGraph_t body = p.conditional.phGraph_out[0];
+        check_cuda(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+                   "cudaStreamBeginCaptureToGraph");
+        const int sms = device_sm_count();
+        admit_kernel<<<1, 32, 0, stream>>>(ring.d, mask, hs.d, ds.d, st.p, adm.p, max_req, cfg.max_batch_codewords,
+                                            cfg.max_batch_llr_floats, mask + 1);
+        layout_kernel<<<2 * sms, 256, 0, stream>>>(st.p, adm.p, llr.p, code_of.p, protect.p, llr_off.p, info_off.p);
+        const int rc = engine_decode(engine, cfg.max_batch_codewords, code_of.p, protect.p, llr.p, llr_off.p, info.p,
+                                     info_off.p, success.p, used.p, iters.p, stream, nullptr, &st.p->count);
+        if (rc != CUDA_OSD_STATUS_OK) {
+            cudaGraph_t dummy;
+            cudaStreamEndCapture(stream, &dummy);
+            throw std::runtime_error(std::string("recording the loop's decode: ") + last_error());
+        }
+        complete_kernel<<<2 * sms, 256, 0, stream>>>(st.p, adm.p, info.p, success.p, used.p, cring.d, mask);
+        publish_kernel<<<1, 1, 0, stream>>>(st.p, hs.d, ds.d, cond,
+                                            static_cast<unsigned long long>(cfg.idle_timeout_ms) * 1000000ull);
+        cudaGraph_t out = nullptr;
+        check_cuda(cudaStreamEndCapture(stream, &out), "cudaStreamEndCapture(loop body)");
+        check_cuda(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate(loop)");
+        recorded = true;
+    }
+
+    void calibrate()
+    {
+        const auto t0 = Clock::now();
+        clock_kernel<<<1, 1, 0, stream>>>(clock.d);
+        check_cuda(cudaStreamSynchronize(stream), "clock");
+        const auto t1 = Clock::now();
+        const auto mid = t0 + (t1 - t0) / 2;
+        clock_base = mid;
+        clock_offset_ns = static_cast<long long>(*clock.h);
+    }
+
+    // device ns -> host time point
+    Clock::time_point host_time(unsigned long long dev_ns) const
+    {
+        return clock_base + std::chrono::nanoseconds(static_cast<long long>(dev_ns) - clock_offset_ns);
+    }
+
+    // Launches the loop if it is not running (the caller holds mu).
+    void ensure_running()
+    {
+        if (launched && !graph_done()) return;
+        if (!recorded) {
+            record();
+            calibrate();
+        }
+        DevSide* d = ds.h;
+        reinterpret_cast<std::atomic<int>*>(&d->ended)->store(0, std::memory_order_relaxed);
+        reinterpret_cast<std::atomic<int>*>(&hs.h->stop)->store(0, std::memory_order_release);
+        check_cuda(cudaMemsetAsync(&st.p->last_active_ns, 0, sizeof(unsigned long long), stream), "loop reset");
+        check_cuda(cudaGraphLaunch(exec, stream), "cudaGraphLaunch(loop)");
+        launched = true;
+        ++stats.launches;
+    }
+};
+
+std::mutex g_mu;
+std::map<unsigned long long, std::shared_ptr<Loop>> g_loops;
+unsigned long long g_next = 0xD100;
+
+std::shared_ptr<Loop> get(unsigned long long h)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_loops.find(h);
+    if (it == g_loops.end()) throw InvalidArgument("invalid device-loop handle");
+    return it->second;
+}
+
+template <class F>
+int guarded(F&& f)
+{
+    try {
+        return f();
+    } catch (const InvalidArgument& e) {
+        set_last_error(e.what());
+        return CUDA_OSD_STATUS_INVALID_ARGUMENT;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return CUDA_OSD_STATUS_INTERNAL_ERROR;
+    }
+}
+
+template <class T>
+T load_acquire(const T* p)
+{
+    return reinterpret_cast<const std::atomic<T>*>(p)->load(std::memory_order_acquire);
+}
+
+template <class T>
+void store_release(T* p, T v)
+{
+    reinterpret_cast<std::atomic<T>*>(p)->store(v, std::memory_order_release);
+}
+
+// The device address of pinned host memory the GPU can use, or nullptr.
+const void* device_address(const void* p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost && a.type != cudaMemoryTypeManaged) return nullptr;
+    return a.devicePointer;
+}
+
+double us_between(Clock::time_point a, Clock::time_point b)
+{
+    return std::chrono::duration<double, std::micro>(b - a).count();
+}
+
+}  // namespace
+}  // namespace sicc
+
+using namespace sicc;
+
+extern "C" {
+
+int sicc_devloop_create(const sicc_devloop_config_t* config, unsigned long long* out_handle)
+{
+    return guarded([&]() -> int {
+        if (!config || !out_handle) throw InvalidArgument("null argument");
+        *out_handle = 0;
+        const sicc_devloop_config_t& c = *config;
+        if (c.max_batch_codewords <= 0 || c.max_batch_llr_floats <= 0)
+            throw InvalidArgument("the iteration budgets must be positive");
+        if (c.max_codes <= 0 || c.max_codes > 64) throw InvalidArgument("max_codes must be 1..64");
+        if (c.ring_requests < 2 || (c.ring_requests & (c.ring_requests - 1)))
+            throw InvalidArgument("ring_requests must be a power of two >= 2");
+        if (c.idle_timeout_ms < 1) throw InvalidArgument("idle_timeout_ms must be >= 1");
+        auto L = std::make_shared<Loop>();
+        L->cfg = c;
+        check_cuda(cudaGetDevice(&L->device), "cudaGetDevice");
+        sicc_engine_config_t ec{};
+        ec.max_codewords = c.max_batch_codewords;
+        ec.max_llr_floats = c.max_batch_llr_floats;
+        ec.max_codes = c.max_codes;
+        if (sicc_engine_create(&ec, &L->engine) != CUDA_OSD_STATUS_OK) throw std::runtime_error(last_error());
+        L->mask = static_cast<unsigned>(c.ring_requests - 1);
+        L->max_req = std::min(c.ring_requests, c.max_batch_codewords);
+        L->ring.alloc(c.ring_requests);
+        L->cring.alloc(c.ring_requests);
+        L->hs.alloc(1);
+        L->ds.alloc(1);
+        L->clock.alloc(1);
+        L->st.alloc(1);
+        L->adm.alloc(static_cast<size_t>(L->max_req));
+        L->llr.alloc(static_cast<size_t>(c.max_batch_llr_floats));
+        for (auto* b : {&L->code_of, &L->protect, &L->success, &L->used, &L->iters})
+            b->alloc(static_cast<size_t>(c.max_batch_codewords));
+        L->llr_off.alloc(static_cast<size_t>(c.max_batch_codewords));
+        L->info_off.alloc(static_cast<size_t>(c.max_batch_codewords));
+        check_cuda(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking), "cudaStreamCreate(loop)");
+        std::lock_guard<std::mutex> lock(g_mu);
+        const unsigned long long h = ++g_next;
+        g_loops[h] = L;
+        *out_handle = h;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_devloop_stop(unsigned long long handle, int wait_ms)
+{
+    return guarded([&]() -> int {
+        auto L = get(handle);
+        std::lock_guard<std::mutex> lock(L->mu);
+        check_cuda(cudaSetDevice(L->device), "cudaSetDevice");
+        if (!L->launched) return CUDA_OSD_STATUS_OK;
+        store_release(&L->hs.h->stop, 1);
+        const auto deadline = Clock::now() + std::chrono::milliseconds(std::max(wait_ms, 1));
+        while (!L->graph_done()) {
+            if (Clock::now() > deadline) throw std::runtime_error("the device loop did not stop in time");
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+        L->launched = false;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_devloop_destroy(unsigned long long handle)
+{
+    return guarded([&]() -> int {
+        std::shared_ptr<Loop> L;
+        {
+            std::lock_guard<std::mutex> lock(g_mu);
+            auto it = g_loops.find(handle);
+            if (it == g_loops.end()) throw InvalidArgument("invalid device-loop handle");
+            L = it->second;
+        }
+        if (sicc_devloop_stop(handle, 10000) != CUDA_OSD_STATUS_OK) throw std::runtime_error(last_error());
+        std::lock_guard<std::mutex> lock(g_mu);
+        g_loops.erase(handle);
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_devloop_add_code(unsigned long long handle, const sicc_engine_code_t* code, int* out_code_id)
+{
+    return guarded([&]() -> int {
+        auto L = get(handle);
+        std::lock_guard<std::mutex> lock(L->mu);
+        if (L->recorded) throw InvalidArgument("codes must be added before the loop starts");
+        if (!code || !out_code_id) throw InvalidArgument("null argument");
+        check_cuda(cudaSetDevice(L->device), "cudaSetDevice");
+        if (sicc_engine_add_code(L->engine, code, out_code_id) != CUDA_OSD_STATUS_OK)
+            throw InvalidArgument(last_error());
+        L->codes.push_back(CodeDims{code->n, code->n - code->m});
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_devloop_start(unsigned long long handle)
+{
+    return guarded([&]() -> int {
+        auto L = get(handle);
+        std::lock_guard<std::mutex> lock(L->mu);
+        if (L->codes.empty()) throw InvalidArgument("no code registered");
+        check_cuda(cudaSetDevice(L->device), "cudaSetDevice");
+        L->ensure_running();
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_devloop_submit(unsigned long long handle, const sicc_request_t* request, unsigned long long* out_request_id)
+{
+    return guarded([&]() -> int {
+        auto L = get(handle);
+        if (!request) throw InvalidArgument("null request");
+        const sicc_request_t& r = *request;
+        if (r.kind != 0) throw InvalidArgument("the device loop serves codeword-LLR requests (kind 0)");
+        std::lock_guard<std::mutex> lock(L->mu);
+        if (r.code_id < 0 || r.code_id >= static_cast<int>(L->codes.size())) throw InvalidArgument("invalid code id");
+        if (r.protection != 0 && r.protection != 1) throw InvalidArgument("protection must be 0 or 1");
+        const CodeDims cd = L->codes[r.code_id];
+        if (r.count <= 0 || r.count > L->cfg.max_batch_codewords ||
+            static_cast<long long>(r.count) * cd.n > L->cfg.max_batch_llr_floats)
+            throw InvalidArgument("request larger than one iteration's budget");
+        check_cuda(cudaSetDevice(L->device), "cudaSetDevice");
+        const void* in = device_address(r.host_input);
+        void* out = const_cast<void*>(device_address(r.host_info));
+        if (!in || !out)
+            throw InvalidArgument("host_input and host_info must be page-locked host memory the GPU can address");
+        if (L->req_tail - load_acquire(&L->ds.h->req_head) >= static_cast<unsigned long long>(L->mask) + 1) {
+            ++L->stats.busy_rejections;
+            set_last_error("request ring full");
+            return static_cast<int>(SICC_SERVER_BUSY);  // an int like every other return of this lambda
+        }
+        const unsigned long long id = L->next_id++;
+        ReqEntry e{};
+        e.id = id;
+        e.tag = r.tag;
+        e.in = static_cast<const float*>(in);
+        e.out = static_cast<unsigned char*>(out);
+        e.code_id = r.code_id;
+        e.count = r.count;
+        e.protection = r.protection;
+        e.n = cd.n;
+        e.k = cd.k;
+        {
+            std::lock_guard<std::mutex> plock(L->poll_mu);
+            L->pending[id] = Pending{Clock::now()};
+        }
+        L->ring.h[L->req_tail & L->mask] = e;
+        ++L->req_tail;
+        store_release(&L->hs.h->req_tail, L->req_tail);  // the entry is complete before the tail moves
+        ++L->stats.submitted;
+        L->ensure_running();
+        if (out_request_id) *out_request_id = id;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_devloop_poll(unsigned long long handle, int max, sicc_completion_t* out, int* out_count, int wait_us)
+{
+    return guarded([&]() -> int {
+        auto L = get(handle);
+        if (!out || !out_count || max <= 0) throw InvalidArgument("bad arguments");
+        *out_count = 0;
+        std::lock_guard<std::mutex> plock(L->poll_mu);
+        const auto deadline = Clock::now() + std::chrono::microseconds(std::max(wait_us, 0));
+        for (;;) {
+            const unsigned long long tail = load_acquire(&L->ds.h->cmp_tail);
+            while (L->cmp_head < tail && *out_count < max) {
+                const CmpEntry c = L->cring.h[L->cmp_head & L->mask];
+                ++L->cmp_head;
+                sicc_completion_t& o = out[(*out_count)++];
+                o = sicc_completion_t{};
+                o.request_id = c.id;
+                o.tag = c.tag;
+                o.status = c.status;
+                o.codewords = c.codewords;
+                o.failed_codewords = c.failed;
+                o.osd_codewords = c.osd;
+                const auto now = Clock::now();
+                auto it = L->pending.find(c.id);
+                if (it != L->pending.end()) {
+                    o.latency_us = us_between(it->second.t_submit, now);
+                    o.queue_us = std::max(0.0, us_between(it->second.t_submit, L->host_time(c.t_start_ns)));
+                    o.launch_us = o.queue_us;
+                    L->pending.erase(it);
+                }
+                o.batch_gpu_us = static_cast<double>(c.t_done_ns - c.t_start_ns) * 1e-3;
+                ++L->stats.completed;
+            }
+            store_release(&L->hs.h->cmp_head, L->cmp_head);
+            if (*out_count > 0 || Clock::now() >= deadline) break;
+            std::this_thread::sleep_for(std::chrono::microseconds(5));
+        }
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_devloop_get_stats(unsigned long long handle, sicc_devloop_stats_t* out)
+{
+    return guarded([&]() -> int {
+        auto L = get(handle);
+        if (!out) throw InvalidArgument("null argument");
+        std::lock_guard<std::mutex> lock(L->mu);
+        *out = L->stats;
+        out->iterations = load_acquire(&L->ds.h->iterations);
+        out->codewords = load_acquire(&L->ds.h->codewords);
+        out->running = (L->launched && !L->graph_done()) ? 1 : 0;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int sicc_devloop_replay(unsigned long long handle, const sicc_request_t* requests, const double* arrival_us, int count,
+                        sicc_completion_t* out_completions, double* out_wall_us)
+{
+    return guarded([&]() -> int {
+        auto L = get(handle);
+        if (!requests || !arrival_us || !out_completions || count <= 0) throw InvalidArgument("bad arguments");
+        // completions can come back before the submitting thread has recorded the id; they wait in
+        // `early` until it has (both threads hold idx_mu around index, early, out_completions, t_last)
+        std::map<unsigned long long, int> index;
+        std::map<unsigned long long, sicc_completion_t> early;
+        std::vector<double> late(count, 0.0);
+        std::mutex idx_mu;
+        std::atomic<int> done{0};
+        std::atomic<bool> failed{false};
+        std::string error;
+        const auto t0 = Clock::now();
+        Clock::time_point t_last = t0;
+        auto finish = [&](int pos, const sicc_completion_t& c) {
+            out_completions[pos] = c;
+            out_completions[pos].latency_us += late[pos];
+            out_completions[pos].queue_us += late[pos];
+            out_completions[pos].launch_us += late[pos];
+            t_last = Clock::now();
+            done.fetch_add(1);
+        };
+        std::thread collector([&] {
+            std::vector<sicc_completion_t> buf(256);
+            const auto give_up = [&] { return Clock::now() - t_last > std::chrono::seconds(30); };
+            while (done.load() < count && !failed.load()) {
+                int got = 0;
+                if (sicc_devloop_poll(handle, 256, buf.data(), &got, 1000) != CUDA_OSD_STATUS_OK) {
+                    error = last_error();
+                    failed.store(true);
+                    break;
+                }
+                std::lock_guard<std::mutex> lock(idx_mu);
+                for (int i = 0; i < got; ++i) {
+                    auto it = index.find(buf[i].request_id);
+                    if (it != index.end()) finish(it->second, buf[i]);
+                    else early.emplace(buf[i].request_id, buf[i]);
+                }
+                if (got == 0 && give_up()) {
+                    error = "no completion for 30 s";
+                    failed.store(true);
+                }
+            }
+        });
+        for (int i = 0; i < count && !failed.load(); ++i) {
+            const auto due = t0 + std::chrono::nanoseconds(static_cast<long long>(arrival_us[i] * 1000.0));
+            while (Clock::now() < due) {
+                const auto left = due - Clock::now();
+                if (left > std::chrono::microseconds(200)) std::this_thread::sleep_for(left - std::chrono::microseconds(100));
+            }
+            unsigned long long id = 0;
+            int st;
+            while ((st = sicc_devloop_submit(handle, &requests[i], &id)) == SICC_SERVER_BUSY && !failed.load())
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
+            if (st != CUDA_OSD_STATUS_OK) {
+                error = last_error();
+                failed.store(true);
+                break;
+            }
+            late[i] = us_between(due, Clock::now());
+            std::lock_guard<std::mutex> lock(idx_mu);
+            index[id] = i;
+            auto e = early.find(id);
+            if (e != early.end()) {
+                finish(i, e->second);
+                early.erase(e);
+            }
+        }
+        collector.join();
+        if (failed.load()) throw std::runtime_error("replay failed: " + error);
+        if (out_wall_us) *out_wall_us = us_between(t0, t_last);
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+}  // extern "C"

@@ -77,10 +77,14 @@ struct MixedIO {
 
 // prepare: counts per code, queue-ordered starts, units, scatter into `order`.
 __global__ void __launch_bounds__(1024)
-prepare_kernel(const uint8_t* __restrict__ code_of, int count, const int* __restrict__ q_code, int K,
-               const int* __restrict__ per_warp, const int* __restrict__ q_warps, int* __restrict__ order,
-               int* __restrict__ q_start, int* __restrict__ q_units, int* __restrict__ counters)
+prepare_kernel(const uint8_t* __restrict__ code_of, int count_max, const int* __restrict__ count_ptr,
+               const int* __restrict__ q_code, int K, const int* __restrict__ per_warp,
+               const int* __restrict__ q_warps, int* __restrict__ order, int* __restrict__ q_start,
+               int* __restrict__ q_units, int* __restrict__ counters)
 {
+    // the batch's codewords: a launch argument, or (a launch recorded once and replayed over
+    // batches of different sizes) a device count, at most count_max
+    const int count = count_ptr ? min(max(*count_ptr, 0), count_max) : count_max;
     __shared__ int cnt[kMaxCodes], fill[kMaxCodes], pos_of_code[kMaxCodes];
     for (int i = threadIdx.x; i < kMaxCodes; i += blockDim.x) {
         cnt[i] = 0;
@@ -815,11 +819,62 @@ int sicc_engine_set_launch_shape(unsigned long long handle, int warps_per_cta, i
 
 namespace sicc {
 
+int engine_bounds(unsigned long long handle, int* out_n_max, int* out_k_max)
+{
+    return guarded([&] {
+        auto e = get(handle);
+        std::lock_guard<std::mutex> lock(e->mu);
+        if (out_n_max) *out_n_max = e->n_max;
+        if (out_k_max) *out_k_max = e->k_max;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int engine_prepare_capture(unsigned long long handle, int max_codewords)
+{
+    return guarded([&] {
+        auto e = get(handle);
+        std::lock_guard<std::mutex> lock(e->mu);
+        if (e->codes.empty()) throw InvalidArgument("no code registered");
+        if (max_codewords <= 0 || max_codewords > e->cfg.max_codewords)
+            throw InvalidArgument("codewords must be in 1..max_codewords");
+        check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+        e->commit();
+        // the mixed kernel's best-posterior scratch for the grid it will use (no allocation later)
+        const int wf = e->warp_floats();
+        int warps = e->warps_per_cta == 4 ? 4 : 8;
+        if (static_cast<size_t>(warps) * wf * sizeof(float) > 200 * 1024) warps = 4;
+        const size_t smem = static_cast<size_t>(warps) * wf * sizeof(float);
+        check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(bp_mixed_kernel<16>), smem),
+                   "cudaFuncSetAttribute(bp_mixed)");
+        int ctas = e->ctas;
+        if (ctas <= 0) {
+            int per_sm = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bp_mixed_kernel<16>, warps * 32, smem) !=
+                    cudaSuccess ||
+                per_sm <= 0)
+                per_sm = 1;
+            ctas = per_sm * device_sm_count();
+        }
+        int slots = 1;
+        for (const auto& c : e->codes)
+            if (c.desc.warps == 1) slots = std::max(slots, 32 / c.desc.group);
+        const size_t need = static_cast<size_t>(ctas) * warps * slots * static_cast<size_t>(e->n_max);
+        if (need > e->best_floats) {
+            if (e->d_best) cudaFree(e->d_best);
+            e->d_best = nullptr;
+            check_cuda(cudaMalloc(&e->d_best, need * sizeof(float)), "cudaMalloc(best)");
+            e->best_floats = need;
+        }
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
 int engine_decode(unsigned long long handle, int codewords, const unsigned char* device_code_ids,
                   const unsigned char* device_protection, const float* device_llr, const long long* device_llr_offsets,
                   unsigned char* device_info, const long long* device_info_offsets, unsigned char* device_success,
                   unsigned char* device_used_osd, unsigned char* device_iterations, cudaStream_t stream,
-                  cudaEvent_t bp_done)
+                  cudaEvent_t bp_done, const int* device_count)
 {
     void* cuda_stream = stream;
     return guarded([&] {
@@ -834,8 +889,8 @@ int engine_decode(unsigned long long handle, int codewords, const unsigned char*
         cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
         const int K = static_cast<int>(e->codes.size());
         check_cuda(cudaEventRecord(e->ev[0], st), "cudaEventRecord");
-        prepare_kernel<<<1, 1024, 0, st>>>(device_code_ids, codewords, e->d_q_code, K, e->d_per_warp, e->d_q_warps,
-                                           e->d_order, e->d_q_start, e->d_q_units, e->d_counters);
+        prepare_kernel<<<1, 1024, 0, st>>>(device_code_ids, codewords, device_count, e->d_q_code, K, e->d_per_warp,
+                                           e->d_q_warps, e->d_order, e->d_q_start, e->d_q_units, e->d_counters);
         check_cuda(cudaGetLastError(), "prepare_kernel launch");
         check_cuda(cudaEventRecord(e->ev[1], st), "cudaEventRecord");
         MixedIO io{};

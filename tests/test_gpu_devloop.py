@@ -1,0 +1,131 @@
+"""The device-resident request loop against decoding each request alone.
+
+The loop (include/sicc_devloop.h) admits, lays out, decodes and completes
+requests inside one CUDA graph repeated on the GPU.  Every request of a mixed
+stream (several codes, BP-only and BP+OSD protection, requests arriving while
+earlier ones decode) must come back with the bits the oracle's BP -> OSD chain
+gives for it alone; the loop must end by itself when idle and start again on
+the next request, stop when asked, and reject buffers the GPU cannot address.
+"""
+import time
+
+import numpy as np
+import pytest
+
+from sicc_gb300 import channel, codes, engine
+
+pytestmark = pytest.mark.gpu
+
+
+def _codes():
+    cs = [c for c in codes.mixed_codes() if engine.osd_supported(c)][:3] + [codes.short_code()]
+    cs.append(next(c for c in codes.mixed_codes() if c.n == 1024))
+    return cs
+
+
+def _loop(cs, **kw):
+    from sicc_gb300.devloop import DevLoop
+    lp = DevLoop(**kw)
+    for c in cs:
+        lp.add_code(c, engine.iteration_cap(c.n), osd_order=2 if engine.osd_supported(c) else -1)
+    return lp
+
+
+def _expected(oracle, c, llr, protection):
+    oc = oracle.code(c.n, c.m, c.row_ptr, c.col_ind)
+    table = oc.systematic_parity() if engine.osd_supported(c) else None
+    out = []
+    for x in llr:
+        r = oc.layered(x, engine.iteration_cap(c.n), 0.75)
+        if r[0] or not protection or table is None:
+            out.append(r[1][: c.k])
+        else:
+            out.append(oracle.osd(table, c.n, c.k, r[3], 2, 64, 4096)[0][: c.k])
+    return np.array(out, np.uint8)
+
+
+def _pinned_llrs(c, cnt, ebn0, seed):
+    from sicc_gb300.devloop import pinned
+    _, _, llr = channel.awgn_llrs(c, cnt, ebn0, seed=seed)
+    buf = pinned(llr.shape, np.float32)
+    buf[:] = llr
+    return buf
+
+
+def test_device_loop_matches_requests_decoded_alone(cuda, oracle):
+    cs = _codes()
+    lp = _loop(cs, max_batch_codewords=2048, max_batch_llr_floats=2048 * 1024, ring_requests=64)
+    lp.start()
+    rng = np.random.default_rng(15)
+    reqs = []
+    for r in range(48):
+        ci = int(rng.integers(0, len(cs)))
+        cnt = int(rng.integers(1, 60))
+        llr = _pinned_llrs(cs[ci], cnt, rng.uniform(1.0, 3.5, cnt), 1900 + r)
+        prot = int(rng.integers(0, 2))
+        req, x, out = lp.request(ci, llr, protection=prot, tag=r)
+        rid = lp.submit_request(req, keep=(x, out))
+        while rid is None:
+            time.sleep(0.0002)
+            rid = lp.submit_request(req, keep=(x, out))
+        reqs.append((ci, llr, prot, rid, out))
+        if r % 7 == 3:
+            time.sleep(0.002)  # some requests arrive while earlier iterations decode
+    done = {}
+    t0 = time.time()
+    while len(done) < len(reqs) and time.time() - t0 < 60:
+        for d in lp.poll(wait_us=100000):
+            done[d.request_id] = d
+    assert len(done) == len(reqs)
+    st = lp.stats()
+    assert st.completed == len(reqs) and st.iterations >= 1 and st.codewords >= sum(r[1].shape[0] for r in reqs)
+    for ci, llr, prot, rid, out in reqs:
+        c = cs[ci]
+        d = done[rid]
+        assert d.status == 0 and d.codewords == llr.shape[0]
+        assert d.latency_us > 0.0 and d.batch_gpu_us >= 0.0
+        assert np.array_equal(out, _expected(oracle, c, llr, prot)), (c.name(), rid)
+        if not prot or not engine.osd_supported(c):
+            assert d.osd_codewords == 0
+    lp.stop()
+    assert lp.stats().running == 0
+    lp.close()
+
+
+def test_device_loop_ends_when_idle_and_restarts(cuda, oracle):
+    c = codes.short_code()
+    lp = _loop([c], max_batch_codewords=256, max_batch_llr_floats=256 * 128, ring_requests=16, idle_timeout_ms=30)
+    lp.start()
+    t0 = time.time()
+    while lp.stats().running and time.time() - t0 < 5.0:
+        time.sleep(0.02)
+    assert lp.stats().running == 0  # the loop ended by itself after its idle timeout
+    llr = _pinned_llrs(c, 20, 2.0, 77)
+    req, x, out = lp.request(0, llr, protection=1)
+    rid = lp.submit_request(req, keep=(x, out))
+    got = []
+    t0 = time.time()
+    while not got and time.time() - t0 < 30:
+        got = lp.poll(wait_us=100000)
+    assert got and got[0].request_id == rid
+    assert lp.stats().launches == 2
+    assert np.array_equal(out, _expected(oracle, c, llr, 1))
+    lp.close()
+
+
+def test_device_loop_rejects_what_it_cannot_serve(cuda):
+    from sicc_gb300 import _lib
+    c = codes.short_code()
+    lp = _loop([c], max_batch_codewords=64, max_batch_llr_floats=64 * 128, ring_requests=8)
+    pageable = np.zeros((4, c.n), np.float32)
+    req, x, out = lp.request(0, pageable)
+    with pytest.raises(_lib.SiccError):
+        lp.submit_request(req, keep=(x, out))
+    big = _pinned_llrs(c, 65, 2.0, 5)
+    req, x, out = lp.request(0, big)
+    with pytest.raises(_lib.SiccError):
+        lp.submit_request(req, keep=(x, out))
+    lp.start()
+    lp.stop(wait_ms=5000)
+    assert lp.stats().running == 0
+    lp.close()
