@@ -11,17 +11,21 @@
  * iteration:
  *   1. admits requests in submission order from a request ring in pinned
  *      host memory, as many as fit the iteration's device state -- its
- *      codeword budget and its LLR budget (the HBM the loop holds for request
- *      state);
- *   2. copies the admitted requests' LLRs from their (pinned) host buffers
- *      into that device state and lays out the batch;
- *   3. decodes the batch with the mixed-code engine: one persistent BP
+ *      codeword, LLR, frame and IQ-sample budgets (the HBM the loop holds
+ *      for request state);
+ *   2. copies the admitted requests' inputs (codeword LLRs, or OFDM IQ
+ *      frames) from their pinned host buffers into that device state and lays
+ *      out the batch;
+ *   3. searches and demodulates the IQ frames of each registered OFDM profile
+ *      (one batched sync + demod launch pair per profile), their LLRs landing
+ *      in the batch beside the LLR requests';
+ *   4. decodes the batch with the mixed-code engine: one persistent BP
  *      launch, then OSD for the codewords whose syndrome fails and whose
  *      request asked for it (protection level 1);
- *   4. copies every request's information bits to its host buffer and
+ *   5. copies every request's information bits to its host buffer and
  *      publishes one completion record per request in a completion ring in
  *      pinned host memory;
- *   5. decides whether to go on: it stops when the host asks it to, after
+ *   6. decides whether to go on: it stops when the host asks it to, after
  *      `idle_timeout_ms` without a request, or after 2^31 iterations.
  * The host only appends requests and reads completions; submit restarts the
  * loop if it has stopped.  Results of a codeword do not depend on what it is
@@ -31,7 +35,9 @@
  * Host buffers (`host_input`, `host_info` of sicc_request_t) must be
  * page-locked memory the GPU can address (cudaHostAlloc / cudaMallocHost /
  * cudaHostRegister) and stay valid until the request's completion is polled.
- * Only codeword-LLR requests (kind 0) are served.  One thread at a time may
+ * Requests are those of sicc_server.h: kind 0 (codeword LLRs of a registered
+ * code) and kind 1 (OFDM IQ frames of a registered profile; frames the search
+ * does not find decode from zero LLRs, as in the pipeline).  One thread at a time may
  * submit; one thread at a time may poll.  Status codes and the last-error
  * string are those of sicc_fec.h; SICC_SERVER_BUSY (sicc_server.h) means the
  * request ring is full.
@@ -51,6 +57,8 @@ typedef struct sicc_devloop_config_t {
     int max_codes;                   /* codes the loop may register, <= 64 */
     int ring_requests;               /* request and completion ring capacity, a power of two */
     int idle_timeout_ms;             /* the loop ends after this long without a request (>= 1) */
+    int max_batch_frames;            /* OFDM frames one iteration demodulates (0: no IQ requests) */
+    long long max_batch_iq_samples;  /* complex IQ samples one iteration holds */
 } sicc_devloop_config_t;
 
 typedef struct sicc_devloop_stats_t {
@@ -64,9 +72,15 @@ SICC_API int sicc_devloop_destroy(unsigned long long handle);
 /* Registers a code (before the first start).  OSD applies to n <= 256, k <= 128
  * (warp kernel) or m <= 1024, n <= 4096 (CTA kernel), as in the engine. */
 SICC_API int sicc_devloop_add_code(unsigned long long handle, const sicc_engine_code_t* code, int* out_code_id);
+/* Registers an OFDM profile (before the first start): the pipeline configuration
+ * and tables of include/sicc_pipe.h, the per-frame stride of a request's IQ
+ * buffer (complex samples) and the registered code of its codewords
+ * (blocks_per_frame of them per frame). */
+SICC_API int sicc_devloop_add_phy(unsigned long long handle, const sicc_pipe_config_t* config,
+                                  const sicc_pipe_tables_t* tables, int frame_stride, int code_id, int* out_phy_id);
 /* Records the loop graph (first call) and launches it on the loop's own stream. */
 SICC_API int sicc_devloop_start(unsigned long long handle);
-/* Appends a kind-0 request; SICC_SERVER_BUSY when the ring is full. */
+/* Appends a request; SICC_SERVER_BUSY when the ring is full. */
 SICC_API int sicc_devloop_submit(unsigned long long handle, const sicc_request_t* request,
                                  unsigned long long* out_request_id);
 /* Up to max completions; waits up to wait_us microseconds for the first one.

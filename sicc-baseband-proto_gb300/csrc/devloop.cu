@@ -11,8 +11,13 @@
 //                    the admission table, publishes the ring head; waits a
 //                    bounded ~100 us for a request when the ring is empty;
 //   layout_kernel    one CTA per admitted request (grid-strided): copies its
-//                    LLRs from pinned host memory into the batch and writes the
-//                    per-codeword tables (code, protection, offsets);
+//                    input (LLRs, or IQ frames) from pinned host memory into the
+//                    batch, writes the per-codeword tables (code, protection,
+//                    offsets) and each profile's frame tables; zeroes the frame
+//                    search's tickets;
+//   sync + demod     per registered OFDM profile, the batched frame search and
+//                    demodulator over its admitted frames (device frame count),
+//                    writing their LLRs into the batch;
 //   engine decode    the mixed-code engine's prepare, BP and OSD launches, sized
 //                    for the largest batch, reading the batch size on the device;
 //   complete_kernel  one CTA per admitted request: copies its information bits
@@ -24,6 +29,7 @@
 // The host side only fills the request ring and drains the completion ring.
 #include "../../include/sicc_devloop.h"
 #include "engine_internal.h"
+#include "pipe_internal.h"
 #include "sicc_common.h"
 
 #include <algorithm>
@@ -41,11 +47,22 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+constexpr int kMaxPhys = 8;
+
 struct alignas(16) ReqEntry {  // host -> device, one per request
     unsigned long long id, tag;
-    const float* in;            // [count][n] LLRs, device-addressable pinned host memory
-    unsigned char* out;         // [count][k] information bits, the same kind of memory
-    int code_id, count, protection, n, k, pad;
+    const float* in;            // kind 0: [count][n] LLRs; kind 1: [count][stride] complex IQ
+                                // (device-addressable pinned host memory)
+    unsigned char* out;         // [codewords][k] information bits, the same kind of memory
+    int kind, code_id, phy_id, count, protection, n, k, codewords, stride, pad;
+};
+
+struct PhyDev {  // a registered OFDM profile's device tables
+    long long* frame_off;      // [max_frames] complex-sample offset of each admitted frame in the IQ buffer
+    long long* llr_frame_off;  // [max_frames] float offset of its LLRs in the batch
+    int* ticket;               // the frame search's tickets, zero before each search
+    int ticket_ints;
+    int blocks;                // codewords per frame
 };
 
 struct alignas(16) CmpEntry {  // device -> host, one per request
@@ -71,12 +88,13 @@ struct LoopState {  // device memory
     unsigned long long head, cmp_tail, iterations, codewords;
     unsigned long long last_active_ns, t_start_ns;
     int nreq, count;
+    int phy_frames[kMaxPhys];  // admitted frames of each profile
 };
 
 struct Admitted {
     ReqEntry e;
-    long long llr_off, info_off;
-    int first_cw;
+    long long llr_off, info_off, iq_off;
+    int first_cw, frame_base;
 };
 
 constexpr int kAdmitPolls = 50;            // ~2 us naps: an empty ring is watched ~100 us per iteration
@@ -110,7 +128,7 @@ __device__ __forceinline__ void store_release_sys(unsigned long long* p, unsigne
 
 __global__ void admit_kernel(const ReqEntry* __restrict__ ring, unsigned mask, const HostSide* hs, DevSide* ds,
                              LoopState* st, Admitted* adm, int max_req, int max_cw, long long max_floats,
-                             unsigned cmp_capacity)
+                             unsigned cmp_capacity, int max_frames, long long max_iq)
 {
     if (threadIdx.x != 0) return;
     unsigned long long head = st->head;
@@ -121,26 +139,42 @@ __global__ void admit_kernel(const ReqEntry* __restrict__ ring, unsigned mask, c
     }
     const unsigned long long consumed = load_acquire_sys(&hs->cmp_head);
     const unsigned long long room = cmp_capacity - (st->cmp_tail - consumed);
-    int nreq = 0, cw = 0;
-    long long floats = 0, info = 0;
+    int nreq = 0, cw = 0, frames = 0;
+    long long floats = 0, info = 0, iq = 0;
+    int pf[kMaxPhys];
+#pragma unroll
+    for (int p = 0; p < kMaxPhys; ++p) pf[p] = 0;
     while (head < tail && nreq < max_req && static_cast<unsigned long long>(nreq) < room) {
         const ReqEntry e = ring[head & mask];
-        const long long f = static_cast<long long>(e.count) * e.n;
-        if (cw + e.count > max_cw || floats + f > max_floats) break;  // in order: the next iteration takes it
+        const long long f = static_cast<long long>(e.codewords) * e.n;
+        const bool iq_req = e.kind == 1;
+        const long long samples = iq_req ? static_cast<long long>(e.count) * e.stride : 0;
+        // in submission order: a request that does not fit waits for the next iteration, and so do those after it
+        if (cw + e.codewords > max_cw || floats + f > max_floats) break;
+        if (iq_req && (frames + e.count > max_frames || iq + samples > max_iq)) break;
         Admitted& a = adm[nreq];
         a.e = e;
         a.first_cw = cw;
         a.llr_off = floats;
         a.info_off = info;
-        cw += e.count;
+        a.iq_off = iq;
+        a.frame_base = iq_req ? pf[e.phy_id] : 0;
+        cw += e.codewords;
         floats += f;
-        info += static_cast<long long>(e.count) * e.k;
+        info += static_cast<long long>(e.codewords) * e.k;
+        if (iq_req) {
+            frames += e.count;
+            iq += samples;
+            pf[e.phy_id] += e.count;
+        }
         ++nreq;
         ++head;
     }
     st->head = head;
     st->nreq = nreq;
     st->count = cw;
+#pragma unroll
+    for (int p = 0; p < kMaxPhys; ++p) st->phy_frames[p] = pf[p];
     const unsigned long long now = globaltimer_ns();
     if (nreq > 0 || st->last_active_ns == 0) st->last_active_ns = now;
     st->t_start_ns = now;
@@ -148,24 +182,39 @@ __global__ void admit_kernel(const ReqEntry* __restrict__ ring, unsigned mask, c
     store_release_sys(&ds->req_head, head);
 }
 
+__device__ __forceinline__ void copy_floats(const float* __restrict__ src, float* __restrict__ dst, long long total)
+{
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0 && (total & 3) == 0) {
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+        float4* d4 = reinterpret_cast<float4*>(dst);
+        for (long long i = threadIdx.x; i < (total >> 2); i += blockDim.x) d4[i] = s4[i];
+    } else {
+        for (long long i = threadIdx.x; i < total; i += blockDim.x) dst[i] = src[i];
+    }
+}
+
 __global__ void layout_kernel(const LoopState* st, const Admitted* __restrict__ adm, float* __restrict__ llr,
+                              float* __restrict__ iq, const PhyDev* __restrict__ phys, int nphys,
                               uint8_t* __restrict__ code_of, uint8_t* __restrict__ protect,
                               long long* __restrict__ llr_off, long long* __restrict__ info_off)
 {
+    if (blockIdx.x == 0)  // every profile's frame search starts from zero tickets
+        for (int p = 0; p < nphys; ++p)
+            for (int i = threadIdx.x; i < phys[p].ticket_ints; i += blockDim.x) phys[p].ticket[i] = 0;
     const int nreq = st->nreq;
     for (int r = blockIdx.x; r < nreq; r += gridDim.x) {
         const Admitted a = adm[r];
-        const long long total = static_cast<long long>(a.e.count) * a.e.n;
-        const float* src = a.e.in;
-        float* dst = llr + a.llr_off;
-        if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0 && (total & 3) == 0) {
-            const float4* s4 = reinterpret_cast<const float4*>(src);
-            float4* d4 = reinterpret_cast<float4*>(dst);
-            for (long long i = threadIdx.x; i < (total >> 2); i += blockDim.x) d4[i] = s4[i];
+        if (a.e.kind == 0) {
+            copy_floats(a.e.in, llr + a.llr_off, static_cast<long long>(a.e.codewords) * a.e.n);
         } else {
-            for (long long i = threadIdx.x; i < total; i += blockDim.x) dst[i] = src[i];
+            copy_floats(a.e.in, iq + 2 * a.iq_off, 2 * static_cast<long long>(a.e.count) * a.e.stride);
+            const PhyDev ph = phys[a.e.phy_id];
+            for (int f = threadIdx.x; f < a.e.count; f += blockDim.x) {
+                ph.frame_off[a.frame_base + f] = a.iq_off + static_cast<long long>(f) * a.e.stride;
+                ph.llr_frame_off[a.frame_base + f] = a.llr_off + static_cast<long long>(f) * ph.blocks * a.e.n;
+            }
         }
-        for (int c = threadIdx.x; c < a.e.count; c += blockDim.x) {
+        for (int c = threadIdx.x; c < a.e.codewords; c += blockDim.x) {
             const int w = a.first_cw + c;
             code_of[w] = static_cast<uint8_t>(a.e.code_id);
             protect[w] = static_cast<uint8_t>(a.e.protection);
@@ -188,11 +237,11 @@ __global__ void complete_kernel(const LoopState* st, const Admitted* __restrict_
             s_osd = 0;
         }
         __syncthreads();
-        const long long bytes = static_cast<long long>(a.e.count) * a.e.k;
+        const long long bytes = static_cast<long long>(a.e.codewords) * a.e.k;
         const uint8_t* src = info + a.info_off;
         for (long long i = threadIdx.x; i < bytes; i += blockDim.x) a.e.out[i] = src[i];
         int failed = 0, osd = 0;
-        for (int c = threadIdx.x; c < a.e.count; c += blockDim.x) {
+        for (int c = threadIdx.x; c < a.e.codewords; c += blockDim.x) {
             const int w = a.first_cw + c;
             const int u = used_osd[w], ok = success[w];
             osd += u;
@@ -208,7 +257,7 @@ __global__ void complete_kernel(const LoopState* st, const Admitted* __restrict_
             c.tag = a.e.tag;
             c.t_start_ns = st->t_start_ns;
             c.t_done_ns = globaltimer_ns();
-            c.codewords = a.e.count;
+            c.codewords = a.e.codewords;
             c.failed = s_failed;
             c.osd = s_osd;
             c.status = 0;
@@ -281,6 +330,18 @@ struct Pending {
     Clock::time_point t_submit;
 };
 
+struct PhyHost {  // a registered OFDM profile
+    unsigned long long pipe = 0;
+    int stride = 0, code_id = 0, blocks = 0;
+    Dev<long long> frame_off, llr_frame_off;
+    Dev<unsigned char> sync, scratch;
+    size_t scratch_bytes = 0, ticket_offset = 0, ticket_bytes = 0;
+    ~PhyHost()
+    {
+        if (pipe) sicc_pipe_destroy(pipe);
+    }
+};
+
 struct Loop {
     sicc_devloop_config_t cfg{};
     int device = 0;
@@ -300,6 +361,9 @@ struct Loop {
     Dev<float> llr;
     Dev<uint8_t> info, code_of, protect, success, used, iters;
     Dev<long long> llr_off, info_off;
+    Dev<float> iqbuf;                    // [max_batch_iq_samples] complex samples
+    std::vector<std::unique_ptr<PhyHost>> phys;
+    Dev<PhyDev> d_phys;
     int info_cap = 0;
     // the graph
     cudaStream_t stream = nullptr;
@@ -340,6 +404,20 @@ struct Loop {
             throw std::runtime_error(last_error());
         info_cap = cfg.max_batch_codewords * k_max;
         info.alloc(static_cast<size_t>(info_cap));
+        std::vector<PhyDev> pd;
+        for (const auto& ph : phys) {
+            PhyDev d{};
+            d.frame_off = ph->frame_off.p;
+            d.llr_frame_off = ph->llr_frame_off.p;
+            d.ticket = reinterpret_cast<int*>(ph->scratch.p + ph->ticket_offset);
+            d.ticket_ints = static_cast<int>(ph->ticket_bytes / sizeof(int));
+            d.blocks = ph->blocks;
+            pd.push_back(d);
+        }
+        d_phys.alloc(std::max<size_t>(pd.size(), 1));
+        if (!pd.empty())
+            check_cuda(cudaMemcpy(d_phys.p, pd.data(), pd.size() * sizeof(PhyDev), cudaMemcpyHostToDevice),
+                       "upload profiles");
         check_cuda(cudaGraphCreate(&graph, 0), "cudaGraphCreate");
         cudaGraphConditionalHandle cond;
         check_cuda(cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault),
@@ -356,8 +434,21 @@ struct Loop {
                    "cudaStreamBeginCaptureToGraph");
         const int sms = device_sm_count();
         admit_kernel<<<1, 32, 0, stream>>>(ring.d, mask, hs.d, ds.d, st.p, adm.p, max_req, cfg.max_batch_codewords,
-                                            cfg.max_batch_llr_floats, mask + 1);
-        layout_kernel<<<2 * sms, 256, 0, stream>>>(st.p, adm.p, llr.p, code_of.p, protect.p, llr_off.p, info_off.p);
+                                            cfg.max_batch_llr_floats, mask + 1, cfg.max_batch_frames,
+                                            cfg.max_batch_iq_samples);
+        layout_kernel<<<2 * sms, 256, 0, stream>>>(st.p, adm.p, llr.p, iqbuf.p, d_phys.p, static_cast<int>(phys.size()),
+                                                    code_of.p, protect.p, llr_off.p, info_off.p);
+        for (size_t q = 0; q < phys.size(); ++q) {  // each profile's admitted frames: search + demodulation
+            const PhyHost& ph = *phys[q];
+            if (pipe_gather_counted(ph.pipe, iqbuf.p, ph.frame_off.p, ph.stride, cfg.max_batch_frames,
+                                    &st.p->phy_frames[q], llr.p, ph.llr_frame_off.p, ph.sync.p, ph.scratch.p,
+                                    ph.scratch_bytes, stream) != CUDA_OSD_STATUS_OK) {
+                const std::string why = last_error();
+                cudaGraph_t dummy;
+                cudaStreamEndCapture(stream, &dummy);
+                throw std::runtime_error("recording the loop's demodulation: " + why);
+            }
+        }
         const int rc = engine_decode(engine, cfg.max_batch_codewords, code_of.p, protect.p, llr.p, llr_off.p, info.p,
                                      info_off.p, success.p, used.p, iters.p, stream, nullptr, &st.p->count);
         if (rc != CUDA_OSD_STATUS_OK) {
@@ -483,6 +574,8 @@ int sicc_devloop_create(const sicc_devloop_config_t* config, unsigned long long*
         if (c.ring_requests < 2 || (c.ring_requests & (c.ring_requests - 1)))
             throw InvalidArgument("ring_requests must be a power of two >= 2");
         if (c.idle_timeout_ms < 1) throw InvalidArgument("idle_timeout_ms must be >= 1");
+        if (c.max_batch_frames < 0 || c.max_batch_iq_samples < 0 || (c.max_batch_frames > 0) != (c.max_batch_iq_samples > 0))
+            throw InvalidArgument("max_batch_frames and max_batch_iq_samples: both positive (IQ requests) or both 0");
         auto L = std::make_shared<Loop>();
         L->cfg = c;
         check_cuda(cudaGetDevice(&L->device), "cudaGetDevice");
@@ -505,6 +598,7 @@ int sicc_devloop_create(const sicc_devloop_config_t* config, unsigned long long*
             b->alloc(static_cast<size_t>(c.max_batch_codewords));
         L->llr_off.alloc(static_cast<size_t>(c.max_batch_codewords));
         L->info_off.alloc(static_cast<size_t>(c.max_batch_codewords));
+        L->iqbuf.alloc(2 * static_cast<size_t>(std::max<long long>(c.max_batch_iq_samples, 1)));
         check_cuda(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking), "cudaStreamCreate(loop)");
         std::lock_guard<std::mutex> lock(g_mu);
         const unsigned long long h = ++g_next;
@@ -564,6 +658,48 @@ int sicc_devloop_add_code(unsigned long long handle, const sicc_engine_code_t* c
     });
 }
 
+int sicc_devloop_add_phy(unsigned long long handle, const sicc_pipe_config_t* config, const sicc_pipe_tables_t* tables,
+                         int frame_stride, int code_id, int* out_phy_id)
+{
+    return guarded([&]() -> int {
+        auto L = get(handle);
+        std::lock_guard<std::mutex> lock(L->mu);
+        if (L->recorded) throw InvalidArgument("profiles must be added before the loop starts");
+        if (!config || !tables || !out_phy_id) throw InvalidArgument("null argument");
+        if (L->cfg.max_batch_frames <= 0) throw InvalidArgument("the loop was created without frame budgets");
+        if (static_cast<int>(L->phys.size()) >= kMaxPhys) throw InvalidArgument("at most 8 OFDM profiles");
+        if (code_id < 0 || code_id >= static_cast<int>(L->codes.size())) throw InvalidArgument("invalid code id");
+        check_cuda(cudaSetDevice(L->device), "cudaSetDevice");
+        auto ph = std::make_unique<PhyHost>();
+        sicc_pipe_config_t c = *config;
+        c.max_batch_frames = L->cfg.max_batch_frames;
+        if (sicc_pipe_create(&c, 1, &ph->pipe) != CUDA_OSD_STATUS_OK) throw InvalidArgument(last_error());
+        if (sicc_pipe_upload_static_tables(ph->pipe, tables) != CUDA_OSD_STATUS_OK) throw InvalidArgument(last_error());
+        PipeDims dims{};
+        if (pipe_dims(ph->pipe, &dims) != CUDA_OSD_STATUS_OK) throw std::runtime_error(last_error());
+        const CodeDims cd = L->codes[code_id];
+        if (dims.code_n != cd.n || dims.code_k != cd.k)
+            throw InvalidArgument("the profile's code_n / code_k differ from the registered code");
+        if (frame_stride < dims.frame_samples) throw InvalidArgument("frame_stride must hold a whole frame");
+        if (static_cast<long long>(frame_stride) > L->cfg.max_batch_iq_samples)
+            throw InvalidArgument("one frame exceeds the iteration's IQ budget");
+        ph->stride = frame_stride;
+        ph->code_id = code_id;
+        ph->blocks = dims.blocks;
+        const int F = L->cfg.max_batch_frames;
+        ph->frame_off.alloc(static_cast<size_t>(F));
+        ph->llr_frame_off.alloc(static_cast<size_t>(F));
+        ph->sync.alloc(static_cast<size_t>(F) * sizeof(sicc_pipe_sync_record_t));
+        if (pipe_gather_scratch(ph->pipe, frame_stride, F, &ph->scratch_bytes, &ph->ticket_offset, &ph->ticket_bytes) !=
+            CUDA_OSD_STATUS_OK)
+            throw std::runtime_error(last_error());
+        ph->scratch.alloc(ph->scratch_bytes);
+        L->phys.push_back(std::move(ph));
+        *out_phy_id = static_cast<int>(L->phys.size()) - 1;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
 int sicc_devloop_start(unsigned long long handle)
 {
     return guarded([&]() -> int {
@@ -582,13 +718,26 @@ int sicc_devloop_submit(unsigned long long handle, const sicc_request_t* request
         auto L = get(handle);
         if (!request) throw InvalidArgument("null request");
         const sicc_request_t& r = *request;
-        if (r.kind != 0) throw InvalidArgument("the device loop serves codeword-LLR requests (kind 0)");
+        if (r.kind != 0 && r.kind != 1) throw InvalidArgument("request kind must be 0 (LLRs) or 1 (OFDM IQ)");
         std::lock_guard<std::mutex> lock(L->mu);
-        if (r.code_id < 0 || r.code_id >= static_cast<int>(L->codes.size())) throw InvalidArgument("invalid code id");
         if (r.protection != 0 && r.protection != 1) throw InvalidArgument("protection must be 0 or 1");
-        const CodeDims cd = L->codes[r.code_id];
-        if (r.count <= 0 || r.count > L->cfg.max_batch_codewords ||
-            static_cast<long long>(r.count) * cd.n > L->cfg.max_batch_llr_floats)
+        if (r.count <= 0) throw InvalidArgument("count must be positive");
+        int code_id = r.code_id, stride = 0, codewords = r.count;
+        if (r.kind == 1) {
+            if (r.phy_id < 0 || r.phy_id >= static_cast<int>(L->phys.size())) throw InvalidArgument("invalid profile id");
+            const PhyHost& ph = *L->phys[r.phy_id];
+            code_id = ph.code_id;
+            stride = ph.stride;
+            codewords = r.count * ph.blocks;
+            if (r.count > L->cfg.max_batch_frames ||
+                static_cast<long long>(r.count) * stride > L->cfg.max_batch_iq_samples)
+                throw InvalidArgument("request larger than one iteration's frame budget");
+        } else if (code_id < 0 || code_id >= static_cast<int>(L->codes.size())) {
+            throw InvalidArgument("invalid code id");
+        }
+        const CodeDims cd = L->codes[code_id];
+        if (codewords > L->cfg.max_batch_codewords ||
+            static_cast<long long>(codewords) * cd.n > L->cfg.max_batch_llr_floats)
             throw InvalidArgument("request larger than one iteration's budget");
         check_cuda(cudaSetDevice(L->device), "cudaSetDevice");
         const void* in = device_address(r.host_input);
@@ -606,11 +755,15 @@ int sicc_devloop_submit(unsigned long long handle, const sicc_request_t* request
         e.tag = r.tag;
         e.in = static_cast<const float*>(in);
         e.out = static_cast<unsigned char*>(out);
-        e.code_id = r.code_id;
+        e.kind = r.kind;
+        e.code_id = code_id;
+        e.phy_id = r.kind == 1 ? r.phy_id : 0;
         e.count = r.count;
         e.protection = r.protection;
         e.n = cd.n;
         e.k = cd.k;
+        e.codewords = codewords;
+        e.stride = stride;
         {
             std::lock_guard<std::mutex> plock(L->poll_mu);
             L->pending[id] = Pending{Clock::now()};

@@ -340,7 +340,8 @@ __device__ SyncOut sync_finish(const float2* __restrict__ x, int avail, int limi
 __global__ void __launch_bounds__(kSyncThreads)
 sync_kernel(const float2* __restrict__ samples, long long stride, const long long* __restrict__ frame_off,
             const int* __restrict__ counts, int count, int frames, int passes, const float2* __restrict__ preamble,
-            SyncParams p, PassResult* __restrict__ pres, int* __restrict__ ticket, SyncOut* __restrict__ out)
+            SyncParams p, PassResult* __restrict__ pres, int* __restrict__ ticket, SyncOut* __restrict__ out,
+            const int* __restrict__ frames_ptr)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float red[4 * (kSyncThreads / 32)];
@@ -354,6 +355,9 @@ sync_kernel(const float2* __restrict__ samples, long long stride, const long lon
     // passes of a frame found early skip their scans
     const int pass = blockIdx.x / frames;
     const int f = blockIdx.x - pass * frames;
+    // a grid sized for `frames` over a batch of *frames_ptr frames: the CTAs of absent frames
+    // leave at once (uniform over the CTA, before any barrier)
+    if (frames_ptr && f >= *frames_ptr) return;
     const int tid = threadIdx.x;
     const float2* x = samples + (frame_off ? frame_off[f] : static_cast<long long>(f) * stride);
     const int avail = counts ? counts[f] : count;
@@ -505,9 +509,28 @@ ingest_extract_kernel(const float2* __restrict__ window, int n, const float2* __
     if (tid == 0) *state = s_st;
 }
 
+static long long sync_passes(long long stride, const int* counts, int count, const SyncParams& p)
+{
+    // passes of the longest search: frames hold at most `stride` samples
+    long long span = counts ? stride : std::min<long long>(count, stride);
+    long long limit = span - p.pre_len + 1;
+    if (p.max_search > 0) limit = std::min<long long>(limit, p.max_search + 1);
+    return std::max<long long>(1, (limit + kSyncPass - 1) / kSyncPass);
+}
+
+SyncScratchLayout sync_scratch_layout(long long stride, const int* counts, int count, int frames, const SyncParams& p)
+{
+    const long long passes = sync_passes(stride, counts, count, p);
+    SyncScratchLayout l;
+    l.ticket_offset = (static_cast<size_t>(frames) * passes * sizeof(PassResult) + 15) & ~size_t(15);
+    l.ticket_bytes = static_cast<size_t>(2) * frames * sizeof(int);
+    l.bytes = l.ticket_offset + l.ticket_bytes;
+    return l;
+}
+
 void launch_sync(const float2* samples, long long stride, const int* counts, int count, int frames,
                  const float2* preamble, const SyncParams& p, SyncOut* out, cudaStream_t st,
-                 const long long* frame_off)
+                 const long long* frame_off, const int* frames_ptr, void* caller_scratch, size_t caller_scratch_bytes)
 {
     if (frames <= 0) return;
     const size_t smem = static_cast<size_t>((kSyncPass + p.pre_len + 1) & ~1) * sizeof(float2) +
@@ -515,30 +538,31 @@ void launch_sync(const float2* samples, long long stride, const int* counts, int
                         static_cast<size_t>(kSyncPass + 2 * kMaxRadius) * sizeof(float);
     if (smem > 200 * 1024) throw InvalidArgument("preamble too long for the sync kernel");
     if (p.radius > kMaxRadius || p.radius < 0) throw InvalidArgument("refinement radius must be 0..511");
-    // passes of the longest search: frames hold at most `stride` samples
-    long long span = counts ? stride : std::min<long long>(count, stride);
-    long long limit = span - p.pre_len + 1;
-    if (p.max_search > 0) limit = std::min<long long>(limit, p.max_search + 1);
-    const long long passes = std::max<long long>(1, (limit + kSyncPass - 1) / kSyncPass);
+    const long long passes = sync_passes(stride, counts, count, p);
     if (passes * frames > 0x7fffffffLL) throw InvalidArgument("sync grid too large");
-    int device = 0;
-    check_cuda(cudaGetDevice(&device), "cudaGetDevice");
-    const size_t res_bytes = static_cast<size_t>(frames) * passes * sizeof(PassResult);
-    const size_t ticket_bytes = static_cast<size_t>(2) * frames * sizeof(int);
-    void* scratch = nullptr;
-    check_cuda(cudaMallocFromPoolAsync(&scratch, res_bytes + ticket_bytes, scratch_pool(device), st),
-               "cudaMallocFromPoolAsync(sync)");
+    const SyncScratchLayout l = sync_scratch_layout(stride, counts, count, frames, p);
+    void* scratch = caller_scratch;
+    const bool own = caller_scratch == nullptr;
+    if (own) {
+        int device = 0;
+        check_cuda(cudaGetDevice(&device), "cudaGetDevice");
+        check_cuda(cudaMallocFromPoolAsync(&scratch, l.bytes, scratch_pool(device), st), "cudaMallocFromPoolAsync(sync)");
+    } else if (caller_scratch_bytes < l.bytes) {
+        throw InvalidArgument("sync scratch smaller than the grid needs");
+    }
     PassResult* pres = static_cast<PassResult*>(scratch);
-    int* ticket = reinterpret_cast<int*>(static_cast<unsigned char*>(scratch) + res_bytes);
-    cudaError_t err = cudaMemsetAsync(ticket, 0, ticket_bytes, st);
+    int* ticket = reinterpret_cast<int*>(static_cast<unsigned char*>(scratch) + l.ticket_offset);
+    // caller scratch: the caller has zeroed the tickets in stream order before this launch
+    cudaError_t err = own ? cudaMemsetAsync(ticket, 0, l.ticket_bytes, st) : cudaSuccess;
     if (err == cudaSuccess)
         err = grant_dynamic_smem(reinterpret_cast<const void*>(sync_kernel), smem);
     if (err == cudaSuccess) {
         sync_kernel<<<static_cast<unsigned>(passes * frames), kSyncThreads, smem, st>>>(
-            samples, stride, frame_off, counts, count, frames, static_cast<int>(passes), preamble, p, pres, ticket, out);
+            samples, stride, frame_off, counts, count, frames, static_cast<int>(passes), preamble, p, pres, ticket, out,
+            frames_ptr);
         err = cudaGetLastError();
     }
-    const cudaError_t ferr = cudaFreeAsync(scratch, st);
+    const cudaError_t ferr = own ? cudaFreeAsync(scratch, st) : cudaSuccess;
     check_cuda(err, "sync_kernel launch");
     check_cuda(ferr, "cudaFreeAsync(sync)");
 }
@@ -713,8 +737,10 @@ __device__ __forceinline__ float sq_dist(float x, float c)
 __global__ void __launch_bounds__(kDemodThreads)
 demod_kernel(DemodView v, const float2* __restrict__ samples, long long stride, const SyncOut* __restrict__ sync,
              float* __restrict__ llr, long long llr_stride, int symbols_per_cta, const long long* __restrict__ frame_off,
-             const long long* __restrict__ llr_off)
+             const long long* __restrict__ llr_off, const int* __restrict__ frames_ptr)
 {
+    // a grid sized for more frames than the batch holds: the CTAs of absent frames leave at once
+    if (frames_ptr && static_cast<int>(blockIdx.x) >= *frames_ptr) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* work = reinterpret_cast<float2*>(smem_raw);  // derotated symbol, FFT buffer
     // stage(b) = work + (1 + b) * nfft: staged raw symbols (two buffers), FFT buffer after use
@@ -875,7 +901,7 @@ unsigned demod_wait_timeouts()
 
 void launch_demod(const DemodView& v, const float2* samples, long long stride, const SyncOut* sync, int frames,
                   float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta, const long long* frame_off,
-                  const long long* llr_off)
+                  const long long* llr_off, const int* frames_ptr)
 {
     if (frames <= 0 || v.num_data <= 0) return;
     if (v.nfft < 4 || (v.nfft & (v.nfft - 1))) throw InvalidArgument("nfft must be a power of two >= 4");
@@ -895,7 +921,7 @@ void launch_demod(const DemodView& v, const float2* samples, long long stride, c
     check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(demod_kernel), smem), "cudaFuncSetAttribute(demod)");
     const dim3 grid(frames, (v.num_data + spc - 1) / spc);
     demod_kernel<<<grid, kDemodThreads, smem, st>>>(v, samples, stride, sync, llr, llr_stride, spc, frame_off,
-                                                    llr_off);
+                                                    llr_off, frames_ptr);
     check_cuda(cudaGetLastError(), "demod_kernel launch");
 }
 

@@ -32,9 +32,21 @@ struct SyncParams {
 // One CTA per frame and pass of 4352 candidates, with stream-ordered scratch.  samples: frame f starts at samples + f*stride (or
 // samples + frame_off[f], device offsets in complex samples) and holds counts[f] (or `count` when counts
 // is null) samples, at most `stride`.
+// With frames_ptr (device int) the grid is sized for `frames` and only the first
+// *frames_ptr frames are searched.  With caller_scratch (at least
+// sync_scratch_layout(...).bytes, its tickets zeroed in stream order before the
+// launch) nothing is allocated; otherwise the scratch comes from a stream-ordered pool.
 void launch_sync(const float2* samples, long long stride, const int* counts, int count, int frames,
                  const float2* preamble, const SyncParams& p, SyncOut* out, cudaStream_t st,
-                 const long long* frame_off = nullptr);
+                 const long long* frame_off = nullptr, const int* frames_ptr = nullptr, void* caller_scratch = nullptr,
+                 size_t caller_scratch_bytes = 0);
+
+struct SyncScratchLayout {
+    size_t bytes;          // the whole scratch
+    size_t ticket_offset;  // the tickets (2 ints per frame), which start at zero
+    size_t ticket_bytes;
+};
+SyncScratchLayout sync_scratch_layout(long long stride, const int* counts, int count, int frames, const SyncParams& p);
 
 // Static demodulation tables resident on the device.
 struct DemodView {
@@ -65,7 +77,8 @@ constexpr int kDemodMaxPilots = 4;
 // complex samples / floats) frame f is read from samples + frame_off[f] and written to llr + llr_off[f].
 void launch_demod(const DemodView& v, const float2* samples, long long stride, const SyncOut* sync, int frames,
                   float* llr, long long llr_stride, cudaStream_t st, int symbols_per_cta,
-                  const long long* frame_off = nullptr, const long long* llr_off = nullptr);
+                  const long long* frame_off = nullptr, const long long* llr_off = nullptr,
+                  const int* frames_ptr = nullptr);
 // Waits of the demodulator on its staged-sample copies that hit their iteration limit
 // since the library loaded on the current device (each one is counted and the symbol is
 // read from global memory instead; never expected).

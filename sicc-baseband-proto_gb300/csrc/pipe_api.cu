@@ -7,6 +7,7 @@
 #include "../../include/sicc_ingest.h"
 #include "../../include/sicc_pipe.h"
 #include "ofdm_kernels.h"
+#include "pipe_internal.h"
 
 #include <algorithm>
 #include <chrono>
@@ -572,6 +573,72 @@ int sicc_pipe_demod_gather(unsigned long long handle, const float* device_iq, co
         return CUDA_OSD_STATUS_OK;
     });
 }
+
+}  // extern "C"
+
+namespace sicc {
+
+int pipe_dims(unsigned long long handle, PipeDims* out)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        require_tables(*p);
+        if (!out) throw InvalidArgument("null argument");
+        out->frame_samples = p->frame_samples;
+        out->coded_bits = p->coded_bits;
+        out->code_n = p->cfg.code_n;
+        out->code_k = p->cfg.code_k;
+        out->blocks = p->cfg.blocks_per_frame;
+        out->preamble_len = p->cfg.preamble_len;
+        out->max_frames = p->batch_frames;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int pipe_gather_scratch(unsigned long long handle, int sample_count, int frames, size_t* out_bytes,
+                        size_t* out_ticket_offset, size_t* out_ticket_bytes)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        require_tables(*p);
+        const SyncScratchLayout l = sync_scratch_layout(sample_count, nullptr, sample_count, frames, p->sync_params(0));
+        if (out_bytes) *out_bytes = l.bytes;
+        if (out_ticket_offset) *out_ticket_offset = l.ticket_offset;
+        if (out_ticket_bytes) *out_ticket_bytes = l.ticket_bytes;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+int pipe_gather_counted(unsigned long long handle, const float* device_iq, const long long* device_frame_offsets,
+                        int sample_count, int max_frames, const int* frames_ptr, float* device_llr,
+                        const long long* device_llr_offsets, void* device_sync, void* scratch, size_t scratch_bytes,
+                        cudaStream_t st)
+{
+    return guarded([&] {
+        auto p = get(handle);
+        std::lock_guard<std::mutex> lock(p->mu);
+        require_tables(*p);
+        if (!device_iq || !device_frame_offsets || !device_llr || !device_llr_offsets || !device_sync || !frames_ptr ||
+            !scratch)
+            throw InvalidArgument("null device pointer");
+        if (max_frames <= 0) throw InvalidArgument("max_frames must be positive");
+        if (sample_count < p->cfg.preamble_len) throw InvalidArgument("sample_count must cover the preamble");
+        check_cuda(cudaSetDevice(p->device), "cudaSetDevice");
+        SyncOut* so = static_cast<SyncOut*>(device_sync);
+        const float2* iq = reinterpret_cast<const float2*>(device_iq);
+        launch_sync(iq, sample_count, nullptr, sample_count, max_frames, p->preamble.p, p->sync_params(0), so, st,
+                    device_frame_offsets, frames_ptr, scratch, scratch_bytes);
+        launch_demod(p->view, iq, 0, so, max_frames, device_llr, 0, st, p->symbols_per_cta, device_frame_offsets,
+                     device_llr_offsets, frames_ptr);
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
+}  // namespace sicc
+
+extern "C" {
 
 int sicc_pipe_upload_tx_tables(unsigned long long handle, const sicc_pipe_tx_tables_t* t)
 {

@@ -19,12 +19,15 @@ import numpy as np
 from . import _lib
 from .codes import QcCode
 from .engine import EngineCode
+from .ofdm import Tables
+from .pipeline import PipeConfig, PipeTables, pipe_structs
 from .server import BUSY, Completion, Request, _done
 
 
 class DevLoopConfig(C.Structure):
     _fields_ = [("max_batch_codewords", C.c_int), ("max_batch_llr_floats", C.c_longlong), ("max_codes", C.c_int),
-                ("ring_requests", C.c_int), ("idle_timeout_ms", C.c_int)]
+                ("ring_requests", C.c_int), ("idle_timeout_ms", C.c_int), ("max_batch_frames", C.c_int),
+                ("max_batch_iq_samples", C.c_longlong)]
 
 
 class DevLoopStats(C.Structure):
@@ -37,6 +40,8 @@ _SIGS = {
     "sicc_devloop_create": (C.c_int, [C.POINTER(DevLoopConfig), C.POINTER(C.c_ulonglong)]),
     "sicc_devloop_destroy": (C.c_int, [C.c_ulonglong]),
     "sicc_devloop_add_code": (C.c_int, [C.c_ulonglong, C.POINTER(EngineCode), C.POINTER(C.c_int)]),
+    "sicc_devloop_add_phy": (C.c_int, [C.c_ulonglong, C.POINTER(PipeConfig), C.POINTER(PipeTables), C.c_int, C.c_int,
+                                       C.POINTER(C.c_int)]),
     "sicc_devloop_start": (C.c_int, [C.c_ulonglong]),
     "sicc_devloop_submit": (C.c_int, [C.c_ulonglong, C.POINTER(Request), C.POINTER(C.c_ulonglong)]),
     "sicc_devloop_poll": (C.c_int, [C.c_ulonglong, C.c_int, C.POINTER(Completion), C.POINTER(C.c_int), C.c_int]),
@@ -55,19 +60,23 @@ def _fn(name):
 def pinned(shape, dtype) -> np.ndarray:
     """A page-locked NumPy array the GPU can address (through torch's pinned allocator)."""
     import torch
-    tdt = {np.dtype(np.float32): torch.float32, np.dtype(np.uint8): torch.uint8}[np.dtype(dtype)]
+    tdt = {np.dtype(np.float32): torch.float32, np.dtype(np.uint8): torch.uint8,
+           np.dtype(np.complex64): torch.complex64}[np.dtype(dtype)]
     return torch.empty(shape, dtype=tdt, pin_memory=True).numpy()
 
 
 class DevLoop:
     def __init__(self, max_batch_codewords: int, max_batch_llr_floats: int, max_codes: int = 64,
-                 ring_requests: int = 4096, idle_timeout_ms: int = 2000):
+                 ring_requests: int = 4096, idle_timeout_ms: int = 2000, max_batch_frames: int = 0,
+                 max_batch_iq_samples: int = 0):
         cfg = DevLoopConfig(max_batch_codewords=max_batch_codewords, max_batch_llr_floats=max_batch_llr_floats,
-                            max_codes=max_codes, ring_requests=ring_requests, idle_timeout_ms=idle_timeout_ms)
+                            max_codes=max_codes, ring_requests=ring_requests, idle_timeout_ms=idle_timeout_ms,
+                            max_batch_frames=max_batch_frames, max_batch_iq_samples=max_batch_iq_samples)
         h = C.c_ulonglong(0)
         _lib.check(_fn("sicc_devloop_create")(C.byref(cfg), C.byref(h)), "sicc_devloop_create")
         self.handle = h.value
         self.codes: list[QcCode] = []
+        self.phys: list[dict] = []
         self._inflight: dict[int, tuple] = {}
 
     def close(self):
@@ -94,6 +103,16 @@ class DevLoop:
         self.codes.append(code)
         return cid.value
 
+    def add_phy(self, tables: Tables, code_id: int, blocks_per_frame: int, noise_var: float, frame_stride: int,
+                sync_radius: int = 0) -> int:
+        code = self.codes[code_id]
+        c, t, keep = pipe_structs(tables, code.n, code.k, blocks_per_frame, noise_var, sync_radius=sync_radius)
+        pid = C.c_int(-1)
+        _lib.check(_fn("sicc_devloop_add_phy")(self.handle, C.byref(c), C.byref(t), frame_stride, code_id,
+                                               C.byref(pid)), "sicc_devloop_add_phy")
+        self.phys.append(dict(code_id=code_id, blocks=blocks_per_frame, stride=frame_stride))
+        return pid.value
+
     def start(self):
         _lib.check(_fn("sicc_devloop_start")(self.handle), "sicc_devloop_start")
 
@@ -109,6 +128,18 @@ class DevLoop:
         req = Request(kind=0, code_id=code_id, phy_id=-1, count=count, protection=protection,
                       host_input=llr.ctypes.data, host_info=out.ctypes.data, tag=tag)
         return req, llr, out
+
+    def iq_request(self, phy_id: int, iq: np.ndarray, protection: int = 1, tag: int = 0, out=None):
+        """(Request, input, output) for pinned IQ frames [count][frame_stride] (complex64); ``out`` pinned uint8
+        [count * blocks][k] (made if None)."""
+        p = self.phys[phy_id]
+        code = self.codes[p["code_id"]]
+        count = iq.shape[0]
+        if out is None:
+            out = pinned((count * p["blocks"], code.k), np.uint8)
+        req = Request(kind=1, code_id=-1, phy_id=phy_id, count=count, protection=protection,
+                      host_input=iq.ctypes.data, host_info=out.ctypes.data, tag=tag)
+        return req, iq, out
 
     def submit_request(self, req: Request, keep=None):
         """Submits a prepared request; None when the ring is full.  ``keep`` is held until polled."""

@@ -4,7 +4,9 @@ The loop (include/sicc_devloop.h) admits, lays out, decodes and completes
 requests inside one CUDA graph repeated on the GPU.  Every request of a mixed
 stream (several codes, BP-only and BP+OSD protection, requests arriving while
 earlier ones decode) must come back with the bits the oracle's BP -> OSD chain
-gives for it alone; the loop must end by itself when idle and start again on
+gives for it alone (LLR requests), or that the pipeline's batched demodulator
+followed by the mixed engine give for it alone (OFDM IQ requests, demodulated
+inside the loop); the loop must end by itself when idle and start again on
 the next request, stop when asked, and reject buffers the GPU cannot address.
 """
 import time
@@ -12,7 +14,7 @@ import time
 import numpy as np
 import pytest
 
-from sicc_gb300 import channel, codes, engine
+from sicc_gb300 import channel, codes, engine, ofdm
 
 pytestmark = pytest.mark.gpu
 
@@ -128,4 +130,68 @@ def test_device_loop_rejects_what_it_cannot_serve(cuda):
     lp.start()
     lp.stop(wait_ms=5000)
     assert lp.stats().running == 0
+    lp.close()
+
+
+def test_device_loop_iq_requests_match_pipeline_then_engine(cuda):
+    """IQ requests are searched and demodulated inside the loop, beside LLR requests of other codes."""
+    torch = cuda
+    from sicc_gb300.devloop import pinned
+    from sicc_gb300.pipeline import RxPipeline, SYNC_RECORD
+    t = ofdm.reference_tables(ofdm.OFDM_SMALL)
+    code = codes.short_code()
+    gen = ofdm.FrameGenerator(t, code, seed=78)
+    blocks = gen.blocks
+    b = gen.batch(12, snr_db=14.0, cfo_subcarriers=0.1, max_offset=100)
+    stride = b.iq.shape[1]
+    nv = float(np.float32(np.mean(b.noise_var)))
+    cs = _codes()
+    cid = len(cs) - 2  # the short code
+    assert cs[cid].n == code.n and cs[cid].k == code.k
+    lp = _loop(cs, max_batch_codewords=1024, max_batch_llr_floats=1024 * 1024, ring_requests=32,
+               max_batch_frames=8, max_batch_iq_samples=8 * stride)
+    pid = lp.add_phy(t, cid, blocks, nv, stride)
+    lp.start()
+    iq_reqs = []
+    for r in range(4):
+        sl = pinned((3, stride), np.complex64)
+        sl[:] = b.iq[3 * r: 3 * r + 3]
+        req, x, out = lp.iq_request(pid, sl, protection=r % 2, tag=r)
+        rid = lp.submit_request(req, keep=(x, out))
+        iq_reqs.append((sl, rid, out))
+        llr = _pinned_llrs(cs[0], 16, 2.0, r)
+        req, x, o2 = lp.request(0, llr, protection=1)
+        lp.submit_request(req, keep=(x, o2))
+    want = {rid for _, rid, _ in iq_reqs}
+    got = {}
+    t0 = time.time()
+    while not want <= set(got) and time.time() - t0 < 60:
+        for d in lp.poll(wait_us=100000):
+            got[d.request_id] = d
+    assert want <= set(got)
+    pipe = RxPipeline(t, code.n, code.k, blocks, nv, max_rx_search_samples=stride, max_batch_frames=16)
+    eng = engine.Engine(max_codewords=3 * blocks, max_llr_floats=3 * blocks * code.n)
+    for c in cs:
+        eng.add_code(c, engine.iteration_cap(c.n), osd_order=2 if engine.osd_supported(c) else -1)
+    for r, (sl, rid, out) in enumerate(iq_reqs):
+        d_iq = torch.from_numpy(np.ascontiguousarray(sl)).cuda()
+        d_llr = torch.zeros((3, blocks * code.n), dtype=torch.float32, device="cuda")
+        d_sync = torch.zeros(3 * SYNC_RECORD.itemsize, dtype=torch.uint8, device="cuda")
+        pipe.demod_batch(d_iq, stride, stride, 3, d_llr, d_sync, torch.cuda.current_stream())
+        cw = 3 * blocks
+        code_ids = torch.full((cw,), cid, dtype=torch.uint8, device="cuda")
+        prot = torch.full((cw,), r % 2, dtype=torch.uint8, device="cuda")
+        llr_off = torch.arange(cw, dtype=torch.int64, device="cuda") * code.n
+        info_off = torch.arange(cw, dtype=torch.int64, device="cuda") * code.k
+        info = torch.zeros(cw * code.k, dtype=torch.uint8, device="cuda")
+        eng.decode_device(cw, code_ids, d_llr, llr_off, info, info_off, stream=torch.cuda.current_stream(),
+                          d_protection=prot)
+        torch.cuda.synchronize()
+        assert got[rid].codewords == cw
+        assert np.array_equal(out.reshape(-1), info.cpu().numpy()), r
+    good = sum(np.array_equal(out.reshape(3, -1)[i], b.info[3 * r + i])
+               for r, (_, _, out) in enumerate(iq_reqs) for i in range(3))
+    assert good >= 9
+    from sicc_gb300.pipeline import wait_timeouts
+    assert wait_timeouts() == 0
     lp.close()
