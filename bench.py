@@ -1219,13 +1219,29 @@ def run_serve(args, rank, world):
         iq_info.append(b.info)
     stride = iq_pool[0][0].shape[1]
 
-    srv = Server(hbm_budget_bytes=40 << 30, max_batch_codewords=args.serve_batch,
-                 max_inflight_batches=args.serve_inflight, max_pending_requests=1 << 16)
+    device_loop = getattr(args, "serve_loop", "host") == "device"
+    if device_loop:
+        # the device-resident loop: one iteration holds up to serve_batch codewords (their LLRs: up to 2048
+        # floats each), 17 x 16 frames of IQ; the rest of the 40 GB budget is not needed by this mix
+        from sicc_gb300.devloop import DevLoop
+        srv = DevLoop(max_batch_codewords=args.serve_batch, max_batch_llr_floats=args.serve_batch * 2048,
+                      ring_requests=4096, idle_timeout_ms=2000, max_batch_frames=272,
+                      max_batch_iq_samples=272 * stride)
+    else:
+        srv = Server(hbm_budget_bytes=40 << 30, max_batch_codewords=args.serve_batch,
+                     max_inflight_batches=args.serve_inflight, max_pending_requests=1 << 16)
     ids = [srv.add_code(c, engine.iteration_cap(c.n), ALPHA, engine.osd_order_for(c),
                         OSD_FLIP, OSD_TESTS) for c in mixed]
     ocid = srv.add_code(ocode, OFDM_ITERS, ALPHA, engine.osd_order_for(ocode))
     phys = [srv.add_phy(t, ocid, blocks, nv, stride) for _, nv in iq_pool]
     srv.start()
+
+    def make_request(kind, ident, data, prot, tag, out):
+        if not device_loop:
+            return srv.request(kind, ident, data, prot, tag=tag, out=out)
+        if kind == 1:
+            return srv.iq_request(ident, data, prot, tag=tag, out=out)
+        return srv.request(ident, data, prot, tag=tag, out=out)
 
     # one request list, reused at every load point (outputs are overwritten)
     n_req = args.serve_requests
@@ -1237,7 +1253,7 @@ def run_serve(args, rank, world):
             f = int(rng.integers(1, 18))
             a = int(rng.integers(0, 24 - f + 1))
             out = pinned((f * blocks, ocode.k), torch.uint8)
-            reqs.append(srv.request(1, phys[s], iq_pool[s][0][a:a + f], prot, tag=r, out=out))
+            reqs.append(make_request(1, phys[s], iq_pool[s][0][a:a + f], prot, r, out))
             truth.append(iq_info[s][a:a + f].reshape(f * blocks, ocode.k))
             info_bits += f * blocks * ocode.k
             iq_reqs += 1
@@ -1246,7 +1262,7 @@ def run_serve(args, rank, world):
             b = int(rng.integers(1, 513))
             a = int(rng.integers(0, 512 - b + 1))
             out = pinned((b, mixed[ci].k), torch.uint8)
-            reqs.append(srv.request(0, ids[ci], llr_pool[ci][a:a + b], prot, tag=r, out=out))
+            reqs.append(make_request(0, ids[ci], llr_pool[ci][a:a + b], prot, r, out))
             truth.append(info_pool[ci][a:a + b])
             info_bits += b * mixed[ci].k
     in_bytes = sum(int(q[1].nbytes) for q in reqs)
@@ -1302,13 +1318,19 @@ def run_serve(args, rank, world):
                       "p50_wait_ms": round(float(np.percentile(wait, 50)), 4),
                       "p50_batch_gpu_ms": round(float(np.percentile(gpu, 50)), 4),
                       "p99_batch_gpu_ms": round(float(np.percentile(gpu, 99)), 4),
-                      "mean_batch_codewords": round((b1.codewords - b0.codewords) / max(b1.batches - b0.batches, 1), 1),
-                      "batches": int(b1.batches - b0.batches)})
+                      "mean_batch_codewords": round((b1.codewords - b0.codewords) /
+                                                    max(_batches(b1) - _batches(b0), 1), 1),
+                      "batches": int(_batches(b1) - _batches(b0))})
     clk = clocks.stop()
     st = srv.stats()
     srv.close()
     p80 = next((x for x in sweep if x["load"] == 0.8), sweep[-1])
-    launches = int(st1.batches - st0.batches) * 3 + args.steps * iq_reqs * 2
+    if device_loop:
+        # per loop iteration: admit, layout, sync + demod per profile, prepare, mixed BP, the OSD launches
+        # (warp kernel and three long-code classes), complete, publish
+        launches = int(_batches(st1) - _batches(st0)) * (2 + 2 * len(phys) + 2 + 4 + 2)
+    else:
+        launches = int(st1.batches - st0.batches) * 3 + args.steps * iq_reqs * 2
     line = {"metric": "served info-bit Mbps (Poisson mixed-code + OFDM IQ requests), p50/p99/p99.9 latency",
             "value": round(peak_mbps, 3), "unit": "Mbit/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(peak_s * 1e3, 3), "higher_is_better": True,
@@ -1323,8 +1345,12 @@ def run_serve(args, rank, world):
                        "l2": "inputs copied host->device every request (pinned host pools)"},
             "fer": round(sum(fe) / cw_total, 5), "load_sweep": sweep,
             "p99_ms_at_80pct_load": p80["p99_ms"],
-            "server": {"batches": int(st.batches), "busy_rejections": int(st.busy_rejections),
-                       "arena_peak_mb": round(st.arena_bytes_peak / 1e6, 1)},
+            "server": ({"loop": "device-resident (one conditional CUDA graph; include/sicc_devloop.h)",
+                        "iterations": int(st.iterations), "graph_launches": int(st.launches),
+                        "busy_rejections": int(st.busy_rejections)} if device_loop else
+                       {"loop": "host scheduler thread (include/sicc_server.h)", "batches": int(st.batches),
+                        "busy_rejections": int(st.busy_rejections),
+                        "arena_peak_mb": round(st.arena_bytes_peak / 1e6, 1)}),
             "gpu_launches": launches, "clocks": clk, "roofline": None,
             "e2e": {"value": round(peak_mbps, 3), "unit": "Mbit/s", "h2d_bytes_per_step": in_bytes,
                     "d2h_bytes_per_step": out_bytes},
@@ -1418,6 +1444,11 @@ def run_frame_pipeline_reference(args, rank, world):
                               "reference_own_benchmark": {"rc": own.returncode, "output": own_lines}})
 
 
+def _batches(st):
+    """Batches launched by the host-scheduled server, or iterations of the device loop."""
+    return st.batches if hasattr(st, "batches") else st.iterations
+
+
 # ------------------------------------------------------------- reference arm
 def run_reference(args, rank, world):
     if rank != 0:
@@ -1462,7 +1493,8 @@ def run_targets(args):
     * Mixed-code batching (100,000 codewords of 15 codes): one persistent batched launch against the
       plain form, one synchronous decode call per request; target: batched >= 50x plain.
     * Serving: every request offered at once gives the peak, then one Poisson pass at 80% of it;
-      target: p99 request latency < 1 ms at 80% load.
+      target: p99 request latency < 1 ms at 80% load.  Run twice: through the host-scheduled server
+      and through the device-resident graph loop.
     """
     import copy
     sub = copy.copy(args)
@@ -1472,6 +1504,8 @@ def run_targets(args):
     sub.steps, sub.warmup, sub.no_e2e, sub.no_cpu_baseline = 3, 1, True, True
     sub.serve_loads = (0.8,)
     serve = run_serve(sub, 0, 1)
+    sub.serve_loop = "device"
+    serve_dev = run_serve(sub, 0, 1)
     plain = mixed["plain_one_code_per_launch"]
     p80 = serve["load_sweep"][0]
     return {"mixed_batched_vs_plain": {"batched_mbps": mixed["value"], "plain_mbps": plain["value"],
@@ -1483,7 +1517,18 @@ def run_targets(args):
                                      "p99_ms": p80["p99_ms"], "p99_9_ms": p80["p99_9_ms"],
                                      "p99_ms_bp_only": p80["p99_ms_bp_only"], "p99_ms_bp_osd": p80["p99_ms_bp_osd"],
                                      "target_p99_ms": 1.0,
-                                     "workload": f"serve_mixed, {serve['config']['requests']} requests"}}
+                                     "workload": f"serve_mixed, {serve['config']['requests']} requests, "
+                                                 "host-scheduled server"},
+            "serving_device_loop_p99_at_80pct": _p80_summary(serve_dev)}
+
+
+def _p80_summary(serve):
+    p80 = serve["load_sweep"][0]
+    return {"peak_mbps": serve["value"], "offered_mbps": p80["offered_mbps"], "achieved_mbps": p80["achieved_mbps"],
+            "p50_ms": p80["p50_ms"], "p99_ms": p80["p99_ms"], "p99_9_ms": p80["p99_9_ms"],
+            "p99_ms_bp_only": p80["p99_ms_bp_only"], "p99_ms_bp_osd": p80["p99_ms_bp_osd"], "target_p99_ms": 1.0,
+            "workload": f"serve_mixed, {serve['config']['requests']} requests, device-resident loop",
+            "iterations": serve["server"].get("iterations")}
 
 
 def spawn_ranks(n, argv):
@@ -1518,6 +1563,8 @@ def main():
     ap.add_argument("--serve-loads", type=float, nargs="*", default=None, help="offered loads (fractions of peak)")
     ap.add_argument("--serve-batch", type=int, default=16384, help="codewords per server launch")
     ap.add_argument("--serve-inflight", type=int, default=4, help="batches overlapping on the device")
+    ap.add_argument("--serve-loop", default="host", choices=["host", "device"],
+                    help="serving loop: host scheduler thread, or the device-resident graph loop")
     ap.add_argument("--mixed-codewords", type=int, default=100_000)
     ap.add_argument("--ofdm-frames", type=int, default=OFDM_FRAMES)
     ap.add_argument("--dvbs2-frames", type=int, default=DVBS2_FRAMES, help="codewords per long-code step")
