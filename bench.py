@@ -1326,9 +1326,10 @@ def run_serve(args, rank, world):
     srv.close()
     p80 = next((x for x in sweep if x["load"] == 0.8), sweep[-1])
     if device_loop:
-        # per loop iteration: admit, layout, sync + demod per profile, prepare, mixed BP, the OSD launches
-        # (warp kernel and three long-code classes), complete, publish
-        launches = int(_batches(st1) - _batches(st0)) * (2 + 2 * len(phys) + 2 + 4 + 2)
+        # every loop iteration: admit, publish; one that admitted requests also: layout, sync + demod per
+        # profile, prepare, mixed BP, the OSD launches (warp kernel and three long-code classes), complete
+        launches = (int(st1.iterations - st0.iterations) * 2
+                    + int(_batches(st1) - _batches(st0)) * (2 + 2 * len(phys) + 2 + 4))
     else:
         launches = int(st1.batches - st0.batches) * 3 + args.steps * iq_reqs * 2
     line = {"metric": "served info-bit Mbps (Poisson mixed-code + OFDM IQ requests), p50/p99/p99.9 latency",
@@ -1445,8 +1446,8 @@ def run_frame_pipeline_reference(args, rank, world):
 
 
 def _batches(st):
-    """Batches launched by the host-scheduled server, or iterations of the device loop."""
-    return st.batches if hasattr(st, "batches") else st.iterations
+    """Batches launched by the host-scheduled server, or device-loop iterations that admitted requests."""
+    return st.batches if hasattr(st, "batches") else st.busy_iterations
 
 
 # ------------------------------------------------------------- reference arm

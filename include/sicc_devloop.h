@@ -27,6 +27,8 @@
  *      pinned host memory;
  *   6. decides whether to go on: it stops when the host asks it to, after
  *      `idle_timeout_ms` without a request, or after 2^31 iterations.
+ * An iteration that admits nothing skips steps 2-5 (a conditional node), so an
+ * idle loop re-reads the ring about every 100 us.
  * The host only appends requests and reads completions; submit restarts the
  * loop if it has stopped.  Results of a codeword do not depend on what it is
  * batched with (the engine's guarantee).  Requests arriving while an
@@ -65,6 +67,7 @@ typedef struct sicc_devloop_stats_t {
     unsigned long long submitted, completed, iterations, busy_rejections, launches;
     unsigned long long codewords;    /* decoded by the loop */
     int running;                     /* the loop graph is on the device */
+    unsigned long long busy_iterations;  /* iterations that admitted a request (the others skip to publication) */
 } sicc_devloop_stats_t;
 
 SICC_API int sicc_devloop_create(const sicc_devloop_config_t* config, unsigned long long* out_handle);

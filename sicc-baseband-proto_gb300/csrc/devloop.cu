@@ -10,6 +10,9 @@
 //                    budgets and the completion ring has room, records them in
 //                    the admission table, publishes the ring head; waits a
 //                    bounded ~100 us for a request when the ring is empty;
+//                    sets the condition of the conditional (if) node that
+//                    holds the next four steps, so an iteration that admitted
+//                    nothing goes straight to publish_kernel;
 //   layout_kernel    one CTA per admitted request (grid-strided): copies its
 //                    input (LLRs, or IQ frames) from pinned host memory into the
 //                    batch, writes the per-codeword tables (code, protection,
@@ -27,6 +30,11 @@
 //                    advances the completion tail and sets the loop condition
 //                    (host stop flag, idle timeout, iteration cap).
 // The host side only fills the request ring and drains the completion ring.
+// An idle loop announces its end (`ended`) and then reads the ring's tail once
+// more; a submit appends, then reads `ended`, and launches the graph again
+// when the loop has gone (each side fences between its write and its read, so
+// at least one of them sees the other).  A poll that finds the graph finished
+// with requests still in the ring launches it again as well.
 #include "../../include/sicc_devloop.h"
 #include "engine_internal.h"
 #include "pipe_internal.h"
@@ -39,6 +47,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -56,6 +65,8 @@ struct alignas(16) ReqEntry {  // host -> device, one per request
     unsigned char* out;         // [codewords][k] information bits, the same kind of memory
     int kind, code_id, phy_id, count, protection, n, k, codewords, stride, pad;
 };
+
+static_assert(sizeof(ReqEntry) % 16 == 0, "ring entries are read as 16-byte words");
 
 struct PhyDev {  // a registered OFDM profile's device tables
     long long* frame_off;      // [max_frames] complex-sample offset of each admitted frame in the IQ buffer
@@ -80,22 +91,29 @@ struct alignas(128) HostSide {  // written by the host, read by the device (pinn
 struct alignas(128) DevSide {  // written by the device, read by the host (pinned)
     unsigned long long req_head;   // requests admitted
     unsigned long long cmp_tail;   // completions published
-    unsigned long long iterations, codewords;
-    int ended;                     // 1: stop flag, 2: idle timeout, 3: iteration cap
+    unsigned long long iterations, codewords, busy_iterations;
+    int ended;                     // 0: running, 1: stop flag, 2: idle timeout, 3: iteration cap
 };
 
 struct LoopState {  // device memory
-    unsigned long long head, cmp_tail, iterations, codewords;
+    unsigned long long head, cmp_tail, iterations, codewords, busy_iterations;
     unsigned long long last_active_ns, t_start_ns;
     int nreq, count;
-    int phy_frames[kMaxPhys];  // admitted frames of each profile
+    int in_chunks, out_chunks;  // copy chunks of the admitted requests
+    int phy_frames[kMaxPhys];   // admitted frames of each profile
 };
 
 struct Admitted {
     ReqEntry e;
     long long llr_off, info_off, iq_off;
     int first_cw, frame_base;
+    int in_chunk, out_chunk;  // its first input / output chunk in the iteration's chunk lists
 };
+
+// Host-memory copies are cut into chunks that every CTA of the layout and
+// completion grids shares, so one large request is not copied by one CTA.
+constexpr long long kInChunkFloats = 16384;  // 64 KB of LLRs or IQ samples
+constexpr long long kOutChunkBytes = 32768;  // information bits
 
 constexpr int kAdmitPolls = 50;            // ~2 us naps: an empty ring is watched ~100 us per iteration
 constexpr unsigned long long kIterationCap = 1ull << 31;
@@ -126,53 +144,99 @@ __device__ __forceinline__ void store_release_sys(unsigned long long* p, unsigne
     asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-__global__ void admit_kernel(const ReqEntry* __restrict__ ring, unsigned mask, const HostSide* hs, DevSide* ds,
-                             LoopState* st, Admitted* adm, int max_req, int max_cw, long long max_floats,
-                             unsigned cmp_capacity, int max_frames, long long max_iq)
+__device__ __forceinline__ void store_release_sys_int(int* p, int v)
 {
-    if (threadIdx.x != 0) return;
+    asm volatile("st.release.sys.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(32) admit_kernel(const ReqEntry* ring, unsigned mask,
+                                                   const HostSide* hs, DevSide* ds, LoopState* st, Admitted* adm,
+                                                   int max_req, int max_cw, long long max_floats, unsigned cmp_capacity,
+                                                   int max_frames, long long max_iq, cudaGraphConditionalHandle work)
+{
+    // one warp: the lanes fetch up to 32 ring entries at once (host memory is far), lane 0 takes them
+    // in order while they fit
+    __shared__ ReqEntry win[32];
+    const int lane = threadIdx.x;
     unsigned long long head = st->head;
-    unsigned long long tail = load_acquire_sys(&hs->req_tail);
-    for (int i = 0; i < kAdmitPolls && tail == head; ++i) {
-        __nanosleep(2000);
+    unsigned long long tail = 0;
+    if (lane == 0) {
         tail = load_acquire_sys(&hs->req_tail);
+        for (int i = 0; i < kAdmitPolls && tail == head; ++i) {
+            __nanosleep(2000);
+            tail = load_acquire_sys(&hs->req_tail);
+        }
     }
+    __syncwarp();  // lane 0's acquire of the tail orders the other lanes' reads of the entries below it
+    tail = __shfl_sync(0xffffffffu, tail, 0);
     const unsigned long long consumed = load_acquire_sys(&hs->cmp_head);
     const unsigned long long room = cmp_capacity - (st->cmp_tail - consumed);
-    int nreq = 0, cw = 0, frames = 0;
+    const unsigned long long limit = min(static_cast<unsigned long long>(max_req), room);
+    int nreq = 0, cw = 0, frames = 0, in_chunks = 0, out_chunks = 0;
     long long floats = 0, info = 0, iq = 0;
     int pf[kMaxPhys];
 #pragma unroll
     for (int p = 0; p < kMaxPhys; ++p) pf[p] = 0;
-    while (head < tail && nreq < max_req && static_cast<unsigned long long>(nreq) < room) {
-        const ReqEntry e = ring[head & mask];
-        const long long f = static_cast<long long>(e.codewords) * e.n;
-        const bool iq_req = e.kind == 1;
-        const long long samples = iq_req ? static_cast<long long>(e.count) * e.stride : 0;
-        // in submission order: a request that does not fit waits for the next iteration, and so do those after it
-        if (cw + e.codewords > max_cw || floats + f > max_floats) break;
-        if (iq_req && (frames + e.count > max_frames || iq + samples > max_iq)) break;
-        Admitted& a = adm[nreq];
-        a.e = e;
-        a.first_cw = cw;
-        a.llr_off = floats;
-        a.info_off = info;
-        a.iq_off = iq;
-        a.frame_base = iq_req ? pf[e.phy_id] : 0;
-        cw += e.codewords;
-        floats += f;
-        info += static_cast<long long>(e.codewords) * e.k;
-        if (iq_req) {
-            frames += e.count;
-            iq += samples;
-            pf[e.phy_id] += e.count;
+    bool full = false;
+    while (!full && head < tail && static_cast<unsigned long long>(nreq) < limit) {
+        const int avail = static_cast<int>(min(32ull, tail - head));
+        if (lane < avail) {  // published before the tail (acquire above); read past every cache
+            const uint4* src = reinterpret_cast<const uint4*>(ring + ((head + lane) & mask));
+            uint4* dst = reinterpret_cast<uint4*>(&win[lane]);
+#pragma unroll
+            for (int q = 0; q < static_cast<int>(sizeof(ReqEntry) / 16); ++q) dst[q] = __ldcv(src + q);
         }
-        ++nreq;
-        ++head;
+        __syncwarp();
+        if (lane == 0) {
+            for (int j = 0; j < avail && static_cast<unsigned long long>(nreq) < limit; ++j) {
+                const ReqEntry& e = win[j];
+                const long long f = static_cast<long long>(e.codewords) * e.n;
+                const bool iq_req = e.kind == 1;
+                const long long samples = iq_req ? static_cast<long long>(e.count) * e.stride : 0;
+                // in submission order: a request that does not fit waits for the next iteration, and so
+                // do those after it
+                if (cw + e.codewords > max_cw || floats + f > max_floats ||
+                    (iq_req && (frames + e.count > max_frames || iq + samples > max_iq))) {
+                    full = true;
+                    break;
+                }
+                Admitted& a = adm[nreq];
+                a.e = e;
+                a.first_cw = cw;
+                a.llr_off = floats;
+                a.info_off = info;
+                a.iq_off = iq;
+                a.frame_base = iq_req ? pf[e.phy_id] : 0;
+                a.in_chunk = in_chunks;
+                a.out_chunk = out_chunks;
+                const long long in_floats = iq_req ? 2 * samples : f;
+                in_chunks += static_cast<int>((in_floats + kInChunkFloats - 1) / kInChunkFloats);
+                out_chunks +=
+                    static_cast<int>((static_cast<long long>(e.codewords) * e.k + kOutChunkBytes - 1) / kOutChunkBytes);
+                cw += e.codewords;
+                floats += f;
+                // each request's information bits and IQ samples start 16-byte aligned (whole 16-byte copies)
+                info += (static_cast<long long>(e.codewords) * e.k + 15) & ~15ll;
+                if (iq_req) {
+                    frames += e.count;
+                    iq += (samples + 1) & ~1ll;
+                    pf[e.phy_id] += e.count;
+                }
+                ++nreq;
+                ++head;
+            }
+        }
+        head = __shfl_sync(0xffffffffu, head, 0);
+        nreq = __shfl_sync(0xffffffffu, nreq, 0);
+        full = __shfl_sync(0xffffffffu, full ? 1 : 0, 0) != 0;
+        __syncwarp();  // the window is rewritten by the next fetch
     }
+    if (lane != 0) return;
     st->head = head;
     st->nreq = nreq;
     st->count = cw;
+    st->in_chunks = in_chunks;
+    st->out_chunks = out_chunks;
 #pragma unroll
     for (int p = 0; p < kMaxPhys; ++p) st->phy_frames[p] = pf[p];
     const unsigned long long now = globaltimer_ns();
@@ -180,34 +244,81 @@ __global__ void admit_kernel(const ReqEntry* __restrict__ ring, unsigned mask, c
     st->t_start_ns = now;
     __threadfence_system();
     store_release_sys(&ds->req_head, head);
+    cudaGraphSetConditional(work, nreq > 0 ? 1u : 0u);  // an empty iteration skips to publication
 }
 
-__device__ __forceinline__ void copy_floats(const float* __restrict__ src, float* __restrict__ dst, long long total)
+// The admitted request whose chunk list holds chunk g: the last r with first(r) <= g.
+template <class F>
+__device__ __forceinline__ int owner_of(int g, int nreq, F first)
 {
-    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0 && (total & 3) == 0) {
-        const float4* s4 = reinterpret_cast<const float4*>(src);
-        float4* d4 = reinterpret_cast<float4*>(dst);
-        for (long long i = threadIdx.x; i < (total >> 2); i += blockDim.x) d4[i] = s4[i];
+    int lo = 0, hi = nreq - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (first(mid) <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// dst[0, count) = src[0, count) by one CTA, four 16-byte accesses in flight per thread when both
+// ends are 16-byte aligned (host memory is far: the loads must overlap)
+__device__ __forceinline__ void copy_bytes(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst,
+                                           long long count)
+{
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0) {
+        const long long n16 = count >> 4;
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
+        uint4* d4 = reinterpret_cast<uint4*>(dst);
+        const long long step = blockDim.x;
+        long long i = threadIdx.x;
+        for (; i + 3 * step < n16; i += 4 * step) {
+            const uint4 a = s4[i], b = s4[i + step], c = s4[i + 2 * step], d = s4[i + 3 * step];
+            d4[i] = a;
+            d4[i + step] = b;
+            d4[i + 2 * step] = c;
+            d4[i + 3 * step] = d;
+        }
+        for (; i < n16; i += step) d4[i] = s4[i];
+        for (long long j = (n16 << 4) + threadIdx.x; j < count; j += step) dst[j] = src[j];
     } else {
-        for (long long i = threadIdx.x; i < total; i += blockDim.x) dst[i] = src[i];
+        for (long long j = threadIdx.x; j < count; j += blockDim.x) dst[j] = src[j];
     }
 }
 
+// One iteration's layout: the admitted requests' inputs are copied chunk by chunk
+// (all CTAs share every request), then each request's codeword and frame tables
+// are written; CTA 0 also zeroes every profile's frame-search tickets and the
+// completion counters.
 __global__ void layout_kernel(const LoopState* st, const Admitted* __restrict__ adm, float* __restrict__ llr,
                               float* __restrict__ iq, const PhyDev* __restrict__ phys, int nphys,
                               uint8_t* __restrict__ code_of, uint8_t* __restrict__ protect,
-                              long long* __restrict__ llr_off, long long* __restrict__ info_off)
+                              long long* __restrict__ llr_off, long long* __restrict__ info_off,
+                              int* __restrict__ chunks_done)
 {
-    if (blockIdx.x == 0)  // every profile's frame search starts from zero tickets
+    __shared__ int s_r;
+    const int nreq = st->nreq;
+    if (blockIdx.x == 0) {
         for (int p = 0; p < nphys; ++p)
             for (int i = threadIdx.x; i < phys[p].ticket_ints; i += blockDim.x) phys[p].ticket[i] = 0;
-    const int nreq = st->nreq;
+        for (int r = threadIdx.x; r < nreq; r += blockDim.x) chunks_done[r] = 0;
+    }
+    const int total = st->in_chunks;
+    for (int g = blockIdx.x; g < total; g += gridDim.x) {
+        if (threadIdx.x == 0) s_r = owner_of(g, nreq, [&](int r) { return adm[r].in_chunk; });
+        __syncthreads();
+        const Admitted& a = adm[s_r];
+        const long long c = g - a.in_chunk;
+        const long long floats =
+            a.e.kind == 0 ? static_cast<long long>(a.e.codewords) * a.e.n : 2 * static_cast<long long>(a.e.count) * a.e.stride;
+        const long long lo = c * kInChunkFloats, hi = min(floats, lo + kInChunkFloats);
+        float* dst = a.e.kind == 0 ? llr + a.llr_off : iq + 2 * a.iq_off;
+        copy_bytes(reinterpret_cast<const unsigned char*>(a.e.in + lo), reinterpret_cast<unsigned char*>(dst + lo),
+                   (hi - lo) * static_cast<long long>(sizeof(float)));
+        __syncthreads();  // s_r is rewritten by the next chunk
+    }
     for (int r = blockIdx.x; r < nreq; r += gridDim.x) {
-        const Admitted a = adm[r];
-        if (a.e.kind == 0) {
-            copy_floats(a.e.in, llr + a.llr_off, static_cast<long long>(a.e.codewords) * a.e.n);
-        } else {
-            copy_floats(a.e.in, iq + 2 * a.iq_off, 2 * static_cast<long long>(a.e.count) * a.e.stride);
+        const Admitted& a = adm[r];
+        if (a.e.kind == 1) {
             const PhyDev ph = phys[a.e.phy_id];
             for (int f = threadIdx.x; f < a.e.count; f += blockDim.x) {
                 ph.frame_off[a.frame_base + f] = a.iq_off + static_cast<long long>(f) * a.e.stride;
@@ -224,46 +335,62 @@ __global__ void layout_kernel(const LoopState* st, const Admitted* __restrict__ 
     }
 }
 
+// One iteration's completion: the information bits go to the requests' host
+// buffers chunk by chunk (all CTAs share every request); the CTA that finishes
+// a request's last chunk counts its BP failures and OSD codewords and writes
+// its completion record.
 __global__ void complete_kernel(const LoopState* st, const Admitted* __restrict__ adm,
                                 const uint8_t* __restrict__ info, const uint8_t* __restrict__ success,
-                                const uint8_t* __restrict__ used_osd, CmpEntry* ring, unsigned mask)
+                                const uint8_t* __restrict__ used_osd, CmpEntry* ring, unsigned mask,
+                                int* __restrict__ chunks_done)
 {
-    __shared__ int s_failed, s_osd;
+    __shared__ int s_r, s_last, s_failed, s_osd;
     const int nreq = st->nreq;
-    for (int r = blockIdx.x; r < nreq; r += gridDim.x) {
-        const Admitted a = adm[r];
+    const int total = st->out_chunks;
+    for (int g = blockIdx.x; g < total; g += gridDim.x) {
         if (threadIdx.x == 0) {
+            s_r = owner_of(g, nreq, [&](int r) { return adm[r].out_chunk; });
             s_failed = 0;
             s_osd = 0;
         }
         __syncthreads();
+        const int r = s_r;
+        const Admitted& a = adm[r];
         const long long bytes = static_cast<long long>(a.e.codewords) * a.e.k;
-        const uint8_t* src = info + a.info_off;
-        for (long long i = threadIdx.x; i < bytes; i += blockDim.x) a.e.out[i] = src[i];
-        int failed = 0, osd = 0;
-        for (int c = threadIdx.x; c < a.e.codewords; c += blockDim.x) {
-            const int w = a.first_cw + c;
-            const int u = used_osd[w], ok = success[w];
-            osd += u;
-            failed += (!u && !ok) ? 1 : 0;
-        }
-        if (failed) atomicAdd(&s_failed, failed);
-        if (osd) atomicAdd(&s_osd, osd);
-        __threadfence_system();  // the information bits reach host memory before the record
+        const int nchunks = static_cast<int>((bytes + kOutChunkBytes - 1) / kOutChunkBytes);
+        const long long lo = static_cast<long long>(g - a.out_chunk) * kOutChunkBytes;
+        const long long hi = min(bytes, lo + kOutChunkBytes);
+        copy_bytes(info + a.info_off + lo, a.e.out + lo, hi - lo);
+        __threadfence_system();  // this CTA's bits reach host memory before the request's record
         __syncthreads();
-        if (threadIdx.x == 0) {
-            CmpEntry c{};
-            c.id = a.e.id;
-            c.tag = a.e.tag;
-            c.t_start_ns = st->t_start_ns;
-            c.t_done_ns = globaltimer_ns();
-            c.codewords = a.e.codewords;
-            c.failed = s_failed;
-            c.osd = s_osd;
-            c.status = 0;
-            ring[(st->cmp_tail + r) & mask] = c;
-        }
+        if (threadIdx.x == 0) s_last = atomicAdd(&chunks_done[r], 1) == nchunks - 1;
         __syncthreads();
+        if (s_last) {
+            __threadfence();  // the other CTAs' chunks of this request are complete (their fences came first)
+            int failed = 0, osd = 0;
+            for (int c = threadIdx.x; c < a.e.codewords; c += blockDim.x) {
+                const int w = a.first_cw + c;
+                const int u = used_osd[w], ok = success[w];
+                osd += u;
+                failed += (!u && !ok) ? 1 : 0;
+            }
+            if (failed) atomicAdd(&s_failed, failed);
+            if (osd) atomicAdd(&s_osd, osd);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                CmpEntry c{};
+                c.id = a.e.id;
+                c.tag = a.e.tag;
+                c.t_start_ns = st->t_start_ns;
+                c.t_done_ns = globaltimer_ns();
+                c.codewords = a.e.codewords;
+                c.failed = s_failed;
+                c.osd = s_osd;
+                c.status = 0;
+                ring[(st->cmp_tail + r) & mask] = c;
+            }
+        }
+        __syncthreads();  // the shared scalars are rewritten by the next chunk
     }
 }
 
@@ -274,6 +401,8 @@ __global__ void publish_kernel(LoopState* st, const HostSide* hs, DevSide* ds, c
     st->cmp_tail += static_cast<unsigned long long>(st->nreq);
     st->iterations += 1;
     st->codewords += static_cast<unsigned long long>(st->count);
+    st->busy_iterations += st->nreq > 0 ? 1ull : 0ull;
+    ds->busy_iterations = st->busy_iterations;
     ds->iterations = st->iterations;
     ds->codewords = st->codewords;
     store_release_sys(&ds->cmp_tail, st->cmp_tail);
@@ -282,8 +411,17 @@ __global__ void publish_kernel(LoopState* st, const HostSide* hs, DevSide* ds, c
     else if (st->nreq == 0 && globaltimer_ns() - st->last_active_ns > idle_ns) reason = 2;
     else if (st->iterations >= kIterationCap) reason = 3;
     if (reason) {
-        ds->ended = reason;
-        __threadfence_system();
+        // Announce the end, then read the ring's tail once more.  The host appends a request, then
+        // reads `ended` (each side with a full fence between its write and its read), so either the
+        // host sees the announcement and launches the loop again, or this read sees the request and
+        // an idle loop carries on.
+        store_release_sys_int(&ds->ended, reason);
+        asm volatile("fence.sc.sys;" ::: "memory");
+        if (reason == 2 && load_acquire_sys(&hs->req_tail) != st->head) {
+            store_release_sys_int(&ds->ended, 0);
+            st->last_active_ns = globaltimer_ns();
+            reason = 0;
+        }
     }
     cudaGraphSetConditional(cond, reason ? 0u : 1u);
 }
@@ -361,15 +499,17 @@ struct Loop {
     Dev<float> llr;
     Dev<uint8_t> info, code_of, protect, success, used, iters;
     Dev<long long> llr_off, info_off;
+    Dev<int> chunks_done;                // [max_req] finished output chunks of each admitted request
     Dev<float> iqbuf;                    // [max_batch_iq_samples] complex samples
     std::vector<std::unique_ptr<PhyHost>> phys;
     Dev<PhyDev> d_phys;
-    int info_cap = 0;
+    long long info_cap = 0;
     // the graph
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    bool recorded = false, launched = false;
+    bool recorded = false;
+    std::atomic<bool> launched{false};  // written under mu; poll reads it
     // host bookkeeping
     unsigned long long next_id = 1, req_tail = 0, cmp_head = 0;
     std::map<unsigned long long, Pending> pending;
@@ -377,7 +517,9 @@ struct Loop {
     Clock::time_point clock_base;
     sicc_devloop_stats_t stats{};
     std::mutex mu;      // submit side
-    std::mutex poll_mu; // poll side
+    std::mutex poll_mu; // poll side (one poller at a time)
+    std::mutex pending_mu;  // pending and completed: held briefly by submit and poll
+    unsigned long long completed = 0;
 
     ~Loop()
     {
@@ -402,7 +544,7 @@ struct Loop {
         if (engine_bounds(engine, &n_max, &k_max) != CUDA_OSD_STATUS_OK) throw std::runtime_error(last_error());
         if (engine_prepare_capture(engine, cfg.max_batch_codewords) != CUDA_OSD_STATUS_OK)
             throw std::runtime_error(last_error());
-        info_cap = cfg.max_batch_codewords * k_max;
+        info_cap = static_cast<long long>(cfg.max_batch_codewords) * k_max + 16ll * max_req;  // + per-request alignment
         info.alloc(static_cast<size_t>(info_cap));
         std::vector<PhyDev> pd;
         for (const auto& ph : phys) {
@@ -419,48 +561,73 @@ struct Loop {
             check_cuda(cudaMemcpy(d_phys.p, pd.data(), pd.size() * sizeof(PhyDev), cudaMemcpyHostToDevice),
                        "upload profiles");
         check_cuda(cudaGraphCreate(&graph, 0), "cudaGraphCreate");
-        cudaGraphConditionalHandle cond;
-        check_cuda(cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault),
-                   "cudaGraphConditionalHandleCreate");
+        // graph: while (loop) { admit; if (admitted) { layout; demod; decode; complete } publish }
+        cudaGraphConditionalHandle loop_cond, work_cond;
+        check_cuda(cudaGraphConditionalHandleCreate(&loop_cond, graph, 1, cudaGraphCondAssignDefault),
+                   "cudaGraphConditionalHandleCreate(loop)");
         cudaGraphNodeParams p{};
         p.type = cudaGraphNodeTypeConditional;
-        p.conditional.handle = cond;
+        p.conditional.handle = loop_cond;
         p.conditional.type = cudaGraphCondTypeWhile;
         p.conditional.size = 1;
         cudaGraphNode_t node;
         check_cuda(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &p), "cudaGraphAddNode(while)");
         cudaGraph_t body = p.conditional.phGraph_out[0];
+        check_cuda(cudaGraphConditionalHandleCreate(&work_cond, body, 0, cudaGraphCondAssignDefault),
+                   "cudaGraphConditionalHandleCreate(work)");
+        auto end_capture = [&](const char* what) {
+            cudaGraph_t out = nullptr;
+            check_cuda(cudaStreamEndCapture(stream, &out), what);
+        };
+        auto abandon = [&](const std::string& why) {
+            cudaGraph_t dummy = nullptr;
+            cudaStreamEndCapture(stream, &dummy);
+            throw std::runtime_error(why);
+        };
+        // 1. admission, the body's first node
         check_cuda(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
-                   "cudaStreamBeginCaptureToGraph");
-        const int sms = device_sm_count();
+                   "cudaStreamBeginCaptureToGraph(admit)");
         admit_kernel<<<1, 32, 0, stream>>>(ring.d, mask, hs.d, ds.d, st.p, adm.p, max_req, cfg.max_batch_codewords,
                                             cfg.max_batch_llr_floats, mask + 1, cfg.max_batch_frames,
-                                            cfg.max_batch_iq_samples);
+                                            cfg.max_batch_iq_samples, work_cond);
+        end_capture("cudaStreamEndCapture(admit)");
+        cudaGraphNode_t admit_node = nullptr;
+        size_t nodes = 1;
+        check_cuda(cudaGraphGetNodes(body, &admit_node, &nodes), "cudaGraphGetNodes(admit)");
+        if (nodes != 1 || !admit_node) throw std::runtime_error("recording the loop: admission is not one node");
+        // 2. the iteration's work, run when admit_kernel admitted a request
+        cudaGraphNodeParams ip{};
+        ip.type = cudaGraphNodeTypeConditional;
+        ip.conditional.handle = work_cond;
+        ip.conditional.type = cudaGraphCondTypeIf;
+        ip.conditional.size = 1;
+        cudaGraphNode_t if_node;
+        check_cuda(cudaGraphAddNode(&if_node, body, &admit_node, nullptr, 1, &ip), "cudaGraphAddNode(if)");
+        cudaGraph_t work = ip.conditional.phGraph_out[0];
+        check_cuda(cudaStreamBeginCaptureToGraph(stream, work, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+                   "cudaStreamBeginCaptureToGraph(work)");
+        const int sms = device_sm_count();
         layout_kernel<<<2 * sms, 256, 0, stream>>>(st.p, adm.p, llr.p, iqbuf.p, d_phys.p, static_cast<int>(phys.size()),
-                                                    code_of.p, protect.p, llr_off.p, info_off.p);
+                                                    code_of.p, protect.p, llr_off.p, info_off.p, chunks_done.p);
         for (size_t q = 0; q < phys.size(); ++q) {  // each profile's admitted frames: search + demodulation
             const PhyHost& ph = *phys[q];
             if (pipe_gather_counted(ph.pipe, iqbuf.p, ph.frame_off.p, ph.stride, cfg.max_batch_frames,
                                     &st.p->phy_frames[q], llr.p, ph.llr_frame_off.p, ph.sync.p, ph.scratch.p,
-                                    ph.scratch_bytes, stream) != CUDA_OSD_STATUS_OK) {
-                const std::string why = last_error();
-                cudaGraph_t dummy;
-                cudaStreamEndCapture(stream, &dummy);
-                throw std::runtime_error("recording the loop's demodulation: " + why);
-            }
+                                    ph.scratch_bytes, stream) != CUDA_OSD_STATUS_OK)
+                abandon(std::string("recording the loop's demodulation: ") + last_error());
         }
         const int rc = engine_decode(engine, cfg.max_batch_codewords, code_of.p, protect.p, llr.p, llr_off.p, info.p,
                                      info_off.p, success.p, used.p, iters.p, stream, nullptr, &st.p->count);
-        if (rc != CUDA_OSD_STATUS_OK) {
-            cudaGraph_t dummy;
-            cudaStreamEndCapture(stream, &dummy);
-            throw std::runtime_error(std::string("recording the loop's decode: ") + last_error());
-        }
-        complete_kernel<<<2 * sms, 256, 0, stream>>>(st.p, adm.p, info.p, success.p, used.p, cring.d, mask);
-        publish_kernel<<<1, 1, 0, stream>>>(st.p, hs.d, ds.d, cond,
+        if (rc != CUDA_OSD_STATUS_OK) abandon(std::string("recording the loop's decode: ") + last_error());
+        complete_kernel<<<2 * sms, 256, 0, stream>>>(st.p, adm.p, info.p, success.p, used.p, cring.d, mask,
+                                                      chunks_done.p);
+        end_capture("cudaStreamEndCapture(work)");
+        // 3. publication, after the work node
+        check_cuda(cudaStreamBeginCaptureToGraph(stream, body, &if_node, nullptr, 1, cudaStreamCaptureModeRelaxed),
+                   "cudaStreamBeginCaptureToGraph(publish)");
+        publish_kernel<<<1, 1, 0, stream>>>(st.p, hs.d, ds.d, loop_cond,
                                             static_cast<unsigned long long>(cfg.idle_timeout_ms) * 1000000ull);
-        cudaGraph_t out = nullptr;
-        check_cuda(cudaStreamEndCapture(stream, &out), "cudaStreamEndCapture(loop body)");
+        end_capture("cudaStreamEndCapture(publish)");
         check_cuda(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate(loop)");
         recorded = true;
     }
@@ -482,10 +649,23 @@ struct Loop {
         return clock_base + std::chrono::nanoseconds(static_cast<long long>(dev_ns) - clock_offset_ns);
     }
 
-    // Launches the loop if it is not running (the caller holds mu).
+    int ended() const { return reinterpret_cast<const std::atomic<int>*>(&ds.h->ended)->load(std::memory_order_acquire); }
+
+    // Launches the loop if it is not running (the caller holds mu).  Called after a request was
+    // appended: a loop that has announced its end (publish_kernel) either took the request back
+    // and carries on, or finishes and is launched again here.
     void ensure_running()
     {
-        if (launched && !graph_done()) return;
+        std::atomic_thread_fence(std::memory_order_seq_cst);  // the tail is out before `ended` is read
+        if (launched) {
+            if (ended() == 0) return;  // running: it admits the request (no stream query on this path)
+            const auto deadline = Clock::now() + std::chrono::seconds(10);
+            while (!graph_done()) {
+                if (ended() == 0) return;  // running, and it will admit the request
+                if (Clock::now() > deadline) throw std::runtime_error("the device loop did not finish ending");
+                std::this_thread::sleep_for(std::chrono::microseconds(2));
+            }
+        }
         if (!recorded) {
             record();
             calibrate();
@@ -598,6 +778,7 @@ int sicc_devloop_create(const sicc_devloop_config_t* config, unsigned long long*
             b->alloc(static_cast<size_t>(c.max_batch_codewords));
         L->llr_off.alloc(static_cast<size_t>(c.max_batch_codewords));
         L->info_off.alloc(static_cast<size_t>(c.max_batch_codewords));
+        L->chunks_done.alloc(static_cast<size_t>(L->max_req));
         L->iqbuf.alloc(2 * static_cast<size_t>(std::max<long long>(c.max_batch_iq_samples, 1)));
         check_cuda(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking), "cudaStreamCreate(loop)");
         std::lock_guard<std::mutex> lock(g_mu);
@@ -765,7 +946,7 @@ int sicc_devloop_submit(unsigned long long handle, const sicc_request_t* request
         e.codewords = codewords;
         e.stride = stride;
         {
-            std::lock_guard<std::mutex> plock(L->poll_mu);
+            std::lock_guard<std::mutex> plock(L->pending_mu);
             L->pending[id] = Pending{Clock::now()};
         }
         L->ring.h[L->req_tail & L->mask] = e;
@@ -786,8 +967,11 @@ int sicc_devloop_poll(unsigned long long handle, int max, sicc_completion_t* out
         *out_count = 0;
         std::lock_guard<std::mutex> plock(L->poll_mu);
         const auto deadline = Clock::now() + std::chrono::microseconds(std::max(wait_us, 0));
+        unsigned spins = 0;
         for (;;) {
             const unsigned long long tail = load_acquire(&L->ds.h->cmp_tail);
+            std::unique_lock<std::mutex> pend(L->pending_mu, std::defer_lock);
+            if (L->cmp_head < tail) pend.lock();
             while (L->cmp_head < tail && *out_count < max) {
                 const CmpEntry c = L->cring.h[L->cmp_head & L->mask];
                 ++L->cmp_head;
@@ -808,10 +992,19 @@ int sicc_devloop_poll(unsigned long long handle, int max, sicc_completion_t* out
                     L->pending.erase(it);
                 }
                 o.batch_gpu_us = static_cast<double>(c.t_done_ns - c.t_start_ns) * 1e-3;
-                ++L->stats.completed;
+                ++L->completed;
             }
+            if (pend.owns_lock()) pend.unlock();
             store_release(&L->hs.h->cmp_head, L->cmp_head);
-            if (*out_count > 0 || Clock::now() >= deadline) break;
+            if (*out_count > 0) break;
+            // nothing to report: a loop that failed is reported, and one that ended with requests
+            // still in its ring is launched again (when no submit holds the loop's lock)
+            if ((++spins & 127) == 0 && L->launched.load() && L->graph_done() &&
+                load_acquire(&L->hs.h->req_tail) != load_acquire(&L->ds.h->req_head)) {
+                std::unique_lock<std::mutex> lock(L->mu, std::try_to_lock);
+                if (lock.owns_lock()) L->ensure_running();
+            }
+            if (Clock::now() >= deadline) break;
             std::this_thread::sleep_for(std::chrono::microseconds(5));
         }
         return CUDA_OSD_STATUS_OK;
@@ -825,8 +1018,13 @@ int sicc_devloop_get_stats(unsigned long long handle, sicc_devloop_stats_t* out)
         if (!out) throw InvalidArgument("null argument");
         std::lock_guard<std::mutex> lock(L->mu);
         *out = L->stats;
+        {
+            std::lock_guard<std::mutex> plock(L->pending_mu);
+            out->completed = L->completed;
+        }
         out->iterations = load_acquire(&L->ds.h->iterations);
         out->codewords = load_acquire(&L->ds.h->codewords);
+        out->busy_iterations = load_acquire(&L->ds.h->busy_iterations);
         out->running = (L->launched && !L->graph_done()) ? 1 : 0;
         return CUDA_OSD_STATUS_OK;
     });
@@ -874,7 +1072,12 @@ int sicc_devloop_replay(unsigned long long handle, const sicc_request_t* request
                     else early.emplace(buf[i].request_id, buf[i]);
                 }
                 if (got == 0 && give_up()) {
-                    error = "no completion for 30 s";
+                    sicc_devloop_stats_t s{};
+                    sicc_devloop_get_stats(handle, &s);
+                    error = "no completion for 30 s (requests submitted " + std::to_string(s.submitted) +
+                            ", admitted " + std::to_string(load_acquire(&L->ds.h->req_head)) + ", completed " +
+                            std::to_string(s.completed) + "; loop iterations " + std::to_string(s.iterations) +
+                            ", running " + std::to_string(s.running) + ", ended " + std::to_string(L->ended()) + ")";
                     failed.store(true);
                 }
             }

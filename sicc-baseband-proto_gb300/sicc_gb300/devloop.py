@@ -2,10 +2,12 @@
 
 The loop is one CUDA graph repeated on the GPU by a conditional node: each
 iteration admits requests from a request ring in pinned host memory (within
-its codeword and LLR budgets), lays them out, decodes them with the mixed-code
-engine (BP, then OSD for failures of requests with protection 1), copies the
-information bits back to the requests' pinned host buffers and publishes
-completions.  The host only appends requests and drains completions.
+its codeword, LLR, frame and IQ budgets), lays them out, demodulates the OFDM
+IQ requests, decodes every codeword with the mixed-code engine (BP, then OSD
+for failures of requests with protection 1), copies the information bits back
+to the requests' pinned host buffers and publishes completions; an iteration
+that admits nothing skips straight to publication.  The host only appends
+requests and drains completions.
 
 Request buffers must be page-locked (e.g. ``torch.empty(..., pin_memory=True)``
 viewed as NumPy); ``pinned`` allocates such arrays.
@@ -33,7 +35,7 @@ class DevLoopConfig(C.Structure):
 class DevLoopStats(C.Structure):
     _fields_ = [("submitted", C.c_ulonglong), ("completed", C.c_ulonglong), ("iterations", C.c_ulonglong),
                 ("busy_rejections", C.c_ulonglong), ("launches", C.c_ulonglong), ("codewords", C.c_ulonglong),
-                ("running", C.c_int)]
+                ("running", C.c_int), ("busy_iterations", C.c_ulonglong)]
 
 
 _SIGS = {

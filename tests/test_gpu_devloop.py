@@ -195,3 +195,35 @@ def test_device_loop_iq_requests_match_pipeline_then_engine(cuda):
     from sicc_gb300.pipeline import wait_timeouts
     assert wait_timeouts() == 0
     lp.close()
+
+
+def test_device_loop_serves_requests_arriving_as_it_goes_idle(cuda, oracle):
+    """With a 1 ms idle timeout and gaps of 0-3 ms between requests, many requests arrive while the loop
+    is deciding to end: each one is served (by the running loop or by a relaunch) and none is left behind."""
+    c = codes.short_code()
+    lp = _loop([c], max_batch_codewords=64, max_batch_llr_floats=64 * 128, ring_requests=64, idle_timeout_ms=1)
+    lp.start()
+    rng = np.random.default_rng(5)
+    llr = _pinned_llrs(c, 8, 2.5, 91)
+    want = _expected(oracle, c, llr, 1)
+    outs, ids, got = [], set(), {}
+    for r in range(150):
+        req, x, out = lp.request(0, llr, protection=1, tag=r)
+        rid = lp.submit_request(req, keep=(x, out))
+        assert rid is not None  # completions are drained below, so the rings never fill
+        outs.append(out)
+        ids.add(rid)
+        time.sleep(float(rng.uniform(0.0, 0.003)))
+        for d in lp.poll(wait_us=0):
+            got[d.request_id] = d
+    t0 = time.time()
+    while len(got) < len(ids) and time.time() - t0 < 30:
+        for d in lp.poll(wait_us=100000):
+            got[d.request_id] = d
+    assert set(got) == ids
+    st = lp.stats()
+    assert st.launches >= 2  # the loop did end and start again along the way
+    assert st.busy_iterations <= st.iterations and st.busy_iterations >= 1
+    for out in outs:
+        assert np.array_equal(out, want)
+    lp.close()
