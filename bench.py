@@ -1221,12 +1221,12 @@ def run_serve(args, rank, world):
 
     device_loop = getattr(args, "serve_loop", "host") == "device"
     if device_loop:
-        # the device-resident loop: one iteration holds up to serve_batch codewords (their LLRs: up to 2048
-        # floats each), 17 x 16 frames of IQ; the rest of the 40 GB budget is not needed by this mix
+        # the device-resident loop: serve_inflight lanes (batches decoded side by side), one lane iteration
+        # holds up to serve_batch codewords (their LLRs: up to 2048 floats each) and 17 x 16 frames of IQ
         from sicc_gb300.devloop import DevLoop
         srv = DevLoop(max_batch_codewords=args.serve_batch, max_batch_llr_floats=args.serve_batch * 2048,
                       ring_requests=4096, idle_timeout_ms=2000, max_batch_frames=272,
-                      max_batch_iq_samples=272 * stride)
+                      max_batch_iq_samples=272 * stride, lanes=args.serve_inflight)
     else:
         srv = Server(hbm_budget_bytes=40 << 30, max_batch_codewords=args.serve_batch,
                      max_inflight_batches=args.serve_inflight, max_pending_requests=1 << 16)
@@ -1346,8 +1346,9 @@ def run_serve(args, rank, world):
                        "l2": "inputs copied host->device every request (pinned host pools)"},
             "fer": round(sum(fe) / cw_total, 5), "load_sweep": sweep,
             "p99_ms_at_80pct_load": p80["p99_ms"],
-            "server": ({"loop": "device-resident (one conditional CUDA graph; include/sicc_devloop.h)",
-                        "iterations": int(st.iterations), "graph_launches": int(st.launches),
+            "server": ({"loop": "device-resident (conditional CUDA graphs sharing the rings; include/sicc_devloop.h)",
+                        "lanes": int(st.lanes), "iterations": int(st.iterations),
+                        "busy_iterations": int(st.busy_iterations), "graph_launches": int(st.launches),
                         "busy_rejections": int(st.busy_rejections)} if device_loop else
                        {"loop": "host scheduler thread (include/sicc_server.h)", "batches": int(st.batches),
                         "busy_rejections": int(st.busy_rejections),

@@ -61,13 +61,16 @@ typedef struct sicc_devloop_config_t {
     int idle_timeout_ms;             /* the loop ends after this long without a request (>= 1) */
     int max_batch_frames;            /* OFDM frames one iteration demodulates (0: no IQ requests) */
     long long max_batch_iq_samples;  /* complex IQ samples one iteration holds */
+    int lanes;                       /* loop graphs sharing the rings, each with its own engine and
+                                        budgets (0: one; at most 8) */
 } sicc_devloop_config_t;
 
 typedef struct sicc_devloop_stats_t {
     unsigned long long submitted, completed, iterations, busy_rejections, launches;
     unsigned long long codewords;    /* decoded by the loop */
-    int running;                     /* the loop graph is on the device */
+    int running;                     /* lanes whose graph is on the device */
     unsigned long long busy_iterations;  /* iterations that admitted a request (the others skip to publication) */
+    int lanes;
 } sicc_devloop_stats_t;
 
 SICC_API int sicc_devloop_create(const sicc_devloop_config_t* config, unsigned long long* out_handle);

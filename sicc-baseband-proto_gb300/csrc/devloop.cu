@@ -1,40 +1,49 @@
 // Device-resident request loop (include/sicc_devloop.h).
 //
-// The loop is a CUDA graph: a conditional while-node whose body is recorded
-// once (stream capture into the node's body graph) and then repeated on the
-// device until its condition kernel clears the condition.  Body of one
-// iteration, in stream order:
-//   admit_kernel     one thread: reads the request ring's tail (host-written,
-//                    pinned, acquire load at system scope), takes requests in
-//                    order while they fit the iteration's codeword and LLR
-//                    budgets and the completion ring has room, records them in
-//                    the admission table, publishes the ring head; waits a
-//                    bounded ~100 us for a request when the ring is empty;
-//                    sets the condition of the conditional (if) node that
-//                    holds the next four steps, so an iteration that admitted
-//                    nothing goes straight to publish_kernel;
-//   layout_kernel    one CTA per admitted request (grid-strided): copies its
-//                    input (LLRs, or IQ frames) from pinned host memory into the
-//                    batch, writes the per-codeword tables (code, protection,
-//                    offsets) and each profile's frame tables; zeroes the frame
-//                    search's tickets;
+// The loop is one or more lanes, each a CUDA graph on its own stream: a
+// conditional while-node whose body is recorded once (stream capture into the
+// node's body graph) and then repeated on the device until its condition
+// kernel clears the condition.  The lanes share the request and completion
+// rings, so while one lane decodes a batch another admits the next (the
+// overlap a host scheduler gets from several batches in flight).  Body of one
+// lane iteration, in stream order:
+//   admit_kernel     one warp: takes the rings' admission lock (a try-lock in
+//                    device memory: a lane that finds it held never waits for
+//                    it, it only tries again within its bounded ~100 us of
+//                    polling and otherwise admits nothing), fetches up to 32
+//                    ring entries at a time from pinned host memory, takes
+//                    requests in order while they fit the lane's codeword, LLR,
+//                    frame and IQ budgets and the completion ring has room,
+//                    reserves their completion slots, publishes the ring head
+//                    and releases the lock; sets the condition of the
+//                    conditional (if) node that holds the next four steps, so
+//                    an iteration that admitted nothing goes straight to
+//                    publish_kernel;
+//   layout_kernel    copies the admitted inputs (LLRs, or IQ frames) from
+//                    pinned host memory into the lane's batch in 64 KB chunks
+//                    shared by every CTA, writes the per-codeword tables (code,
+//                    protection, offsets) and each profile's frame tables;
+//                    zeroes the frame search's tickets;
 //   sync + demod     per registered OFDM profile, the batched frame search and
 //                    demodulator over its admitted frames (device frame count),
 //                    writing their LLRs into the batch;
-//   engine decode    the mixed-code engine's prepare, BP and OSD launches, sized
-//                    for the largest batch, reading the batch size on the device;
-//   complete_kernel  one CTA per admitted request: copies its information bits
-//                    to the request's pinned host buffer, counts its BP
-//                    failures and OSD codewords, writes its completion record;
+//   engine decode    the lane's mixed-code engine: prepare, BP and OSD launches,
+//                    sized for the largest batch, reading the batch size on the
+//                    device;
+//   complete_kernel  copies the information bits to the requests' pinned host
+//                    buffers in chunks shared by every CTA; the CTA that ends a
+//                    request's last chunk writes its completion record into its
+//                    reserved slot, sequence number last;
 //   publish_kernel   one thread: makes the iteration's host writes visible,
-//                    advances the completion tail and sets the loop condition
+//                    updates the lane's counters and sets the loop condition
 //                    (host stop flag, idle timeout, iteration cap).
-// The host side only fills the request ring and drains the completion ring.
-// An idle loop announces its end (`ended`) and then reads the ring's tail once
-// more; a submit appends, then reads `ended`, and launches the graph again
-// when the loop has gone (each side fences between its write and its read, so
-// at least one of them sees the other).  A poll that finds the graph finished
-// with requests still in the ring launches it again as well.
+// The host side only fills the request ring and drains the completion ring,
+// taking each record whose sequence number is set (lanes finish out of order).
+// An idle lane announces its end (`ended`) and then reads the ring's tail once
+// more; a submit appends, then reads every lane's `ended`, and launches again
+// each lane that has gone (each side fences between its write and its read, so
+// at least one of them sees the other).  A poll that finds lanes finished with
+// requests still in the ring launches them again as well.
 #include "../../include/sicc_devloop.h"
 #include "engine_internal.h"
 #include "pipe_internal.h"
@@ -57,6 +66,7 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 constexpr int kMaxPhys = 8;
+constexpr int kMaxLanes = 8;
 
 struct alignas(16) ReqEntry {  // host -> device, one per request
     unsigned long long id, tag;
@@ -68,7 +78,7 @@ struct alignas(16) ReqEntry {  // host -> device, one per request
 
 static_assert(sizeof(ReqEntry) % 16 == 0, "ring entries are read as 16-byte words");
 
-struct PhyDev {  // a registered OFDM profile's device tables
+struct PhyDev {  // a registered OFDM profile's device tables in one lane
     long long* frame_off;      // [max_frames] complex-sample offset of each admitted frame in the IQ buffer
     long long* llr_frame_off;  // [max_frames] float offset of its LLRs in the batch
     int* ticket;               // the frame search's tickets, zero before each search
@@ -80,23 +90,34 @@ struct alignas(16) CmpEntry {  // device -> host, one per request
     unsigned long long id, tag;
     unsigned long long t_start_ns, t_done_ns;  // device clock: its iteration's decode start, publication
     int codewords, failed, osd, status;
+    unsigned long long seq;                    // slot + 1 once the record is complete (written last)
 };
 
 struct alignas(128) HostSide {  // written by the host, read by the device (pinned)
     unsigned long long req_tail;   // requests published
-    unsigned long long cmp_head;   // completions consumed
+    unsigned long long cmp_head;   // completion slots below this are consumed
     int stop;
 };
 
-struct alignas(128) DevSide {  // written by the device, read by the host (pinned)
-    unsigned long long req_head;   // requests admitted
-    unsigned long long cmp_tail;   // completions published
+struct alignas(128) DevSide {  // written by the admitting lane, read by the host (pinned)
+    unsigned long long req_head;      // requests admitted
+    unsigned long long cmp_reserved;  // completion slots reserved
+};
+
+struct alignas(128) LaneSide {  // written by one lane, read by the host (pinned)
     unsigned long long iterations, codewords, busy_iterations;
     int ended;                     // 0: running, 1: stop flag, 2: idle timeout, 3: iteration cap
 };
 
-struct LoopState {  // device memory
-    unsigned long long head, cmp_tail, iterations, codewords, busy_iterations;
+struct Shared {  // device memory, shared by the lanes (changed under the admission lock)
+    unsigned long long head;         // next request to admit
+    unsigned long long cmp_reserve;  // next completion slot
+    int lock;
+};
+
+struct LoopState {  // device memory, one per lane
+    unsigned long long cmp_base;  // the iteration's first completion slot
+    unsigned long long iterations, codewords, busy_iterations;
     unsigned long long last_active_ns, t_start_ns;
     int nreq, count;
     int in_chunks, out_chunks;  // copy chunks of the admitted requests
@@ -149,90 +170,120 @@ __device__ __forceinline__ void store_release_sys_int(int* p, int v)
     asm volatile("st.release.sys.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-__global__ void __launch_bounds__(32) admit_kernel(const ReqEntry* ring, unsigned mask,
-                                                   const HostSide* hs, DevSide* ds, LoopState* st, Admitted* adm,
-                                                   int max_req, int max_cw, long long max_floats, unsigned cmp_capacity,
+__device__ __forceinline__ unsigned long long shared_head(const Shared* sh)
+{
+    return *reinterpret_cast<const volatile unsigned long long*>(&sh->head);
+}
+
+__global__ void __launch_bounds__(32) admit_kernel(const ReqEntry* ring, unsigned mask, const HostSide* hs,
+                                                   DevSide* ds, Shared* sh, LoopState* st, Admitted* adm, int max_req,
+                                                   int max_cw, long long max_floats, unsigned cmp_capacity,
                                                    int max_frames, long long max_iq, cudaGraphConditionalHandle work)
 {
-    // one warp: the lanes fetch up to 32 ring entries at once (host memory is far), lane 0 takes them
-    // in order while they fit
+    // one warp: lane 0 takes the admission lock; the lanes fetch up to 32 ring entries at once (host
+    // memory is far), lane 0 takes them in order while they fit
     __shared__ ReqEntry win[32];
     const int lane = threadIdx.x;
-    unsigned long long head = st->head;
-    unsigned long long tail = 0;
+    int locked = 0;
     if (lane == 0) {
-        tail = load_acquire_sys(&hs->req_tail);
-        for (int i = 0; i < kAdmitPolls && tail == head; ++i) {
+        for (int i = 0;; ++i) {
+            const unsigned long long tail = load_acquire_sys(&hs->req_tail);
+            if (tail != shared_head(sh) && atomicCAS(&sh->lock, 0, 1) == 0) {
+                locked = 1;
+                break;
+            }
+            if (i >= kAdmitPolls) break;  // bounded: a held lock or an empty ring ends in an empty iteration
             __nanosleep(2000);
-            tail = load_acquire_sys(&hs->req_tail);
         }
+        __threadfence();  // the lock holder's view of the shared state follows the previous holder's writes
     }
-    __syncwarp();  // lane 0's acquire of the tail orders the other lanes' reads of the entries below it
-    tail = __shfl_sync(0xffffffffu, tail, 0);
-    const unsigned long long consumed = load_acquire_sys(&hs->cmp_head);
-    const unsigned long long room = cmp_capacity - (st->cmp_tail - consumed);
-    const unsigned long long limit = min(static_cast<unsigned long long>(max_req), room);
+    locked = __shfl_sync(0xffffffffu, locked, 0);
     int nreq = 0, cw = 0, frames = 0, in_chunks = 0, out_chunks = 0;
     long long floats = 0, info = 0, iq = 0;
     int pf[kMaxPhys];
 #pragma unroll
     for (int p = 0; p < kMaxPhys; ++p) pf[p] = 0;
-    bool full = false;
-    while (!full && head < tail && static_cast<unsigned long long>(nreq) < limit) {
-        const int avail = static_cast<int>(min(32ull, tail - head));
-        if (lane < avail) {  // published before the tail (acquire above); read past every cache
-            const uint4* src = reinterpret_cast<const uint4*>(ring + ((head + lane) & mask));
-            uint4* dst = reinterpret_cast<uint4*>(&win[lane]);
-#pragma unroll
-            for (int q = 0; q < static_cast<int>(sizeof(ReqEntry) / 16); ++q) dst[q] = __ldcv(src + q);
-        }
-        __syncwarp();
+    if (locked) {
+        unsigned long long head = 0, tail = 0, reserve = 0, consumed = 0;
         if (lane == 0) {
-            for (int j = 0; j < avail && static_cast<unsigned long long>(nreq) < limit; ++j) {
-                const ReqEntry& e = win[j];
-                const long long f = static_cast<long long>(e.codewords) * e.n;
-                const bool iq_req = e.kind == 1;
-                const long long samples = iq_req ? static_cast<long long>(e.count) * e.stride : 0;
-                // in submission order: a request that does not fit waits for the next iteration, and so
-                // do those after it
-                if (cw + e.codewords > max_cw || floats + f > max_floats ||
-                    (iq_req && (frames + e.count > max_frames || iq + samples > max_iq))) {
-                    full = true;
-                    break;
-                }
-                Admitted& a = adm[nreq];
-                a.e = e;
-                a.first_cw = cw;
-                a.llr_off = floats;
-                a.info_off = info;
-                a.iq_off = iq;
-                a.frame_base = iq_req ? pf[e.phy_id] : 0;
-                a.in_chunk = in_chunks;
-                a.out_chunk = out_chunks;
-                const long long in_floats = iq_req ? 2 * samples : f;
-                in_chunks += static_cast<int>((in_floats + kInChunkFloats - 1) / kInChunkFloats);
-                out_chunks +=
-                    static_cast<int>((static_cast<long long>(e.codewords) * e.k + kOutChunkBytes - 1) / kOutChunkBytes);
-                cw += e.codewords;
-                floats += f;
-                // each request's information bits and IQ samples start 16-byte aligned (whole 16-byte copies)
-                info += (static_cast<long long>(e.codewords) * e.k + 15) & ~15ll;
-                if (iq_req) {
-                    frames += e.count;
-                    iq += (samples + 1) & ~1ll;
-                    pf[e.phy_id] += e.count;
-                }
-                ++nreq;
-                ++head;
-            }
+            head = shared_head(sh);
+            reserve = *reinterpret_cast<const volatile unsigned long long*>(&sh->cmp_reserve);
+            tail = load_acquire_sys(&hs->req_tail);
+            consumed = load_acquire_sys(&hs->cmp_head);
         }
+        __syncwarp();  // lane 0's acquire of the tail orders the other lanes' reads of the entries below it
         head = __shfl_sync(0xffffffffu, head, 0);
-        nreq = __shfl_sync(0xffffffffu, nreq, 0);
-        full = __shfl_sync(0xffffffffu, full ? 1 : 0, 0) != 0;
-        __syncwarp();  // the window is rewritten by the next fetch
+        tail = __shfl_sync(0xffffffffu, tail, 0);
+        reserve = __shfl_sync(0xffffffffu, reserve, 0);
+        consumed = __shfl_sync(0xffffffffu, consumed, 0);
+        const unsigned long long room = cmp_capacity - (reserve - consumed);
+        const unsigned long long limit = min(static_cast<unsigned long long>(max_req), room);
+        bool full = false;
+        while (!full && head < tail && static_cast<unsigned long long>(nreq) < limit) {
+            const int avail = static_cast<int>(min(32ull, tail - head));
+            if (lane < avail) {  // published before the tail (acquire above); read past every cache
+                const uint4* src = reinterpret_cast<const uint4*>(ring + ((head + lane) & mask));
+                uint4* dst = reinterpret_cast<uint4*>(&win[lane]);
+#pragma unroll
+                for (int q = 0; q < static_cast<int>(sizeof(ReqEntry) / 16); ++q) dst[q] = __ldcv(src + q);
+            }
+            __syncwarp();
+            if (lane == 0) {
+                for (int j = 0; j < avail && static_cast<unsigned long long>(nreq) < limit; ++j) {
+                    const ReqEntry& e = win[j];
+                    const long long f = static_cast<long long>(e.codewords) * e.n;
+                    const bool iq_req = e.kind == 1;
+                    const long long samples = iq_req ? static_cast<long long>(e.count) * e.stride : 0;
+                    // in submission order: a request that does not fit waits for the next iteration, and so
+                    // do those after it
+                    if (cw + e.codewords > max_cw || floats + f > max_floats ||
+                        (iq_req && (frames + e.count > max_frames || iq + samples > max_iq))) {
+                        full = true;
+                        break;
+                    }
+                    Admitted& a = adm[nreq];
+                    a.e = e;
+                    a.first_cw = cw;
+                    a.llr_off = floats;
+                    a.info_off = info;
+                    a.iq_off = iq;
+                    a.frame_base = iq_req ? pf[e.phy_id] : 0;
+                    a.in_chunk = in_chunks;
+                    a.out_chunk = out_chunks;
+                    const long long in_floats = iq_req ? 2 * samples : f;
+                    in_chunks += static_cast<int>((in_floats + kInChunkFloats - 1) / kInChunkFloats);
+                    out_chunks += static_cast<int>((static_cast<long long>(e.codewords) * e.k + kOutChunkBytes - 1) /
+                                                   kOutChunkBytes);
+                    cw += e.codewords;
+                    floats += f;
+                    // each request's information bits and IQ samples start 16-byte aligned (whole 16-byte copies)
+                    info += (static_cast<long long>(e.codewords) * e.k + 15) & ~15ll;
+                    if (iq_req) {
+                        frames += e.count;
+                        iq += (samples + 1) & ~1ll;
+                        pf[e.phy_id] += e.count;
+                    }
+                    ++nreq;
+                    ++head;
+                }
+            }
+            head = __shfl_sync(0xffffffffu, head, 0);
+            nreq = __shfl_sync(0xffffffffu, nreq, 0);
+            full = __shfl_sync(0xffffffffu, full ? 1 : 0, 0) != 0;
+            __syncwarp();  // the window is rewritten by the next fetch
+        }
+        if (lane == 0) {
+            sh->head = head;
+            sh->cmp_reserve = reserve + static_cast<unsigned long long>(nreq);
+            st->cmp_base = reserve;
+            __threadfence_system();  // the admission table holds the entries before their slots are freed
+            store_release_sys(&ds->cmp_reserved, reserve + static_cast<unsigned long long>(nreq));
+            store_release_sys(&ds->req_head, head);
+            __threadfence();
+            atomicExch(&sh->lock, 0);
+        }
     }
     if (lane != 0) return;
-    st->head = head;
     st->nreq = nreq;
     st->count = cw;
     st->in_chunks = in_chunks;
@@ -242,8 +293,6 @@ __global__ void __launch_bounds__(32) admit_kernel(const ReqEntry* ring, unsigne
     const unsigned long long now = globaltimer_ns();
     if (nreq > 0 || st->last_active_ns == 0) st->last_active_ns = now;
     st->t_start_ns = now;
-    __threadfence_system();
-    store_release_sys(&ds->req_head, head);
     cudaGraphSetConditional(work, nreq > 0 ? 1u : 0u);  // an empty iteration skips to publication
 }
 
@@ -338,7 +387,8 @@ __global__ void layout_kernel(const LoopState* st, const Admitted* __restrict__ 
 // One iteration's completion: the information bits go to the requests' host
 // buffers chunk by chunk (all CTAs share every request); the CTA that finishes
 // a request's last chunk counts its BP failures and OSD codewords and writes
-// its completion record.
+// its completion record into the slot its admission reserved, the sequence
+// number last.
 __global__ void complete_kernel(const LoopState* st, const Admitted* __restrict__ adm,
                                 const uint8_t* __restrict__ info, const uint8_t* __restrict__ success,
                                 const uint8_t* __restrict__ used_osd, CmpEntry* ring, unsigned mask,
@@ -378,34 +428,34 @@ __global__ void complete_kernel(const LoopState* st, const Admitted* __restrict_
             if (osd) atomicAdd(&s_osd, osd);
             __syncthreads();
             if (threadIdx.x == 0) {
-                CmpEntry c{};
-                c.id = a.e.id;
-                c.tag = a.e.tag;
-                c.t_start_ns = st->t_start_ns;
-                c.t_done_ns = globaltimer_ns();
-                c.codewords = a.e.codewords;
-                c.failed = s_failed;
-                c.osd = s_osd;
-                c.status = 0;
-                ring[(st->cmp_tail + r) & mask] = c;
+                const unsigned long long slot = st->cmp_base + static_cast<unsigned long long>(r);
+                CmpEntry* c = ring + (slot & mask);
+                c->id = a.e.id;
+                c->tag = a.e.tag;
+                c->t_start_ns = st->t_start_ns;
+                c->t_done_ns = globaltimer_ns();
+                c->codewords = a.e.codewords;
+                c->failed = s_failed;
+                c->osd = s_osd;
+                c->status = 0;
+                __threadfence_system();
+                store_release_sys(&c->seq, slot + 1);
             }
         }
         __syncthreads();  // the shared scalars are rewritten by the next chunk
     }
 }
 
-__global__ void publish_kernel(LoopState* st, const HostSide* hs, DevSide* ds, cudaGraphConditionalHandle cond,
-                               unsigned long long idle_ns)
+__global__ void publish_kernel(LoopState* st, const HostSide* hs, const Shared* sh, LaneSide* ls,
+                               cudaGraphConditionalHandle cond, unsigned long long idle_ns)
 {
-    __threadfence_system();  // every record of this iteration is out before the tail moves
-    st->cmp_tail += static_cast<unsigned long long>(st->nreq);
+    __threadfence_system();  // every host write of this iteration is out before the counters move
     st->iterations += 1;
     st->codewords += static_cast<unsigned long long>(st->count);
     st->busy_iterations += st->nreq > 0 ? 1ull : 0ull;
-    ds->busy_iterations = st->busy_iterations;
-    ds->iterations = st->iterations;
-    ds->codewords = st->codewords;
-    store_release_sys(&ds->cmp_tail, st->cmp_tail);
+    ls->iterations = st->iterations;
+    ls->codewords = st->codewords;
+    ls->busy_iterations = st->busy_iterations;
     int reason = 0;
     if (load_acquire_sys(&hs->stop)) reason = 1;
     else if (st->nreq == 0 && globaltimer_ns() - st->last_active_ns > idle_ns) reason = 2;
@@ -413,12 +463,12 @@ __global__ void publish_kernel(LoopState* st, const HostSide* hs, DevSide* ds, c
     if (reason) {
         // Announce the end, then read the ring's tail once more.  The host appends a request, then
         // reads `ended` (each side with a full fence between its write and its read), so either the
-        // host sees the announcement and launches the loop again, or this read sees the request and
-        // an idle loop carries on.
-        store_release_sys_int(&ds->ended, reason);
+        // host sees the announcement and launches the lane again, or this read sees the request and
+        // an idle lane carries on.
+        store_release_sys_int(&ls->ended, reason);
         asm volatile("fence.sc.sys;" ::: "memory");
-        if (reason == 2 && load_acquire_sys(&hs->req_tail) != st->head) {
-            store_release_sys_int(&ds->ended, 0);
+        if (reason == 2 && load_acquire_sys(&hs->req_tail) != shared_head(sh)) {
+            store_release_sys_int(&ls->ended, 0);
             st->last_active_ns = globaltimer_ns();
             reason = 0;
         }
@@ -468,11 +518,9 @@ struct Pending {
     Clock::time_point t_submit;
 };
 
-struct PhyHost {  // a registered OFDM profile
+struct PhyHost {  // a registered OFDM profile (its tables serve every lane)
     unsigned long long pipe = 0;
     int stride = 0, code_id = 0, blocks = 0;
-    Dev<long long> frame_off, llr_frame_off;
-    Dev<unsigned char> sync, scratch;
     size_t scratch_bytes = 0, ticket_offset = 0, ticket_bytes = 0;
     ~PhyHost()
     {
@@ -480,48 +528,28 @@ struct PhyHost {  // a registered OFDM profile
     }
 };
 
-struct Loop {
-    sicc_devloop_config_t cfg{};
-    int device = 0;
+struct LanePhy {  // a profile's per-lane buffers
+    Dev<long long> frame_off, llr_frame_off;
+    Dev<unsigned char> sync, scratch;
+};
+
+struct Lane {  // one loop graph, its stream, engine and batch state
     unsigned long long engine = 0;
-    std::vector<CodeDims> codes;
-    int max_req = 0;
-    unsigned mask = 0;
-    // rings and control blocks (pinned, mapped)
-    Pinned<ReqEntry> ring;
-    Pinned<CmpEntry> cring;
-    Pinned<HostSide> hs;
-    Pinned<DevSide> ds;
-    Pinned<unsigned long long> clock;
-    // device state
     Dev<LoopState> st;
     Dev<Admitted> adm;
     Dev<float> llr;
     Dev<uint8_t> info, code_of, protect, success, used, iters;
     Dev<long long> llr_off, info_off;
-    Dev<int> chunks_done;                // [max_req] finished output chunks of each admitted request
-    Dev<float> iqbuf;                    // [max_batch_iq_samples] complex samples
-    std::vector<std::unique_ptr<PhyHost>> phys;
+    Dev<int> chunks_done;  // [max_req] finished output chunks of each admitted request
+    Dev<float> iqbuf;      // [max_batch_iq_samples] complex samples
+    std::vector<std::unique_ptr<LanePhy>> phys;
     Dev<PhyDev> d_phys;
-    long long info_cap = 0;
-    // the graph
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    bool recorded = false;
-    std::atomic<bool> launched{false};  // written under mu; poll reads it
-    // host bookkeeping
-    unsigned long long next_id = 1, req_tail = 0, cmp_head = 0;
-    std::map<unsigned long long, Pending> pending;
-    long long clock_offset_ns = 0;  // device globaltimer - host steady clock (ns)
-    Clock::time_point clock_base;
-    sicc_devloop_stats_t stats{};
-    std::mutex mu;      // submit side
-    std::mutex poll_mu; // poll side (one poller at a time)
-    std::mutex pending_mu;  // pending and completed: held briefly by submit and poll
-    unsigned long long completed = 0;
+    std::atomic<bool> launched{false};  // written under the loop's mu; poll reads it
 
-    ~Loop()
+    ~Lane()
     {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
@@ -537,33 +565,74 @@ struct Loop {
         check_cuda(q, "loop stream");
         return true;
     }
+};
 
-    void record()
+struct Loop {
+    sicc_devloop_config_t cfg{};
+    int device = 0;
+    std::vector<CodeDims> codes;
+    int max_req = 0;
+    unsigned mask = 0;
+    // rings and control blocks (pinned, mapped)
+    Pinned<ReqEntry> ring;
+    Pinned<CmpEntry> cring;
+    Pinned<HostSide> hs;
+    Pinned<DevSide> ds;
+    Pinned<LaneSide> lane_side;  // [lanes]
+    Pinned<unsigned long long> clock;
+    Dev<Shared> sh;
+    std::vector<std::unique_ptr<PhyHost>> phys;
+    std::vector<std::unique_ptr<Lane>> lanes;
+    long long info_cap = 0;
+    bool recorded = false;
+    // host bookkeeping
+    unsigned long long next_id = 1, req_tail = 0, cmp_head = 0;
+    std::vector<uint8_t> taken;  // [ring] completion slots consumed ahead of cmp_head
+    std::map<unsigned long long, Pending> pending;
+    long long clock_offset_ns = 0;  // device globaltimer - host steady clock (ns)
+    Clock::time_point clock_base;
+    sicc_devloop_stats_t stats{};
+    std::mutex mu;          // submit side
+    std::mutex poll_mu;     // poll side (one poller at a time)
+    std::mutex pending_mu;  // pending and completed: held briefly by submit and poll
+    unsigned long long completed = 0;
+
+    int ended(int l) const
     {
-        int n_max = 0, k_max = 0;
-        if (engine_bounds(engine, &n_max, &k_max) != CUDA_OSD_STATUS_OK) throw std::runtime_error(last_error());
-        if (engine_prepare_capture(engine, cfg.max_batch_codewords) != CUDA_OSD_STATUS_OK)
+        return reinterpret_cast<const std::atomic<int>*>(&lane_side.h[l].ended)->load(std::memory_order_acquire);
+    }
+
+    bool all_done() const
+    {
+        for (const auto& ln : lanes)
+            if (!ln->graph_done()) return false;
+        return true;
+    }
+
+    void record_lane(Lane& ln, int l)
+    {
+        if (engine_prepare_capture(ln.engine, cfg.max_batch_codewords) != CUDA_OSD_STATUS_OK)
             throw std::runtime_error(last_error());
-        info_cap = static_cast<long long>(cfg.max_batch_codewords) * k_max + 16ll * max_req;  // + per-request alignment
-        info.alloc(static_cast<size_t>(info_cap));
+        ln.info.alloc(static_cast<size_t>(info_cap));
         std::vector<PhyDev> pd;
-        for (const auto& ph : phys) {
+        for (size_t q = 0; q < phys.size(); ++q) {
             PhyDev d{};
-            d.frame_off = ph->frame_off.p;
-            d.llr_frame_off = ph->llr_frame_off.p;
-            d.ticket = reinterpret_cast<int*>(ph->scratch.p + ph->ticket_offset);
-            d.ticket_ints = static_cast<int>(ph->ticket_bytes / sizeof(int));
-            d.blocks = ph->blocks;
+            d.frame_off = ln.phys[q]->frame_off.p;
+            d.llr_frame_off = ln.phys[q]->llr_frame_off.p;
+            d.ticket = reinterpret_cast<int*>(ln.phys[q]->scratch.p + phys[q]->ticket_offset);
+            d.ticket_ints = static_cast<int>(phys[q]->ticket_bytes / sizeof(int));
+            d.blocks = phys[q]->blocks;
             pd.push_back(d);
         }
-        d_phys.alloc(std::max<size_t>(pd.size(), 1));
+        ln.d_phys.alloc(std::max<size_t>(pd.size(), 1));
         if (!pd.empty())
-            check_cuda(cudaMemcpy(d_phys.p, pd.data(), pd.size() * sizeof(PhyDev), cudaMemcpyHostToDevice),
+            check_cuda(cudaMemcpy(ln.d_phys.p, pd.data(), pd.size() * sizeof(PhyDev), cudaMemcpyHostToDevice),
                        "upload profiles");
-        check_cuda(cudaGraphCreate(&graph, 0), "cudaGraphCreate");
+        cudaStream_t stream = ln.stream;
+        check_cuda(cudaGraphCreate(&ln.graph, 0), "cudaGraphCreate");
         // graph: while (loop) { admit; if (admitted) { layout; demod; decode; complete } publish }
         cudaGraphConditionalHandle loop_cond, work_cond;
-        check_cuda(cudaGraphConditionalHandleCreate(&loop_cond, graph, 1, cudaGraphCondAssignDefault),
+        check_cuda(cudaGraphConditionalHandleCreate(&loop_cond, ln.graph, 1, cudaGraphCondAssignDefault),
                    "cudaGraphConditionalHandleCreate(loop)");
         cudaGraphNodeParams p{};
         p.type = cudaGraphNodeTypeConditional;
@@ -571,7 +640,7 @@ struct Loop {
         p.conditional.type = cudaGraphCondTypeWhile;
         p.conditional.size = 1;
         cudaGraphNode_t node;
-        check_cuda(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &p), "cudaGraphAddNode(while)");
+        check_cuda(cudaGraphAddNode(&node, ln.graph, nullptr, nullptr, 0, &p), "cudaGraphAddNode(while)");
         cudaGraph_t body = p.conditional.phGraph_out[0];
         check_cuda(cudaGraphConditionalHandleCreate(&work_cond, body, 0, cudaGraphCondAssignDefault),
                    "cudaGraphConditionalHandleCreate(work)");
@@ -587,9 +656,9 @@ struct Loop {
         // 1. admission, the body's first node
         check_cuda(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
                    "cudaStreamBeginCaptureToGraph(admit)");
-        admit_kernel<<<1, 32, 0, stream>>>(ring.d, mask, hs.d, ds.d, st.p, adm.p, max_req, cfg.max_batch_codewords,
-                                            cfg.max_batch_llr_floats, mask + 1, cfg.max_batch_frames,
-                                            cfg.max_batch_iq_samples, work_cond);
+        admit_kernel<<<1, 32, 0, stream>>>(ring.d, mask, hs.d, ds.d, sh.p, ln.st.p, ln.adm.p, max_req,
+                                            cfg.max_batch_codewords, cfg.max_batch_llr_floats, mask + 1,
+                                            cfg.max_batch_frames, cfg.max_batch_iq_samples, work_cond);
         end_capture("cudaStreamEndCapture(admit)");
         cudaGraphNode_t admit_node = nullptr;
         size_t nodes = 1;
@@ -607,36 +676,48 @@ struct Loop {
         check_cuda(cudaStreamBeginCaptureToGraph(stream, work, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
                    "cudaStreamBeginCaptureToGraph(work)");
         const int sms = device_sm_count();
-        layout_kernel<<<2 * sms, 256, 0, stream>>>(st.p, adm.p, llr.p, iqbuf.p, d_phys.p, static_cast<int>(phys.size()),
-                                                    code_of.p, protect.p, llr_off.p, info_off.p, chunks_done.p);
+        layout_kernel<<<2 * sms, 256, 0, stream>>>(ln.st.p, ln.adm.p, ln.llr.p, ln.iqbuf.p, ln.d_phys.p,
+                                                    static_cast<int>(phys.size()), ln.code_of.p, ln.protect.p,
+                                                    ln.llr_off.p, ln.info_off.p, ln.chunks_done.p);
         for (size_t q = 0; q < phys.size(); ++q) {  // each profile's admitted frames: search + demodulation
             const PhyHost& ph = *phys[q];
-            if (pipe_gather_counted(ph.pipe, iqbuf.p, ph.frame_off.p, ph.stride, cfg.max_batch_frames,
-                                    &st.p->phy_frames[q], llr.p, ph.llr_frame_off.p, ph.sync.p, ph.scratch.p,
+            LanePhy& lp = *ln.phys[q];
+            if (pipe_gather_counted(ph.pipe, ln.iqbuf.p, lp.frame_off.p, ph.stride, cfg.max_batch_frames,
+                                    &ln.st.p->phy_frames[q], ln.llr.p, lp.llr_frame_off.p, lp.sync.p, lp.scratch.p,
                                     ph.scratch_bytes, stream) != CUDA_OSD_STATUS_OK)
                 abandon(std::string("recording the loop's demodulation: ") + last_error());
         }
-        const int rc = engine_decode(engine, cfg.max_batch_codewords, code_of.p, protect.p, llr.p, llr_off.p, info.p,
-                                     info_off.p, success.p, used.p, iters.p, stream, nullptr, &st.p->count);
+        const int rc = engine_decode(ln.engine, cfg.max_batch_codewords, ln.code_of.p, ln.protect.p, ln.llr.p,
+                                     ln.llr_off.p, ln.info.p, ln.info_off.p, ln.success.p, ln.used.p, ln.iters.p,
+                                     stream, nullptr, &ln.st.p->count);
         if (rc != CUDA_OSD_STATUS_OK) abandon(std::string("recording the loop's decode: ") + last_error());
-        complete_kernel<<<2 * sms, 256, 0, stream>>>(st.p, adm.p, info.p, success.p, used.p, cring.d, mask,
-                                                      chunks_done.p);
+        complete_kernel<<<2 * sms, 256, 0, stream>>>(ln.st.p, ln.adm.p, ln.info.p, ln.success.p, ln.used.p, cring.d,
+                                                      mask, ln.chunks_done.p);
         end_capture("cudaStreamEndCapture(work)");
         // 3. publication, after the work node
         check_cuda(cudaStreamBeginCaptureToGraph(stream, body, &if_node, nullptr, 1, cudaStreamCaptureModeRelaxed),
                    "cudaStreamBeginCaptureToGraph(publish)");
-        publish_kernel<<<1, 1, 0, stream>>>(st.p, hs.d, ds.d, loop_cond,
+        publish_kernel<<<1, 1, 0, stream>>>(ln.st.p, hs.d, sh.p, lane_side.d + l, loop_cond,
                                             static_cast<unsigned long long>(cfg.idle_timeout_ms) * 1000000ull);
         end_capture("cudaStreamEndCapture(publish)");
-        check_cuda(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate(loop)");
+        check_cuda(cudaGraphInstantiate(&ln.exec, ln.graph, 0), "cudaGraphInstantiate(loop)");
+    }
+
+    void record()
+    {
+        int n_max = 0, k_max = 0;
+        if (engine_bounds(lanes[0]->engine, &n_max, &k_max) != CUDA_OSD_STATUS_OK)
+            throw std::runtime_error(last_error());
+        info_cap = static_cast<long long>(cfg.max_batch_codewords) * k_max + 16ll * max_req;  // + per-request alignment
+        for (size_t l = 0; l < lanes.size(); ++l) record_lane(*lanes[l], static_cast<int>(l));
         recorded = true;
     }
 
     void calibrate()
     {
         const auto t0 = Clock::now();
-        clock_kernel<<<1, 1, 0, stream>>>(clock.d);
-        check_cuda(cudaStreamSynchronize(stream), "clock");
+        clock_kernel<<<1, 1, 0, lanes[0]->stream>>>(clock.d);
+        check_cuda(cudaStreamSynchronize(lanes[0]->stream), "clock");
         const auto t1 = Clock::now();
         const auto mid = t0 + (t1 - t0) / 2;
         clock_base = mid;
@@ -649,34 +730,40 @@ struct Loop {
         return clock_base + std::chrono::nanoseconds(static_cast<long long>(dev_ns) - clock_offset_ns);
     }
 
-    int ended() const { return reinterpret_cast<const std::atomic<int>*>(&ds.h->ended)->load(std::memory_order_acquire); }
-
-    // Launches the loop if it is not running (the caller holds mu).  Called after a request was
-    // appended: a loop that has announced its end (publish_kernel) either took the request back
-    // and carries on, or finishes and is launched again here.
+    // Launches every lane that is not running (the caller holds mu).  Called after a request was
+    // appended: a lane that has announced its end (publish_kernel) either took the request back and
+    // carries on, or finishes and is launched again here.
     void ensure_running()
     {
         std::atomic_thread_fence(std::memory_order_seq_cst);  // the tail is out before `ended` is read
-        if (launched) {
-            if (ended() == 0) return;  // running: it admits the request (no stream query on this path)
-            const auto deadline = Clock::now() + std::chrono::seconds(10);
-            while (!graph_done()) {
-                if (ended() == 0) return;  // running, and it will admit the request
-                if (Clock::now() > deadline) throw std::runtime_error("the device loop did not finish ending");
-                std::this_thread::sleep_for(std::chrono::microseconds(2));
-            }
-        }
         if (!recorded) {
             record();
             calibrate();
         }
-        DevSide* d = ds.h;
-        reinterpret_cast<std::atomic<int>*>(&d->ended)->store(0, std::memory_order_relaxed);
-        reinterpret_cast<std::atomic<int>*>(&hs.h->stop)->store(0, std::memory_order_release);
-        check_cuda(cudaMemsetAsync(&st.p->last_active_ns, 0, sizeof(unsigned long long), stream), "loop reset");
-        check_cuda(cudaGraphLaunch(exec, stream), "cudaGraphLaunch(loop)");
-        launched = true;
-        ++stats.launches;
+        for (size_t l = 0; l < lanes.size(); ++l) {
+            Lane& ln = *lanes[l];
+            if (ln.launched) {
+                if (ended(static_cast<int>(l)) == 0) continue;  // running (no stream query on this path)
+                const auto deadline = Clock::now() + std::chrono::seconds(10);
+                bool carries_on = false;
+                while (!ln.graph_done()) {
+                    if (ended(static_cast<int>(l)) == 0) {
+                        carries_on = true;  // it saw the request and goes on
+                        break;
+                    }
+                    if (Clock::now() > deadline) throw std::runtime_error("a device-loop lane did not finish ending");
+                    std::this_thread::sleep_for(std::chrono::microseconds(2));
+                }
+                if (carries_on) continue;
+            }
+            reinterpret_cast<std::atomic<int>*>(&lane_side.h[l].ended)->store(0, std::memory_order_relaxed);
+            reinterpret_cast<std::atomic<int>*>(&hs.h->stop)->store(0, std::memory_order_release);
+            check_cuda(cudaMemsetAsync(&ln.st.p->last_active_ns, 0, sizeof(unsigned long long), ln.stream),
+                       "loop reset");
+            check_cuda(cudaGraphLaunch(ln.exec, ln.stream), "cudaGraphLaunch(loop)");
+            ln.launched = true;
+            ++stats.launches;
+        }
     }
 };
 
@@ -756,31 +843,40 @@ int sicc_devloop_create(const sicc_devloop_config_t* config, unsigned long long*
         if (c.idle_timeout_ms < 1) throw InvalidArgument("idle_timeout_ms must be >= 1");
         if (c.max_batch_frames < 0 || c.max_batch_iq_samples < 0 || (c.max_batch_frames > 0) != (c.max_batch_iq_samples > 0))
             throw InvalidArgument("max_batch_frames and max_batch_iq_samples: both positive (IQ requests) or both 0");
+        if (c.lanes < 0 || c.lanes > kMaxLanes) throw InvalidArgument("lanes must be 0..8 (0: one lane)");
         auto L = std::make_shared<Loop>();
         L->cfg = c;
+        L->cfg.lanes = std::max(1, c.lanes);
         check_cuda(cudaGetDevice(&L->device), "cudaGetDevice");
-        sicc_engine_config_t ec{};
-        ec.max_codewords = c.max_batch_codewords;
-        ec.max_llr_floats = c.max_batch_llr_floats;
-        ec.max_codes = c.max_codes;
-        if (sicc_engine_create(&ec, &L->engine) != CUDA_OSD_STATUS_OK) throw std::runtime_error(last_error());
         L->mask = static_cast<unsigned>(c.ring_requests - 1);
         L->max_req = std::min(c.ring_requests, c.max_batch_codewords);
         L->ring.alloc(c.ring_requests);
         L->cring.alloc(c.ring_requests);
+        L->taken.assign(static_cast<size_t>(c.ring_requests), 0);
         L->hs.alloc(1);
         L->ds.alloc(1);
+        L->lane_side.alloc(static_cast<size_t>(L->cfg.lanes));
         L->clock.alloc(1);
-        L->st.alloc(1);
-        L->adm.alloc(static_cast<size_t>(L->max_req));
-        L->llr.alloc(static_cast<size_t>(c.max_batch_llr_floats));
-        for (auto* b : {&L->code_of, &L->protect, &L->success, &L->used, &L->iters})
-            b->alloc(static_cast<size_t>(c.max_batch_codewords));
-        L->llr_off.alloc(static_cast<size_t>(c.max_batch_codewords));
-        L->info_off.alloc(static_cast<size_t>(c.max_batch_codewords));
-        L->chunks_done.alloc(static_cast<size_t>(L->max_req));
-        L->iqbuf.alloc(2 * static_cast<size_t>(std::max<long long>(c.max_batch_iq_samples, 1)));
-        check_cuda(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking), "cudaStreamCreate(loop)");
+        L->sh.alloc(1);
+        for (int l = 0; l < L->cfg.lanes; ++l) {
+            auto ln = std::make_unique<Lane>();
+            sicc_engine_config_t ec{};
+            ec.max_codewords = c.max_batch_codewords;
+            ec.max_llr_floats = c.max_batch_llr_floats;
+            ec.max_codes = c.max_codes;
+            if (sicc_engine_create(&ec, &ln->engine) != CUDA_OSD_STATUS_OK) throw std::runtime_error(last_error());
+            ln->st.alloc(1);
+            ln->adm.alloc(static_cast<size_t>(L->max_req));
+            ln->llr.alloc(static_cast<size_t>(c.max_batch_llr_floats));
+            for (auto* b : {&ln->code_of, &ln->protect, &ln->success, &ln->used, &ln->iters})
+                b->alloc(static_cast<size_t>(c.max_batch_codewords));
+            ln->llr_off.alloc(static_cast<size_t>(c.max_batch_codewords));
+            ln->info_off.alloc(static_cast<size_t>(c.max_batch_codewords));
+            ln->chunks_done.alloc(static_cast<size_t>(L->max_req));
+            ln->iqbuf.alloc(2 * static_cast<size_t>(std::max<long long>(c.max_batch_iq_samples, 1)));
+            check_cuda(cudaStreamCreateWithFlags(&ln->stream, cudaStreamNonBlocking), "cudaStreamCreate(loop)");
+            L->lanes.push_back(std::move(ln));
+        }
         std::lock_guard<std::mutex> lock(g_mu);
         const unsigned long long h = ++g_next;
         g_loops[h] = L;
@@ -795,14 +891,13 @@ int sicc_devloop_stop(unsigned long long handle, int wait_ms)
         auto L = get(handle);
         std::lock_guard<std::mutex> lock(L->mu);
         check_cuda(cudaSetDevice(L->device), "cudaSetDevice");
-        if (!L->launched) return CUDA_OSD_STATUS_OK;
         store_release(&L->hs.h->stop, 1);
         const auto deadline = Clock::now() + std::chrono::milliseconds(std::max(wait_ms, 1));
-        while (!L->graph_done()) {
+        while (!L->all_done()) {
             if (Clock::now() > deadline) throw std::runtime_error("the device loop did not stop in time");
             std::this_thread::sleep_for(std::chrono::microseconds(50));
         }
-        L->launched = false;
+        for (auto& ln : L->lanes) ln->launched = false;
         return CUDA_OSD_STATUS_OK;
     });
 }
@@ -832,9 +927,15 @@ int sicc_devloop_add_code(unsigned long long handle, const sicc_engine_code_t* c
         if (L->recorded) throw InvalidArgument("codes must be added before the loop starts");
         if (!code || !out_code_id) throw InvalidArgument("null argument");
         check_cuda(cudaSetDevice(L->device), "cudaSetDevice");
-        if (sicc_engine_add_code(L->engine, code, out_code_id) != CUDA_OSD_STATUS_OK)
-            throw InvalidArgument(last_error());
+        int id = -1;
+        for (auto& ln : L->lanes) {  // every lane's engine holds the same codes under the same ids
+            int lid = -1;
+            if (sicc_engine_add_code(ln->engine, code, &lid) != CUDA_OSD_STATUS_OK) throw InvalidArgument(last_error());
+            if (id >= 0 && lid != id) throw std::runtime_error("the lanes' engines gave different code ids");
+            id = lid;
+        }
         L->codes.push_back(CodeDims{code->n, code->n - code->m});
+        *out_code_id = id;
         return CUDA_OSD_STATUS_OK;
     });
 }
@@ -868,13 +969,17 @@ int sicc_devloop_add_phy(unsigned long long handle, const sicc_pipe_config_t* co
         ph->code_id = code_id;
         ph->blocks = dims.blocks;
         const int F = L->cfg.max_batch_frames;
-        ph->frame_off.alloc(static_cast<size_t>(F));
-        ph->llr_frame_off.alloc(static_cast<size_t>(F));
-        ph->sync.alloc(static_cast<size_t>(F) * sizeof(sicc_pipe_sync_record_t));
         if (pipe_gather_scratch(ph->pipe, frame_stride, F, &ph->scratch_bytes, &ph->ticket_offset, &ph->ticket_bytes) !=
             CUDA_OSD_STATUS_OK)
             throw std::runtime_error(last_error());
-        ph->scratch.alloc(ph->scratch_bytes);
+        for (auto& ln : L->lanes) {  // the search and demodulator's buffers, one set per lane
+            auto lp = std::make_unique<LanePhy>();
+            lp->frame_off.alloc(static_cast<size_t>(F));
+            lp->llr_frame_off.alloc(static_cast<size_t>(F));
+            lp->sync.alloc(static_cast<size_t>(F) * sizeof(sicc_pipe_sync_record_t));
+            lp->scratch.alloc(ph->scratch_bytes);
+            ln->phys.push_back(std::move(lp));
+        }
         L->phys.push_back(std::move(ph));
         *out_phy_id = static_cast<int>(L->phys.size()) - 1;
         return CUDA_OSD_STATUS_OK;
@@ -969,12 +1074,17 @@ int sicc_devloop_poll(unsigned long long handle, int max, sicc_completion_t* out
         const auto deadline = Clock::now() + std::chrono::microseconds(std::max(wait_us, 0));
         unsigned spins = 0;
         for (;;) {
-            const unsigned long long tail = load_acquire(&L->ds.h->cmp_tail);
+            // lanes finish out of order: take every record whose sequence number is set, then move the
+            // head over the consumed prefix (which frees those slots for the lanes)
+            const unsigned long long reserved = load_acquire(&L->ds.h->cmp_reserved);
             std::unique_lock<std::mutex> pend(L->pending_mu, std::defer_lock);
-            if (L->cmp_head < tail) pend.lock();
-            while (L->cmp_head < tail && *out_count < max) {
-                const CmpEntry c = L->cring.h[L->cmp_head & L->mask];
-                ++L->cmp_head;
+            for (unsigned long long s = L->cmp_head; s < reserved && *out_count < max; ++s) {
+                const size_t slot = static_cast<size_t>(s & L->mask);
+                if (L->taken[slot]) continue;
+                const CmpEntry& c = L->cring.h[slot];
+                if (load_acquire(&c.seq) != s + 1) continue;
+                L->taken[slot] = 1;
+                if (!pend.owns_lock()) pend.lock();
                 sicc_completion_t& o = out[(*out_count)++];
                 o = sicc_completion_t{};
                 o.request_id = c.id;
@@ -995,14 +1105,23 @@ int sicc_devloop_poll(unsigned long long handle, int max, sicc_completion_t* out
                 ++L->completed;
             }
             if (pend.owns_lock()) pend.unlock();
+            while (L->cmp_head < reserved && L->taken[L->cmp_head & L->mask]) {
+                L->taken[L->cmp_head & L->mask] = 0;
+                ++L->cmp_head;
+            }
             store_release(&L->hs.h->cmp_head, L->cmp_head);
             if (*out_count > 0) break;
-            // nothing to report: a loop that failed is reported, and one that ended with requests
-            // still in its ring is launched again (when no submit holds the loop's lock)
-            if ((++spins & 127) == 0 && L->launched.load() && L->graph_done() &&
+            // nothing to report: a lane that failed is reported, and lanes that ended with requests still
+            // in the ring are launched again (when no submit holds the loop's lock)
+            if ((++spins & 127) == 0 &&
                 load_acquire(&L->hs.h->req_tail) != load_acquire(&L->ds.h->req_head)) {
-                std::unique_lock<std::mutex> lock(L->mu, std::try_to_lock);
-                if (lock.owns_lock()) L->ensure_running();
+                bool stopped = false;
+                for (auto& ln : L->lanes)
+                    if (ln->launched.load() && ln->graph_done()) stopped = true;
+                if (stopped) {
+                    std::unique_lock<std::mutex> lock(L->mu, std::try_to_lock);
+                    if (lock.owns_lock()) L->ensure_running();
+                }
             }
             if (Clock::now() >= deadline) break;
             std::this_thread::sleep_for(std::chrono::microseconds(5));
@@ -1022,10 +1141,16 @@ int sicc_devloop_get_stats(unsigned long long handle, sicc_devloop_stats_t* out)
             std::lock_guard<std::mutex> plock(L->pending_mu);
             out->completed = L->completed;
         }
-        out->iterations = load_acquire(&L->ds.h->iterations);
-        out->codewords = load_acquire(&L->ds.h->codewords);
-        out->busy_iterations = load_acquire(&L->ds.h->busy_iterations);
-        out->running = (L->launched && !L->graph_done()) ? 1 : 0;
+        out->iterations = out->codewords = out->busy_iterations = 0;
+        out->running = 0;
+        for (size_t l = 0; l < L->lanes.size(); ++l) {
+            const LaneSide& s = L->lane_side.h[l];
+            out->iterations += load_acquire(&s.iterations);
+            out->codewords += load_acquire(&s.codewords);
+            out->busy_iterations += load_acquire(&s.busy_iterations);
+            if (L->lanes[l]->launched && !L->lanes[l]->graph_done()) ++out->running;
+        }
+        out->lanes = static_cast<int>(L->lanes.size());
         return CUDA_OSD_STATUS_OK;
     });
 }
@@ -1077,7 +1202,7 @@ int sicc_devloop_replay(unsigned long long handle, const sicc_request_t* request
                     error = "no completion for 30 s (requests submitted " + std::to_string(s.submitted) +
                             ", admitted " + std::to_string(load_acquire(&L->ds.h->req_head)) + ", completed " +
                             std::to_string(s.completed) + "; loop iterations " + std::to_string(s.iterations) +
-                            ", running " + std::to_string(s.running) + ", ended " + std::to_string(L->ended()) + ")";
+                            ", lanes running " + std::to_string(s.running) + ")";
                     failed.store(true);
                 }
             }

@@ -29,13 +29,13 @@ from .server import BUSY, Completion, Request, _done
 class DevLoopConfig(C.Structure):
     _fields_ = [("max_batch_codewords", C.c_int), ("max_batch_llr_floats", C.c_longlong), ("max_codes", C.c_int),
                 ("ring_requests", C.c_int), ("idle_timeout_ms", C.c_int), ("max_batch_frames", C.c_int),
-                ("max_batch_iq_samples", C.c_longlong)]
+                ("max_batch_iq_samples", C.c_longlong), ("lanes", C.c_int)]
 
 
 class DevLoopStats(C.Structure):
     _fields_ = [("submitted", C.c_ulonglong), ("completed", C.c_ulonglong), ("iterations", C.c_ulonglong),
                 ("busy_rejections", C.c_ulonglong), ("launches", C.c_ulonglong), ("codewords", C.c_ulonglong),
-                ("running", C.c_int), ("busy_iterations", C.c_ulonglong)]
+                ("running", C.c_int), ("busy_iterations", C.c_ulonglong), ("lanes", C.c_int)]
 
 
 _SIGS = {
@@ -70,10 +70,11 @@ def pinned(shape, dtype) -> np.ndarray:
 class DevLoop:
     def __init__(self, max_batch_codewords: int, max_batch_llr_floats: int, max_codes: int = 64,
                  ring_requests: int = 4096, idle_timeout_ms: int = 2000, max_batch_frames: int = 0,
-                 max_batch_iq_samples: int = 0):
+                 max_batch_iq_samples: int = 0, lanes: int = 1):
         cfg = DevLoopConfig(max_batch_codewords=max_batch_codewords, max_batch_llr_floats=max_batch_llr_floats,
                             max_codes=max_codes, ring_requests=ring_requests, idle_timeout_ms=idle_timeout_ms,
-                            max_batch_frames=max_batch_frames, max_batch_iq_samples=max_batch_iq_samples)
+                            max_batch_frames=max_batch_frames, max_batch_iq_samples=max_batch_iq_samples,
+                            lanes=lanes)
         h = C.c_ulonglong(0)
         _lib.check(_fn("sicc_devloop_create")(C.byref(cfg), C.byref(h)), "sicc_devloop_create")
         self.handle = h.value

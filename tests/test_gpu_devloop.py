@@ -54,9 +54,11 @@ def _pinned_llrs(c, cnt, ebn0, seed):
     return buf
 
 
-def test_device_loop_matches_requests_decoded_alone(cuda, oracle):
+@pytest.mark.parametrize("lanes", [1, 3])
+def test_device_loop_matches_requests_decoded_alone(cuda, oracle, lanes):
+    """One lane, and three lanes sharing the rings (batches decoded side by side, finishing out of order)."""
     cs = _codes()
-    lp = _loop(cs, max_batch_codewords=2048, max_batch_llr_floats=2048 * 1024, ring_requests=64)
+    lp = _loop(cs, max_batch_codewords=2048, max_batch_llr_floats=2048 * 1024, ring_requests=64, lanes=lanes)
     lp.start()
     rng = np.random.default_rng(15)
     reqs = []
@@ -81,6 +83,7 @@ def test_device_loop_matches_requests_decoded_alone(cuda, oracle):
     assert len(done) == len(reqs)
     st = lp.stats()
     assert st.completed == len(reqs) and st.iterations >= 1 and st.codewords >= sum(r[1].shape[0] for r in reqs)
+    assert st.lanes == lanes
     for ci, llr, prot, rid, out in reqs:
         c = cs[ci]
         d = done[rid]
@@ -149,7 +152,7 @@ def test_device_loop_iq_requests_match_pipeline_then_engine(cuda):
     cid = len(cs) - 2  # the short code
     assert cs[cid].n == code.n and cs[cid].k == code.k
     lp = _loop(cs, max_batch_codewords=1024, max_batch_llr_floats=1024 * 1024, ring_requests=32,
-               max_batch_frames=8, max_batch_iq_samples=8 * stride)
+               max_batch_frames=8, max_batch_iq_samples=8 * stride, lanes=2)
     pid = lp.add_phy(t, cid, blocks, nv, stride)
     lp.start()
     iq_reqs = []
@@ -201,7 +204,8 @@ def test_device_loop_serves_requests_arriving_as_it_goes_idle(cuda, oracle):
     """With a 1 ms idle timeout and gaps of 0-3 ms between requests, many requests arrive while the loop
     is deciding to end: each one is served (by the running loop or by a relaunch) and none is left behind."""
     c = codes.short_code()
-    lp = _loop([c], max_batch_codewords=64, max_batch_llr_floats=64 * 128, ring_requests=64, idle_timeout_ms=1)
+    lp = _loop([c], max_batch_codewords=64, max_batch_llr_floats=64 * 128, ring_requests=64, idle_timeout_ms=1,
+               lanes=2)
     lp.start()
     rng = np.random.default_rng(5)
     llr = _pinned_llrs(c, 8, 2.5, 91)
