@@ -1221,12 +1221,12 @@ def run_serve(args, rank, world):
 
     device_loop = getattr(args, "serve_loop", "host") == "device"
     if device_loop:
-        # the device-resident loop: serve_inflight lanes (batches decoded side by side), one lane iteration
-        # holds up to serve_batch codewords (their LLRs: up to 2048 floats each) and 17 x 16 frames of IQ
+        # the device-resident loop: loop_lanes lanes (batches decoded side by side), one lane iteration
+        # holds up to loop_batch codewords (their LLRs: up to 2048 floats each) and 17 x 16 frames of IQ
         from sicc_gb300.devloop import DevLoop
-        srv = DevLoop(max_batch_codewords=args.serve_batch, max_batch_llr_floats=args.serve_batch * 2048,
+        srv = DevLoop(max_batch_codewords=args.loop_batch, max_batch_llr_floats=args.loop_batch * 2048,
                       ring_requests=4096, idle_timeout_ms=2000, max_batch_frames=272,
-                      max_batch_iq_samples=272 * stride, lanes=args.serve_inflight)
+                      max_batch_iq_samples=272 * stride, lanes=args.loop_lanes)
     else:
         srv = Server(hbm_budget_bytes=40 << 30, max_batch_codewords=args.serve_batch,
                      max_inflight_batches=args.serve_inflight, max_pending_requests=1 << 16)
@@ -1339,7 +1339,8 @@ def run_serve(args, rank, world):
             "data": "synthetic (seeded BPSK/AWGN LLRs; seeded OFDM IQ: 6-tap Rayleigh, CFO 0.1 sc, SNR 8/12/16 dB)",
             "config": {"workload": "serve_mixed", "requests": n_req, "iq_requests": iq_reqs,
                        "codewords": cw_total, "info_bits": info_bits, "hbm_budget_gb": 40,
-                       "max_batch_codewords": args.serve_batch, "inflight_batches": args.serve_inflight,
+                       "max_batch_codewords": args.loop_batch if device_loop else args.serve_batch,
+                       "inflight_batches": args.loop_lanes if device_loop else args.serve_inflight,
                        "burst": "U{1..512} codewords or U{1..17} OFDM frames (p=0.3)",
                        "protection": "BP or BP+OSD (p=1/2); OSD order 2 (n <= 256), order 1 (n >= 512)",
                        "step": "every request offered at once (peak); then one Poisson pass per load point",
@@ -1565,6 +1566,8 @@ def main():
     ap.add_argument("--serve-loads", type=float, nargs="*", default=None, help="offered loads (fractions of peak)")
     ap.add_argument("--serve-batch", type=int, default=16384, help="codewords per server launch")
     ap.add_argument("--serve-inflight", type=int, default=4, help="batches overlapping on the device")
+    ap.add_argument("--loop-lanes", type=int, default=8, help="device-loop lanes (batches side by side)")
+    ap.add_argument("--loop-batch", type=int, default=4096, help="codewords per device-loop lane iteration")
     ap.add_argument("--serve-loop", default="host", choices=["host", "device"],
                     help="serving loop: host scheduler thread, or the device-resident graph loop")
     ap.add_argument("--mixed-codewords", type=int, default=100_000)

@@ -6,13 +6,15 @@
  * the decode thread of its receive loop (source/cpp_cuda/uhd_cpp/src/
  * uhd_ldpc_ofdm_link.cpp:9922-10130), which batches on the host.
  *
- * The loop is one CUDA graph whose body is repeated on the device by a
- * conditional (while) node, with no host work between iterations.  Each
- * iteration:
+ * The loop is one or more lanes, each a CUDA graph on its own stream whose
+ * body is repeated on the device by a conditional (while) node, with no host
+ * work between iterations.  The lanes share the request and completion rings
+ * (each has its own engine and budgets), so one lane admits and decodes while
+ * another finishes a batch.  Each lane iteration:
  *   1. admits requests in submission order from a request ring in pinned
  *      host memory, as many as fit the iteration's device state -- its
- *      codeword, LLR, frame and IQ-sample budgets (the HBM the loop holds
- *      for request state);
+ *      codeword, LLR, frame and IQ-sample budgets (the HBM each lane holds
+ *      for request state) -- when no other lane is admitting at that moment;
  *   2. copies the admitted requests' inputs (codeword LLRs, or OFDM IQ
  *      frames) from their pinned host buffers into that device state and lays
  *      out the batch;
@@ -24,13 +26,15 @@
  *      request asked for it (protection level 1);
  *   5. copies every request's information bits to its host buffer and
  *      publishes one completion record per request in a completion ring in
- *      pinned host memory;
+ *      pinned host memory (lanes complete out of order; poll returns records
+ *      as they appear);
  *   6. decides whether to go on: it stops when the host asks it to, after
  *      `idle_timeout_ms` without a request, or after 2^31 iterations.
  * An iteration that admits nothing skips steps 2-5 (a conditional node), so an
  * idle loop re-reads the ring about every 100 us.
  * The host only appends requests and reads completions; submit restarts the
- * loop if it has stopped.  Results of a codeword do not depend on what it is
+ * lanes that have stopped.  Completions must be polled: a full completion
+ * ring stops admission.  Results of a codeword do not depend on what it is
  * batched with (the engine's guarantee).  Requests arriving while an
  * iteration runs join the next one.
  *
