@@ -412,32 +412,42 @@ def run_ours(args, rank, world):
                 h.numpy()[:] = inputs[e][b][2]
                 pinned[e].append(h.numpy())
         # the reference's streaming use (L:3309-3432, the receive loop L:11482-11633): frames are
-        # submitted as they arrive and results polled as they come back.  Step s submits its frames
-        # (a submit returns once its host copy is done), then collects the previous step's results,
-        # so uploads and host-side result copies overlap the decode; the last step is flushed and
-        # drained before the clock stops.  Every step's LLRs cross host->device and its information
-        # bits device->host inside the timed region.
-        bufs = dec_api[EBN0[0]].poll_buffers(BATCH)
+        # submitted as they arrive and results polled as they come back.  Each receive chain (Eb/N0
+        # point) has its own host thread, as a receiver runs one decode thread per chain: step s
+        # submits the chain's frames (a submit returns once its host copy is done), then collects
+        # the chain's step s - 2, so the GPU always holds a queued batch while the host uploads and
+        # copies results out; the last steps are flushed and drained before the clock stops.  Every step's LLRs cross
+        # host->device and its information bits device->host inside the timed region.  The C ABI
+        # calls release the interpreter lock, so the chains' host work runs side by side.
+        bufs = {e: dec_api[e].poll_buffers(BATCH) for e in EBN0}
         blocks = np.arange(BATCH, dtype=np.uint32)
 
-        def e2e_submit(s):
-            for i, e in enumerate(EBN0):
-                dec_api[e].submit(pinned[e][s % 2], np.full(BATCH, 2 * s + i, np.uint64), blocks)
-
-        def e2e_collect():
-            for e in EBN0:
-                got = 0
-                while got < BATCH:
-                    got += len(dec_api[e].poll(BATCH - got, bufs)[0])
+        def e2e_chain(e, i, steps, errors):
+            try:
+                def collect():
+                    got = 0
+                    while got < BATCH:
+                        got += len(dec_api[e].poll(BATCH - got, bufs[e])[0])
+                lag = 2  # batches in flight per chain beyond the one being collected (the ring holds 4)
+                for s in range(steps):
+                    dec_api[e].submit(pinned[e][s % 2], np.full(BATCH, 2 * s + i, np.uint64), blocks)
+                    if s >= lag:
+                        collect()
+                dec_api[e].flush()
+                for _ in range(min(lag, steps)):
+                    collect()
+            except Exception as exc:  # reported by the caller
+                errors.append(exc)
 
         def e2e_run(steps):
-            for s in range(steps):
-                e2e_submit(s)
-                if s > 0:
-                    e2e_collect()
-            for e in EBN0:
-                dec_api[e].flush()
-            e2e_collect()
+            errors = []
+            threads = [threading.Thread(target=e2e_chain, args=(e, i, steps, errors)) for i, e in enumerate(EBN0)]
+            for t in threads:
+                t.start()
+            for t in threads:
+                t.join()
+            if errors:
+                raise errors[0]
 
         e2e_run(min(args.warmup, 2))
         torch.cuda.synchronize()
@@ -448,9 +458,9 @@ def run_ours(args, rank, world):
         e2e = {"value": round(world * bits_per_step * args.steps / e2e_s / 1e6, 3), "unit": "Mbit/s",
                "h2d_bytes_per_step": len(EBN0) * BATCH * code.n * 4,
                "d2h_bytes_per_step": len(EBN0) * BATCH * (code.k + 1),
-               "api": "cuda_osd_submit_codewords + cuda_osd_poll_ready, one stream decoder per Eb/N0 chain, "
-                      "streaming (a step's submits overlap the previous step's decode; flush + drain at the end), "
-                      "pinned host LLRs"}
+               "api": "cuda_osd_submit_codewords + cuda_osd_poll_ready, one stream decoder and one host thread "
+                      "per Eb/N0 chain, streaming (step s is submitted while steps s-1 and s-2 decode and are "
+                      "collected; flush + drain at the end), pinned host LLRs"}
 
     # ---- roofline of the dominant kernel (layered BP) ----
     peak, peak_kind = peaks()

@@ -359,28 +359,28 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
 #pragma unroll
                     for (int r = 0; r < kRound; ++r) {
                         const bool valid = j - r >= 0 && t + np < m;  // warp-uniform
-                        // each lane: its lowest unpivoted set row (as a mask), and the later
-                        // candidates (bits r+1..) and the basis (bits ..r-1) at that row; the
-                        // lowest such lane holds the pivot
+                        // each lane: its lowest unpivoted set row (as a mask); the lowest such lane
+                        // holds the pivot.  The later candidates (c > r) and the basis (c < r) at
+                        // each lane's row are balloted at once, before the pivot lane is known, so
+                        // the chain from one candidate to the next is one ballot deep: the pivot
+                        // lane's bit of each ballot is that vector's bit at the pivot row.
                         const unsigned x = valid ? (v[r] & ~pivw) : 0u;
                         const unsigned lb = x & (0u - x);
-                        unsigned mv = 0u, mu = 0u;
+                        const unsigned bx = __ballot_sync(0xffffffffu, x != 0u);
+                        unsigned bc[kRound];
 #pragma unroll
-                        for (int c = 0; c < kRound; ++c) {
-                            if (c > r && (v[c] & lb)) mv |= 1u << c;
-                            if (c < r && (U[c] & lb)) mu |= 1u << c;
-                        }
-                        const unsigned l0u = __reduce_min_sync(0xffffffffu, x ? static_cast<unsigned>(lane) : 32u);
-                        const bool piv = l0u < 32u;
-                        const int l0 = static_cast<int>(l0u & 31u);
-                        const unsigned mk = piv ? __shfl_sync(0xffffffffu, mv, l0) : 0u;   // on the chain
-                        const unsigned mkU = piv ? __shfl_sync(0xffffffffu, mu, l0) : 0u;  // off it
-                        const bool me = piv && lane == l0;
+                        for (int c = 0; c < kRound; ++c)
+                            bc[c] = c > r   ? __ballot_sync(0xffffffffu, (v[c] & lb) != 0u)
+                                    : c < r ? __ballot_sync(0xffffffffu, (U[c] & lb) != 0u)
+                                            : 0u;
+                        const bool piv = bx != 0u;
+                        const unsigned sel = bx & (0u - bx);  // the pivot lane's bit (0: no pivot)
+                        const bool me = (sel >> lane) & 1u;
                         const unsigned W = me ? (v[r] ^ lb) : v[r];
 #pragma unroll
                         for (int c = 0; c < kRound; ++c) {
-                            if (c > r) v[c] ^= ((mk >> c) & 1u) ? W : 0u;
-                            if (c < r) U[c] ^= ((mkU >> c) & 1u) ? W : 0u;
+                            if (c > r) v[c] ^= (bc[c] & sel) ? W : 0u;
+                            if (c < r) U[c] ^= (bc[c] & sel) ? W : 0u;
                         }
                         U[r] = piv ? W : 0u;
                         pl[r] = me ? lane * 32 + __ffs(lb) - 1 : -1;
