@@ -27,7 +27,9 @@
  *   5. copies every request's information bits to its host buffer and
  *      publishes one completion record per request in a completion ring in
  *      pinned host memory (lanes complete out of order; poll returns records
- *      as they appear);
+ *      as they appear): requests whose codewords are all final after BP
+ *      (BP only, or no protected failure) as soon as BP ends, while OSD runs
+ *      for the others, which complete after it;
  *   6. decides whether to go on: it stops when the host asks it to, after
  *      `idle_timeout_ms` without a request, or after 2^31 iterations.
  * An iteration that admits nothing skips steps 2-5 (a conditional node), so an
@@ -66,7 +68,7 @@ typedef struct sicc_devloop_config_t {
     int max_batch_frames;            /* OFDM frames one iteration demodulates (0: no IQ requests) */
     long long max_batch_iq_samples;  /* complex IQ samples one iteration holds */
     int lanes;                       /* loop graphs sharing the rings, each with its own engine and
-                                        budgets (0: one; at most 8) */
+                                        budgets (0: one; at most 16) */
 } sicc_devloop_config_t;
 
 typedef struct sicc_devloop_stats_t {

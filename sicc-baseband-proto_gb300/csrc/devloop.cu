@@ -30,10 +30,16 @@
 //   engine decode    the lane's mixed-code engine: prepare, BP and OSD launches,
 //                    sized for the largest batch, reading the batch size on the
 //                    device;
-//   complete_kernel  copies the information bits to the requests' pinned host
-//                    buffers in chunks shared by every CTA; the CTA that ends a
-//                    request's last chunk writes its completion record into its
-//                    reserved slot, sequence number last;
+//   classify_kernel  on a side stream as soon as BP is done: marks the requests
+//     + complete_kernel that wait for OSD (a protected codeword failed BP and its
+//     (phase 0)      code goes on to OSD) and completes every other request
+//                    while the OSD launches run;
+//   complete_kernel  (phase 1, after OSD and the side stream) the remaining
+//                    requests.  Both phases copy the information bits to the
+//                    requests' pinned host buffers in chunks shared by every CTA;
+//                    the CTA that ends a request's last chunk writes its
+//                    completion record into its reserved slot, sequence number
+//                    last;
 //   publish_kernel   one thread: makes the iteration's host writes visible,
 //                    updates the lane's counters and sets the loop condition
 //                    (host stop flag, idle timeout, iteration cap).
@@ -66,7 +72,7 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 constexpr int kMaxPhys = 8;
-constexpr int kMaxLanes = 8;
+constexpr int kMaxLanes = 16;
 
 struct alignas(16) ReqEntry {  // host -> device, one per request
     unsigned long long id, tag;
@@ -384,15 +390,37 @@ __global__ void layout_kernel(const LoopState* st, const Admitted* __restrict__ 
     }
 }
 
-// One iteration's completion: the information bits go to the requests' host
-// buffers chunk by chunk (all CTAs share every request); the CTA that finishes
-// a request's last chunk counts its BP failures and OSD codewords and writes
-// its completion record into the slot its admission reserved, the sequence
-// number last.
+// After BP: a request is late (phase 1) when one of its codewords failed BP,
+// is protected and its code goes on to OSD; every other request's bits are
+// final (phase 0).  One CTA per request (grid-strided).
+__global__ void classify_kernel(const LoopState* st, const Admitted* __restrict__ adm,
+                                const uint8_t* __restrict__ code_of, const uint8_t* __restrict__ protect,
+                                const uint8_t* __restrict__ success, const uint8_t* __restrict__ routes,
+                                uint8_t* __restrict__ late)
+{
+    const int nreq = st->nreq;
+    for (int r = blockIdx.x; r < nreq; r += gridDim.x) {
+        const Admitted& a = adm[r];
+        int osd = 0;
+        for (int c = threadIdx.x; c < a.e.codewords; c += blockDim.x) {
+            const int w = a.first_cw + c;
+            osd |= (!success[w] && protect[w] && routes[code_of[w]]) ? 1 : 0;
+        }
+        osd = __syncthreads_or(osd);
+        if (threadIdx.x == 0) late[r] = static_cast<uint8_t>(osd);
+    }
+}
+
+// One iteration's completion of the requests of one phase (0: final after BP,
+// 1: after OSD): the information bits go to the requests' host buffers chunk
+// by chunk (all CTAs share every request); the CTA that finishes a request's
+// last chunk counts its BP failures and OSD codewords and writes its
+// completion record into the slot its admission reserved, the sequence number
+// last.
 __global__ void complete_kernel(const LoopState* st, const Admitted* __restrict__ adm,
                                 const uint8_t* __restrict__ info, const uint8_t* __restrict__ success,
                                 const uint8_t* __restrict__ used_osd, CmpEntry* ring, unsigned mask,
-                                int* __restrict__ chunks_done)
+                                int* __restrict__ chunks_done, const uint8_t* __restrict__ late, int phase)
 {
     __shared__ int s_r, s_last, s_failed, s_osd;
     const int nreq = st->nreq;
@@ -405,6 +433,10 @@ __global__ void complete_kernel(const LoopState* st, const Admitted* __restrict_
         }
         __syncthreads();
         const int r = s_r;
+        if (late[r] != phase) {  // the other phase's request (uniform over the CTA)
+            __syncthreads();  // s_r is rewritten by the next chunk
+            continue;
+        }
         const Admitted& a = adm[r];
         const long long bytes = static_cast<long long>(a.e.codewords) * a.e.k;
         const int nchunks = static_cast<int>((bytes + kOutChunkBytes - 1) / kOutChunkBytes);
@@ -541,6 +573,10 @@ struct Lane {  // one loop graph, its stream, engine and batch state
     Dev<uint8_t> info, code_of, protect, success, used, iters;
     Dev<long long> llr_off, info_off;
     Dev<int> chunks_done;  // [max_req] finished output chunks of each admitted request
+    Dev<uint8_t> late;     // [max_req] 1: the request waits for OSD
+    Dev<uint8_t> routes;   // [max_codes] 1: the code's protected BP failures go to OSD
+    cudaStream_t side = nullptr;  // completion of the requests that are final after BP
+    cudaEvent_t bp_done = nullptr, early_done = nullptr;
     Dev<float> iqbuf;      // [max_batch_iq_samples] complex samples
     std::vector<std::unique_ptr<LanePhy>> phys;
     Dev<PhyDev> d_phys;
@@ -553,6 +589,9 @@ struct Lane {  // one loop graph, its stream, engine and batch state
     {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
+        if (bp_done) cudaEventDestroy(bp_done);
+        if (early_done) cudaEventDestroy(early_done);
+        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
         if (engine) sicc_engine_destroy(engine);
     }
@@ -614,6 +653,13 @@ struct Loop {
         if (engine_prepare_capture(ln.engine, cfg.max_batch_codewords) != CUDA_OSD_STATUS_OK)
             throw std::runtime_error(last_error());
         ln.info.alloc(static_cast<size_t>(info_cap));
+        {
+            unsigned char r[64] = {0};
+            int nc = 0;
+            if (engine_code_routes(ln.engine, r, 64, &nc) != CUDA_OSD_STATUS_OK) throw std::runtime_error(last_error());
+            ln.routes.alloc(64);
+            check_cuda(cudaMemcpy(ln.routes.p, r, sizeof(r), cudaMemcpyHostToDevice), "upload code routes");
+        }
         std::vector<PhyDev> pd;
         for (size_t q = 0; q < phys.size(); ++q) {
             PhyDev d{};
@@ -689,10 +735,18 @@ struct Loop {
         }
         const int rc = engine_decode(ln.engine, cfg.max_batch_codewords, ln.code_of.p, ln.protect.p, ln.llr.p,
                                      ln.llr_off.p, ln.info.p, ln.info_off.p, ln.success.p, ln.used.p, ln.iters.p,
-                                     stream, nullptr, &ln.st.p->count);
+                                     stream, ln.bp_done, &ln.st.p->count);
         if (rc != CUDA_OSD_STATUS_OK) abandon(std::string("recording the loop's decode: ") + last_error());
+        // requests final after BP complete on the side stream while OSD runs; the rest after OSD
+        check_cuda(cudaStreamWaitEvent(ln.side, ln.bp_done, 0), "cudaStreamWaitEvent(bp done)");
+        classify_kernel<<<2 * sms, 256, 0, ln.side>>>(ln.st.p, ln.adm.p, ln.code_of.p, ln.protect.p, ln.success.p,
+                                                      ln.routes.p, ln.late.p);
+        complete_kernel<<<2 * sms, 256, 0, ln.side>>>(ln.st.p, ln.adm.p, ln.info.p, ln.success.p, ln.used.p,
+                                                      cring.d, mask, ln.chunks_done.p, ln.late.p, 0);
+        check_cuda(cudaEventRecord(ln.early_done, ln.side), "cudaEventRecord(early completions)");
+        check_cuda(cudaStreamWaitEvent(stream, ln.early_done, 0), "cudaStreamWaitEvent(early completions)");
         complete_kernel<<<2 * sms, 256, 0, stream>>>(ln.st.p, ln.adm.p, ln.info.p, ln.success.p, ln.used.p, cring.d,
-                                                      mask, ln.chunks_done.p);
+                                                      mask, ln.chunks_done.p, ln.late.p, 1);
         end_capture("cudaStreamEndCapture(work)");
         // 3. publication, after the work node
         check_cuda(cudaStreamBeginCaptureToGraph(stream, body, &if_node, nullptr, 1, cudaStreamCaptureModeRelaxed),
@@ -843,7 +897,7 @@ int sicc_devloop_create(const sicc_devloop_config_t* config, unsigned long long*
         if (c.idle_timeout_ms < 1) throw InvalidArgument("idle_timeout_ms must be >= 1");
         if (c.max_batch_frames < 0 || c.max_batch_iq_samples < 0 || (c.max_batch_frames > 0) != (c.max_batch_iq_samples > 0))
             throw InvalidArgument("max_batch_frames and max_batch_iq_samples: both positive (IQ requests) or both 0");
-        if (c.lanes < 0 || c.lanes > kMaxLanes) throw InvalidArgument("lanes must be 0..8 (0: one lane)");
+        if (c.lanes < 0 || c.lanes > kMaxLanes) throw InvalidArgument("lanes must be 0..16 (0: one lane)");
         auto L = std::make_shared<Loop>();
         L->cfg = c;
         L->cfg.lanes = std::max(1, c.lanes);
@@ -873,8 +927,12 @@ int sicc_devloop_create(const sicc_devloop_config_t* config, unsigned long long*
             ln->llr_off.alloc(static_cast<size_t>(c.max_batch_codewords));
             ln->info_off.alloc(static_cast<size_t>(c.max_batch_codewords));
             ln->chunks_done.alloc(static_cast<size_t>(L->max_req));
+            ln->late.alloc(static_cast<size_t>(L->max_req));
             ln->iqbuf.alloc(2 * static_cast<size_t>(std::max<long long>(c.max_batch_iq_samples, 1)));
             check_cuda(cudaStreamCreateWithFlags(&ln->stream, cudaStreamNonBlocking), "cudaStreamCreate(loop)");
+            check_cuda(cudaStreamCreateWithFlags(&ln->side, cudaStreamNonBlocking), "cudaStreamCreate(loop side)");
+            check_cuda(cudaEventCreateWithFlags(&ln->bp_done, cudaEventDisableTiming), "cudaEventCreate(loop)");
+            check_cuda(cudaEventCreateWithFlags(&ln->early_done, cudaEventDisableTiming), "cudaEventCreate(loop)");
             L->lanes.push_back(std::move(ln));
         }
         std::lock_guard<std::mutex> lock(g_mu);

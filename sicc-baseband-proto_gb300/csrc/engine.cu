@@ -830,6 +830,20 @@ int engine_bounds(unsigned long long handle, int* out_n_max, int* out_k_max)
     });
 }
 
+int engine_code_routes(unsigned long long handle, unsigned char* out_routes, int max_codes, int* out_count)
+{
+    return guarded([&] {
+        auto e = get(handle);
+        std::lock_guard<std::mutex> lock(e->mu);
+        if (!out_routes || !out_count) throw InvalidArgument("null argument");
+        const int K = static_cast<int>(e->codes.size());
+        if (K > max_codes) throw InvalidArgument("more codes than the output holds");
+        for (int i = 0; i < K; ++i) out_routes[i] = e->codes[i].desc.route_osd ? 1 : 0;
+        *out_count = K;
+        return CUDA_OSD_STATUS_OK;
+    });
+}
+
 int engine_prepare_capture(unsigned long long handle, int max_codewords)
 {
     return guarded([&] {

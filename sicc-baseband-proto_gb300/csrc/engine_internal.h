@@ -25,4 +25,8 @@ int engine_prepare_capture(unsigned long long handle, int max_codewords);
 // The device the engine's tables live on, its largest n and k (for buffer sizing).
 int engine_bounds(unsigned long long handle, int* out_n_max, int* out_k_max);
 
+// Per registered code (in id order, at most `max_codes`): 1 when a protected codeword of it that
+// BP fails goes on to OSD, else 0 (its BP result is final).
+int engine_code_routes(unsigned long long handle, unsigned char* out_routes, int max_codes, int* out_count);
+
 }  // namespace sicc
