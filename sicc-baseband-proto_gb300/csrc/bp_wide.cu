@@ -3,8 +3,9 @@
 //
 // One CTA of 512 threads decodes one codeword at a time and takes the next
 // from a global counter when it stops.  The posteriors live in shared memory
-// when they fit (n <= ~50k), else in the CTA's slice of a global scratch
-// block; the compressed check messages (alpha*min1, alpha*min2, argmin,
+// when they fit (n <= ~50k); for longer codes the layered kernel keeps the
+// first 51,200 in shared memory and the rest in the CTA's slice of a global
+// scratch block (the flooding kernel keeps them all there); the compressed check messages (alpha*min1, alpha*min2, argmin,
 // signs per row) and, for the flooding schedule, the variable-to-check
 // messages of every edge live in that slice too.  A slice is touched by one
 // CTA only, so it stays in L2 when the grid's slices fit there (the launcher
@@ -61,14 +62,15 @@ __device__ __forceinline__ unsigned cta_min(unsigned v, int* red)
 }
 
 // Outputs of a finished codeword (the shared-memory kernels' finalize step).
-__device__ void wide_finish(const BpParams& p, const BpIO& io, int c, int n, int w, int iter, const float* app,
+template <class App>
+__device__ void wide_finish(const BpParams& p, const BpIO& io, int c, int n, int w, int iter, const App& app,
                             const float* best, bool track_best, int* red, int* s_slot)
 {
     const int tid = threadIdx.x;
     bool accept = (w == 0);
     if (accept && p.min_abs_accept > 0.0f) {
         unsigned mn = 0x7f800000u;
-        for (int i = tid; i < n; i += kWideThreads) mn = min(mn, __float_as_uint(fabsf(app[i])));
+        for (int i = tid; i < n; i += kWideThreads) mn = min(mn, __float_as_uint(fabsf(app.ld(i))));
         accept = __uint_as_float(cta_min(mn, red)) >= p.min_abs_accept;
     }
     const bool route = !accept && p.route_failures_to_osd && io.osd_llr != nullptr;
@@ -80,18 +82,17 @@ __device__ void wide_finish(const BpParams& p, const BpIO& io, int c, int n, int
     }
     if (io.out_bits) {
         uint8_t* dst = io.out_bits + static_cast<size_t>(c) * io.out_stride;
-        for (int i = tid; i < io.out_len; i += kWideThreads) dst[i] = app[i] < 0.0f ? 1 : 0;
+        for (int i = tid; i < io.out_len; i += kWideThreads) dst[i] = app.ld(i) < 0.0f ? 1 : 0;
     }
     if (io.app_out) {
         float* dst = io.app_out + static_cast<size_t>(c) * n;
-        for (int i = tid; i < n; i += kWideThreads) dst[i] = app[i];
+        for (int i = tid; i < n; i += kWideThreads) dst[i] = app.ld(i);
     }
     __syncthreads();  // s_slot
     if (route) {
         const int s = *s_slot;
-        const float* b = track_best ? best : app;
         float* dst = io.osd_llr + static_cast<size_t>(s) * n;
-        for (int i = tid; i < n; i += kWideThreads) dst[i] = b[i];
+        for (int i = tid; i < n; i += kWideThreads) dst[i] = track_best ? best[i] : app.ld(i);
         if (tid == 0) io.osd_index[s] = c;
     }
 }
@@ -105,6 +106,21 @@ __device__ __forceinline__ int wide_next(const BpIO& io, int* s_next)
     return *s_next;
 }
 
+// Posteriors of the layered wide kernel: those of variables below `split` in shared
+// memory, the rest in the CTA's global slice (L2), so a code a little too long for shared
+// memory keeps most of its posterior gathers on chip.
+struct SplitApp {
+    float* s;   // shared memory, variables [0, split)
+    float* g;   // global slice, indexed by the variable (entries below split unused)
+    int split;
+    __device__ __forceinline__ float ld(int v) const { return v < split ? s[v] : g[v]; }
+    __device__ __forceinline__ void st(int v, float x) const
+    {
+        if (v < split) s[v] = x;
+        else g[v] = x;
+    }
+};
+
 // Rows a thread updates together in a layer: their loads are all issued before the
 // first store (the rows of a layer touch disjoint variables), so the latencies overlap.
 // Two for row degrees up to 16; one above, where the registers would spill.
@@ -116,7 +132,7 @@ constexpr int row_batch() { return D <= 16 ? 2 : 1; }
 // arrays: the shared-memory layered kernel's per-row arithmetic (bp_kernels.cu).
 template <int D, int kRowBatch = row_batch<D>()>
 __device__ __forceinline__ void wide_rows(const LayeredView& cv, const BpParams& p, int L, int rs0, int rows,
-                                          int first, float* app, float* r1, float* r2, unsigned* meta)
+                                          int first, const SplitApp& app, float* r1, float* r2, unsigned* meta)
 {
     int v[kRowBatch][D];
     float o1[kRowBatch], o2[kRowBatch], x[kRowBatch][D];
@@ -136,7 +152,7 @@ __device__ __forceinline__ void wide_rows(const LayeredView& cv, const BpParams&
 #pragma unroll
     for (int b = 0; b < kRowBatch; ++b)
 #pragma unroll
-        for (int j = 0; j < D; ++j) x[b][j] = v[b][j] >= 0 ? app[v[b][j]] : 0.0f;
+        for (int j = 0; j < D; ++j) x[b][j] = v[b][j] >= 0 ? app.ld(v[b][j]) : 0.0f;
 #pragma unroll
     for (int b = 0; b < kRowBatch; ++b) {
         if (v[b][0] < 0) continue;  // past the layer
@@ -166,7 +182,7 @@ __device__ __forceinline__ void wide_rows(const LayeredView& cv, const BpParams&
             if (v[b][j] >= 0) {
                 const unsigned sg = (nm >> j) & 1u;
                 const float mag = (j == idx) ? n2 : n1;
-                app[v[b][j]] = __fadd_rn(q[j], sg ? -mag : mag);
+                app.st(v[b][j], __fadd_rn(q[j], sg ? -mag : mag));
             }
         }
         const int ridx = first + rs0 + b * kWideThreads;
@@ -178,7 +194,7 @@ __device__ __forceinline__ void wide_rows(const LayeredView& cv, const BpParams&
 
 // Unsatisfied checks among the same rows under hard(app).
 template <int D, int kRowBatch = row_batch<D>()>
-__device__ __forceinline__ int wide_parity(const LayeredView& cv, int L, int rs0, int rows, const float* app)
+__device__ __forceinline__ int wide_parity(const LayeredView& cv, int L, int rs0, int rows, const SplitApp& app)
 {
     int v[kRowBatch][D];
 #pragma unroll
@@ -195,7 +211,7 @@ __device__ __forceinline__ int wide_parity(const LayeredView& cv, int L, int rs0
         unsigned par = 0;
 #pragma unroll
         for (int j = 0; j < D; ++j)
-            if (v[b][j] >= 0) par ^= (app[v[b][j]] < 0.0f) ? 1u : 0u;
+            if (v[b][j] >= 0) par ^= (app.ld(v[b][j]) < 0.0f) ? 1u : 0u;
         cnt += static_cast<int>(par);
     }
     return cnt;
@@ -205,7 +221,7 @@ __device__ __forceinline__ int wide_parity(const LayeredView& cv, int L, int rs0
 
 template <int D>
 __global__ void __launch_bounds__(kWideThreads, 1)
-bp_layered_wide_kernel(LayeredView cv, BpParams p, BpIO io, float* scratch, long long slice, int app_smem,
+bp_layered_wide_kernel(LayeredView cv, BpParams p, BpIO io, float* scratch, long long slice, int split,
                        int track_best)
 {
     extern __shared__ __align__(16) float s_app[];
@@ -215,8 +231,10 @@ bp_layered_wide_kernel(LayeredView cv, BpParams p, BpIO io, float* scratch, long
     const int n = cv.n, n_pad = (n + 3) & ~3;
     const int mp = cv.m;  // messages of the rows in layer order, packed
     float* g = scratch + static_cast<size_t>(blockIdx.x) * static_cast<size_t>(slice);
-    float* app = app_smem ? s_app : g;
-    float* best = app_smem ? g : g + n_pad;
+    // posteriors [0, split) in shared memory; with split < n the slice starts with n_pad posteriors
+    const bool all_smem = split >= n;
+    const SplitApp app{s_app, g, split};
+    float* best = all_smem ? g : g + n_pad;
     float* r1 = best + (track_best ? n_pad : 0);
     float* r2 = r1 + mp;
     unsigned* meta = reinterpret_cast<unsigned*>(r2 + mp);
@@ -235,7 +253,7 @@ bp_layered_wide_kernel(LayeredView cv, BpParams p, BpIO io, float* scratch, long
         const float* src = io.llr + static_cast<size_t>(c) * n;
         for (int i = tid; i < n; i += kWideThreads) {
             const float v = __ldcs(src + i);
-            app[i] = v;
+            app.st(i, v);
             if (track_best) best[i] = v;
         }
         for (int r = tid; r < mp; r += kWideThreads) {
@@ -256,7 +274,7 @@ bp_layered_wide_kernel(LayeredView cv, BpParams p, BpIO io, float* scratch, long
             w = syndrome();
             ++iter;
             if (track_best && (w < best_w || (w == 0 && best_w == 0))) {
-                for (int i = tid; i < n; i += kWideThreads) best[i] = app[i];
+                for (int i = tid; i < n; i += kWideThreads) best[i] = app.ld(i);
                 __syncthreads();  // copied before the next layer rewrites the posteriors
             }
             if (w < best_w) best_w = w;
@@ -265,6 +283,12 @@ bp_layered_wide_kernel(LayeredView cv, BpParams p, BpIO io, float* scratch, long
         wide_finish(p, io, c, n, w, iter, app, best, track_best != 0, s_red, &s_slot);
     }
 }
+
+// Plain posterior array for the flooding kernel's finish step.
+struct PlainApp {
+    const float* a;
+    __device__ __forceinline__ float ld(int v) const { return a[v]; }
+};
 
 __global__ void __launch_bounds__(kWideThreads, 1)
 bp_flooding_wide_kernel(FloodView cv, BpParams p, BpIO io, float* scratch, long long slice, int app_smem,
@@ -367,7 +391,7 @@ bp_flooding_wide_kernel(FloodView cv, BpParams p, BpIO io, float* scratch, long 
             }
             __syncthreads();
         }
-        wide_finish(p, io, c, n, w, iter, app, best, track_best != 0, s_red, &s_slot);
+        wide_finish(p, io, c, n, w, iter, PlainApp{app}, best, track_best != 0, s_red, &s_slot);
     }
 }
 
@@ -420,14 +444,31 @@ void launch_layered_wide_t(const LayeredView& cv, const BpParams& p, const BpIO&
     const long long n_pad = (cv.n + 3) & ~3;
     const long long mp = cv.m;
     const size_t app_bytes = static_cast<size_t>(n_pad) * sizeof(float);
-    const bool app_smem = app_bytes <= 200 * 1024;
-    long long slice = (app_smem ? 0 : n_pad) + (track_best ? n_pad : 0) + 3 * mp;
+    // posteriors in shared memory up to 200 KB: all of them, or the first 51,200 (variables
+    // beyond stay in the slice)
+    constexpr size_t kSmemApp = 200 * 1024;
+    const bool all_smem = app_bytes <= kSmemApp;
+    const int split = all_smem ? cv.n : static_cast<int>(kSmemApp / sizeof(float));
+    const size_t smem = all_smem ? app_bytes : kSmemApp;
+    long long slice = (all_smem ? 0 : n_pad) + (track_best ? n_pad : 0) + 3 * mp;
     slice = (slice + 31) & ~31LL;  // 128-byte aligned slices
-    launch_wide(bp_layered_wide_kernel<D>, app_bytes, slice, io.count, st,
-                [&](int ctas, size_t smem, float* scratch, int in_smem) {
-                    bp_layered_wide_kernel<D><<<ctas, kWideThreads, smem, st>>>(cv, p, io, scratch, slice, in_smem,
-                                                                                 track_best ? 1 : 0);
-                });
+    const auto kernel = bp_layered_wide_kernel<D>;
+    check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(kernel), smem), "cudaFuncSetAttribute(bp wide)");
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWideThreads, smem) != cudaSuccess || per_sm <= 0)
+        per_sm = 1;
+    const size_t slice_bytes = static_cast<size_t>(slice) * sizeof(float);
+    const int ctas = wide_grid(io.count, per_sm, slice_bytes);
+    int device = 0;
+    check_cuda(cudaGetDevice(&device), "cudaGetDevice");
+    void* scratch = nullptr;
+    check_cuda(cudaMallocFromPoolAsync(&scratch, std::max<size_t>(slice_bytes * ctas, 16), scratch_pool(device), st),
+               "cudaMallocFromPoolAsync(bp wide)");
+    kernel<<<ctas, kWideThreads, smem, st>>>(cv, p, io, static_cast<float*>(scratch), slice, split, track_best ? 1 : 0);
+    const cudaError_t err = cudaGetLastError();
+    const cudaError_t ferr = cudaFreeAsync(scratch, st);
+    check_cuda(err, "bp wide kernel launch");
+    check_cuda(ferr, "cudaFreeAsync(bp wide)");
 }
 
 }  // namespace
