@@ -4,7 +4,7 @@
 // One CTA of 512 threads decodes one codeword at a time and takes the next
 // from a global counter when it stops.  The posteriors live in shared memory
 // when they fit (n <= ~50k); for longer codes the layered kernel keeps the
-// first 51,200 in shared memory and the rest in the CTA's slice of a global
+// first 56,320 in shared memory and the rest in the CTA's slice of a global
 // scratch block (the flooding kernel keeps them all there); the compressed check messages (alpha*min1, alpha*min2, argmin,
 // signs per row) and, for the flooding schedule, the variable-to-check
 // messages of every edge live in that slice too.  A slice is touched by one
@@ -444,12 +444,12 @@ void launch_layered_wide_t(const LayeredView& cv, const BpParams& p, const BpIO&
     const long long n_pad = (cv.n + 3) & ~3;
     const long long mp = cv.m;
     const size_t app_bytes = static_cast<size_t>(n_pad) * sizeof(float);
-    // posteriors in shared memory up to 200 KB: all of them, or the first 51,200 (variables
-    // beyond stay in the slice)
-    constexpr size_t kSmemApp = 200 * 1024;
+    // posteriors in shared memory: all of them up to 200 KB, else the first 56,320 (220 KB;
+    // variables beyond stay in the slice)
+    constexpr size_t kSmemApp = 200 * 1024, kSplitApp = 220 * 1024;
     const bool all_smem = app_bytes <= kSmemApp;
-    const int split = all_smem ? cv.n : static_cast<int>(kSmemApp / sizeof(float));
-    const size_t smem = all_smem ? app_bytes : kSmemApp;
+    const int split = all_smem ? cv.n : static_cast<int>(kSplitApp / sizeof(float));
+    const size_t smem = all_smem ? app_bytes : kSplitApp;
     long long slice = (all_smem ? 0 : n_pad) + (track_best ? n_pad : 0) + 3 * mp;
     slice = (slice + 31) & ~31LL;  // 128-byte aligned slices
     const auto kernel = bp_layered_wide_kernel<D>;
