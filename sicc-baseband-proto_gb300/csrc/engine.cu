@@ -511,6 +511,8 @@ struct Engine {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaStream_t side[kOsdHClasses - 1] = {};  // large-code OSD classes beside the first
     cudaEvent_t fork = nullptr, join[kOsdHClasses - 1] = {};
+    cudaStream_t warp_side = nullptr;  // the short-code (warp) OSD beside the large-code classes
+    cudaEvent_t warp_fork = nullptr, warp_join = nullptr;
     bool timed = false;
     std::mutex mu;
     ~Engine()
@@ -528,6 +530,9 @@ struct Engine {
             if (e) cudaEventDestroy(e);
         for (auto& q : side)
             if (q) cudaStreamDestroy(q);
+        if (warp_fork) cudaEventDestroy(warp_fork);
+        if (warp_join) cudaEventDestroy(warp_join);
+        if (warp_side) cudaStreamDestroy(warp_side);
     }
     bool has_osd_h() const
     {
@@ -679,6 +684,9 @@ int sicc_engine_create(const sicc_engine_config_t* config, unsigned long long* o
         for (auto& q : e->side) check_cuda(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking), "cudaStreamCreate(engine side)");
         check_cuda(cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming), "cudaEventCreate(engine fork)");
         for (auto& ev : e->join) check_cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate(engine join)");
+        check_cuda(cudaStreamCreateWithFlags(&e->warp_side, cudaStreamNonBlocking), "cudaStreamCreate(engine warp OSD)");
+        check_cuda(cudaEventCreateWithFlags(&e->warp_fork, cudaEventDisableTiming), "cudaEventCreate(engine warp fork)");
+        check_cuda(cudaEventCreateWithFlags(&e->warp_join, cudaEventDisableTiming), "cudaEventCreate(engine warp join)");
         std::lock_guard<std::mutex> lock(g_mu);
         *out_handle = ++g_next;
         g_engines[*out_handle] = e;
@@ -948,14 +956,24 @@ int engine_decode(unsigned long long handle, int codewords, const unsigned char*
             oio.code_of = device_code_ids;
             oio.row_off = e->d_osd_rowoff;
             oio.info_off = device_info_offsets;
-            if (e->osd_nmax > 0) {  // short codes, one warp per codeword
+            // short codes (one warp per codeword) beside the long-code classes (one CTA per
+            // codeword): the kernels take disjoint codewords of the work list
+            const bool both = e->osd_nmax > 0 && e->has_osd_h();
+            if (e->osd_nmax > 0) {
                 OsdView shape{};
                 shape.n = e->osd_nmax;
                 shape.k = e->osd_kmax;
-                launch_osd(shape, oio, codewords, st);
+                cudaStream_t ws = st;
+                if (both) {
+                    check_cuda(cudaEventRecord(e->warp_fork, st), "cudaEventRecord(warp OSD fork)");
+                    check_cuda(cudaStreamWaitEvent(e->warp_side, e->warp_fork, 0), "cudaStreamWaitEvent(warp OSD)");
+                    ws = e->warp_side;
+                }
+                launch_osd(shape, oio, codewords, ws);
+                if (both) check_cuda(cudaEventRecord(e->warp_join, ws), "cudaEventRecord(warp OSD join)");
             }
-            if (e->has_osd_h())  // long codes, one CTA per codeword
-                launch_osd_h(e->h_cls, oio, codewords, st, e->side, e->fork, e->join);
+            if (e->has_osd_h()) launch_osd_h(e->h_cls, oio, codewords, st, e->side, e->fork, e->join);
+            if (both) check_cuda(cudaStreamWaitEvent(st, e->warp_join, 0), "cudaStreamWaitEvent(warp OSD join)");
         }
         check_cuda(cudaEventRecord(e->ev[3], st), "cudaEventRecord");
         e->timed = true;
