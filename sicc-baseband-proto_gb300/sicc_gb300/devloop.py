@@ -1,13 +1,16 @@
 """Host wrapper of the device-resident request loop (include/sicc_devloop.h).
 
-The loop is one CUDA graph repeated on the GPU by a conditional node: each
-iteration admits requests from a request ring in pinned host memory (within
-its codeword, LLR, frame and IQ budgets), lays them out, demodulates the OFDM
-IQ requests, decodes every codeword with the mixed-code engine (BP, then OSD
-for failures of requests with protection 1), copies the information bits back
-to the requests' pinned host buffers and publishes completions; an iteration
-that admits nothing skips straight to publication.  The host only appends
-requests and drains completions.
+The loop is one or more lanes, each a CUDA graph repeated on the GPU by a
+conditional node, sharing one request ring and one completion ring in pinned
+host memory.  Each lane iteration admits requests (within the lane's codeword,
+LLR, frame and IQ budgets, while no other lane is admitting), lays them out,
+demodulates the OFDM IQ requests, decodes every codeword with the lane's
+mixed-code engine (BP, then OSD for failures of requests with protection 1),
+copies the information bits back to the requests' pinned host buffers and
+publishes completions -- the requests that are final after BP while OSD runs,
+the others after it; an iteration that admits nothing skips straight to
+publication.  The host only appends requests and drains completions (which
+arrive in any order).
 
 Request buffers must be page-locked (e.g. ``torch.empty(..., pin_memory=True)``
 viewed as NumPy); ``pinned`` allocates such arrays.
