@@ -44,6 +44,8 @@ struct OsdSmem {
     unsigned long long rows[KR * 32][NW];  // reduced rows by pivot index
     unsigned long long frows[kFlipRows<NW, KR> ? KR * 32 : 1][NW];  // the same rows by flip-pool rank
     int16_t mrb_pos[KR * 32];
+    float prel[KR * 32];      // flip-pool rank -> |llr| of its position (non-decreasing)
+    int16_t rstart[KR * 32];  // order-2 rows: first surviving pair of row a in the compact list
 };
 
 __device__ __forceinline__ unsigned long long shfl_u64(unsigned long long v, int src)
@@ -299,6 +301,7 @@ osd_kernel(OsdView ov0, OsdIO io)
             const int r = (k - lo) + (t - a);
             if (r < ov.pool) {
                 s.flip[r] = static_cast<int16_t>(t);
+                s.prel[r] = s.rel_sorted[s.mrb_pos[t]];
                 if (kFlipRows<NW, KR>)
 #pragma unroll
                     for (int w = 0; w < NW; ++w) s.frows[kFlipRows<NW, KR> ? r : 0][w] = s.rows[t][w];
@@ -312,67 +315,143 @@ osd_kernel(OsdView ov0, OsdIO io)
         // pruned (strict >), so the first minimum in test order still wins.
         unsigned long long best_key = ~0ull;
         float thr = INFINITY;
-        const int rounds = (ov.num_tests + 31) / 32;
         const int share = io.share_rounds > 0 ? io.share_rounds : 2;
-        for (int rd = 0; rd < rounds; ++rd) {
-            const int q = rd * 32 + lane;
-            if (q < ov.num_tests) {
-                unsigned long long d[NW];
+        // the metric of test q, whose flips are pool ranks f0, f1, f2 (-1: none), pruned against thr
+        auto evaluate = [&](int q, int f0, int f1, int f2) {
+            unsigned long long d[NW];
 #pragma unroll
-                for (int w = 0; w < NW; ++w) d[w] = acc[w];
-                if (q > 0) {
-                    const uint32_t cmb = ov.combos[q - 1];
+            for (int w = 0; w < NW; ++w) d[w] = acc[w];
+            const int fl[3] = {f0, f1, f2};
 #pragma unroll
-                    for (int f = 0; f < 3; ++f) {
-                        const uint32_t fi = (cmb >> (10 * f)) & 0x3FFu;
-                        if (fi != 0x3FFu) {
-                            if (kFlipRows<NW, KR>) {
+            for (int f = 0; f < 3; ++f) {
+                const int fi = fl[f];
+                if (fi >= 0) {
+                    if (kFlipRows<NW, KR>) {
 #pragma unroll
-                                for (int w = 0; w < NW; ++w) d[w] ^= s.frows[kFlipRows<NW, KR> ? fi : 0][w];
-                            } else {
-                                const int t = s.flip[fi];
+                        for (int w = 0; w < NW; ++w) d[w] ^= s.frows[kFlipRows<NW, KR> ? fi : 0][w];
+                    } else {
+                        const int t = s.flip[fi];
 #pragma unroll
-                                for (int w = 0; w < NW; ++w) d[w] ^= s.rows[t][w];
-                            }
-                        }
-                    }
-                }
-                float metric = 0.0f;
-                bool pruned = false;
-#pragma unroll
-                for (int h = 0; h < 2 * NW; ++h) {
-                    unsigned bits = static_cast<unsigned>(d[h >> 1] >> ((h & 1) * 32));
-                    const float* rel = s.rel_sorted + h * 32;
-                    while (bits && !pruned) {
-                        const int b = __ffs(bits) - 1;
-                        metric = __fadd_rn(metric, rel[b]);
-                        bits &= bits - 1;
-                        pruned = metric > thr;
-                    }
-                }
-                if (!pruned) {
-                    const unsigned long long key =
-                        (static_cast<unsigned long long>(__float_as_uint(metric)) << 32) | static_cast<unsigned>(q);
-                    if (key < best_key) {
-                        best_key = key;
-                        thr = fminf(thr, metric);
+                        for (int w = 0; w < NW; ++w) d[w] ^= s.rows[t][w];
                     }
                 }
             }
-            if (rd % share == share - 1) {  // share the best metric so far across the warp
+            float metric = 0.0f;
+            bool pruned = false;
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const unsigned long long other = shfl_xor_u64(best_key, o);
-                    best_key = other < best_key ? other : best_key;
+            for (int h = 0; h < 2 * NW; ++h) {
+                unsigned bits = static_cast<unsigned>(d[h >> 1] >> ((h & 1) * 32));
+                const float* rel = s.rel_sorted + h * 32;
+                while (bits && !pruned) {
+                    const int b = __ffs(bits) - 1;
+                    metric = __fadd_rn(metric, rel[b]);
+                    bits &= bits - 1;
+                    pruned = metric > thr;
                 }
-                if (best_key != ~0ull) thr = __uint_as_float(static_cast<unsigned>(best_key >> 32));
+            }
+            if (!pruned) {
+                const unsigned long long key =
+                    (static_cast<unsigned long long>(__float_as_uint(metric)) << 32) | static_cast<unsigned>(q);
+                if (key < best_key) {
+                    best_key = key;
+                    thr = fminf(thr, metric);
+                }
+            }
+        };
+        auto share_best = [&]() {  // the best metric so far, to every lane
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long other = shfl_xor_u64(best_key, o);
+                best_key = other < best_key ? other : best_key;
+            }
+            if (best_key != ~0ull) thr = __uint_as_float(static_cast<unsigned>(best_key >> 32));
+        };
+        auto flips_of = [&](int q, int& f0, int& f1, int& f2) {
+            f0 = f1 = f2 = -1;
+            if (q > 0) {
+                const uint32_t cmb = ov.combos[q - 1];
+                const uint32_t a = cmb & 0x3FFu, b = (cmb >> 10) & 0x3FFu, c = (cmb >> 20) & 0x3FFu;
+                f0 = a != 0x3FFu ? static_cast<int>(a) : -1;
+                f1 = b != 0x3FFu ? static_cast<int>(b) : -1;
+                f2 = c != 0x3FFu ? static_cast<int>(c) : -1;
+            }
+        };
+        const int P = ov.pool;
+        const bool complete2 = P >= 2 && ov.num_tests == 1 + P + P * (P - 1) / 2;
+        if (complete2) {
+            // The tests are the base, the P single flips, then every pair (a, b), a < b, in
+            // lexicographic order (test 1 + P + a (2P - a - 1) / 2 + b - a - 1).  A candidate
+            // differs from the hard decision at its flipped positions, and the metric, summed in
+            // position order, is at least those terms summed alone (each rounded partial sum of
+            // a sum of non-negative terms is at least that of any of its subsequences): a pair
+            // whose two |llr| already add up above the best metric of the base and single-flip
+            // tests cannot win.  The pool is weakest first, so within row a the bound grows
+            // with b and each row keeps a prefix (binary search); only those pairs are
+            // evaluated, 32 at a time from a compact list.
+            const int single = 1 + P;
+            for (int rd = 0; rd * 32 < single; ++rd) {
+                const int q = rd * 32 + lane;
+                if (q < single) evaluate(q, q > 0 ? q - 1 : -1, -1, -1);
+            }
+            share_best();
+            const int R = (P - 1 + 31) / 32;  // rows a = 0 .. P-2, R consecutive rows per lane
+            int mine = 0;
+            for (int i = 0; i < R; ++i) {
+                const int a = lane * R + i;
+                int cnt = 0;
+                if (a < P - 1) {
+                    const float ra = s.prel[a];
+                    int lo = a + 1, hi = P;  // first b with bound > thr
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (__fadd_rn(ra, s.prel[mid]) > thr) hi = mid;
+                        else lo = mid + 1;
+                    }
+                    cnt = lo - (a + 1);
+                }
+                if (a < P - 1) s.rstart[a] = static_cast<int16_t>(mine);  // lane-local offset for now
+                mine += cnt;
+            }
+            int incl = mine;  // inclusive scan of the lanes' pair counts
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int up = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += up;
+            }
+            const int base = incl - mine, total = __shfl_sync(0xffffffffu, incl, 31);
+            for (int i = 0; i < R; ++i) {
+                const int a = lane * R + i;
+                if (a < P - 1) s.rstart[a] = static_cast<int16_t>(s.rstart[a] + base);
+            }
+            __syncwarp();
+            int rd = 0;
+            for (int i0 = 0; i0 < total; i0 += 32, ++rd) {
+                const int idx = i0 + lane;
+                if (idx < total) {
+                    int lo = 0, hi = P - 2;  // the last row a with rstart[a] <= idx
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (s.rstart[mid] <= idx) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    const int a = lo, b = a + 1 + (idx - s.rstart[a]);
+                    evaluate(single + a * (2 * P - a - 1) / 2 + (b - a - 1), a, b, -1);
+                }
+                if (rd % share == share - 1) share_best();
+            }
+        } else {
+            const int rounds = (ov.num_tests + 31) / 32;
+            for (int rd = 0; rd < rounds; ++rd) {
+                const int q = rd * 32 + lane;
+                if (q < ov.num_tests) {
+                    int f0, f1, f2;
+                    flips_of(q, f0, f1, f2);
+                    evaluate(q, f0, f1, f2);
+                }
+                if (rd % share == share - 1) share_best();
             }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long other = shfl_xor_u64(best_key, o);
-            best_key = other < best_key ? other : best_key;
-        }
+        share_best();
         // ---- 7. winner -> original positions ----
         const int qbest = static_cast<int>(best_key & 0xffffffffull);
         unsigned long long d[NW];
