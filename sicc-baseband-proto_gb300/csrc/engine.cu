@@ -676,7 +676,7 @@ int sicc_engine_create(const sicc_engine_config_t* config, unsigned long long* o
         check_cuda(cudaMalloc(&e->d_order, sizeof(int) * config->max_codewords), "cudaMalloc(order)");
         check_cuda(cudaMalloc(&e->d_q_start, sizeof(int) * (kMaxCodes + 1)), "cudaMalloc(q_start)");
         check_cuda(cudaMalloc(&e->d_q_units, sizeof(int) * (kMaxCodes + 1)), "cudaMalloc(q_units)");
-        check_cuda(cudaMalloc(&e->d_counters, sizeof(int) * 8), "cudaMalloc(counters)");
+        check_cuda(cudaMalloc(&e->d_counters, sizeof(int) * 16), "cudaMalloc(counters)");  // [8..11]: OSD work
         check_cuda(cudaMalloc(&e->d_osd_rowoff, sizeof(long long) * config->max_codewords), "cudaMalloc(osd rows)");
         check_cuda(cudaMalloc(&e->d_osd_index, sizeof(int) * config->max_codewords), "cudaMalloc(osd index)");
         check_cuda(cudaMalloc(&e->d_osd_llr, sizeof(float) * config->max_llr_floats), "cudaMalloc(osd rows)");
@@ -956,6 +956,8 @@ int engine_decode(unsigned long long handle, int codewords, const unsigned char*
             oio.code_of = device_code_ids;
             oio.row_off = e->d_osd_rowoff;
             oio.info_off = device_info_offsets;
+            oio.work = e->d_counters + 8;
+            oio.work_h = e->d_counters + 9;
             // short codes (one warp per codeword) beside the long-code classes (one CTA per
             // codeword): the kernels take disjoint codewords of the work list
             const bool both = e->osd_nmax > 0 && e->has_osd_h();

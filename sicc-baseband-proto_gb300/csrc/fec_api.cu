@@ -106,13 +106,13 @@ uint64_t now_us()
 struct Scratch {
     DevBuf<float> osd_llr;
     DevBuf<int> osd_index;
-    DevBuf<int> counters;  // [0] osd count, [1] work counter
+    DevBuf<int> counters;  // [0] osd count, [1] BP work counter, [2] OSD work counter
     DevBuf<uint8_t> success, used_osd, iterations, bits;
     void alloc(int cap, int n, int bits_per_cw)
     {
         osd_llr.alloc(static_cast<size_t>(cap) * n);
         osd_index.alloc(static_cast<size_t>(cap));
-        counters.alloc(2);
+        counters.alloc(3);
         success.alloc(cap);
         used_osd.alloc(cap);
         iterations.alloc(cap);
@@ -191,6 +191,7 @@ void run_bp_osd(const DeviceCode& code, const BpParams& bp, const BpLaunch& shap
         oio.info_stride = out_stride;
         oio.used_osd = d_used_osd;
         oio.share_rounds = shape.osd_share_rounds;
+        oio.work = s.counters.p + 2;
         launch_osd(code.osd_view(), oio, count, st, 0, shape.osd_ctas);
     }
     if (rec) {
@@ -791,7 +792,7 @@ void validate_stream_config(const cuda_osd_stream_config_t* c)
 // Decodes with a stream decoder's code tables and settings, but with the
 // BP -> OSD hand-off scratch supplied by the caller (used by the entry point
 // whose scratch is a static device array).  Layout of `scratch`:
-// [0, 256) two int counters; [256, 256 + 4*cap) OSD index list;
+// [0, 256) the counters (OSD items, BP work, OSD work); [256, 256 + 4*cap) OSD index list;
 // then cap rows of n floats (256-byte aligned).
 int decode_with_caller_scratch(unsigned long long handle, const float* d_llr, int count, uint8_t* d_info,
                                uint8_t* d_success, uint8_t* d_used_osd, uint8_t* d_iter,
@@ -836,6 +837,7 @@ int decode_with_caller_scratch(unsigned long long handle, const float* d_llr, in
         oio.info_stride = d->k;
         oio.used_osd = d_used_osd;
         oio.share_rounds = d->shape.osd_share_rounds;
+        oio.work = counters + 2;  // inside the counters' 256 bytes
         launch_osd(d->code->osd_view(), oio, count, st, 0, d->shape.osd_ctas);
     }
     return CUDA_OSD_STATUS_OK;

@@ -88,7 +88,13 @@ osd_kernel(OsdView ov0, OsdIO io)
     const int count = io.count_ptr ? *io.count_ptr : io.count;
     const int total_warps = gridDim.x * kOsdWarps;
 
-    for (int item = blockIdx.x * kOsdWarps + warp; item < count; item += total_warps) {
+    auto next_item = [&](int prev) -> int {  // the warp's next work item
+        if (!io.work) return prev < 0 ? static_cast<int>(blockIdx.x) * kOsdWarps + warp : prev + total_warps;
+        int it = 0;
+        if (lane == 0) it = atomicAdd(io.work, 1);
+        return __shfl_sync(0xffffffffu, it, 0);
+    };
+    for (int item = next_item(-1); item < count; item = next_item(item)) {
         const int cw = io.index ? io.index[item] : item;
         const OsdView ov = io.views ? io.views[io.code_of[cw]] : ov0;
         if (ov.n == 0) continue;  // code without warp-kernel tables (uniform over the warp)
@@ -505,6 +511,7 @@ void launch_osd(const OsdView& ov, const OsdIO& io, int max_items, cudaStream_t 
 {
     (void)warps_per_cta;
     if (max_items <= 0) return;
+    if (io.work) check_cuda(cudaMemsetAsync(io.work, 0, sizeof(int), st), "reset OSD work counter");
     // for a mixed-code batch `ov` carries the largest n and k of its codes
     const int nw = (ov.n + 63) / 64;
     const int kr = (ov.k + 31) / 32;

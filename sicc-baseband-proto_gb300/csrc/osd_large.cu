@@ -150,11 +150,19 @@ osd_h_kernel(OsdHView hv0, OsdHLayout lay, OsdIO io)
     __shared__ int s_rp[2][kRound];
     __shared__ int s_np[2], s_used[2], s_jstop[2];
     __shared__ unsigned long long s_best;
+    __shared__ int s_item;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int TS = lay.ts;
     const int count = io.count_ptr ? *io.count_ptr : io.count;
 
-    for (int item = blockIdx.x; item < count; item += gridDim.x) {
+    auto next_item = [&](int prev) -> int {  // the CTA's next work item (all threads get it)
+        if (!io.work_h) return prev < 0 ? static_cast<int>(blockIdx.x) : prev + static_cast<int>(gridDim.x);
+        __syncthreads();  // every thread has read the previous one
+        if (tid == 0) s_item = atomicAdd(io.work_h, 1);
+        __syncthreads();
+        return s_item;
+    };
+    for (int item = next_item(-1); item < count; item = next_item(item)) {
         const int cw = io.index ? io.index[item] : item;
         const OsdHView hv = io.hviews ? io.hviews[io.code_of[cw]] : hv0;
         if (hv.n == 0 || hv.m <= lay.mlo || hv.m > lay.mhi) continue;  // another kernel's item (uniform over the CTA)
@@ -741,8 +749,11 @@ OsdHLayout osd_h_layout(const OsdHBounds& bd, int threads, int mlo, int mhi)
 }
 
 template <int kThreads>
-void launch_osd_h_class(const OsdHBounds& bd, int mlo, int mhi, const OsdIO& io, int max_items, cudaStream_t st)
+void launch_osd_h_class(const OsdHBounds& bd, int mlo, int mhi, const OsdIO& io_all, int max_items, cudaStream_t st,
+                        int cls)
 {
+    OsdIO io = io_all;  // the class's own work counter
+    io.work_h = io_all.work_h ? io_all.work_h + cls : nullptr;
     OsdHLayout l = osd_h_layout(bd, kThreads, mlo, mhi);
     size_t smem = carve(l, nullptr, nullptr);
     if (smem > 227 * 1024) throw InvalidArgument("large-code OSD tables exceed shared memory (m <= 1024, n <= 4096)");
@@ -795,6 +806,7 @@ void launch_osd_h(const OsdHBounds* cls, const OsdIO& io, int max_items, cudaStr
         if (cls[c].mmax > kOsdHClassMaxM[c]) throw InvalidArgument("large-code OSD: code in the wrong class (m <= 1024)");
     }
     if (present == 0) return;
+    if (io.work_h) check_cuda(cudaMemsetAsync(io.work_h, 0, kOsdHClasses * sizeof(int), st), "reset OSD work counters");
     // the classes run side by side: the first present one on st, the others on side streams
     const bool fan = present > 1 && side && fork && join;
     if (fan) check_cuda(cudaEventRecord(fork, st), "cudaEventRecord(osd fork)");
@@ -807,8 +819,8 @@ void launch_osd_h(const OsdHBounds* cls, const OsdIO& io, int max_items, cudaStr
             check_cuda(cudaStreamWaitEvent(cs, fork, 0), "cudaStreamWaitEvent(osd fork)");
         }
         const int mlo = c == 0 ? 0 : kOsdHClassMaxM[c - 1];
-        if (kOsdHClassThreads[c] == 256) launch_osd_h_class<256>(cls[c], mlo, kOsdHClassMaxM[c], io, max_items, cs);
-        else launch_osd_h_class<512>(cls[c], mlo, kOsdHClassMaxM[c], io, max_items, cs);
+        if (kOsdHClassThreads[c] == 256) launch_osd_h_class<256>(cls[c], mlo, kOsdHClassMaxM[c], io, max_items, cs, c);
+        else launch_osd_h_class<512>(cls[c], mlo, kOsdHClassMaxM[c], io, max_items, cs, c);
         if (fan && used > 0) {
             check_cuda(cudaEventRecord(join[used - 1], cs), "cudaEventRecord(osd join)");
             check_cuda(cudaStreamWaitEvent(st, join[used - 1], 0), "cudaStreamWaitEvent(osd join)");

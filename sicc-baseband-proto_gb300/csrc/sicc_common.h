@@ -146,6 +146,11 @@ struct OsdIO {
     // warp's best metric, which tightens every lane's pruning bound (0 = 2);
     // the winner does not depend on it
     int share_rounds;
+    // Work counters (device ints the launcher zeroes on the stream): each warp (warp kernel) or
+    // CTA (large-code kernel, one counter per class) takes its next item from them, so a few
+    // expensive codewords do not hold up one warp's share.  Null: items by static striding.
+    int* work;      // warp kernel
+    int* work_h;    // [kOsdHClasses] large-code kernel
 };
 
 }  // namespace sicc
