@@ -1406,7 +1406,7 @@ FRAME_BENCH_SRC = os.path.join(ROOT, "tests", "cpp", "ofdm_frame_bench.cpp")
 
 
 def _frame_bench_line(impl, res, wall_s, frames, clk, extra):
-    """JSON line of the per-frame Pipeline workload from the driver's output."""
+    """JSON line of the per-frame Pipeline workload from the benchmark program's output."""
     mbps = res["rx_fps"] * res["info_bits_per_frame"] / 1e6
     line = {"metric": "frames/s through Pipeline::demod_frame_to_host_llr (host frame -> sync + demod -> host LLRs), "
                       "reference GPU pipeline benchmark configuration",
