@@ -438,17 +438,12 @@ osd_kernel(OsdView ov0, OsdIO io)
                 if (a < P - 1) s.rstart[a] = static_cast<int16_t>(s.rstart[a] + base);
             }
             __syncwarp();
-            int rd = 0;
+            int rd = 0, a = 0;  // a: the last row with rstart[a] <= idx (idx only grows: walk forward)
             for (int i0 = 0; i0 < total; i0 += 32, ++rd) {
                 const int idx = i0 + lane;
                 if (idx < total) {
-                    int lo = 0, hi = P - 2;  // the last row a with rstart[a] <= idx
-                    while (lo < hi) {
-                        const int mid = (lo + hi + 1) >> 1;
-                        if (s.rstart[mid] <= idx) lo = mid;
-                        else hi = mid - 1;
-                    }
-                    const int a = lo, b = a + 1 + (idx - s.rstart[a]);
+                    while (a < P - 2 && s.rstart[a + 1] <= idx) ++a;
+                    const int b = a + 1 + (idx - s.rstart[a]);
                     evaluate(single + a * (2 * P - a - 1) / 2 + (b - a - 1), a, b, -1);
                 }
                 if (rd % share == share - 1) share_best();
