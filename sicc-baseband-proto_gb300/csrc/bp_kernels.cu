@@ -29,10 +29,11 @@ namespace sicc {
 namespace {
 
 // Group-local syndrome weight of hard(app) under the layered tables; a row's
-// D slots are loaded together (no chain of dependent loads per slot).
+// D slots are loaded together (no chain of dependent loads per slot).  Empty
+// slots hold the dummy posterior's index (+inf: never flips a parity).
 template <int D>
 __device__ __forceinline__ int layered_syndrome(const LayeredView& cv, const int* s_vars, const float* app,
-                                                int gl, int G, unsigned gmask)
+                                                int gl, int G, unsigned gmask, int dummy)
 {
     int cnt = 0;
     for (int L = 0; L < cv.num_layers; ++L) {
@@ -46,11 +47,11 @@ __device__ __forceinline__ int layered_syndrome(const LayeredView& cv, const int
 #pragma unroll
                 for (int x = 0; x < 8; ++x) {
                     const int j = j0 + x;
-                    v[x] = (j < D && j < cv.maxdeg) ? vp[j * cv.width] : -1;
+                    v[x] = (j < D && j < cv.maxdeg) ? vp[j * cv.width] : dummy;
                 }
 #pragma unroll
                 for (int x = 0; x < 8; ++x)
-                    if (v[x] >= 0) par ^= (app[v[x]] < 0.0f) ? 1u : 0u;
+                    if (j0 + x < D) par ^= (app[v[x]] < 0.0f) ? 1u : 0u;
             }
             cnt += static_cast<int>(par);
         }
@@ -66,8 +67,16 @@ bp_layered_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int sl
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int table = cv.num_layers * cv.maxdeg * cv.width;
+    // Empty edge slots (short rows, row slots past a layer's last row) point at a dummy
+    // posterior held at +inf behind each slot's posteriors: such an edge never sets a row's
+    // minima, argmin or sign and never flips a parity, and its update leaves it at +inf, so
+    // the row loops need no per-edge test.
+    const int dummy = (cv.n + 3) & ~3;
     int* s_vars = reinterpret_cast<int*>(smem);
-    for (int i = threadIdx.x; i < table; i += blockDim.x) s_vars[i] = cv.vars[i];
+    for (int i = threadIdx.x; i < table; i += blockDim.x) {
+        const int v = cv.vars[i];
+        s_vars[i] = v >= 0 ? v : dummy;
+    }
     __syncthreads();
 
     const int G = cv.group;
@@ -82,8 +91,8 @@ bp_layered_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int sl
     const int n_pad = (n + 3) & ~3;
     const int mp = cv.num_layers * cv.width;
     float* app = reinterpret_cast<float*>(smem) + ((table + 3) & ~3) + static_cast<size_t>(slot) * slot_floats;
-    float* best = app + n_pad;  // only when track_best
-    float* r1 = app + (track_best ? 2 : 1) * n_pad;
+    float* best = app + n_pad + 4;  // only when track_best (app[n_pad] is the dummy)
+    float* r1 = app + (track_best ? 2 : 1) * n_pad + 4;
     float* r2 = r1 + mp;
     unsigned* meta = reinterpret_cast<unsigned*>(r2 + mp);
 
@@ -114,10 +123,11 @@ bp_layered_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int sl
             meta[r] = 0u;
         }
         __syncwarp(gmask);
-        best_w = layered_syndrome<D>(cv, s_vars, app, gl, G, gmask);
+        best_w = layered_syndrome<D>(cv, s_vars, app, gl, G, gmask, dummy);
         iter = 0;
     };
 
+    if (gl == 0) app[dummy] = __int_as_float(0x7f800000);  // +inf, before init's __syncwarp
     if (active) init(c);
 
     while (__any_sync(0xffffffffu, active)) {
@@ -127,28 +137,27 @@ bp_layered_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int sl
                 for (int rr = 0; rr < cv.rows_per_lane; ++rr) {
                     const int rs = gl + rr * G;
                     const int ridx = L * cv.width + rs;
+                    const int* vp = s_vars + (L * cv.maxdeg) * cv.width + rs;
+                    int v[D];
+#pragma unroll
+                    for (int j = 0; j < D; ++j) v[j] = (j < cv.maxdeg) ? vp[j * cv.width] : dummy;
+                    if (v[0] == dummy) continue;  // row slot past the layer's last row
                     const float o1 = r1[ridx], o2 = r2[ridx];
                     const unsigned om = meta[ridx];
-                    const int* vp = s_vars + (L * cv.maxdeg) * cv.width + rs;
                     float q[D];
-                    int v[D];
                     float m1 = FLT_MAX, m2 = FLT_MAX;
                     int idx = 0;
                     unsigned neg = 0;
 #pragma unroll
                     for (int j = 0; j < D; ++j) {
-                        v[j] = (j < cv.maxdeg) ? vp[j * cv.width] : -1;
-                        q[j] = 0.0f;
-                        if (v[j] >= 0) {
-                            const float qj = __fsub_rn(app[v[j]], rebuild(o1, o2, om, j));
-                            q[j] = qj;
-                            neg |= (qj < 0.0f) ? (1u << j) : 0u;
-                            const float a = fabsf(qj);
-                            // first strict minimum and second minimum (magnitudes are >= +0)
-                            idx = (a < m1) ? j : idx;
-                            m2 = fminf(m2, fmaxf(m1, a));
-                            m1 = fminf(m1, a);
-                        }
+                        const float qj = __fsub_rn(app[v[j]], rebuild(o1, o2, om, j));
+                        q[j] = qj;
+                        neg |= (qj < 0.0f) ? (1u << j) : 0u;
+                        const float a = fabsf(qj);
+                        // first strict minimum and second minimum (magnitudes are >= +0)
+                        idx = (a < m1) ? j : idx;
+                        m2 = fminf(m2, fmaxf(m1, a));
+                        m1 = fminf(m1, a);
                     }
                     const unsigned tot = static_cast<unsigned>(__popc(neg)) & 1u;
                     const float n1 = nms_mag(p.alpha, p.beta, m1);
@@ -158,11 +167,9 @@ bp_layered_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int sl
                     const unsigned nm = ((neg ^ (0u - tot)) & 0x07FFFFFFu) | (static_cast<unsigned>(idx) << 27);
 #pragma unroll
                     for (int j = 0; j < D; ++j) {
-                        if (v[j] >= 0) {
-                            const unsigned s = (nm >> j) & 1u;
-                            const float mag = (j == idx) ? n2 : n1;
-                            app[v[j]] = __fadd_rn(q[j], s ? -mag : mag);
-                        }
+                        const unsigned s = (nm >> j) & 1u;
+                        const float mag = (j == idx) ? n2 : n1;
+                        app[v[j]] = __fadd_rn(q[j], s ? -mag : mag);
                     }
                     r1[ridx] = n1;
                     r2[ridx] = n2;
@@ -170,7 +177,7 @@ bp_layered_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int sl
                 }
                 __syncwarp(gmask);
             }
-            const int w = layered_syndrome<D>(cv, s_vars, app, gl, G, gmask);
+            const int w = layered_syndrome<D>(cv, s_vars, app, gl, G, gmask, dummy);
             ++iter;
             if (track_best && (w < best_w || (w == 0 && best_w == 0))) {
                 for (int i = gl; i < n; i += G) best[i] = app[i];
@@ -225,7 +232,11 @@ bp_layered_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int sl
 // tables (variable indices) stay in registers for the whole launch and its
 // rows' compressed messages in registers for the codeword, so the row updates
 // and the syndrome go to shared memory only for the posteriors.  Rows, order
-// and arithmetic are those of bp_layered_kernel.
+// and arithmetic are those of bp_layered_kernel.  A row shorter than D (and a
+// row slot past its layer's last row) points its missing edges at a dummy
+// posterior held at +inf behind the slot's posteriors: such an edge never sets
+// the row's minima, argmin or sign and never flips a parity, and its update
+// leaves it at +inf, so the row loops need no per-edge test.
 template <int D, int NL>
 __global__ void __launch_bounds__(kBpThreads, 3)
 bp_layered_reg_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, int slot_floats, int track_best)
@@ -244,16 +255,21 @@ bp_layered_reg_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, in
     const int rpl = cv.rows_per_lane;
     const int nrows = cv.num_layers * rpl;
     float* app = reinterpret_cast<float*>(smem) + static_cast<size_t>(slot) * slot_floats;
-    float* best = app + n_pad;  // only when track_best
+    const int dummy = n_pad;           // app[dummy] = +inf for the whole launch
+    float* best = app + n_pad + 4;     // only when track_best
 
     // row t of this lane: layer t / rpl, slot gl + (t mod rpl) G
     int vr[NL][D];
+    unsigned real_rows = 0;  // bit t: row t of this lane exists
 #pragma unroll
     for (int t = 0; t < NL; ++t) {
         const int L = t / rpl, rs = gl + (t - L * rpl) * G;
 #pragma unroll
-        for (int j = 0; j < D; ++j)
-            vr[t][j] = (t < nrows && j < cv.maxdeg) ? __ldg(cv.vars + (L * cv.maxdeg + j) * cv.width + rs) : -1;
+        for (int j = 0; j < D; ++j) {
+            const int v = (t < nrows && j < cv.maxdeg) ? __ldg(cv.vars + (L * cv.maxdeg + j) * cv.width + rs) : -1;
+            vr[t][j] = v >= 0 ? v : dummy;
+        }
+        real_rows |= (vr[t][0] != dummy) ? (1u << t) : 0u;
     }
     float m1r[NL], m2r[NL];
     unsigned mr[NL];
@@ -264,8 +280,7 @@ bp_layered_reg_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, in
         for (int t = 0; t < NL; ++t) {
             unsigned par = 0;
 #pragma unroll
-            for (int j = 0; j < D; ++j)
-                if (vr[t][j] >= 0) par ^= (app[vr[t][j]] < 0.0f) ? 1u : 0u;
+            for (int j = 0; j < D; ++j) par ^= (app[vr[t][j]] < 0.0f) ? 1u : 0u;
             cnt += static_cast<int>(par);
         }
         return static_cast<int>(__reduce_add_sync(gmask, static_cast<unsigned>(cnt)));
@@ -303,6 +318,7 @@ bp_layered_reg_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, in
         iter = 0;
     };
 
+    if (gl == 0) app[dummy] = __int_as_float(0x7f800000);  // +inf, before init's __syncwarp
     if (active) init(c);
 
     while (__any_sync(0xffffffffu, active)) {
@@ -310,23 +326,20 @@ bp_layered_reg_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, in
             // ---- one layered iteration ----
 #pragma unroll
             for (int t = 0; t < NL; ++t) {
-                if (vr[t][0] >= 0) {
+                if ((real_rows >> t) & 1u) {
                     float q[D];
                     float m1 = FLT_MAX, m2 = FLT_MAX;
                     int idx = 0;
                     unsigned neg = 0;
 #pragma unroll
                     for (int j = 0; j < D; ++j) {
-                        q[j] = 0.0f;
-                        if (vr[t][j] >= 0) {
-                            const float qj = __fsub_rn(app[vr[t][j]], rebuild(m1r[t], m2r[t], mr[t], j));
-                            q[j] = qj;
-                            neg |= (qj < 0.0f) ? (1u << j) : 0u;
-                            const float a = fabsf(qj);
-                            idx = (a < m1) ? j : idx;
-                            m2 = fminf(m2, fmaxf(m1, a));
-                            m1 = fminf(m1, a);
-                        }
+                        const float qj = __fsub_rn(app[vr[t][j]], rebuild(m1r[t], m2r[t], mr[t], j));
+                        q[j] = qj;
+                        neg |= (qj < 0.0f) ? (1u << j) : 0u;
+                        const float a = fabsf(qj);
+                        idx = (a < m1) ? j : idx;
+                        m2 = fminf(m2, fmaxf(m1, a));
+                        m1 = fminf(m1, a);
                     }
                     const unsigned tot = static_cast<unsigned>(__popc(neg)) & 1u;
                     const float n1 = nms_mag(p.alpha, p.beta, m1);
@@ -334,11 +347,9 @@ bp_layered_reg_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, in
                     const unsigned nm = ((neg ^ (0u - tot)) & 0x07FFFFFFu) | (static_cast<unsigned>(idx) << 27);
 #pragma unroll
                     for (int j = 0; j < D; ++j) {
-                        if (vr[t][j] >= 0) {
-                            const unsigned sg = (nm >> j) & 1u;
-                            const float mag = (j == idx) ? n2 : n1;
-                            app[vr[t][j]] = __fadd_rn(q[j], sg ? -mag : mag);
-                        }
+                        const unsigned sg = (nm >> j) & 1u;
+                        const float mag = (j == idx) ? n2 : n1;
+                        app[vr[t][j]] = __fadd_rn(q[j], sg ? -mag : mag);
                     }
                     m1r[t] = n1;
                     m2r[t] = n2;
@@ -348,12 +359,16 @@ bp_layered_reg_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, in
             }
             const int w = syndrome();
             ++iter;
-            if (track_best && (w < best_w || (w == 0 && best_w == 0))) {
+            // The best posterior so far (a zero syndrome always is).  A zero syndrome's is app
+            // itself, so its copy is skipped where that costs no spill (D = 8 would spill).
+            const bool last = w == 0 || iter >= p.max_iter;
+            const bool zero_in_app = D <= 6 && w == 0;
+            if (track_best && (w < best_w || (w == 0 && best_w == 0)) && !zero_in_app) {
                 for (int i = gl; i < n; i += G) best[i] = app[i];
                 __syncwarp(gmask);
             }
             if (w < best_w) best_w = w;
-            if (w == 0 || iter >= p.max_iter) {
+            if (last) {
                 // ---- finalize (bp_layered_kernel's) ----
                 bool accept = (w == 0);
                 if (accept && p.min_abs_accept > 0.0f) {
@@ -380,7 +395,7 @@ bp_layered_reg_kernel(LayeredView cv, BpParams p, BpIO io, int slots_per_cta, in
                     int s = 0;
                     if (gl == 0) s = atomicAdd(io.osd_count, 1);
                     s = __shfl_sync(gmask, s, leader);
-                    const float* b = track_best ? best : app;
+                    const float* b = (track_best && !zero_in_app) ? best : app;
                     float* dst = io.osd_llr + static_cast<size_t>(s) * n;
                     for (int i = gl; i < n; i += G) dst[i] = b[i];
                     if (gl == 0) io.osd_index[s] = c;
@@ -538,7 +553,8 @@ size_t layered_smem_bytes(const LayeredView& cv, int slots, bool track_best, int
 {
     const int n_pad = (cv.n + 3) & ~3;
     const int mp = cv.num_layers * cv.width;
-    int slot_floats = ((track_best ? 2 : 1) * n_pad + 3 * mp + 3) & ~3;
+    // posteriors, the dummy edge's +inf (padded to 4 floats), the best posteriors, messages
+    int slot_floats = ((track_best ? 2 : 1) * n_pad + 4 + 3 * mp + 3) & ~3;
     slot_floats = pad_slot_stride(slot_floats, cv.group);
     if (slot_floats_out) *slot_floats_out = slot_floats;
     const int table = (cv.num_layers * cv.maxdeg * cv.width + 3) & ~3;
@@ -562,7 +578,8 @@ static void launch_layered_reg_t(const LayeredView& cv, const BpParams& p, const
                                  bool track_best, cudaStream_t st)
 {
     const int n_pad = (cv.n + 3) & ~3;
-    int slot_floats = ((track_best ? 2 : 1) * n_pad + 3) & ~3;
+    // posteriors, the dummy edge's +inf (padded to 4 floats), then the best posteriors
+    int slot_floats = (track_best ? 2 : 1) * n_pad + 4;
     slot_floats = pad_slot_stride(slot_floats, cv.group);
     const size_t smem = static_cast<size_t>(slots) * slot_floats * sizeof(float);
     const auto kernel = bp_layered_reg_kernel<D, kRegRows>;

@@ -131,6 +131,19 @@ __device__ __forceinline__ int row_var(const CodeDesc& d, int L, int j, int rs)
     return __ldg(d.vars + (L * d.maxdeg + j) * d.width + rs);
 }
 
+// Empty edge slots (short rows, row slots past a layer's last row) point at a
+// dummy posterior held at +inf right after a slot's posteriors: such an edge
+// never sets a row's minima, argmin or sign and never flips a parity, and its
+// update leaves it at +inf, so the row loops need no per-edge test.
+__device__ __forceinline__ int dummy_var(const CodeDesc& d) { return (d.n + 3) & ~3; }
+
+// Variable of slot j (j < D) of row rs in layer L, or the dummy.
+__device__ __forceinline__ int slot_var(const CodeDesc& d, int L, int j, int rs)
+{
+    const int v = (j < d.maxdeg) ? row_var(d, L, j, rs) : -1;
+    return v >= 0 ? v : dummy_var(d);
+}
+
 // Unsatisfied checks among the rows gl, gl + G, ... of every layer; a row's
 // D slots are loaded together (no chain of dependent loads per slot).
 template <int D>
@@ -145,13 +158,10 @@ __device__ __forceinline__ int lane_syndrome(const CodeDesc& d, const float* app
             for (int j0 = 0; j0 < D; j0 += 8) {  // groups of 8 slots bound the registers held
                 int v[8];
 #pragma unroll
-                for (int x = 0; x < 8; ++x) {
-                    const int j = j0 + x;
-                    v[x] = (j < D && j < d.maxdeg) ? row_var(d, L, j, rs) : -1;
-                }
+                for (int x = 0; x < 8; ++x) v[x] = (j0 + x < D) ? slot_var(d, L, j0 + x, rs) : 0;
 #pragma unroll
                 for (int x = 0; x < 8; ++x)
-                    if (v[x] >= 0) par ^= (app[v[x]] < 0.0f) ? 1u : 0u;
+                    if (j0 + x < D) par ^= (app[v[x]] < 0.0f) ? 1u : 0u;
             }
             cnt += static_cast<int>(par);
         }
@@ -173,27 +183,26 @@ __device__ __forceinline__ void update_row(const CodeDesc& d, float* app, float*
                                            int rs)
 {
     const int ridx = L * d.width + rs;
+    int v[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) v[j] = slot_var(d, L, j, rs);
+    if (v[0] == dummy_var(d)) return;  // row slot past the layer's last row
     const float o1 = r1[ridx], o2 = r2[ridx];
     const unsigned om = meta[ridx];
     float qv[D];
-    int v[D];
     float m1 = FLT_MAX, m2 = FLT_MAX;
     int idx = 0;
     unsigned neg = 0;
 #pragma unroll
     for (int j = 0; j < D; ++j) {
-        v[j] = (j < d.maxdeg) ? row_var(d, L, j, rs) : -1;
-        qv[j] = 0.0f;
-        if (v[j] >= 0) {
-            const float qj = __fsub_rn(app[v[j]], rebuild(o1, o2, om, j));
-            qv[j] = qj;
-            neg |= (qj < 0.0f) ? (1u << j) : 0u;
-            const float a = fabsf(qj);
-            // first strict minimum and second minimum (magnitudes are >= +0)
-            idx = (a < m1) ? j : idx;
-            m2 = fminf(m2, fmaxf(m1, a));
-            m1 = fminf(m1, a);
-        }
+        const float qj = __fsub_rn(app[v[j]], rebuild(o1, o2, om, j));
+        qv[j] = qj;
+        neg |= (qj < 0.0f) ? (1u << j) : 0u;
+        const float a = fabsf(qj);
+        // first strict minimum and second minimum (magnitudes are >= +0)
+        idx = (a < m1) ? j : idx;
+        m2 = fminf(m2, fmaxf(m1, a));
+        m1 = fminf(m1, a);
     }
     const unsigned tot = static_cast<unsigned>(__popc(neg)) & 1u;
     const float n1 = nms_mag(d.alpha, d.beta, m1);
@@ -203,11 +212,9 @@ __device__ __forceinline__ void update_row(const CodeDesc& d, float* app, float*
     const unsigned nm = ((neg ^ (0u - tot)) & 0x07FFFFFFu) | (static_cast<unsigned>(idx) << 27);
 #pragma unroll
     for (int j = 0; j < D; ++j) {
-        if (v[j] >= 0) {
-            const unsigned sgn = (nm >> j) & 1u;
-            const float mag = (j == idx) ? n2 : n1;
-            app[v[j]] = __fadd_rn(qv[j], sgn ? -mag : mag);
-        }
+        const unsigned sgn = (nm >> j) & 1u;
+        const float mag = (j == idx) ? n2 : n1;
+        app[v[j]] = __fadd_rn(qv[j], sgn ? -mag : mag);
     }
     r1[ridx] = n1;
     r2[ridx] = n2;
@@ -228,10 +235,11 @@ __device__ __forceinline__ void wide_unit(const MixedIO& io, const CodeDesc& d, 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = d.n;
     const int mp = d.num_layers * d.width;
-    float* r1 = app + ((n + 3) & ~3);
+    float* r1 = app + dummy_var(d) + 4;
     float* r2 = r1 + mp;
     unsigned* meta = reinterpret_cast<unsigned*>(r2 + mp);
     const float* src = io.llr + io.llr_off[cw];
+    if (gl == 0) app[dummy_var(d)] = __int_as_float(0x7f800000);  // +inf
     for (int i = gl; i < n; i += G) {
         const float x = __ldcs(src + i);
         app[i] = x;
@@ -344,13 +352,14 @@ __device__ __forceinline__ void narrow_unit(const MixedIO& io, const CodeDesc& d
     const int n_pad = (n + 3) & ~3;
     const int mp = d.num_layers * d.width;
     float* app = wbase + sub * d.slot_floats;
-    float* r1 = app + n_pad;
+    float* r1 = app + n_pad + 4;  // app[n_pad]: the dummy posterior
     float* r2 = r1 + mp;
     unsigned* meta = reinterpret_cast<unsigned*>(r2 + mp);
     float* best = io.best + (static_cast<size_t>(gwarp) * io.best_slots + sub) * io.n_max;
     int iter = 0, best_w = 0;
     if (active) {
         const float* src = io.llr + io.llr_off[cw];
+        if (gl == 0) app[n_pad] = __int_as_float(0x7f800000);  // +inf, before the __syncwarp below
         for (int i = gl; i < n; i += G) {
             const float v = __ldcs(src + i);
             app[i] = v;
@@ -477,7 +486,8 @@ void set_code_warps(EngineCode& ec, int warps)
         d.rows_per_lane = lv.width / d.group;
     }
     const int n_pad = (d.n + 3) & ~3;
-    int sf = (n_pad + 3 * d.num_layers * d.width + 3) & ~3;
+    // posteriors, the dummy edge's +inf (padded to 4 floats), then the row messages
+    int sf = (n_pad + 4 + 3 * d.num_layers * d.width + 3) & ~3;
     sf = pad_slot_stride(sf, d.group);
     d.slot_floats = sf;
 }
