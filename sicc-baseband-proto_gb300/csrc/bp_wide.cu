@@ -127,12 +127,20 @@ struct SplitApp {
 template <int D>
 constexpr int row_batch() { return D <= 16 ? 2 : 1; }
 
+// Empty edge slots of short rows point at a dummy posterior (+inf: never a row's minimum,
+// argmin or sign, never a parity flip, and left at +inf by its update), so the edge loops
+// test only `j < cv.maxdeg`, the same for every thread.  Above D = 8 the slots keep -1 and
+// a per-edge test: the dummy form's registers would spill there.
+template <int D>
+constexpr bool dummy_slots() { return D <= 8; }
+
 // Layered update of rows rs0, rs0 + kWideThreads, ... (kRowBatch of them, those below
 // `rows`) of layer L, whose messages start at row `first` of the layer-ordered message
 // arrays: the shared-memory layered kernel's per-row arithmetic (bp_kernels.cu).
 template <int D, int kRowBatch = row_batch<D>()>
 __device__ __forceinline__ void wide_rows(const LayeredView& cv, const BpParams& p, int L, int rs0, int rows,
-                                          int first, const SplitApp& app, float* r1, float* r2, unsigned* meta)
+                                          int first, const SplitApp& app, int dummy, float* r1, float* r2,
+                                          unsigned* meta)
 {
     int v[kRowBatch][D];
     float o1[kRowBatch], o2[kRowBatch], x[kRowBatch][D];
@@ -143,19 +151,33 @@ __device__ __forceinline__ void wide_rows(const LayeredView& cv, const BpParams&
         const bool live = rs < rows;
         const int* vp = cv.vars + (L * cv.maxdeg) * cv.width + rs;
 #pragma unroll
-        for (int j = 0; j < D; ++j) v[b][j] = (live && j < cv.maxdeg) ? __ldg(vp + j * cv.width) : -1;
+        for (int j = 0; j < D; ++j) {
+            const int vj = (live && j < cv.maxdeg) ? __ldg(vp + j * cv.width) : -1;
+            v[b][j] = (vj >= 0 || !dummy_slots<D>()) ? vj : dummy;
+        }
         const int ridx = first + rs;
         o1[b] = live ? r1[ridx] : 0.0f;
         o2[b] = live ? r2[ridx] : 0.0f;
         om[b] = live ? meta[ridx] : 0u;
     }
+    auto used = [&](int b, int j) { return dummy_slots<D>() ? j < cv.maxdeg : v[b][j] >= 0; };
+    if constexpr (dummy_slots<D>()) {
 #pragma unroll
-    for (int b = 0; b < kRowBatch; ++b)
+        for (int b = 0; b < kRowBatch; ++b) {
+            if (rs0 + b * kWideThreads < rows) {
 #pragma unroll
-        for (int j = 0; j < D; ++j) x[b][j] = v[b][j] >= 0 ? app.ld(v[b][j]) : 0.0f;
+                for (int j = 0; j < D; ++j) x[b][j] = (j < cv.maxdeg) ? app.ld(v[b][j]) : 0.0f;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int b = 0; b < kRowBatch; ++b)
+#pragma unroll
+            for (int j = 0; j < D; ++j) x[b][j] = v[b][j] >= 0 ? app.ld(v[b][j]) : 0.0f;
+    }
 #pragma unroll
     for (int b = 0; b < kRowBatch; ++b) {
-        if (v[b][0] < 0) continue;  // past the layer
+        if (dummy_slots<D>() ? rs0 + b * kWideThreads >= rows : v[b][0] < 0) continue;  // past the layer
         float q[D];
         float m1 = FLT_MAX, m2 = FLT_MAX;
         int idx = 0;
@@ -163,7 +185,7 @@ __device__ __forceinline__ void wide_rows(const LayeredView& cv, const BpParams&
 #pragma unroll
         for (int j = 0; j < D; ++j) {
             q[j] = 0.0f;
-            if (v[b][j] >= 0) {
+            if (used(b, j)) {
                 const float qj = __fsub_rn(x[b][j], rebuild(o1[b], o2[b], om[b], j));
                 q[j] = qj;
                 neg |= (qj < 0.0f) ? (1u << j) : 0u;
@@ -179,7 +201,7 @@ __device__ __forceinline__ void wide_rows(const LayeredView& cv, const BpParams&
         const unsigned nm = ((neg ^ (0u - tot)) & 0x07FFFFFFu) | (static_cast<unsigned>(idx) << 27);
 #pragma unroll
         for (int j = 0; j < D; ++j) {
-            if (v[b][j] >= 0) {
+            if (used(b, j)) {
                 const unsigned sg = (nm >> j) & 1u;
                 const float mag = (j == idx) ? n2 : n1;
                 app.st(v[b][j], __fadd_rn(q[j], sg ? -mag : mag));
@@ -194,7 +216,8 @@ __device__ __forceinline__ void wide_rows(const LayeredView& cv, const BpParams&
 
 // Unsatisfied checks among the same rows under hard(app).
 template <int D, int kRowBatch = row_batch<D>()>
-__device__ __forceinline__ int wide_parity(const LayeredView& cv, int L, int rs0, int rows, const SplitApp& app)
+__device__ __forceinline__ int wide_parity(const LayeredView& cv, int L, int rs0, int rows, const SplitApp& app,
+                                           int dummy)
 {
     int v[kRowBatch][D];
 #pragma unroll
@@ -203,15 +226,19 @@ __device__ __forceinline__ int wide_parity(const LayeredView& cv, int L, int rs0
         const bool live = rs < rows;
         const int* vp = cv.vars + (L * cv.maxdeg) * cv.width + rs;
 #pragma unroll
-        for (int j = 0; j < D; ++j) v[b][j] = (live && j < cv.maxdeg) ? __ldg(vp + j * cv.width) : -1;
+        for (int j = 0; j < D; ++j) {
+            const int vj = (live && j < cv.maxdeg) ? __ldg(vp + j * cv.width) : -1;
+            v[b][j] = (vj >= 0 || !dummy_slots<D>()) ? vj : dummy;
+        }
     }
     int cnt = 0;
 #pragma unroll
     for (int b = 0; b < kRowBatch; ++b) {
+        if (dummy_slots<D>() && rs0 + b * kWideThreads >= rows) continue;  // past the layer
         unsigned par = 0;
 #pragma unroll
         for (int j = 0; j < D; ++j)
-            if (v[b][j] >= 0) par ^= (app.ld(v[b][j]) < 0.0f) ? 1u : 0u;
+            if (dummy_slots<D>() ? j < cv.maxdeg : v[b][j] >= 0) par ^= (app.ld(v[b][j]) < 0.0f) ? 1u : 0u;
         cnt += static_cast<int>(par);
     }
     return cnt;
@@ -231,10 +258,13 @@ bp_layered_wide_kernel(LayeredView cv, BpParams p, BpIO io, float* scratch, long
     const int n = cv.n, n_pad = (n + 3) & ~3;
     const int mp = cv.m;  // messages of the rows in layer order, packed
     float* g = scratch + static_cast<size_t>(blockIdx.x) * static_cast<size_t>(slice);
-    // posteriors [0, split) in shared memory; with split < n the slice starts with n_pad posteriors
-    const bool all_smem = split >= n;
+    // posteriors [0, split) in shared memory.  The dummy posterior (index n_pad, +inf) takes the
+    // empty edge slots of short rows: with split > n_pad it and every posterior are in shared
+    // memory, else the slice starts with n_pad posteriors and the dummy (4 floats).
+    const bool all_smem = split > n_pad;
     const SplitApp app{s_app, g, split};
-    float* best = all_smem ? g : g + n_pad;
+    const int dummy = n_pad;
+    float* best = all_smem ? g : g + n_pad + 4;
     float* r1 = best + (track_best ? n_pad : 0);
     float* r2 = r1 + mp;
     unsigned* meta = reinterpret_cast<unsigned*>(r2 + mp);
@@ -244,11 +274,12 @@ bp_layered_wide_kernel(LayeredView cv, BpParams p, BpIO io, float* scratch, long
         for (int L = 0; L < cv.num_layers; ++L) {
             const int first = __ldg(cv.layer_start + L), rows = __ldg(cv.layer_start + L + 1) - first;
             for (int rs0 = tid; rs0 < rows; rs0 += row_batch<D>() * kWideThreads)
-                cnt += wide_parity<D>(cv, L, rs0, rows, app);
+                cnt += wide_parity<D>(cv, L, rs0, rows, app, dummy);
         }
         return cta_sum(cnt, s_red);
     };
 
+    if (tid == 0) app.st(dummy, __int_as_float(0x7f800000));  // +inf, before the first __syncthreads
     for (int c = blockIdx.x; c < io.count; c = wide_next(io, &s_next)) {
         const float* src = io.llr + static_cast<size_t>(c) * n;
         for (int i = tid; i < n; i += kWideThreads) {
@@ -268,7 +299,7 @@ bp_layered_wide_kernel(LayeredView cv, BpParams p, BpIO io, float* scratch, long
             for (int L = 0; L < cv.num_layers; ++L) {
                 const int first = __ldg(cv.layer_start + L), rows = __ldg(cv.layer_start + L + 1) - first;
                 for (int rs0 = tid; rs0 < rows; rs0 += row_batch<D>() * kWideThreads)
-                    wide_rows<D>(cv, p, L, rs0, rows, first, app, r1, r2, meta);
+                    wide_rows<D>(cv, p, L, rs0, rows, first, app, dummy, r1, r2, meta);
                 __syncthreads();
             }
             w = syndrome();
@@ -443,14 +474,15 @@ void launch_layered_wide_t(const LayeredView& cv, const BpParams& p, const BpIO&
 {
     const long long n_pad = (cv.n + 3) & ~3;
     const long long mp = cv.m;
-    const size_t app_bytes = static_cast<size_t>(n_pad) * sizeof(float);
+    // the posteriors and the dummy posterior (index n_pad, padded to 4 floats)
+    const size_t app_bytes = static_cast<size_t>(n_pad + 4) * sizeof(float);
     // posteriors in shared memory: all of them up to 200 KB, else the first 56,320 (220 KB;
-    // variables beyond stay in the slice)
+    // variables beyond and the dummy stay in the slice)
     constexpr size_t kSmemApp = 200 * 1024, kSplitApp = 220 * 1024;
     const bool all_smem = app_bytes <= kSmemApp;
-    const int split = all_smem ? cv.n : static_cast<int>(kSplitApp / sizeof(float));
+    const int split = all_smem ? static_cast<int>(n_pad + 4) : static_cast<int>(kSplitApp / sizeof(float));
     const size_t smem = all_smem ? app_bytes : kSplitApp;
-    long long slice = (all_smem ? 0 : n_pad) + (track_best ? n_pad : 0) + 3 * mp;
+    long long slice = (all_smem ? 0 : n_pad + 4) + (track_best ? n_pad : 0) + 3 * mp;
     slice = (slice + 31) & ~31LL;  // 128-byte aligned slices
     const auto kernel = bp_layered_wide_kernel<D>;
     check_cuda(grant_dynamic_smem(reinterpret_cast<const void*>(kernel), smem), "cudaFuncSetAttribute(bp wide)");
