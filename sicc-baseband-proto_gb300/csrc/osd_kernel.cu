@@ -212,53 +212,56 @@ osd_kernel(OsdView ov0, OsdIO io)
             }
         }
         // ---- 3. column-scan elimination: pivots = most reliable basis ----
-        // Column j lives in word j / 64 of every row: the scan runs word by word, so the
-        // column's word is a register known at compile time (no selection among the words).
-        unsigned pivoted = 0;  // bit a: my row in slot a is a pivot row
-        unsigned live = 0;     // bit a: my row in slot a exists (r < k)
+        // Column j lives in bit j % 32 of 32-bit half (j / 32) % 2 of word j / 64 of every row:
+        // the scan runs half-word by half-word, so the column's half is a register known at
+        // compile time and each row test is one 32-bit operation.
+        unsigned avail = 0;  // bit a: my row in slot a exists (r < k) and is not yet a pivot row
 #pragma unroll
-        for (int a = 0; a < KR; ++a) live |= (a * 32 + lane < k) ? 1u << a : 0u;
+        for (int a = 0; a < KR; ++a) avail |= (a * 32 + lane < k) ? 1u << a : 0u;
         int rank = 0;
 #pragma unroll
         for (int W = 0; W < NW; ++W) {
-            for (int bit = 0; bit < 64 && rank < k; ++bit) {
-                const int j = W * 64 + bit;
-                if (j >= n) break;
-                const unsigned long long bj = 1ull << bit;
-                int ps = -1, pl = 0;
 #pragma unroll
-                for (int a = 0; a < KR; ++a) {
-                    const bool cand = ((live & ~pivoted) >> a & 1u) && (rows[a][W] & bj);
-                    const unsigned bal = __ballot_sync(0xffffffffu, cand);
-                    if (ps < 0 && bal) {
-                        ps = a;
-                        pl = __ffs(bal) - 1;
+            for (int hh = 0; hh < 2; ++hh) {
+                for (int b = 0; b < 32 && rank < k; ++b) {
+                    const int j = W * 64 + hh * 32 + b;
+                    if (j >= n) break;
+                    const unsigned bm = 1u << b;
+                    auto has = [&](int a) { return (static_cast<unsigned>(rows[a][W] >> (hh * 32)) & bm) != 0u; };
+                    int ps = -1, pl = 0;
+#pragma unroll
+                    for (int a = 0; a < KR; ++a) {
+                        const unsigned bal = __ballot_sync(0xffffffffu, ((avail >> a) & 1u) && has(a));
+                        if (ps < 0 && bal) {
+                            ps = a;
+                            pl = __ffs(bal) - 1;
+                        }
                     }
-                }
-                if (ps < 0) continue;  // dependent position
-                unsigned long long pw[NW];
+                    if (ps < 0) continue;  // dependent position
+                    unsigned long long pw[NW];
 #pragma unroll
-                for (int w = 0; w < NW; ++w) {
-                    unsigned long long mine = 0ull;
+                    for (int w = 0; w < NW; ++w) {
+                        unsigned long long mine = 0ull;
 #pragma unroll
-                    for (int a = 0; a < KR; ++a)
-                        if (a == ps) mine = rows[a][w];
-                    pw[w] = shfl_u64(mine, pl);
-                }
-#pragma unroll
-                for (int a = 0; a < KR; ++a) {
-                    const bool is_p = (a == ps) && (lane == pl);
-                    if (!is_p && (rows[a][W] & bj)) {
-#pragma unroll
-                        for (int w = 0; w < NW; ++w) rows[a][w] ^= pw[w];
+                        for (int a = 0; a < KR; ++a)
+                            if (a == ps) mine = rows[a][w];
+                        pw[w] = shfl_u64(mine, pl);
                     }
-                    if (is_p) pivoted |= 1u << a;
+#pragma unroll
+                    for (int a = 0; a < KR; ++a) {
+                        const bool is_p = (a == ps) && (lane == pl);
+                        if (!is_p && has(a)) {
+#pragma unroll
+                            for (int w = 0; w < NW; ++w) rows[a][w] ^= pw[w];
+                        }
+                        if (is_p) avail &= ~(1u << a);
+                    }
+                    if (lane == 0) {
+                        s.rowpiv[ps * 32 + pl] = static_cast<int16_t>(rank);
+                        s.mrb_pos[rank] = static_cast<int16_t>(j);
+                    }
+                    ++rank;
                 }
-                if (lane == 0) {
-                    s.rowpiv[ps * 32 + pl] = static_cast<int16_t>(rank);
-                    s.mrb_pos[rank] = static_cast<int16_t>(j);
-                }
-                ++rank;
             }
         }
         __syncwarp();
