@@ -22,6 +22,7 @@
 #include "bp_kernels.h"
 
 #include <algorithm>
+#include <type_traits>
 
 namespace sicc {
 
@@ -333,8 +334,10 @@ osd_kernel(OsdView ov0, OsdIO io)
         unsigned long long best_key = ~0ull;
         float thr = INFINITY;
         const int share = io.share_rounds > 0 ? io.share_rounds : 2;
-        // the metric of test q, whose flips are pool ranks f0, f1, f2 (-1: none), pruned against thr
-        auto evaluate = [&](int q, int f0, int f1, int f2) {
+        // The metric of test q, whose flips are pool ranks f0, f1, f2, pruned against thr.  The
+        // first `kSure` flips are known to exist (no test); the others may be -1 (none).
+        auto evaluate = [&](auto sure, int q, int f0, int f1, int f2) {
+            constexpr int kSure = decltype(sure)::value;
             unsigned long long d[NW];
 #pragma unroll
             for (int w = 0; w < NW; ++w) d[w] = acc[w];
@@ -342,7 +345,7 @@ osd_kernel(OsdView ov0, OsdIO io)
 #pragma unroll
             for (int f = 0; f < 3; ++f) {
                 const int fi = fl[f];
-                if (fi >= 0) {
+                if (f < kSure || fi >= 0) {
                     if (kFlipRows<NW, KR>) {
 #pragma unroll
                         for (int w = 0; w < NW; ++w) d[w] ^= s.frows[kFlipRows<NW, KR> ? fi : 0][w];
@@ -408,7 +411,7 @@ osd_kernel(OsdView ov0, OsdIO io)
             const int single = 1 + P;
             for (int rd = 0; rd * 32 < single; ++rd) {
                 const int q = rd * 32 + lane;
-                if (q < single) evaluate(q, q > 0 ? q - 1 : -1, -1, -1);
+                if (q < single) evaluate(std::integral_constant<int, 0>(), q, q > 0 ? q - 1 : -1, -1, -1);
             }
             share_best();
             const int R = (P - 1 + 31) / 32;  // rows a = 0 .. P-2, R consecutive rows per lane
@@ -447,7 +450,7 @@ osd_kernel(OsdView ov0, OsdIO io)
                 if (idx < total) {
                     while (a < P - 2 && s.rstart[a + 1] <= idx) ++a;
                     const int b = a + 1 + (idx - s.rstart[a]);
-                    evaluate(single + a * (2 * P - a - 1) / 2 + (b - a - 1), a, b, -1);
+                    evaluate(std::integral_constant<int, 2>(), single + a * (2 * P - a - 1) / 2 + (b - a - 1), a, b, -1);
                 }
                 if (rd % share == share - 1) share_best();
             }
@@ -458,7 +461,7 @@ osd_kernel(OsdView ov0, OsdIO io)
                 if (q < ov.num_tests) {
                     int f0, f1, f2;
                     flips_of(q, f0, f1, f2);
-                    evaluate(q, f0, f1, f2);
+                    evaluate(std::integral_constant<int, 0>(), q, f0, f1, f2);
                 }
                 if (rd % share == share - 1) share_best();
             }
